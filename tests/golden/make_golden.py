@@ -1,0 +1,196 @@
+"""Generate golden vectors by running the reference (annayesy/slabLU) itself.
+
+Run in a container where the reference source is mounted:
+
+    python tests/golden/make_golden.py [/root/reference]
+
+The reference needs SciPy sparse indexing to accept torch index tensors
+(SciPy >= 1.11 rejects them).  This script installs that conversion as a
+monkeypatch in its own process; the reference source is not modified.
+Outputs are small .npz files beside this script; they are committed and read
+by the CPU tests (the reference source is not needed afterwards).
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF = sys.argv[1] if len(sys.argv) > 1 else '/root/reference'
+os.environ['CUDA_VISIBLE_DEVICES'] = ''
+
+import torch  # noqa: E402
+import scipy.sparse._index as _sp_index  # noqa: E402
+
+torch.set_default_dtype(torch.double)
+_get, _set = _sp_index.IndexMixin.__getitem__, _sp_index.IndexMixin.__setitem__
+
+
+def _np_key(k):
+    if isinstance(k, torch.Tensor):
+        return k.numpy()
+    if isinstance(k, tuple):
+        return tuple(_np_key(x) for x in k)
+    return k
+
+
+_sp_index.IndexMixin.__getitem__ = lambda self, k: _get(self, _np_key(k))
+_sp_index.IndexMixin.__setitem__ = lambda self, k, v: _set(self, _np_key(k), v)
+sys.path.insert(0, REF)
+
+from src_disc.hps_subdomain_disc import HPS_Disc  # noqa: E402
+from src_disc import hps_parallel_leaf_ops as leaf_ops  # noqa: E402
+from src_disc import hps_multidomain_disc  # noqa: E402
+from src_disc import pdo as ref_pdo  # noqa: E402
+import src_disc.built_in_funcs as bif  # noqa: E402
+import src_solver.block_tridiag_solver_dense as ref_bt  # noqa: E402
+from src_solver.slablu_solver import Domain_Solver  # noqa: E402
+
+
+def save(name, **arrs):
+    path = os.path.join(HERE, name)
+    np.savez_compressed(path, **arrs)
+    print('wrote', name, sum(v.nbytes for v in map(np.asarray, arrs.values())) // 1024, 'KiB')
+
+
+def bumps32(xx, seed=0):
+    """b = 1 + 0.5 sum of 32 Gaussian bumps (width 0.02) at seeded centres."""
+    rng = np.random.default_rng(seed)
+    cen = rng.random((32, 2))
+    x = np.asarray(xx)
+    d2 = ((x[:, None, :] - cen[None]) ** 2).sum(-1)
+    return 1.0 + 0.5 * np.exp(-d2 / (2 * 0.02 ** 2)).sum(1)
+
+
+def leaf_fixtures():
+    for p, a in ((8, 0.0125), (12, 0.0125), (22, 0.005), (16, 1 / (2 * 71))):
+        H = HPS_Disc(a, p, 2)
+        J = H.JJ
+        extra = {}
+        if p <= 12:
+            extra = dict(D1=H.Ds.D1, D2=H.Ds.D2, D11=H.Ds.D11, D22=H.Ds.D22)
+        save(f'leaf_p{p}.npz', p=p, a=a, zz=H.zz, Jl=J.Jl, Jr=J.Jr, Jd=J.Jd, Ju=J.Ju,
+             Jx=J.Jx, Jc=J.Jc, Jxreorder=J.Jxreorder, Nx=H.Nx, Interp_mat=H.Interp_mat, **extra)
+
+
+def dtn_fixture(p, a, nbox_side, picks, kh, name, seed=0):
+    """Reference form_DtNs (build and solve) on selected leaves of a grid."""
+    md = hps_multidomain_disc.HPS_Multidomain(
+        ref_pdo.PDO_2d(ref_pdo.ones, ref_pdo.ones), torch.tensor([[0, 1.0], [0, 1.0]]), a, p)
+    xx = md.grid_xx[picks].clone()
+    cvals = torch.tensor(-(kh ** 2) * bumps32(xx.reshape(-1, 2).numpy(), seed)).reshape(len(picks), -1)
+    lut = {}
+
+    def cfun(x):
+        key = x.shape[0]
+        return lut[key]
+
+    lut[len(picks) * p * p] = cvals.reshape(-1)
+    op = ref_pdo.PDO_2d(ref_pdo.ones, ref_pdo.ones, c=cfun)
+    H = md.H
+    Nx = torch.tensor(H.Nx)
+    Jx = torch.tensor(H.JJ.Jx)
+    Jc = torch.tensor(H.JJ.Jc)
+    Jxr = torch.tensor(H.JJ.Jxreorder)
+    Im = torch.tensor(H.Interp_mat)
+    dev = torch.device('cpu')
+    DtN = leaf_ops.form_DtNs(p, 2, xx, Nx, Jx, Jc, Jxr, H.Ds, Im, op, 0, len(picks), dev,
+                             'build', torch.zeros(len(picks), 4 * (p - 2), 1), None)
+    rng = np.random.default_rng(seed + 1)
+    uface = torch.tensor(rng.standard_normal((len(picks), 4 * (p - 2), 2)))
+    usol = leaf_ops.form_DtNs(p, 2, xx, Nx, Jx, Jc, Jxr, H.Ds, Im, op, 0, len(picks), dev,
+                              'solve', uface, None)
+    save(name, p=p, a=a, kh=kh, picks=np.asarray(picks), xx=xx.numpy(), c=cvals.numpy(),
+         dtn=DtN.numpy(), u_face=uface.numpy(), u_solve=usol.numpy())
+
+
+def assembly_fixture():
+    p, a = 8, 0.0125
+    geom = torch.tensor([[0, 4 * 2 * a], [0, 3 * 2 * a]])
+    kh = 25.0
+    op = ref_pdo.PDO_2d(ref_pdo.ones, ref_pdo.ones, c=lambda xx: bif.bfield_gaussian_bumps(xx, kh).reshape(-1))
+    md = hps_multidomain_disc.HPS_Multidomain(op, geom, a, p)
+    A, _ = md.sparse_mat(torch.device('cpu'))
+    A.sort_indices()
+    save('assembly_p8.npz', p=p, a=a, kh=kh, box_geom=geom.numpy(), data=A.data, indices=A.indices,
+         indptr=A.indptr, shape=np.array(A.shape), I_unique=md.I_unique.numpy(),
+         I_copy1=md.I_copy1.numpy(), I_copy2=md.I_copy2.numpy(), xx_active=md.xx_active.numpy(),
+         xx_tot=md.xx_tot.numpy())
+
+
+def partition_fixture():
+    out = {}
+    for (p, n) in ((8, 48), (12, 400), (22, 400), (22, 2000), (22, 1000), (16, 994)):
+        a = 1 / (2 * (n / (p - 2)))
+        op = ref_pdo.PDO_2d(ref_pdo.ones, ref_pdo.ones)
+        dom = Domain_Solver(torch.tensor([[0, 1.0], [0, 1.0]]), op, 0.0, a, p=p, buf_constant=1.0)
+        tag = f'p{p}_n{n}'
+        out[tag + '_buf'] = np.array(dom.buf_pans)
+        out[tag + '_Npan'] = np.array(dom.Npan)
+        out[tag + '_nbox'] = dom.hps.n.numpy()
+        for nm in ('I_C', 'I_L', 'I_R', 'I_D', 'I_U', 'I_Ctot', 'I_Xtot'):
+            out[tag + '_' + nm] = np.asarray(getattr(dom, nm))
+    save('partition.npz', **out)
+
+
+def blocktri_fixture():
+    rng = np.random.default_rng(7)
+    out = {}
+    for (b, m, bs) in ((3, 5, 4), (2, 7, 6), (4, 2, 3)):
+        diag = torch.tensor(rng.standard_normal((b, m, bs, bs)) + 3 * np.eye(bs))
+        sub = torch.tensor(rng.standard_normal((b, m - 1, bs, bs)))
+        sup = torch.tensor(rng.standard_normal((b, m - 1, bs, bs)))
+        f = torch.tensor(rng.standard_normal((b, m * bs, 3)))
+        T = ref_bt.Block_Tridiagonal(b, m, bs)
+        T.build_sweep(diag.clone(), sub.clone(), sup.clone(), fast_LU=False)
+        x = T.lusolve_sweep(f.clone())
+        xt = T.lusolve_sweep(f.clone(), transpose=True)
+        tag = f'b{b}_m{m}_bs{bs}'
+        so, po = m, m + (m - 1)
+        out[tag + '_diag'] = diag.numpy(); out[tag + '_sub'] = sub.numpy(); out[tag + '_sup'] = sup.numpy()
+        out[tag + '_f'] = f.numpy(); out[tag + '_x'] = x.numpy(); out[tag + '_xt'] = xt.numpy()
+        out[tag + '_LU'] = T.Tdata[:, :so].numpy(); out[tag + '_Lsub'] = T.Tdata[:, so:po].numpy()
+        out[tag + '_Usup'] = T.Tdata[:, po:po + m - 1].numpy()
+        out[tag + '_piv'] = ref_bt.unpack_pivs(b, m, bs, T.Tdata, torch.device('cpu')).numpy()
+    save('blocktri.npz', **out)
+
+
+def run_domain(p, n, ppw, pde, solver, bc='free_space'):
+    nwaves = int(n / ppw)
+    kh = (nwaves + 0.03) * 2 * np.pi + 1.8
+    if pde == 'bfield_constant':
+        cf = lambda xx: bif.bfield_constant(xx, kh)
+    else:
+        cf = lambda xx: bif.bfield_gaussian_bumps(xx, kh).reshape(-1)
+    op = ref_pdo.PDO_2d(ref_pdo.ones, ref_pdo.ones, c=cf)
+    a = 1 / (2 * (n / (p - 2)))
+    dom = Domain_Solver(torch.tensor([[0, 1.0], [0, 1.0]]), op, kh, a, p=p, buf_constant=1.0)
+    dom.build('reduced_cpu', solver, verbose=False)
+    if bc == 'free_space':
+        uu = lambda xx: bif.uu_dir_func_greens(xx, kh)
+    else:
+        uu = lambda xx: torch.ones(xx.shape[0], 1)
+    sol, res, tres, rloc, _ = dom.solve(uu, None, known_sol=(bc == 'free_space'))
+    sol, res, tres, rloc, _ = dom.solve(uu, None, known_sol=(bc == 'free_space'))
+    return dom, kh, sol.numpy(), float(res), float(tres), float(rloc)
+
+
+def solve_fixtures():
+    dom, kh, sol, res, tres, rloc = run_domain(8, 48, 10, 'bfield_gaussian_bumps', 'superLU')
+    save('solve_superlu_p8_n48.npz', p=8, n=48, kh=kh, sol=sol, res=res, trueres=tres, resloc=rloc)
+    for (p, n, ppw, pde) in ((12, 400, 10, 'bfield_constant'), (22, 400, 40, 'bfield_constant')):
+        dom, kh, sol, res, tres, rloc = run_domain(p, n, ppw, pde, 'slabLU')
+        stride = 7
+        save(f'slablu_p{p}_n{n}_ppw{ppw}.npz', p=p, n=n, ppw=ppw, kh=kh, stride=stride,
+             sol_sub=sol[::stride], sol_norm=np.linalg.norm(sol), res=res, trueres=tres,
+             resloc=rloc)
+
+
+if __name__ == '__main__':
+    leaf_fixtures()
+    dtn_fixture(22, 0.005, 100, [0, 57, 4950, 9999, 1234, 6789, 3210, 8888], 1258.6, 'dtn_p22.npz')
+    dtn_fixture(12, 0.0125, 40, [0, 7, 800, 1599], 253.3, 'dtn_p12.npz', seed=3)
+    assembly_fixture()
+    partition_fixture()
+    blocktri_fixture()
+    solve_fixtures()
