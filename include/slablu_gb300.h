@@ -1,0 +1,137 @@
+/*
+ * slablu_gb300 -- C ABI of the GB300-native SlabLU factor-and-solve path.
+ *
+ * Conventions shared by every entry point:
+ *   - pointers named d_* are device pointers (CUDA global memory of the current
+ *     device); h_* are host pointers.  Nothing in this header takes a torch type.
+ *   - dense matrices crossing the ABI are row-major (C order), as the reference's
+ *     torch/NumPy tensors are.
+ *   - `stream` is a cudaStream_t passed as void* (NULL = legacy default stream).
+ *   - return value: SLAB_OK (0); > 0 is a pivot breakdown in the LAPACK `info`
+ *     sense (1-based column of the first exactly-zero pivot); < 0 is an error
+ *     code below.  slab_last_error() describes the most recent failure of the
+ *     calling thread.
+ *   - leaf discretisation conventions are the reference's
+ *     (src_disc/hps_subdomain_disc.py:105-152): p x p tensor Chebyshev nodes,
+ *     node k = i1*p + i2 with i1 the x index; interior nodes Jc in ascending
+ *     order; face nodes Jx = [Jl, Jr, Jd, Ju]; D is the 1-D derivative matrix
+ *     (scaled by 1/a) with D1 = -kron(D, I), D2 = -kron(I, D), Dsq = D @ D.
+ *   - reduced face unknowns are numbered as the reference numbers them
+ *     (src_disc/hps_multidomain_disc.py:63-81): face f, node k -> f*(p-2) + k.
+ */
+#ifndef SLABLU_GB300_H
+#define SLABLU_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SLAB_OK 0
+#define SLAB_ERR_ARG (-1)
+#define SLAB_ERR_CUDA (-2)
+#define SLAB_ERR_ALLOC (-3)
+#define SLAB_ERR_STATE (-4)
+#define SLAB_ERR_NOCONV (-5)
+
+/* Arithmetic of the factorization. */
+#define SLAB_PREC_FP64 0  /* everything in FP64                                         */
+#define SLAB_PREC_MIXED 1 /* FP32 leaf + slab factors, FP64 interface LU, FP64 residual */
+#define SLAB_PREC_FP32 2  /* FP32 factors everywhere, FP64 residual                     */
+
+/* Library version as an integer (major*10000 + minor*100 + patch). */
+int slab_version(void);
+
+/* Human-readable description of the last error on this thread. */
+const char* slab_last_error(void);
+
+/*
+ * Batched leaf Dirichlet-to-Neumann maps.
+ * Replaces form_DtNs(mode='build') and get_DtNs_helper
+ * (src_disc/hps_parallel_leaf_ops.py:40-72, :113-140) for the c12 = None case:
+ *   Aloc = -c11 D11 - c22 D22 + c1 D1 + c2 D2 + diag(c)      (:10-37)
+ *   S    = -Aloc[Jc,Jc]^{-1} Aloc[Jc,Jx]
+ *   DtN  = Nx[:,Jc] S + Nx[:,Jx]
+ * d_c11 .. d_c: coefficient values at the p*p nodes of each leaf, nleaf*p*p
+ *   doubles each, or NULL for an absent term (c11/c22 NULL mean zero).
+ * d_D, d_Dsq: p*p doubles.  d_Nx: 4(p-2) x p*p doubles (HPS_Disc.Nx).
+ * precision: SLAB_PREC_FP64 or SLAB_PREC_FP32 (factor arithmetic).
+ * d_work: scratch of slab_leaf_dtn_work_bytes() bytes (holds the leaf LU factors).
+ * d_dtn: nleaf x 4(p-2) x 4(p-2) doubles (row-major per leaf).
+ * d_S: optional (NULL) nleaf x (p-2)^2 x 4(p-2) doubles receiving S.
+ * d_info: nleaf ints, per-leaf LAPACK-style info (0 = success).
+ */
+size_t slab_leaf_dtn_work_bytes(int nleaf, int p, int precision);
+int slab_leaf_dtn(int nleaf, int p, const double* d_c11, const double* d_c22, const double* d_c1,
+                  const double* d_c2, const double* d_c, const double* d_D, const double* d_Dsq,
+                  const double* d_Nx, int precision, void* d_work, size_t work_bytes, double* d_dtn,
+                  double* d_S, int* d_info, void* stream);
+
+/*
+ * Factor-and-solve engine for the unit-square HPS SlabLU path.
+ * Replaces Domain_Solver.build (src_solver/slablu_solver.py:440-487: leaf DtN
+ * assembly, build_slabLU :297-358, build_Tred_solver :668-687) and
+ * Domain_Solver.solve (:543-666 with leaf recovery,
+ * src_disc/hps_multidomain_disc.py:227-243) for solver_type='slabLU',
+ * non-periodic, c12 = None.
+ *
+ * Geometry: n0 x n1 leaves (leaf index i*n1 + j, i = x index), polynomial
+ * order p, slab width buf leaves (n0 % buf == 0).  Host arrays:
+ *   h_D, h_Dsq  p*p doubles;  h_Nx 4(p-2) x p*p doubles;
+ *   h_interp    4(p-1) x 4(p-2) doubles (HPS_Disc.Interp_mat);
+ *   h_jxreorder 4(p-1) ints (JJ.Jxreorder).
+ * The engine owns its device memory; it is not re-entrant; all work is
+ * ordered on `stream`.
+ */
+typedef struct slab_engine slab_engine;
+
+int slab_engine_create(slab_engine** out, int p, int n0, int n1, int buf, int precision, const double* h_D,
+                       const double* h_Dsq, const double* h_Nx, const double* h_interp,
+                       const int* h_jxreorder, void* stream);
+int slab_engine_destroy(slab_engine* e);
+
+/* Number of reduced face unknowns (p-2)(n0(2 n1 + 1) + n1) and of leaves. */
+long long slab_engine_nfaces(const slab_engine* e);
+long long slab_engine_nleaves(const slab_engine* e);
+
+/* Factor the operator with coefficients at every leaf node (nleaf*p*p
+ * doubles each, NULL = absent).  Returns >0 on pivot breakdown. */
+int slab_engine_factor(slab_engine* e, const double* d_c11, const double* d_c22, const double* d_c1,
+                       const double* d_c2, const double* d_c);
+
+/*
+ * Solve for nrhs right-hand sides with FP64 iterative refinement.
+ * d_bnd:   nfaces x nrhs (column-major) face values; only the Dirichlet
+ *          (domain-boundary) faces are read.
+ * d_fbody: nleaf*p*p x nrhs body load at leaf nodes (column-major) or NULL.
+ * tol:     stop when ||correction|| <= tol * ||solution|| (FP64 norms).
+ * Outputs: d_ufaces nfaces x nrhs (column-major, may be NULL),
+ *          d_uleaf  nleaf*p*p x nrhs solution at every leaf node (column-major,
+ *                   corners and faces through Interp_mat as the reference does),
+ *          h_iters  refinement steps taken,
+ *          h_stats  5 doubles: [last relative correction, final residual norm,
+ *                   initial residual norm, interior (leaf-local) residual norm,
+ *                   relative residual].
+ * Returns SLAB_ERR_NOCONV if max_iter steps did not reach tol (outputs hold
+ * the last iterate).
+ */
+int slab_engine_solve(slab_engine* e, int nrhs, const double* d_bnd, const double* d_fbody, double tol,
+                      int max_iter, double* d_ufaces, double* d_uleaf, int* h_iters, double* h_stats);
+
+/* FP64 residual of the full HPS collocation system at (u_faces, u_int):
+ * r_int = f - Aloc[Jc,:] u per leaf, r_faces = -sum of leaf fluxes Nx u at
+ * interior faces (nfaces x nrhs column-major; zero on Dirichlet faces).
+ * d_uint / d_rint: interior values leaf-major, element (leaf, rhs c, interior
+ * node r) at (leaf*nrhs + c)*(p-2)^2 + r.  d_fbody as for slab_engine_solve. */
+int slab_engine_residual(slab_engine* e, int nrhs, const double* d_ufaces, const double* d_uint,
+                         const double* d_fbody, double* d_rint, double* d_rfaces);
+
+/* Bytes of device memory held by the engine's factorization. */
+size_t slab_engine_factor_bytes(const slab_engine* e);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SLABLU_GB300_H */

@@ -1,0 +1,17 @@
+"""slablu_gb300: GB300-native SlabLU factor-and-solve path (HPS, unit square).
+
+Public API mirrors the reference (annayesy/slabLU):
+    Domain_Solver(box_geom, pdo_op, kh, a, p=..., buf_constant=...)
+        .build(sparse_assembly='reduced_gpu', solver_type='slabLU')
+        .solve(uu_dir_func, ff_body_func=None, known_sol=False)
+plus SlabEngine / leaf_dtn for direct use of the C ABI (include/slablu_gb300.h).
+"""
+import torch
+
+torch.set_default_dtype(torch.double)  # the reference's modules set this on import
+
+from . import pdo, built_in_funcs, hps  # noqa: E402,F401
+from .engine import SlabEngine, leaf_dtn  # noqa: E402,F401
+from .slablu_solver import Domain_Solver  # noqa: E402,F401
+
+__all__ = ['Domain_Solver', 'SlabEngine', 'leaf_dtn', 'pdo', 'built_in_funcs', 'hps']

@@ -1,0 +1,188 @@
+// Host launchers for the dense building blocks (float and double).
+#include <cstdarg>
+#include <mutex>
+#include <string>
+
+#include "dense.cuh"
+
+namespace slab {
+
+namespace {
+thread_local std::string g_last_error;
+}
+
+int set_error(int status, const char* fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return status;
+}
+
+const char* last_error() { return g_last_error.c_str(); }
+
+size_t smem_limit_bytes() {
+  static size_t v = 0;
+  if (v == 0) {
+    int dev = 0, optin = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    v = optin > 0 ? (size_t)optin : 48 * 1024;
+  }
+  return v;
+}
+
+__global__ void perm_from_ipiv_kernel(const int* ipiv, int n, int* perm) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  for (int i = 0; i < n; ++i) perm[i] = i;
+  for (int j = 0; j < n; ++j) {
+    const int pj = ipiv[j];
+    if (pj != j && pj >= 0 && pj < n) {
+      const int t = perm[j];
+      perm[j] = perm[pj];
+      perm[pj] = t;
+    }
+  }
+}
+
+int build_perm(cudaStream_t s, const int* ipiv, int n, int* perm) {
+  perm_from_ipiv_kernel<<<1, 1, 0, s>>>(ipiv, n, perm);
+  SLAB_CHECK_LAUNCH();
+  return SLAB_OK;
+}
+
+template <typename T>
+int gemm(cudaStream_t s, int m, int n, int k, T alpha, const T* A, const long long* offA, long long strideA,
+         int lda, const T* B, const long long* offB, long long strideB, int ldb, T beta, T* C,
+         const long long* offC, long long strideC, int ldc, int batch) {
+  if (m <= 0 || n <= 0 || batch <= 0) return SLAB_OK;
+  if (batch > 65535) {
+    // grid.z limit: split the batch (offset arrays or strides advance per chunk)
+    for (int b0 = 0; b0 < batch; b0 += 65535) {
+      const int nb = batch - b0 < 65535 ? batch - b0 : 65535;
+      SLAB_TRY(gemm<T>(s, m, n, k, alpha, offA ? A : A + strideA * b0, offA ? offA + b0 : nullptr, strideA, lda,
+                       offB ? B : B + strideB * b0, offB ? offB + b0 : nullptr, strideB, ldb, beta,
+                       offC ? C : C + strideC * b0, offC ? offC + b0 : nullptr, strideC, ldc, nb));
+    }
+    return SLAB_OK;
+  }
+  // k == 0 leaves the k loop empty: C = beta*C
+  dim3 grid(ceil_div(m, 64), ceil_div(n, 64), batch);
+  gemm_kernel<T><<<grid, 256, 0, s>>>(m, n, k < 0 ? 0 : k, alpha, A, offA, strideA, lda, B, offB, strideB, ldb,
+                                      beta, C, offC, strideC, ldc);
+  SLAB_CHECK_LAUNCH();
+  return SLAB_OK;
+}
+
+template <typename T>
+int getrf_batched(cudaStream_t s, int n, int nc, T* A, const long long* offA, long long strideA, int lda,
+                  int* piv, const long long* offP, long long strideP, int* info, int batch) {
+  if (n <= 0 || batch <= 0) return SLAB_OK;
+  const size_t bytes = (size_t)getrf_smem_elems(n) * sizeof(T);
+  if (bytes > smem_limit_bytes())
+    return set_error(SLAB_ERR_ARG, "getrf_batched: order %d needs %zu bytes of shared memory", n, bytes);
+  SLAB_CUDA_TRY(cudaFuncSetAttribute(getrf_batched_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)bytes));
+  getrf_batched_kernel<T><<<batch, kNT, bytes, s>>>(n, nc, A, offA, strideA, lda, piv, offP, strideP, info);
+  SLAB_CHECK_LAUNCH();
+  return SLAB_OK;
+}
+
+template <typename T>
+int getrs_batched(cudaStream_t s, int n, int nrhs, const T* LU, const long long* offLU, long long strideLU,
+                  int lda, const int* piv, const long long* offP, long long strideP, T* B,
+                  const long long* offB, long long strideB, int ldb, int batch, bool lower, bool upper) {
+  if (n <= 0 || nrhs <= 0 || batch <= 0) return SLAB_OK;
+  const size_t limit = smem_limit_bytes();
+  const int tile = getrs_tile_cols(n, sizeof(T), limit);
+  if (tile <= 0) return set_error(SLAB_ERR_ARG, "getrs_batched: order %d too large for shared memory", n);
+  const size_t bytes = (size_t)getrs_smem_elems(n, tile) * sizeof(T);
+  SLAB_CUDA_TRY(cudaFuncSetAttribute(getrs_batched_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)bytes));
+  const int ntiles = ceil_div(nrhs, tile);
+  if (ntiles > 65535) return set_error(SLAB_ERR_ARG, "getrs_batched: %d right-hand sides is too many", nrhs);
+  dim3 grid(batch, ntiles);
+  getrs_batched_kernel<T><<<grid, kNT, bytes, s>>>(n, nrhs, tile, LU, offLU, strideLU, lda, piv, offP, strideP, B,
+                                                  offB, strideB, ldb, lower ? 1 : 0, upper ? 1 : 0);
+  SLAB_CHECK_LAUNCH();
+  return SLAB_OK;
+}
+
+template <typename T>
+int biglu(cudaStream_t s, T* A, int lda, int n, int* ipiv, int* info) {
+  for (int k0 = 0; k0 < n; k0 += kNB) {
+    const int nb = n - k0 < kNB ? n - k0 : kNB;
+    biglu_panel_kernel<T><<<1, 1024, 0, s>>>(A, lda, n, k0, nb, ipiv, info);
+    SLAB_CHECK_LAUNCH();
+    if (n - nb > 0) {
+      biglu_swap_kernel<T><<<ceil_div(n - nb, 256), 256, 0, s>>>(A, lda, n, k0, nb, ipiv);
+      SLAB_CHECK_LAUNCH();
+    }
+    const int rest = n - k0 - nb;
+    if (rest > 0) {
+      trsm_block_kernel<T><<<ceil_div(rest, 64), 256, 0, s>>>(A, lda, k0, nb, A + (size_t)(k0 + nb) * lda, lda,
+                                                             rest, 0);
+      SLAB_CHECK_LAUNCH();
+      SLAB_TRY(gemm<T>(s, rest, rest, nb, T(-1), A + (size_t)k0 * lda + k0 + nb, nullptr, 0, lda,
+                       A + (size_t)(k0 + nb) * lda + k0, nullptr, 0, lda, T(1),
+                       A + (size_t)(k0 + nb) * lda + k0 + nb, nullptr, 0, lda, 1));
+    }
+  }
+  return SLAB_OK;
+}
+
+template <typename T>
+int bigtrs(cudaStream_t s, const T* LU, int lda, int n, const int* perm, const T* B, int ldb, T* X, int ldx,
+           int nrhs, bool lower, bool upper) {
+  if (n <= 0 || nrhs <= 0) return SLAB_OK;
+  if (lower) {
+    const long long tot = (long long)n * nrhs;
+    permute_rows_kernel<T><<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(B, ldb, X, ldx, n, nrhs, perm);
+    SLAB_CHECK_LAUNCH();
+  } else if (B != X) {
+    SLAB_CUDA_TRY(cudaMemcpy2DAsync(X, (size_t)ldx * sizeof(T), B, (size_t)ldb * sizeof(T), (size_t)n * sizeof(T),
+                                    nrhs, cudaMemcpyDeviceToDevice, s));
+  }
+  const int ctiles = ceil_div(nrhs, 64);
+  if (lower) {
+    for (int k0 = 0; k0 < n; k0 += kNB) {
+      const int nb = n - k0 < kNB ? n - k0 : kNB;
+      trsm_block_kernel<T><<<ctiles, 256, 0, s>>>(LU, lda, k0, nb, X, ldx, nrhs, 0);
+      SLAB_CHECK_LAUNCH();
+      const int rest = n - k0 - nb;
+      if (rest > 0)
+        SLAB_TRY(gemm<T>(s, rest, nrhs, nb, T(-1), LU + (size_t)k0 * lda + k0 + nb, nullptr, 0, lda, X + k0,
+                         nullptr, 0, ldx, T(1), X + k0 + nb, nullptr, 0, ldx, 1));
+    }
+  }
+  if (upper) {
+    const int klast = ((n - 1) / kNB) * kNB;
+    for (int k0 = klast; k0 >= 0; k0 -= kNB) {
+      const int nb = n - k0 < kNB ? n - k0 : kNB;
+      trsm_block_kernel<T><<<ctiles, 256, 0, s>>>(LU, lda, k0, nb, X, ldx, nrhs, 1);
+      SLAB_CHECK_LAUNCH();
+      if (k0 > 0)
+        SLAB_TRY(gemm<T>(s, k0, nrhs, nb, T(-1), LU + (size_t)k0 * lda, nullptr, 0, lda, X + k0, nullptr, 0, ldx,
+                         T(1), X, nullptr, 0, ldx, 1));
+    }
+  }
+  return SLAB_OK;
+}
+
+#define SLAB_INSTANTIATE(T)                                                                                   \
+  template int gemm<T>(cudaStream_t, int, int, int, T, const T*, const long long*, long long, int, const T*,  \
+                       const long long*, long long, int, T, T*, const long long*, long long, int, int);       \
+  template int getrf_batched<T>(cudaStream_t, int, int, T*, const long long*, long long, int, int*,           \
+                                const long long*, long long, int*, int);                                      \
+  template int getrs_batched<T>(cudaStream_t, int, int, const T*, const long long*, long long, int,           \
+                                const int*, const long long*, long long, T*, const long long*, long long,     \
+                                int, int, bool, bool);                                                        \
+  template int biglu<T>(cudaStream_t, T*, int, int, int*, int*);                                              \
+  template int bigtrs<T>(cudaStream_t, const T*, int, int, const int*, const T*, int, T*, int, int, bool, bool);
+
+SLAB_INSTANTIATE(float)
+SLAB_INSTANTIATE(double)
+
+}  // namespace slab

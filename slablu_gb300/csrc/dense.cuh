@@ -1,0 +1,640 @@
+// Dense linear-algebra building blocks for the SlabLU path (FP32 / FP64).
+//
+// All matrices are column-major.  Pivots follow LAPACK getrf semantics with
+// 0-based indices: ipiv[j] is the row interchanged with row j at step j.
+//
+// CTA-level routines (one thread block owns one matrix) serve the batched
+// leaf and merge factorizations; the "big" kernels (one matrix spread over
+// the whole GPU, host loop over panels) serve the FP64 interface blocks.
+#pragma once
+
+#include <climits>
+
+#include "common.cuh"
+
+namespace slab {
+
+constexpr int kNT = 256;    // threads per CTA of the CTA-level routines
+constexpr int kNB = 32;     // panel width
+constexpr int kCT = 128;    // column tile of trailing updates
+constexpr int kCTLD = kCT + 4;  // shared-memory leading dimension of a transposed tile
+constexpr int kPad = 64;    // slack elements after a staged panel (micro-kernel over-read)
+
+// ---------------------------------------------------------------------------
+// Block-wide argmax of |x| with LAPACK tie-break (smallest index wins).
+// Every thread passes its local best (value, index); all threads get the index.
+// sv/si need 33 slots.  Contains two __syncthreads.
+template <typename T>
+__device__ __forceinline__ void argmax_merge(T& v, int& i, T v2, int i2) {
+  if (v2 > v || (v2 == v && i2 < i)) {
+    v = v2;
+    i = i2;
+  }
+}
+
+template <typename T>
+__device__ int cta_argmax(T v, int i, T* sv, int* si) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    T v2 = __shfl_down_sync(0xffffffffu, v, o);
+    int i2 = __shfl_down_sync(0xffffffffu, i, o);
+    argmax_merge(v, i, v2, i2);
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) {
+    sv[warp] = v;
+    si[warp] = i;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    const int nw = blockDim.x >> 5;
+    v = lane < nw ? sv[lane] : T(-1);
+    i = lane < nw ? si[lane] : INT_MAX;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      T v2 = __shfl_down_sync(0xffffffffu, v, o);
+      int i2 = __shfl_down_sync(0xffffffffu, i, o);
+      argmax_merge(v, i, v2, i2);
+    }
+    if (lane == 0) si[32] = i;
+  }
+  __syncthreads();
+  return si[32];
+}
+
+// ---------------------------------------------------------------------------
+// Unblocked LU with partial pivoting of an m x nb panel held in shared memory
+// (column-major, leading dimension ldp).  piv[j] receives the panel-local row
+// swapped with row j.  The first exactly-zero (or NaN) pivot is recorded in
+// *info_s as col_offset + j + 1 (LAPACK info); elimination continues.
+template <typename T>
+__device__ void cta_panel_lu(T* P, int ldp, int m, int nb, int* piv, T* sv, int* si, int* info_s,
+                             int col_offset) {
+  const int tid = threadIdx.x;
+  for (int j = 0; j < nb && j < m; ++j) {
+    T best = T(-1);
+    int bi = INT_MAX;
+    for (int r = j + tid; r < m; r += blockDim.x) {
+      T a = tabs(P[r + j * ldp]);
+      if (a > best) {
+        best = a;
+        bi = r;
+      }
+    }
+    int pr = cta_argmax(best, bi, sv, si);
+    if (pr == INT_MAX) pr = j;  // whole column NaN: keep the diagonal, flagged below
+    if (tid == 0) piv[j] = pr;
+    if (pr != j) {
+      for (int c = tid; c < nb; c += blockDim.x) {
+        T t = P[j + c * ldp];
+        P[j + c * ldp] = P[pr + c * ldp];
+        P[pr + c * ldp] = t;
+      }
+    }
+    __syncthreads();
+    const T d = P[j + j * ldp];
+    if (d == T(0) || d != d) {
+      if (tid == 0 && *info_s == 0) *info_s = col_offset + j + 1;
+    } else {
+      const T rd = T(1) / d;
+      for (int r = j + 1 + tid; r < m; r += blockDim.x) {
+        const T l = P[r + j * ldp] * rd;
+        P[r + j * ldp] = l;
+        for (int c = j + 1; c < nb; ++c) P[r + c * ldp] -= l * P[j + c * ldp];
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// C[r, c] -= sum_k A(r, k) * B(c, k) for r < mrows, c < ncols, k < kd.
+// A in shared memory (element (r,k) at As[r + k*lda], lda % 4 == 0, As 16B aligned,
+// readable up to 63 rows past mrows); B transposed in shared memory
+// (element (c,k) at Bs[c + k*ldb], ldb % 4 == 0, readable up to 63 columns past
+// ncols).  C is a generic pointer (global or shared), leading dimension ldc.
+// Requires blockDim.x == 256 (16 x 16 threads, 4 x 4 outputs each).
+template <typename T>
+__device__ void cta_gemm_sub(T* C, int ldc, int mrows, int ncols, const T* As, int lda, const T* Bs,
+                             int ldb, int kd) {
+  const int tr = threadIdx.x & 15, tc = threadIdx.x >> 4;
+  for (int cb = 0; cb < ncols; cb += 64) {
+    for (int rb = 0; rb < mrows; rb += 64) {
+      T acc[4][4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = T(0);
+      const T* ap = As + rb + 4 * tr;
+      const T* bp = Bs + cb + 4 * tc;
+#pragma unroll 4
+      for (int kk = 0; kk < kd; ++kk) {
+        const vec4<T> a = ld4(ap + kk * lda);
+        const vec4<T> b = ld4(bp + kk * ldb);
+        acc[0][0] += a.x * b.x; acc[0][1] += a.x * b.y; acc[0][2] += a.x * b.z; acc[0][3] += a.x * b.w;
+        acc[1][0] += a.y * b.x; acc[1][1] += a.y * b.y; acc[1][2] += a.y * b.z; acc[1][3] += a.y * b.w;
+        acc[2][0] += a.z * b.x; acc[2][1] += a.z * b.y; acc[2][2] += a.z * b.z; acc[2][3] += a.z * b.w;
+        acc[3][0] += a.w * b.x; acc[3][1] += a.w * b.y; acc[3][2] += a.w * b.z; acc[3][3] += a.w * b.w;
+      }
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int c = cb + 4 * tc + j;
+        if (c >= ncols) continue;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const int r = rb + 4 * tr + i;
+          if (r < mrows) C[r + (size_t)c * ldc] -= acc[i][j];
+        }
+      }
+    }
+  }
+}
+
+// Shared-memory footprint (elements of T) of cta_getrf_aug / cta_backsub for order n.
+__host__ __device__ inline int getrf_smem_elems(int n) {
+  return round_up(n, 4) * kNB + kPad + kCTLD * kNB + kPad;
+}
+
+// ---------------------------------------------------------------------------
+// Blocked right-looking LU with partial pivoting of the leading n x n block of
+// the column-major n x nc matrix A (global memory, lda), applying the same row
+// operations to all nc columns.  On return A[:, :n] holds L (unit, strictly
+// lower) and U; A[:, n:] holds L^{-1} P A[:, n:]; ipiv[0..n) the pivots.
+// *info_out = 0 or the LAPACK info of the first zero pivot.
+template <typename T>
+__device__ void cta_getrf_aug(T* A, int lda, int n, int nc, int* ipiv, T* smem, int* info_out) {
+  __shared__ int piv_s[kNB];
+  __shared__ T sv[33];
+  __shared__ int si[33];
+  __shared__ int info_s;
+  const int tid = threadIdx.x;
+  if (tid == 0) info_s = 0;
+  T* Psm = smem;
+  T* Bt = smem + round_up(n, 4) * kNB + kPad;
+  for (int k0 = 0; k0 < n; k0 += kNB) {
+    const int nb = min(kNB, n - k0);
+    const int m = n - k0;
+    const int ldq = round_up(m, 4);
+    __syncthreads();
+    for (int idx = tid; idx < m * nb; idx += blockDim.x) {
+      const int r = idx % m, c = idx / m;
+      Psm[r + c * ldq] = A[(size_t)(k0 + c) * lda + k0 + r];
+    }
+    __syncthreads();
+    cta_panel_lu(Psm, ldq, m, nb, piv_s, sv, si, &info_s, k0);
+    for (int idx = tid; idx < m * nb; idx += blockDim.x) {
+      const int r = idx % m, c = idx / m;
+      A[(size_t)(k0 + c) * lda + k0 + r] = Psm[r + c * ldq];
+    }
+    if (tid < nb) ipiv[k0 + tid] = k0 + piv_s[tid];
+    // row interchanges on every column outside the panel
+    for (int c = tid; c < nc - nb; c += blockDim.x) {
+      const int col = c < k0 ? c : c + nb;
+      T* cp = A + (size_t)col * lda;
+      for (int j = 0; j < nb; ++j) {
+        const int pr = k0 + piv_s[j];
+        if (pr != k0 + j) {
+          T t = cp[k0 + j];
+          cp[k0 + j] = cp[pr];
+          cp[pr] = t;
+        }
+      }
+    }
+    __syncthreads();
+    const int m2 = m - nb;
+    for (int c0 = k0 + nb; c0 < nc; c0 += kCT) {
+      const int ct = min(kCT, nc - c0);
+      for (int idx = tid; idx < nb * ct; idx += blockDim.x) {
+        const int kk = idx % nb, c = idx / nb;
+        Bt[c + kk * kCTLD] = A[(size_t)(c0 + c) * lda + k0 + kk];
+      }
+      __syncthreads();
+      // U12 = L11^{-1} A12 (unit lower), one thread per column
+      for (int c = tid; c < ct; c += blockDim.x) {
+        for (int i = 1; i < nb; ++i) {
+          T s = Bt[c + i * kCTLD];
+          for (int k = 0; k < i; ++k) s -= Psm[i + k * ldq] * Bt[c + k * kCTLD];
+          Bt[c + i * kCTLD] = s;
+        }
+      }
+      __syncthreads();
+      for (int idx = tid; idx < nb * ct; idx += blockDim.x) {
+        const int kk = idx % nb, c = idx / nb;
+        A[(size_t)(c0 + c) * lda + k0 + kk] = Bt[c + kk * kCTLD];
+      }
+      if (m2 > 0) cta_gemm_sub(A + (size_t)c0 * lda + k0 + nb, lda, m2, ct, Psm + nb, ldq, Bt, kCTLD, nb);
+      __syncthreads();
+    }
+  }
+  __syncthreads();
+  if (tid == 0 && info_out) *info_out = info_s;
+}
+
+// ---------------------------------------------------------------------------
+// Back substitution U X = Y in place for the nr (<= kCT) columns Y = A[:, c0 : c0+nr]
+// where U is the upper triangle of A[:, :n] (global, lda).  smem as cta_getrf_aug.
+template <typename T>
+__device__ void cta_backsub(T* A, int lda, int n, int c0, int nr, T* smem) {
+  const int tid = threadIdx.x;
+  T* Psm = smem;
+  T* Bt = smem + round_up(n, 4) * kNB + kPad;
+  T* Y = A + (size_t)c0 * lda;
+  const int klast = ((n - 1) / kNB) * kNB;
+  for (int k0 = klast; k0 >= 0; k0 -= kNB) {
+    const int nb = min(kNB, n - k0);
+    const int rows = k0 + nb;  // stage U[0 : k0+nb, k0 : k0+nb]
+    const int ldq = round_up(rows, 4);
+    __syncthreads();
+    for (int idx = tid; idx < rows * nb; idx += blockDim.x) {
+      const int r = idx % rows, c = idx / rows;
+      Psm[r + c * ldq] = A[(size_t)(k0 + c) * lda + r];
+    }
+    for (int idx = tid; idx < nb * nr; idx += blockDim.x) {
+      const int kk = idx % nb, c = idx / nb;
+      Bt[c + kk * kCTLD] = Y[(size_t)c * lda + k0 + kk];
+    }
+    __syncthreads();
+    for (int c = tid; c < nr; c += blockDim.x) {
+      for (int i = nb - 1; i >= 0; --i) {
+        T s = Bt[c + i * kCTLD];
+        for (int k = i + 1; k < nb; ++k) s -= Psm[k0 + i + k * ldq] * Bt[c + k * kCTLD];
+        Bt[c + i * kCTLD] = s / Psm[k0 + i + i * ldq];
+      }
+    }
+    __syncthreads();
+    for (int idx = tid; idx < nb * nr; idx += blockDim.x) {
+      const int kk = idx % nb, c = idx / nb;
+      Y[(size_t)c * lda + k0 + kk] = Bt[c + kk * kCTLD];
+    }
+    if (k0 > 0) cta_gemm_sub(Y, lda, k0, nr, Psm, ldq, Bt, kCTLD, nb);
+  }
+  __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// X = U^{-1} L^{-1} P B for an n x ncols right-hand-side tile held in shared
+// memory (Bsm, column-major, odd leading dimension ldbs).  LU/ipiv in global.
+// Psm/Bt as for cta_getrf_aug.  lower/upper select the stages applied.
+template <typename T>
+__device__ void cta_getrs_smem(const T* LU, int lda, int n, const int* ipiv, T* Bsm, int ldbs, int ncols,
+                               T* Psm, T* Bt, bool lower, bool upper) {
+  const int tid = threadIdx.x;
+  if (lower) {
+    for (int c = tid; c < ncols; c += blockDim.x) {
+      T* cp = Bsm + (size_t)c * ldbs;
+      for (int j = 0; j < n; ++j) {
+        const int pr = ipiv[j];
+        if (pr != j) {
+          T t = cp[j];
+          cp[j] = cp[pr];
+          cp[pr] = t;
+        }
+      }
+    }
+    for (int k0 = 0; k0 < n; k0 += kNB) {
+      const int nb = min(kNB, n - k0);
+      const int m = n - k0;
+      const int ldq = round_up(m, 4);
+      __syncthreads();
+      for (int idx = tid; idx < m * nb; idx += blockDim.x) {
+        const int r = idx % m, c = idx / m;
+        Psm[r + c * ldq] = LU[(size_t)(k0 + c) * lda + k0 + r];
+      }
+      __syncthreads();
+      for (int c = tid; c < ncols; c += blockDim.x) {
+        T* cp = Bsm + (size_t)c * ldbs + k0;
+        for (int i = 1; i < nb; ++i) {
+          T s = cp[i];
+          for (int k = 0; k < i; ++k) s -= Psm[i + k * ldq] * cp[k];
+          cp[i] = s;
+        }
+      }
+      __syncthreads();
+      if (m > nb) {
+        for (int idx = tid; idx < nb * ncols; idx += blockDim.x) {
+          const int kk = idx % nb, c = idx / nb;
+          Bt[c + kk * kCTLD] = Bsm[(size_t)c * ldbs + k0 + kk];
+        }
+        __syncthreads();
+        cta_gemm_sub(Bsm + k0 + nb, ldbs, m - nb, ncols, Psm + nb, ldq, Bt, kCTLD, nb);
+      }
+    }
+  }
+  if (upper) {
+    const int klast = ((n - 1) / kNB) * kNB;
+    for (int k0 = klast; k0 >= 0; k0 -= kNB) {
+      const int nb = min(kNB, n - k0);
+      const int rows = k0 + nb;
+      const int ldq = round_up(rows, 4);
+      __syncthreads();
+      for (int idx = tid; idx < rows * nb; idx += blockDim.x) {
+        const int r = idx % rows, c = idx / rows;
+        Psm[r + c * ldq] = LU[(size_t)(k0 + c) * lda + r];
+      }
+      __syncthreads();
+      for (int c = tid; c < ncols; c += blockDim.x) {
+        T* cp = Bsm + (size_t)c * ldbs + k0;
+        for (int i = nb - 1; i >= 0; --i) {
+          T s = cp[i];
+          for (int k = i + 1; k < nb; ++k) s -= Psm[k0 + i + k * ldq] * cp[k];
+          cp[i] = s / Psm[k0 + i + i * ldq];
+        }
+      }
+      __syncthreads();
+      if (k0 > 0) {
+        for (int idx = tid; idx < nb * ncols; idx += blockDim.x) {
+          const int kk = idx % nb, c = idx / nb;
+          Bt[c + kk * kCTLD] = Bsm[(size_t)c * ldbs + k0 + kk];
+        }
+        __syncthreads();
+        cta_gemm_sub(Bsm, ldbs, k0, ncols, Psm, ldq, Bt, kCTLD, nb);
+      }
+    }
+  }
+  __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// Batched pointer arithmetic: element offsets per batch entry, or a stride.
+__device__ __forceinline__ long long batch_off(const long long* off, long long stride, int b) {
+  return off ? off[b] : stride * (long long)b;
+}
+
+// Batched LU of n x n matrices (nc = n) or augmented n x nc matrices.
+template <typename T>
+__global__ void __launch_bounds__(kNT) getrf_batched_kernel(int n, int nc, T* A, const long long* offA,
+                                                           long long strideA, int lda, int* piv,
+                                                           const long long* offP, long long strideP,
+                                                           int* info) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int b = blockIdx.x;
+  cta_getrf_aug<T>(A + batch_off(offA, strideA, b), lda, n, nc, piv + batch_off(offP, strideP, b),
+                   reinterpret_cast<T*>(smem_raw), info ? info + b : nullptr);
+}
+
+// Shared-memory elements for cta_getrs_smem with an n x ncols tile.
+__host__ __device__ inline int getrs_smem_elems(int n, int ncols) {
+  return round_up(n, 4) * kNB + kPad + kCTLD * kNB + kPad + (n | 1) * ncols + 4;
+}
+
+// Largest column tile (multiple of 4, <= kCT) whose getrs footprint fits `bytes`.
+inline int getrs_tile_cols(int n, size_t elem, size_t bytes) {
+  for (int c = kCT; c >= 4; c -= 4)
+    if ((size_t)getrs_smem_elems(n, c) * elem <= bytes) return c;
+  return (size_t)getrs_smem_elems(n, 1) * elem <= bytes ? 1 : 0;
+}
+
+// Batched X = U^{-1} L^{-1} P B; grid (batch, column tiles).  B is n x nrhs (ldb).
+template <typename T>
+__global__ void __launch_bounds__(kNT) getrs_batched_kernel(int n, int nrhs, int tile, const T* LU,
+                                                           const long long* offLU, long long strideLU,
+                                                           int lda, const int* piv, const long long* offP,
+                                                           long long strideP, T* B, const long long* offB,
+                                                           long long strideB, int ldb, int lower,
+                                                           int upper) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* smem = reinterpret_cast<T*>(smem_raw);
+  T* Psm = smem;
+  T* Bt = Psm + round_up(n, 4) * kNB + kPad;
+  T* Bsm = Bt + kCTLD * kNB + kPad;
+  const int ldbs = n | 1;
+  const int b = blockIdx.x;
+  const int c0 = blockIdx.y * tile;
+  const int ncols = min(tile, nrhs - c0);
+  if (ncols <= 0) return;
+  T* Bg = B + batch_off(offB, strideB, b) + (size_t)c0 * ldb;
+  for (int idx = threadIdx.x; idx < n * ncols; idx += blockDim.x) {
+    const int r = idx % n, c = idx / n;
+    Bsm[r + (size_t)c * ldbs] = Bg[r + (size_t)c * ldb];
+  }
+  __syncthreads();
+  cta_getrs_smem<T>(LU + batch_off(offLU, strideLU, b), lda, n, piv + batch_off(offP, strideP, b), Bsm, ldbs,
+                    ncols, Psm, Bt, lower != 0, upper != 0);
+  for (int idx = threadIdx.x; idx < n * ncols; idx += blockDim.x) {
+    const int r = idx % n, c = idx / n;
+    Bg[r + (size_t)c * ldb] = Bsm[r + (size_t)c * ldbs];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Batched GEMM  C = beta*C + alpha * A B  (m x k times k x n), column-major.
+// 64 x 64 output tile per CTA, k staged 16 at a time; grid (m/64, n/64, batch).
+constexpr int kGK = 16;
+constexpr int kGLD = 68;
+template <typename T>
+__global__ void __launch_bounds__(256) gemm_kernel(int m, int n, int k, T alpha, const T* __restrict__ A,
+                                                  const long long* offA, long long strideA, int lda,
+                                                  const T* __restrict__ B, const long long* offB,
+                                                  long long strideB, int ldb, T beta, T* C,
+                                                  const long long* offC, long long strideC, int ldc) {
+  __shared__ __align__(16) T As[kGK * kGLD];
+  __shared__ __align__(16) T Bs[kGK * kGLD];
+  const int bz = blockIdx.z;
+  A += batch_off(offA, strideA, bz);
+  B += batch_off(offB, strideB, bz);
+  C += batch_off(offC, strideC, bz);
+  const int r0 = blockIdx.x * 64, c0 = blockIdx.y * 64;
+  const int tid = threadIdx.x;
+  const int tr = tid & 15, tc = tid >> 4;
+  T acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = T(0);
+  for (int k0 = 0; k0 < k; k0 += kGK) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int r = tid & 63, kk = (tid >> 6) + 4 * q;
+      const int gr = r0 + r, gk = k0 + kk;
+      As[r + kk * kGLD] = (gr < m && gk < k) ? A[gr + (size_t)gk * lda] : T(0);
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int kk = tid & 15, c = (tid >> 4) + 16 * q;
+      const int gc = c0 + c, gk = k0 + kk;
+      Bs[c + kk * kGLD] = (gc < n && gk < k) ? B[gk + (size_t)gc * ldb] : T(0);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < kGK; ++kk) {
+      const vec4<T> a = ld4(As + 4 * tr + kk * kGLD);
+      const vec4<T> b = ld4(Bs + 4 * tc + kk * kGLD);
+      acc[0][0] += a.x * b.x; acc[0][1] += a.x * b.y; acc[0][2] += a.x * b.z; acc[0][3] += a.x * b.w;
+      acc[1][0] += a.y * b.x; acc[1][1] += a.y * b.y; acc[1][2] += a.y * b.z; acc[1][3] += a.y * b.w;
+      acc[2][0] += a.z * b.x; acc[2][1] += a.z * b.y; acc[2][2] += a.z * b.z; acc[2][3] += a.z * b.w;
+      acc[3][0] += a.w * b.x; acc[3][1] += a.w * b.y; acc[3][2] += a.w * b.z; acc[3][3] += a.w * b.w;
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const int c = c0 + 4 * tc + j;
+    if (c >= n) continue;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int r = r0 + 4 * tr + i;
+      if (r >= m) continue;
+      T* cp = C + r + (size_t)c * ldc;
+      *cp = (beta == T(0) ? T(0) : beta * *cp) + alpha * acc[i][j];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Large single-matrix LU (FP64 interface blocks): host loop over panels.
+
+// Panel factorization in global memory: rows [k0, n), columns [k0, k0+nb).
+template <typename T>
+__global__ void __launch_bounds__(1024) biglu_panel_kernel(T* A, int lda, int n, int k0, int nb, int* ipiv,
+                                                          int* info) {
+  __shared__ T sv[33];
+  __shared__ int si[33];
+  const int tid = threadIdx.x;
+  for (int j = 0; j < nb; ++j) {
+    const int col = k0 + j;
+    T* cj = A + (size_t)col * lda;
+    T best = T(-1);
+    int bi = INT_MAX;
+    for (int r = col + tid; r < n; r += blockDim.x) {
+      const T a = tabs(cj[r]);
+      if (a > best) {
+        best = a;
+        bi = r;
+      }
+    }
+    int pr = cta_argmax(best, bi, sv, si);
+    if (pr == INT_MAX) pr = col;
+    if (tid == 0) ipiv[col] = pr;
+    if (pr != col) {
+      for (int c = tid; c < nb; c += blockDim.x) {
+        T* cc = A + (size_t)(k0 + c) * lda;
+        T t = cc[col];
+        cc[col] = cc[pr];
+        cc[pr] = t;
+      }
+    }
+    __syncthreads();
+    const T d = cj[col];
+    if (d == T(0) || d != d) {
+      if (tid == 0 && info && *info == 0) *info = col + 1;
+    } else {
+      const T rd = T(1) / d;
+      for (int r = col + 1 + tid; r < n; r += blockDim.x) {
+        const T l = cj[r] * rd;
+        cj[r] = l;
+        for (int c = j + 1; c < nb; ++c) {
+          T* cc = A + (size_t)(k0 + c) * lda;
+          cc[r] -= l * cc[col];
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// Apply the panel's row interchanges ipiv[k0 .. k0+nb) to every column outside
+// the panel (one thread per column).
+template <typename T>
+__global__ void biglu_swap_kernel(T* A, int lda, int ncols_total, int k0, int nb, const int* ipiv) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncols_total - nb) return;
+  const int col = c < k0 ? c : c + nb;
+  T* cp = A + (size_t)col * lda;
+  for (int j = 0; j < nb; ++j) {
+    const int pr = ipiv[k0 + j];
+    if (pr != k0 + j) {
+      T t = cp[k0 + j];
+      cp[k0 + j] = cp[pr];
+      cp[pr] = t;
+    }
+  }
+}
+
+// Triangular solve with the nb x nb diagonal block D = A[k0 : k0+nb, k0 : k0+nb]
+// applied to rows [k0, k0+nb) of X (columns [0, ncols)):
+//   upper == 0: X_blk = L_D^{-1} X_blk (unit lower);  upper == 1: X_blk = U_D^{-1} X_blk.
+// grid: column tiles of 64.
+template <typename T>
+__global__ void __launch_bounds__(256) trsm_block_kernel(const T* A, int lda, int k0, int nb, T* X, int ldx,
+                                                        int ncols, int upper) {
+  __shared__ T Dsm[kNB * (kNB + 1)];
+  __shared__ T Xs[kNB * 65];
+  const int c0 = blockIdx.x * 64;
+  const int nc = min(64, ncols - c0);
+  const int tid = threadIdx.x;
+  for (int idx = tid; idx < nb * nb; idx += blockDim.x) {
+    const int r = idx % nb, c = idx / nb;
+    Dsm[r + c * (kNB + 1)] = A[(size_t)(k0 + c) * lda + k0 + r];
+  }
+  for (int idx = tid; idx < nb * nc; idx += blockDim.x) {
+    const int r = idx % nb, c = idx / nb;
+    Xs[c + r * 65] = X[(size_t)(c0 + c) * ldx + k0 + r];
+  }
+  __syncthreads();
+  if (tid < nc) {
+    const int c = tid;
+    if (!upper) {
+      for (int i = 1; i < nb; ++i) {
+        T s = Xs[c + i * 65];
+        for (int k = 0; k < i; ++k) s -= Dsm[i + k * (kNB + 1)] * Xs[c + k * 65];
+        Xs[c + i * 65] = s;
+      }
+    } else {
+      for (int i = nb - 1; i >= 0; --i) {
+        T s = Xs[c + i * 65];
+        for (int k = i + 1; k < nb; ++k) s -= Dsm[i + k * (kNB + 1)] * Xs[c + k * 65];
+        Xs[c + i * 65] = s / Dsm[i + i * (kNB + 1)];
+      }
+    }
+  }
+  __syncthreads();
+  for (int idx = tid; idx < nb * nc; idx += blockDim.x) {
+    const int r = idx % nb, c = idx / nb;
+    X[(size_t)(c0 + c) * ldx + k0 + r] = Xs[c + r * 65];
+  }
+}
+
+// Final row permutation of a sequence of interchanges: perm[i] = source row of row i.
+__global__ void perm_from_ipiv_kernel(const int* ipiv, int n, int* perm);
+
+// out[i, c] = in[perm[i], c]
+template <typename T>
+__global__ void permute_rows_kernel(const T* in, int ldi, T* out, int ldo, int n, int ncols, const int* perm) {
+  const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (idx >= (long long)n * ncols) return;
+  const int r = (int)(idx % n), c = (int)(idx / n);
+  out[r + (size_t)c * ldo] = in[perm[r] + (size_t)c * ldi];
+}
+
+// ---------------------------------------------------------------------------
+// Host-side launchers (defined in dense.cu for float and double).
+template <typename T>
+int gemm(cudaStream_t s, int m, int n, int k, T alpha, const T* A, const long long* offA, long long strideA,
+         int lda, const T* B, const long long* offB, long long strideB, int ldb, T beta, T* C,
+         const long long* offC, long long strideC, int ldc, int batch);
+
+template <typename T>
+int getrf_batched(cudaStream_t s, int n, int nc, T* A, const long long* offA, long long strideA, int lda,
+                  int* piv, const long long* offP, long long strideP, int* info, int batch);
+
+template <typename T>
+int getrs_batched(cudaStream_t s, int n, int nrhs, const T* LU, const long long* offLU, long long strideLU,
+                  int lda, const int* piv, const long long* offP, long long strideP, T* B,
+                  const long long* offB, long long strideB, int ldb, int batch, bool lower = true,
+                  bool upper = true);
+
+// Large single-matrix LU in place (n x n, lda); ipiv/info device pointers.
+template <typename T>
+int biglu(cudaStream_t s, T* A, int lda, int n, int* ipiv, int* info);
+
+// X = U^{-1} L^{-1} P B for one large factored matrix; B (n x nrhs, ldb) is
+// permuted into X (ldx), then solved in place.  perm from perm_from_ipiv_kernel.
+template <typename T>
+int bigtrs(cudaStream_t s, const T* LU, int lda, int n, const int* perm, const T* B, int ldb, T* X, int ldx,
+           int nrhs, bool lower = true, bool upper = true);
+
+int build_perm(cudaStream_t s, const int* ipiv, int n, int* perm);
+
+size_t smem_limit_bytes();
+
+}  // namespace slab

@@ -1,0 +1,957 @@
+// SlabLU factor-and-solve engine for the unit-square HPS discretisation.
+//
+// Factorization
+//   1. leaf_factor_kernel: per leaf LU of A_cc, S = -A_cc^{-1} A_cx, DtN
+//      (Dirichlet faces decoupled as identity rows/columns).
+//   2. Slab elimination as a multifrontal merge tree inside every slab:
+//      leaves of a slab row merged left to right into strips (eliminating the
+//      vertical faces), then strips merged by a balanced binary tree over the
+//      rows (eliminating the horizontal faces).  A merge of children A, B
+//      eliminates their shared faces E:
+//          M = A[E,E] + B[E,E],  W = M^{-1} [A|B][E,O],  F_parent = base - col W
+//      The slab root is the exact dense interface operator T = [[LL LR];[RL RR]]
+//      of the slab (the reference samples it with HBS sketches,
+//      src_solver/slablu_solver.py:1139-1308).
+//   3. Interface block-tridiagonal system over the Npan-1 slab interfaces,
+//      factored by the sequential block LU of
+//      src_solver/block_tridiag_solver_structured.py:34-76:
+//          S_0 = D_0,  X_j = S_j^{-1} sup_j,  S_{j+1} = D_{j+1} - sub_{j+1} X_j
+//      in the interface precision (FP64 unless SLAB_PREC_FP32).
+// Solve (one application of the factorization to a residual)
+//   leaf forward (w = A_cc^{-1} r_c, face RHS -= Nx_c w), tree forward
+//   (y = M^{-1} g_E, g_O -= col y), interface sweep, tree backward
+//   (u_E = y - W u_O), leaf backward (u_c = w + S u_x).
+// Refinement: FP64 residual of the full collocation system, corrections from
+// the (possibly FP32) factorization, until ||du|| <= tol ||u||.
+#include <algorithm>
+#include <cmath>
+#include <map>
+#include <memory>
+#include <tuple>
+#include <vector>
+
+#include "leaf.cuh"
+
+namespace slab {
+
+const char* last_error();
+
+// ---------------------------------------------------------------------------
+// Device memory owner.
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  int alloc(size_t b) {
+    release();
+    if (b == 0) return SLAB_OK;
+    cudaError_t e = cudaMalloc(&p, b);
+    if (e != cudaSuccess) {
+      p = nullptr;
+      return set_error(SLAB_ERR_ALLOC, "cudaMalloc(%zu) failed: %s", b, cudaGetErrorString(e));
+    }
+    bytes = b;
+    return SLAB_OK;
+  }
+  int ensure(size_t b) { return b <= bytes ? SLAB_OK : alloc(b); }
+  template <typename U>
+  U* as() const {
+    return static_cast<U*>(p);
+  }
+};
+
+template <typename U>
+static int upload(DevBuf& d, const std::vector<U>& h, cudaStream_t s) {
+  SLAB_TRY(d.alloc(h.size() * sizeof(U)));
+  if (!h.empty()) SLAB_CUDA_TRY(cudaMemcpyAsync(d.p, h.data(), h.size() * sizeof(U), cudaMemcpyHostToDevice, s));
+  return SLAB_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Elementwise helper kernels.
+template <typename T>
+__global__ void gather_kernel(const T* __restrict__ vec, long long ldv, const int* __restrict__ glob, int len,
+                              int count, int nrhs, T* __restrict__ out) {
+  const long long tot = (long long)count * len * nrhs;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < tot; i += (long long)gridDim.x * blockDim.x) {
+    const int r = (int)(i % len);
+    const long long ec = i / len;
+    const int c = (int)(ec % nrhs);
+    const long long e = ec / nrhs;
+    out[i] = vec[glob[e * len + r] + (long long)c * ldv];
+  }
+}
+
+template <typename T>
+__global__ void scatter_add_kernel(T* vec, long long ldv, const int* __restrict__ glob, int len, int count, int nrhs,
+                                   const T* __restrict__ in, T sign, const unsigned char* __restrict__ skip) {
+  const long long tot = (long long)count * len * nrhs;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < tot; i += (long long)gridDim.x * blockDim.x) {
+    const int r = (int)(i % len);
+    const long long ec = i / len;
+    const int c = (int)(ec % nrhs);
+    const long long e = ec / nrhs;
+    const int g = glob[e * len + r];
+    if (skip && skip[g]) continue;
+    atomicAdd(&vec[g + (long long)c * ldv], sign * in[i]);
+  }
+}
+
+template <typename T>
+__global__ void scatter_set_kernel(T* vec, long long ldv, const int* __restrict__ glob, int len, int count, int nrhs,
+                                   const T* __restrict__ in) {
+  const long long tot = (long long)count * len * nrhs;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < tot; i += (long long)gridDim.x * blockDim.x) {
+    const int r = (int)(i % len);
+    const long long ec = i / len;
+    const int c = (int)(ec % nrhs);
+    const long long e = ec / nrhs;
+    vec[glob[e * len + r] + (long long)c * ldv] = in[i];
+  }
+}
+
+template <typename Tout, typename Tin>
+__global__ void convert_kernel(const Tin* __restrict__ in, Tout* __restrict__ out, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    out[i] = (Tout)in[i];
+}
+
+template <typename Tin>
+__global__ void axpy_kernel(double* __restrict__ y, const Tin* __restrict__ x, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    y[i] += (double)x[i];
+}
+
+// boundary values on Dirichlet face nodes, zero elsewhere
+__global__ void init_faces_kernel(const double* __restrict__ bnd, const unsigned char* __restrict__ dir,
+                                  double* __restrict__ ux, long long ntot, int nrhs) {
+  const long long tot = ntot * nrhs;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < tot; i += (long long)gridDim.x * blockDim.x) {
+    const long long g = i % ntot;
+    ux[i] = dir[g] ? bnd[i] : 0.0;
+  }
+}
+
+template <typename T>
+__global__ void sumsq_kernel(const T* __restrict__ x, long long n, double* __restrict__ acc) {
+  double s = 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const double v = (double)x[i];
+    s += v * v;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  __shared__ double ws[32];
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    s = threadIdx.x < (blockDim.x >> 5) ? ws[threadIdx.x] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (threadIdx.x == 0) atomicAdd(acc, s);
+  }
+}
+
+static unsigned grid_for(long long n) {
+  long long g = (n + 255) / 256;
+  if (g > 4096) g = 4096;
+  if (g < 1) g = 1;
+  return (unsigned)g;
+}
+
+// Merge-tree assembly: parent F, M | row (Maug), col.
+struct MergeGatherArgs {
+  int nA, nB, nE, nO, count;
+  const int* eA;
+  const int* eB;
+  const int* oChild;  // 0 = A, 1 = B
+  const int* oPos;
+  const long long* offA;
+  const long long* offB;
+  long long offP0, offM0, offC0;
+};
+
+template <typename T>
+__global__ void merge_gather_kernel(MergeGatherArgs a, const T* __restrict__ pool, T* __restrict__ ppool,
+                                    T* __restrict__ fpool) {
+  const int e = blockIdx.y;
+  const T* A = pool + a.offA[e];
+  const T* B = pool + a.offB[e];
+  T* P = ppool + a.offP0 + (long long)e * a.nO * a.nO;
+  T* M = fpool + a.offM0 + (long long)e * a.nE * (a.nE + a.nO);
+  T* C = fpool + a.offC0 + (long long)e * a.nO * a.nE;
+  const int nE = a.nE, nO = a.nO;
+  const long long totP = (long long)nO * nO;
+  const long long totM = (long long)nE * (nE + nO);
+  const long long totC = (long long)nO * nE;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < totP + totM + totC;
+       i += (long long)gridDim.x * blockDim.x) {
+    if (i < totP) {
+      const int r = (int)(i % nO), c = (int)(i / nO);
+      const int cr = a.oChild[r], cc = a.oChild[c];
+      T v = T(0);
+      if (cr == cc) {
+        if (cr == 0)
+          v = A[a.oPos[r] + (long long)a.oPos[c] * a.nA];
+        else
+          v = B[a.oPos[r] + (long long)a.oPos[c] * a.nB];
+      }
+      P[i] = v;
+    } else if (i < totP + totM) {
+      const long long j = i - totP;
+      const int r = (int)(j % nE), c = (int)(j / nE);
+      T v;
+      if (c < nE) {
+        v = A[a.eA[r] + (long long)a.eA[c] * a.nA] + B[a.eB[r] + (long long)a.eB[c] * a.nB];
+      } else {
+        const int o = c - nE;
+        v = a.oChild[o] == 0 ? A[a.eA[r] + (long long)a.oPos[o] * a.nA] : B[a.eB[r] + (long long)a.oPos[o] * a.nB];
+      }
+      M[j] = v;
+    } else {
+      const long long j = i - totP - totM;
+      const int r = (int)(j % nO), c = (int)(j / nO);
+      C[j] = a.oChild[r] == 0 ? A[a.oPos[r] + (long long)a.eA[c] * a.nA] : B[a.oPos[r] + (long long)a.eB[c] * a.nB];
+    }
+  }
+}
+
+// Interface blocks from slab roots (root order [L | R | D | U], nR = 2 nI + extra).
+template <typename TI, typename T>
+__global__ void iface_gather_kernel(const T* __restrict__ pool, const long long* __restrict__ rootoff, int nR, int nI,
+                                    int nb, TI* __restrict__ diag, TI* __restrict__ sub, TI* __restrict__ sup) {
+  const long long blk = (long long)nI * nI;
+  const long long tot = blk * nb * 3;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < tot; i += (long long)gridDim.x * blockDim.x) {
+    const int which = (int)(i / (blk * nb));
+    const long long k = i % (blk * nb);
+    const int j = (int)(k / blk);
+    const int rc = (int)(k % blk);
+    const int r = rc % nI, c = rc / nI;
+    const T* Rj = pool + rootoff[j];
+    const T* Rj1 = pool + rootoff[j + 1];
+    if (which == 0) {
+      diag[k] = (TI)Rj[(nI + r) + (long long)(nI + c) * nR] + (TI)Rj1[r + (long long)c * nR];
+    } else if (which == 1) {
+      if (j >= 1) sub[k] = (TI)Rj[(nI + r) + (long long)c * nR];  // block row j, column j-1
+    } else {
+      if (j <= nb - 2) sup[k] = (TI)Rj1[r + (long long)(nI + c) * nR];  // block row j, column j+1
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Host-side plan.
+struct HNode {
+  long long off = -1;
+  std::vector<int> faces;
+};
+
+struct HMerge {
+  int A, B, P;  // node indices
+  int level;
+};
+
+struct Batch {
+  int level = 0, count = 0, nA = 0, nB = 0, nE = 0, nO = 0;
+  std::vector<int> merges;
+  DevBuf eA, eB, oChild, oPos, offA, offB, Eglob, Oglob;
+  long long offP0 = 0, offM0 = 0, offC0 = 0, offPiv0 = 0, offY0 = 0;
+  std::vector<long long> hoffA, hoffB;
+};
+
+struct EngineBase {
+  virtual ~EngineBase() = default;
+  virtual int factor(const LeafCoeffs& co) = 0;
+  virtual int solve(int nrhs, const double* bnd, const double* fbody, double tol, int max_iter, double* ufaces,
+                    double* uleaf, int* iters, double* stats) = 0;
+  virtual int residual(int nrhs, const double* ufaces, const double* uint, const double* fbody, double* rint,
+                       double* rfaces) = 0;
+  virtual size_t factor_bytes() const = 0;
+  long long ntot = 0, nleaf = 0;
+};
+
+template <typename T, typename TI>
+struct EngineImpl : EngineBase {
+  int p, q, n, nx, n0, n1, buf, npan;
+  cudaStream_t s;
+  DevBuf D, Dsq, Nx, NxcT, NxxT, interp, jxr, leafglob, dirmask;
+  DevBuf coef[5];
+  bool has[5] = {false, false, false, false, false};
+  // leaf factors
+  DevBuf G, piv, leafinfo;
+  // tree
+  std::vector<HNode> nodes;
+  std::vector<HMerge> merges;
+  std::vector<std::unique_ptr<Batch>> batches;
+  DevBuf nodepool, fpool, pivpool, mergeinfo;
+  long long nodepool_elems = 0, fpool_elems = 0, pivpool_elems = 0;
+  std::vector<int> roots;
+  DevBuf rootoff;
+  int nR = 0;
+  // interface
+  int nI = 0, nbI = 0;
+  DevBuf ifLU, ifPiv, ifPerm, ifX, ifSub, ifSup, ifInfo, ifGlob;
+  // solve buffers
+  int cap_nrhs = 0;
+  DevBuf wc, flux, gvec, uvec, Ybuf, Zbuf, ifF, ifZ, ux_d, uc_d, rc_d, rx_d, rcT, acc;
+  size_t factor_bytes_ = 0;
+  bool factored = false;
+
+  EngineImpl(int p_, int n0_, int n1_, int buf_, cudaStream_t s_)
+      : p(p_), q(p_ - 2), n((p_ - 2) * (p_ - 2)), nx(4 * (p_ - 2)), n0(n0_), n1(n1_), buf(buf_), npan(n0_ / buf_),
+        s(s_) {
+    ntot = (long long)q * ((long long)n0 * (2 * n1 + 1) + n1);
+    nleaf = (long long)n0 * n1;
+  }
+
+  int faceL(int I, int J) const { return (2 * n1 + 1) * I + J; }
+  int faceR(int I, int J) const { return (2 * n1 + 1) * (I + 1) + J; }
+  int faceD(int I, int J) const { return (2 * n1 + 1) * I + n1 + J; }
+  int faceU(int I, int J) const { return (2 * n1 + 1) * I + n1 + J + 1; }
+
+  int add_node(std::vector<int> faces) {
+    HNode h;
+    h.faces = std::move(faces);
+    nodes.push_back(std::move(h));
+    return (int)nodes.size() - 1;
+  }
+
+  std::vector<int> strip_faces(int I0, int I1, int J) const {  // columns I0..I1 inclusive
+    std::vector<int> f{faceL(I0, J), faceR(I1, J)};
+    for (int I = I0; I <= I1; ++I) f.push_back(faceD(I, J));
+    for (int I = I0; I <= I1; ++I) f.push_back(faceU(I, J));
+    return f;
+  }
+
+  std::vector<int> range_faces(int s_, int lo, int hi) const {
+    const int c0 = s_ * buf, c1 = c0 + buf - 1;
+    std::vector<int> f;
+    for (int J = lo; J < hi; ++J) f.push_back(faceL(c0, J));
+    for (int J = lo; J < hi; ++J) f.push_back(faceR(c1, J));
+    for (int I = c0; I <= c1; ++I) f.push_back(faceD(I, lo));
+    for (int I = c0; I <= c1; ++I) f.push_back(faceU(I, hi - 1));
+    return f;
+  }
+
+  int build_range(int s_, int lo, int hi, std::vector<int>& strip_of_row, std::vector<int>& height) {
+    if (hi - lo == 1) return strip_of_row[lo];
+    const int mid = lo + (hi - lo) / 2;
+    const int a = build_range(s_, lo, mid, strip_of_row, height);
+    const int b = build_range(s_, mid, hi, strip_of_row, height);
+    const int P = add_node(range_faces(s_, lo, hi));
+    height.resize(nodes.size(), 0);
+    height[P] = 1 + std::max(height[a], height[b]);
+    merges.push_back({a, b, P, (buf - 1) + height[P]});
+    return P;
+  }
+
+  int build_plan() {
+    // leaves
+    for (int I = 0; I < n0; ++I)
+      for (int J = 0; J < n1; ++J) {
+        const int id = add_node({faceL(I, J), faceR(I, J), faceD(I, J), faceU(I, J)});
+        nodes[id].off = (long long)id * nx * nx;
+      }
+    std::vector<int> height(nodes.size(), 0);
+    for (int sl = 0; sl < npan; ++sl) {
+      std::vector<int> strip_of_row(n1);
+      for (int J = 0; J < n1; ++J) {
+        const int c0 = sl * buf;
+        int cur = c0 * n1 + J;
+        for (int k = 1; k < buf; ++k) {
+          const int leaf = (c0 + k) * n1 + J;
+          const int P = add_node(strip_faces(c0, c0 + k, J));
+          merges.push_back({cur, leaf, P, k});
+          cur = P;
+        }
+        strip_of_row[J] = cur;
+      }
+      height.resize(nodes.size(), 0);
+      roots.push_back(build_range(sl, 0, n1, strip_of_row, height));
+    }
+    // group merges into batches of identical shape and maps
+    std::vector<int> order(merges.size());
+    for (size_t i = 0; i < order.size(); ++i) order[i] = (int)i;
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return merges[x].level < merges[y].level; });
+    std::map<std::tuple<int, int, int, int>, std::vector<int>> groups;  // (level, nA, nB, nO)
+    std::vector<std::tuple<int, int, int, int>> keys;
+    for (int mi : order) {
+      const HMerge& m = merges[mi];
+      auto key = std::make_tuple(m.level, (int)nodes[m.A].faces.size(), (int)nodes[m.B].faces.size(),
+                                 (int)nodes[m.P].faces.size());
+      if (!groups.count(key)) keys.push_back(key);
+      groups[key].push_back(mi);
+    }
+    std::stable_sort(keys.begin(), keys.end(), [](const auto& x, const auto& y) { return std::get<0>(x) < std::get<0>(y); });
+    long long node_cursor = nleaf * nx * nx;
+    long long fcur = 0, pcur = 0;
+    for (auto& key : keys) {
+      auto& list = groups[key];
+      // maps of the first entry; every entry must agree
+      std::vector<int> eA, eB, oC, oP;
+      bool first = true;
+      auto b = std::make_unique<Batch>();
+      b->level = std::get<0>(key);
+      std::vector<int> Eg, Og;
+      for (int mi : list) {
+        const HMerge& m = merges[mi];
+        const auto& fa = nodes[m.A].faces;
+        const auto& fb = nodes[m.B].faces;
+        const auto& fp = nodes[m.P].faces;
+        std::vector<int> E, ea, eb;
+        for (size_t i = 0; i < fa.size(); ++i) {
+          auto it = std::find(fb.begin(), fb.end(), fa[i]);
+          if (it != fb.end()) {
+            E.push_back(fa[i]);
+            ea.push_back((int)i);
+            eb.push_back((int)(it - fb.begin()));
+          }
+        }
+        std::vector<int> oc, op;
+        for (int f : fp) {
+          auto ia = std::find(fa.begin(), fa.end(), f);
+          auto ib = std::find(fb.begin(), fb.end(), f);
+          if (ia != fa.end() && ib == fb.end()) {
+            oc.push_back(0);
+            op.push_back((int)(ia - fa.begin()));
+          } else if (ib != fb.end() && ia == fa.end()) {
+            oc.push_back(1);
+            op.push_back((int)(ib - fb.begin()));
+          } else {
+            return set_error(SLAB_ERR_STATE, "plan: parent face %d not owned by exactly one child", f);
+          }
+        }
+        if (first) {
+          eA = ea; eB = eb; oC = oc; oP = op;
+          first = false;
+        } else if (ea != eA || eb != eB || oc != oC || op != oP) {
+          return set_error(SLAB_ERR_STATE, "plan: merges of one batch differ in structure");
+        }
+        for (int f : E)
+          for (int k = 0; k < q; ++k) Eg.push_back(f * q + k);
+        for (int f : fp)
+          for (int k = 0; k < q; ++k) Og.push_back(f * q + k);
+        b->hoffA.push_back(nodes[m.A].off);
+        b->hoffB.push_back(nodes[m.B].off);
+        if (nodes[m.A].off < 0 || nodes[m.B].off < 0) return set_error(SLAB_ERR_STATE, "plan: child not placed");
+      }
+      b->merges = list;
+      b->count = (int)list.size();
+      b->nA = (int)nodes[merges[list[0]].A].faces.size() * q;
+      b->nB = (int)nodes[merges[list[0]].B].faces.size() * q;
+      b->nE = (int)eA.size() * q;
+      b->nO = (int)oC.size() * q;
+      if (b->nE == 0) return set_error(SLAB_ERR_STATE, "plan: merge without shared faces");
+      // node-position maps
+      std::vector<int> meA, meB, moC, moP;
+      for (size_t i = 0; i < eA.size(); ++i)
+        for (int k = 0; k < q; ++k) {
+          meA.push_back(eA[i] * q + k);
+          meB.push_back(eB[i] * q + k);
+        }
+      for (size_t i = 0; i < oC.size(); ++i)
+        for (int k = 0; k < q; ++k) {
+          moC.push_back(oC[i]);
+          moP.push_back(oP[i] * q + k);
+        }
+      b->offP0 = node_cursor;
+      for (int e = 0; e < b->count; ++e) nodes[merges[list[e]].P].off = node_cursor + (long long)e * b->nO * b->nO;
+      node_cursor += (long long)b->count * b->nO * b->nO;
+      b->offM0 = fcur;
+      fcur += (long long)b->count * b->nE * (b->nE + b->nO);
+      b->offC0 = fcur;
+      fcur += (long long)b->count * b->nO * b->nE;
+      b->offPiv0 = pcur;
+      pcur += (long long)b->count * b->nE;
+      SLAB_TRY(upload(b->eA, meA, s));
+      SLAB_TRY(upload(b->eB, meB, s));
+      SLAB_TRY(upload(b->oChild, moC, s));
+      SLAB_TRY(upload(b->oPos, moP, s));
+      SLAB_TRY(upload(b->offA, b->hoffA, s));
+      SLAB_TRY(upload(b->offB, b->hoffB, s));
+      SLAB_TRY(upload(b->Eglob, Eg, s));
+      SLAB_TRY(upload(b->Oglob, Og, s));
+      batches.push_back(std::move(b));
+    }
+    nodepool_elems = node_cursor;
+    fpool_elems = fcur;
+    pivpool_elems = pcur;
+    // roots and interface geometry
+    std::vector<long long> ro;
+    for (int r : roots) ro.push_back(nodes[r].off);
+    nR = (int)nodes[roots[0]].faces.size() * q;
+    nI = n1 * q;
+    nbI = npan - 1;
+    SLAB_TRY(upload(rootoff, ro, s));
+    std::vector<int> ig;
+    for (int j = 0; j < nbI; ++j)
+      for (int J = 0; J < n1; ++J)
+        for (int k = 0; k < q; ++k) ig.push_back(faceR((j + 1) * buf - 1, J) * q + k);
+    SLAB_TRY(upload(ifGlob, ig, s));
+    // leaf face maps and Dirichlet mask
+    std::vector<int> lg((size_t)nleaf * nx);
+    for (int I = 0; I < n0; ++I)
+      for (int J = 0; J < n1; ++J) {
+        const int l = I * n1 + J;
+        const int f[4] = {faceL(I, J), faceR(I, J), faceD(I, J), faceU(I, J)};
+        for (int t = 0; t < 4; ++t)
+          for (int k = 0; k < q; ++k) lg[(size_t)l * nx + t * q + k] = f[t] * q + k;
+      }
+    SLAB_TRY(upload(leafglob, lg, s));
+    std::vector<unsigned char> dm((size_t)ntot, 0);
+    auto mark = [&](int f) {
+      for (int k = 0; k < q; ++k) dm[(size_t)f * q + k] = 1;
+    };
+    for (int J = 0; J < n1; ++J) {
+      mark(faceL(0, J));
+      mark(faceR(n0 - 1, J));
+    }
+    for (int I = 0; I < n0; ++I) {
+      mark(faceD(I, 0));
+      mark(faceU(I, n1 - 1));
+    }
+    SLAB_TRY(upload(dirmask, dm, s));
+    return SLAB_OK;
+  }
+
+  int init(const double* hD, const double* hDsq, const double* hNx, const double* hinterp, const int* hjxr) {
+    SLAB_TRY(upload(D, std::vector<double>(hD, hD + p * p), s));
+    SLAB_TRY(upload(Dsq, std::vector<double>(hDsq, hDsq + p * p), s));
+    SLAB_TRY(upload(Nx, std::vector<double>(hNx, hNx + (size_t)nx * p * p), s));
+    SLAB_TRY(upload(interp, std::vector<double>(hinterp, hinterp + (size_t)4 * (p - 1) * nx), s));
+    SLAB_TRY(upload(jxr, std::vector<int>(hjxr, hjxr + 4 * (p - 1)), s));
+    SLAB_TRY(NxcT.alloc((size_t)nx * n * sizeof(T)));
+    SLAB_TRY(NxxT.alloc((size_t)nx * nx * sizeof(T)));
+    split_nx_kernel<T><<<64, 256, 0, s>>>(Nx.as<double>(), p, q, NxcT.as<T>(), NxxT.as<T>());
+    SLAB_CHECK_LAUNCH();
+    SLAB_TRY(build_plan());
+    // factor storage
+    SLAB_TRY(G.alloc((size_t)nleaf * n * (n + nx) * sizeof(T)));
+    SLAB_TRY(piv.alloc((size_t)nleaf * n * sizeof(int)));
+    SLAB_TRY(leafinfo.alloc((size_t)nleaf * sizeof(int)));
+    SLAB_TRY(nodepool.alloc((size_t)nodepool_elems * sizeof(T)));
+    SLAB_TRY(fpool.alloc((size_t)std::max<long long>(fpool_elems, 1) * sizeof(T)));
+    SLAB_TRY(pivpool.alloc((size_t)std::max<long long>(pivpool_elems, 1) * sizeof(int)));
+    int ninfo = 0;
+    for (auto& b : batches) ninfo += b->count;
+    SLAB_TRY(mergeinfo.alloc((size_t)std::max(ninfo, 1) * sizeof(int)));
+    if (nbI > 0) {
+      const size_t blk = (size_t)nI * nI;
+      SLAB_TRY(ifLU.alloc(blk * nbI * sizeof(TI)));
+      SLAB_TRY(ifPiv.alloc((size_t)nI * nbI * sizeof(int)));
+      SLAB_TRY(ifPerm.alloc((size_t)nI * nbI * sizeof(int)));
+      SLAB_TRY(ifSub.alloc(blk * nbI * sizeof(TI)));
+      SLAB_TRY(ifSup.alloc(blk * nbI * sizeof(TI)));
+      SLAB_TRY(ifX.alloc(blk * nbI * sizeof(TI)));
+      SLAB_TRY(ifInfo.alloc(sizeof(int)));
+    }
+    SLAB_TRY(acc.alloc(4 * sizeof(double)));
+    factor_bytes_ = G.bytes + piv.bytes + nodepool.bytes + fpool.bytes + pivpool.bytes + ifLU.bytes + ifPiv.bytes +
+                    ifPerm.bytes + ifSub.bytes + ifSup.bytes + ifX.bytes;
+    return SLAB_OK;
+  }
+
+  size_t factor_bytes() const override { return factor_bytes_; }
+
+  int factor(const LeafCoeffs& co_in) override {
+    const size_t cbytes = (size_t)nleaf * p * p * sizeof(double);
+    const double* src[5] = {co_in.c11, co_in.c22, co_in.c1, co_in.c2, co_in.c};
+    for (int i = 0; i < 5; ++i) {
+      has[i] = src[i] != nullptr;
+      if (has[i]) {
+        SLAB_TRY(coef[i].ensure(cbytes));
+        SLAB_CUDA_TRY(cudaMemcpyAsync(coef[i].p, src[i], cbytes, cudaMemcpyDeviceToDevice, s));
+      }
+    }
+    LeafCoeffs co = coeffs();
+    SLAB_CUDA_TRY(cudaMemsetAsync(leafinfo.p, 0, leafinfo.bytes, s));
+    SLAB_CUDA_TRY(cudaMemsetAsync(mergeinfo.p, 0, mergeinfo.bytes, s));
+    LeafFactorArgs<T> a{};
+    a.p = p; a.q = q; a.n = n; a.nx = nx;
+    a.co = co; a.D = D.as<double>(); a.Dsq = Dsq.as<double>();
+    a.Nxc = NxcT.as<T>(); a.Nxx = NxxT.as<T>();
+    a.G = G.as<T>(); a.strideG = (long long)n * (n + nx); a.piv = piv.as<int>();
+    a.dtn = nodepool.as<T>(); a.info = leafinfo.as<int>();
+    a.decouple = 1; a.n0 = n0; a.n1 = n1; a.leaf_begin = 0;
+    SLAB_TRY(leaf_factor<T>(s, a, (int)nleaf));
+    // merge tree, level by level
+    int info_ofs = 0;
+    for (auto& bp : batches) {
+      Batch& b = *bp;
+      MergeGatherArgs g{b.nA, b.nB, b.nE, b.nO, b.count, b.eA.as<int>(), b.eB.as<int>(), b.oChild.as<int>(),
+                        b.oPos.as<int>(), b.offA.as<long long>(), b.offB.as<long long>(), b.offP0, b.offM0, b.offC0};
+      const long long per = (long long)b.nO * b.nO + (long long)b.nE * (b.nE + b.nO) + (long long)b.nO * b.nE;
+      dim3 grid((unsigned)std::min<long long>((per + 255) / 256, 1024), b.count);
+      merge_gather_kernel<T><<<grid, 256, 0, s>>>(g, nodepool.as<T>(), nodepool.as<T>(), fpool.as<T>());
+      SLAB_CHECK_LAUNCH();
+      T* Maug = fpool.as<T>() + b.offM0;
+      const long long strideM = (long long)b.nE * (b.nE + b.nO);
+      int* pv = pivpool.as<int>() + b.offPiv0;
+      SLAB_TRY(getrf_batched<T>(s, b.nE, b.nE, Maug, nullptr, strideM, b.nE, pv, nullptr, b.nE,
+                                mergeinfo.as<int>() + info_ofs, b.count));
+      SLAB_TRY(getrs_batched<T>(s, b.nE, b.nO, Maug, nullptr, strideM, b.nE, pv, nullptr, b.nE,
+                                Maug + (long long)b.nE * b.nE, nullptr, strideM, b.nE, b.count));
+      SLAB_TRY(gemm<T>(s, b.nO, b.nO, b.nE, T(-1), fpool.as<T>() + b.offC0, nullptr, (long long)b.nO * b.nE, b.nO,
+                       Maug + (long long)b.nE * b.nE, nullptr, strideM, b.nE, T(1), nodepool.as<T>() + b.offP0,
+                       nullptr, (long long)b.nO * b.nO, b.nO, b.count));
+      info_ofs += b.count;
+    }
+    // interface
+    if (nbI > 0) {
+      const long long blk = (long long)nI * nI;
+      SLAB_CUDA_TRY(cudaMemsetAsync(ifInfo.p, 0, sizeof(int), s));
+      iface_gather_kernel<TI, T><<<grid_for(blk * nbI * 3), 256, 0, s>>>(
+          nodepool.as<T>(), rootoff.as<long long>(), nR, nI, nbI, ifLU.as<TI>(), ifSub.as<TI>(), ifSup.as<TI>());
+      SLAB_CHECK_LAUNCH();
+      for (int j = 0; j < nbI; ++j) {
+        TI* Sj = ifLU.as<TI>() + blk * j;
+        if (j > 0) {
+          TI* Xprev = ifX.as<TI>() + blk * (j - 1);
+          SLAB_TRY(bigtrs<TI>(s, ifLU.as<TI>() + blk * (j - 1), nI, nI, ifPerm.as<int>() + (long long)nI * (j - 1),
+                              ifSup.as<TI>() + blk * (j - 1), nI, Xprev, nI, nI));
+          SLAB_TRY(gemm<TI>(s, nI, nI, nI, TI(-1), ifSub.as<TI>() + blk * j, nullptr, 0, nI, Xprev, nullptr, 0, nI,
+                            TI(1), Sj, nullptr, 0, nI, 1));
+        }
+        SLAB_TRY(biglu<TI>(s, Sj, nI, nI, ifPiv.as<int>() + (long long)nI * j, ifInfo.as<int>()));
+        SLAB_TRY(build_perm(s, ifPiv.as<int>() + (long long)nI * j, nI, ifPerm.as<int>() + (long long)nI * j));
+      }
+    }
+    // breakdown report
+    std::vector<int> hinfo((size_t)nleaf);
+    SLAB_CUDA_TRY(cudaMemcpyAsync(hinfo.data(), leafinfo.p, leafinfo.bytes, cudaMemcpyDeviceToHost, s));
+    std::vector<int> minfo(mergeinfo.bytes / sizeof(int));
+    SLAB_CUDA_TRY(cudaMemcpyAsync(minfo.data(), mergeinfo.p, mergeinfo.bytes, cudaMemcpyDeviceToHost, s));
+    int iinfo = 0;
+    if (nbI > 0) SLAB_CUDA_TRY(cudaMemcpyAsync(&iinfo, ifInfo.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    SLAB_CUDA_TRY(cudaStreamSynchronize(s));
+    factored = true;
+    for (size_t i = 0; i < hinfo.size(); ++i)
+      if (hinfo[i] > 0) {
+        set_error(hinfo[i], "leaf %zu: zero pivot at column %d", i, hinfo[i]);
+        return hinfo[i];
+      }
+    for (size_t i = 0; i < minfo.size(); ++i)
+      if (minfo[i] > 0) {
+        set_error(minfo[i], "merge %zu: zero pivot at column %d", i, minfo[i]);
+        return minfo[i];
+      }
+    if (iinfo > 0) {
+      set_error(iinfo, "interface block: zero pivot at column %d", iinfo);
+      return iinfo;
+    }
+    return SLAB_OK;
+  }
+
+  LeafCoeffs coeffs() const {
+    return LeafCoeffs{has[0] ? coef[0].as<double>() : nullptr, has[1] ? coef[1].as<double>() : nullptr,
+                      has[2] ? coef[2].as<double>() : nullptr, has[3] ? coef[3].as<double>() : nullptr,
+                      has[4] ? coef[4].as<double>() : nullptr};
+  }
+
+  int reserve(int nrhs) {
+    if (nrhs <= cap_nrhs) return SLAB_OK;
+    long long ymax = 0, zmax = 0;
+    for (auto& b : batches) {
+      b->offY0 = ymax;
+      ymax += (long long)b->count * b->nE * nrhs;
+      zmax = std::max(zmax, (long long)b->count * b->nO * nrhs);
+    }
+    SLAB_TRY(wc.alloc((size_t)nleaf * n * nrhs * sizeof(T)));
+    SLAB_TRY(flux.alloc((size_t)nleaf * nx * nrhs * sizeof(T)));
+    SLAB_TRY(gvec.alloc((size_t)ntot * nrhs * sizeof(T)));
+    SLAB_TRY(uvec.alloc((size_t)ntot * nrhs * sizeof(T)));
+    SLAB_TRY(Ybuf.alloc((size_t)std::max<long long>(ymax, 1) * sizeof(T)));
+    SLAB_TRY(Zbuf.alloc((size_t)std::max<long long>(zmax, (long long)nleaf * nx * nrhs) * sizeof(T)));
+    if (nbI > 0) {
+      SLAB_TRY(ifF.alloc((size_t)nbI * nI * nrhs * sizeof(TI)));
+      SLAB_TRY(ifZ.alloc((size_t)nbI * nI * nrhs * sizeof(TI)));
+    }
+    SLAB_TRY(ux_d.alloc((size_t)ntot * nrhs * sizeof(double)));
+    SLAB_TRY(uc_d.alloc((size_t)nleaf * n * nrhs * sizeof(double)));
+    SLAB_TRY(rc_d.alloc((size_t)nleaf * n * nrhs * sizeof(double)));
+    SLAB_TRY(rx_d.alloc((size_t)ntot * nrhs * sizeof(double)));
+    SLAB_TRY(rcT.alloc((size_t)nleaf * n * nrhs * sizeof(T)));
+    cap_nrhs = nrhs;
+    return SLAB_OK;
+  }
+
+  // One application of the factorization: input rcT (interior residual,
+  // leaf-major) and gvec (face residual); output uvec (face correction) and
+  // wc (interior correction, leaf-major).
+  int apply(int nrhs) {
+    T* g = gvec.as<T>();
+    T* u = uvec.as<T>();
+    T* w = wc.as<T>();
+    const long long strideG = (long long)n * (n + nx);
+    SLAB_CUDA_TRY(cudaMemcpyAsync(w, rcT.p, (size_t)nleaf * n * nrhs * sizeof(T), cudaMemcpyDeviceToDevice, s));
+    SLAB_TRY(getrs_batched<T>(s, n, nrhs, G.as<T>(), nullptr, strideG, n, piv.as<int>(), nullptr, n, w, nullptr,
+                              (long long)n * nrhs, n, (int)nleaf));
+    SLAB_TRY(gemm<T>(s, nx, nrhs, n, T(1), NxcT.as<T>(), nullptr, 0, nx, w, nullptr, (long long)n * nrhs, n, T(0),
+                     flux.as<T>(), nullptr, (long long)nx * nrhs, nx, (int)nleaf));
+    scatter_add_kernel<T><<<grid_for(nleaf * nx * nrhs), 256, 0, s>>>(g, ntot, leafglob.as<int>(), nx, (int)nleaf,
+                                                                     nrhs, flux.as<T>(), T(-1), dirmask.as<unsigned char>());
+    SLAB_CHECK_LAUNCH();
+    // tree forward
+    for (auto& bp : batches) {
+      Batch& b = *bp;
+      T* Y = Ybuf.as<T>() + b.offY0;
+      T* Z = Zbuf.as<T>();
+      const long long strideM = (long long)b.nE * (b.nE + b.nO);
+      T* Maug = fpool.as<T>() + b.offM0;
+      gather_kernel<T><<<grid_for((long long)b.count * b.nE * nrhs), 256, 0, s>>>(g, ntot, b.Eglob.as<int>(), b.nE,
+                                                                                b.count, nrhs, Y);
+      SLAB_CHECK_LAUNCH();
+      SLAB_TRY(getrs_batched<T>(s, b.nE, nrhs, Maug, nullptr, strideM, b.nE, pivpool.as<int>() + b.offPiv0, nullptr,
+                                b.nE, Y, nullptr, (long long)b.nE * nrhs, b.nE, b.count));
+      SLAB_TRY(gemm<T>(s, b.nO, nrhs, b.nE, T(1), fpool.as<T>() + b.offC0, nullptr, (long long)b.nO * b.nE, b.nO, Y,
+                       nullptr, (long long)b.nE * nrhs, b.nE, T(0), Z, nullptr, (long long)b.nO * nrhs, b.nO,
+                       b.count));
+      scatter_add_kernel<T><<<grid_for((long long)b.count * b.nO * nrhs), 256, 0, s>>>(
+          g, ntot, b.Oglob.as<int>(), b.nO, b.count, nrhs, Z, T(-1), nullptr);
+      SLAB_CHECK_LAUNCH();
+    }
+    SLAB_CUDA_TRY(cudaMemsetAsync(u, 0, (size_t)ntot * nrhs * sizeof(T), s));
+    // interface sweep
+    if (nbI > 0) {
+      const long long blk = (long long)nI * nI;
+      const long long vb = (long long)nI * nrhs;
+      TI* F = ifF.as<TI>();
+      TI* Zi = ifZ.as<TI>();
+      // gather with conversion through the T-typed Zbuf
+      gather_kernel<T><<<grid_for((long long)nbI * vb), 256, 0, s>>>(g, ntot, ifGlob.as<int>(), nI, nbI, nrhs,
+                                                                    Zbuf.as<T>());
+      SLAB_CHECK_LAUNCH();
+      convert_kernel<TI, T><<<grid_for(nbI * vb), 256, 0, s>>>(Zbuf.as<T>(), F, nbI * vb);
+      SLAB_CHECK_LAUNCH();
+      for (int j = 0; j < nbI; ++j) {
+        if (j > 0)
+          SLAB_TRY(gemm<TI>(s, nI, nrhs, nI, TI(-1), ifSub.as<TI>() + blk * j, nullptr, 0, nI, Zi + vb * (j - 1),
+                            nullptr, 0, nI, TI(1), F + vb * j, nullptr, 0, nI, 1));
+        SLAB_TRY(bigtrs<TI>(s, ifLU.as<TI>() + blk * j, nI, nI, ifPerm.as<int>() + (long long)nI * j, F + vb * j, nI,
+                            Zi + vb * j, nI, nrhs));
+      }
+      for (int j = nbI - 2; j >= 0; --j)
+        SLAB_TRY(gemm<TI>(s, nI, nrhs, nI, TI(-1), ifX.as<TI>() + blk * j, nullptr, 0, nI, Zi + vb * (j + 1), nullptr,
+                          0, nI, TI(1), Zi + vb * j, nullptr, 0, nI, 1));
+      convert_kernel<T, TI><<<grid_for(nbI * vb), 256, 0, s>>>(Zi, Zbuf.as<T>(), nbI * vb);
+      SLAB_CHECK_LAUNCH();
+      scatter_set_kernel<T><<<grid_for((long long)nbI * vb), 256, 0, s>>>(u, ntot, ifGlob.as<int>(), nI, nbI, nrhs,
+                                                                         Zbuf.as<T>());
+      SLAB_CHECK_LAUNCH();
+    }
+    // tree backward
+    for (auto it = batches.rbegin(); it != batches.rend(); ++it) {
+      Batch& b = **it;
+      T* Y = Ybuf.as<T>() + b.offY0;
+      T* Z = Zbuf.as<T>();
+      const long long strideM = (long long)b.nE * (b.nE + b.nO);
+      T* Maug = fpool.as<T>() + b.offM0;
+      gather_kernel<T><<<grid_for((long long)b.count * b.nO * nrhs), 256, 0, s>>>(u, ntot, b.Oglob.as<int>(), b.nO,
+                                                                                b.count, nrhs, Z);
+      SLAB_CHECK_LAUNCH();
+      SLAB_TRY(gemm<T>(s, b.nE, nrhs, b.nO, T(-1), Maug + (long long)b.nE * b.nE, nullptr, strideM, b.nE, Z, nullptr,
+                       (long long)b.nO * nrhs, b.nO, T(1), Y, nullptr, (long long)b.nE * nrhs, b.nE, b.count));
+      scatter_set_kernel<T><<<grid_for((long long)b.count * b.nE * nrhs), 256, 0, s>>>(u, ntot, b.Eglob.as<int>(),
+                                                                                     b.nE, b.count, nrhs, Y);
+      SLAB_CHECK_LAUNCH();
+    }
+    // leaf backward: w += S u_x
+    gather_kernel<T><<<grid_for(nleaf * nx * nrhs), 256, 0, s>>>(u, ntot, leafglob.as<int>(), nx, (int)nleaf, nrhs,
+                                                                flux.as<T>());
+    SLAB_CHECK_LAUNCH();
+    SLAB_TRY(gemm<T>(s, n, nrhs, nx, T(1), G.as<T>() + (long long)n * n, nullptr, strideG, n, flux.as<T>(), nullptr,
+                     (long long)nx * nrhs, nx, T(1), w, nullptr, (long long)n * nrhs, n, (int)nleaf));
+    return SLAB_OK;
+  }
+
+  int residual_impl(int nrhs, const double* ux, const double* uc, const double* fbody, double* rc, double* rx) {
+    SLAB_CUDA_TRY(cudaMemsetAsync(rx, 0, (size_t)ntot * nrhs * sizeof(double), s));
+    ResidualArgs r{};
+    r.p = p; r.q = q; r.n = n; r.nx = nx; r.nleaf = (int)nleaf; r.nrhs = nrhs; r.ntot = ntot;
+    r.co = coeffs(); r.D = D.as<double>(); r.Dsq = Dsq.as<double>();
+    r.leafglob = leafglob.as<int>(); r.dirmask = dirmask.as<unsigned char>();
+    r.ux = ux; r.uc = uc; r.fbody = fbody; r.rc = rc; r.rx = rx;
+    residual_kernel<<<(unsigned)nleaf, 256, 3 * (size_t)p * p * sizeof(double), s>>>(r);
+    SLAB_CHECK_LAUNCH();
+    return SLAB_OK;
+  }
+
+  int norms(const void* x1, bool x1d, long long n1_, const void* x2, bool x2d, long long n2_, double* out) {
+    SLAB_CUDA_TRY(cudaMemsetAsync(acc.p, 0, sizeof(double), s));
+    if (n1_ > 0) {
+      if (x1d)
+        sumsq_kernel<double><<<grid_for(n1_), 256, 0, s>>>((const double*)x1, n1_, acc.as<double>());
+      else
+        sumsq_kernel<T><<<grid_for(n1_), 256, 0, s>>>((const T*)x1, n1_, acc.as<double>());
+      SLAB_CHECK_LAUNCH();
+    }
+    if (n2_ > 0) {
+      if (x2d)
+        sumsq_kernel<double><<<grid_for(n2_), 256, 0, s>>>((const double*)x2, n2_, acc.as<double>());
+      else
+        sumsq_kernel<T><<<grid_for(n2_), 256, 0, s>>>((const T*)x2, n2_, acc.as<double>());
+      SLAB_CHECK_LAUNCH();
+    }
+    double h = 0;
+    SLAB_CUDA_TRY(cudaMemcpyAsync(&h, acc.p, sizeof(double), cudaMemcpyDeviceToHost, s));
+    SLAB_CUDA_TRY(cudaStreamSynchronize(s));
+    *out = std::sqrt(h);
+    return SLAB_OK;
+  }
+
+  int solve(int nrhs, const double* bnd, const double* fbody, double tol, int max_iter, double* ufaces,
+            double* uleaf, int* iters, double* stats) override {
+    if (!factored) return set_error(SLAB_ERR_STATE, "slab_engine_solve: engine not factored");
+    if (nrhs <= 0 || !bnd) return set_error(SLAB_ERR_ARG, "slab_engine_solve: invalid arguments");
+    SLAB_TRY(reserve(nrhs));
+    const long long nc_el = nleaf * n * nrhs, nf_el = ntot * nrhs;
+    init_faces_kernel<<<grid_for(nf_el), 256, 0, s>>>(bnd, dirmask.as<unsigned char>(), ux_d.as<double>(), ntot, nrhs);
+    SLAB_CHECK_LAUNCH();
+    SLAB_CUDA_TRY(cudaMemsetAsync(uc_d.p, 0, (size_t)nc_el * sizeof(double), s));
+    // body load in leaf-major interior layout is read directly by the residual kernel
+    double r0 = 0, rn = 0, rel = 1.0, dn = 0, un = 0;
+    int it = 0;
+    bool converged = false;
+    for (; it < max_iter; ++it) {
+      SLAB_TRY(residual_impl(nrhs, ux_d.as<double>(), uc_d.as<double>(), fbody, rc_d.as<double>(), rx_d.as<double>()));
+      SLAB_TRY(norms(rc_d.p, true, nc_el, rx_d.p, true, nf_el, &rn));
+      if (it == 0) r0 = rn;
+      if (rn == 0.0) {
+        converged = true;
+        rel = 0.0;
+        break;
+      }
+      convert_kernel<T, double><<<grid_for(nc_el), 256, 0, s>>>(rc_d.as<double>(), rcT.as<T>(), nc_el);
+      SLAB_CHECK_LAUNCH();
+      convert_kernel<T, double><<<grid_for(nf_el), 256, 0, s>>>(rx_d.as<double>(), gvec.as<T>(), nf_el);
+      SLAB_CHECK_LAUNCH();
+      SLAB_TRY(apply(nrhs));
+      axpy_kernel<T><<<grid_for(nc_el), 256, 0, s>>>(uc_d.as<double>(), wc.as<T>(), nc_el);
+      SLAB_CHECK_LAUNCH();
+      axpy_kernel<T><<<grid_for(nf_el), 256, 0, s>>>(ux_d.as<double>(), uvec.as<T>(), nf_el);
+      SLAB_CHECK_LAUNCH();
+      SLAB_TRY(norms(wc.p, false, nc_el, uvec.p, false, nf_el, &dn));
+      SLAB_TRY(norms(uc_d.p, true, nc_el, ux_d.p, true, nf_el, &un));
+      rel = un > 0 ? dn / un : 0.0;
+      if (rel <= tol) {
+        converged = true;
+        ++it;
+        break;
+      }
+    }
+    // final residual and interior-residual norm
+    SLAB_TRY(residual_impl(nrhs, ux_d.as<double>(), uc_d.as<double>(), fbody, rc_d.as<double>(), rx_d.as<double>()));
+    double rloc = 0;
+    SLAB_TRY(norms(rc_d.p, true, nc_el, nullptr, true, 0, &rloc));
+    SLAB_TRY(norms(rc_d.p, true, nc_el, rx_d.p, true, nf_el, &rn));
+    if (ufaces)
+      SLAB_CUDA_TRY(cudaMemcpyAsync(ufaces, ux_d.p, (size_t)nf_el * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    if (uleaf) {
+      AssembleArgs aa{};
+      aa.p = p; aa.q = q; aa.n = n; aa.nx = nx; aa.nleaf = (int)nleaf; aa.nrhs = nrhs; aa.ntot = ntot;
+      aa.leafglob = leafglob.as<int>(); aa.interp = interp.as<double>(); aa.jxreorder = jxr.as<int>();
+      aa.ux = ux_d.as<double>(); aa.uc = uc_d.as<double>(); aa.out = uleaf;
+      assemble_solution_kernel<<<(unsigned)nleaf, 256, (size_t)nx * sizeof(double), s>>>(aa);
+      SLAB_CHECK_LAUNCH();
+    }
+    if (iters) *iters = it;
+    if (stats) {
+      stats[0] = rel;
+      stats[1] = rn;
+      stats[2] = r0;
+      stats[3] = rloc;
+      stats[4] = r0 > 0 ? rn / r0 : 0.0;
+    }
+    SLAB_CUDA_TRY(cudaStreamSynchronize(s));
+    if (!converged) {
+      set_error(SLAB_ERR_NOCONV, "refinement: relative correction %.3e after %d steps (tol %.1e)", rel, it, tol);
+      return SLAB_ERR_NOCONV;
+    }
+    return SLAB_OK;
+  }
+
+  int residual(int nrhs, const double* ufaces, const double* uint, const double* fbody, double* rint,
+               double* rfaces) override {
+    if (!factored && !has[0] && !has[1] && !has[4])
+      return set_error(SLAB_ERR_STATE, "slab_engine_residual: coefficients not set (call factor first)");
+    SLAB_TRY(residual_impl(nrhs, ufaces, uint, fbody, rint, rfaces));
+    SLAB_CUDA_TRY(cudaStreamSynchronize(s));
+    return SLAB_OK;
+  }
+};
+
+}  // namespace slab
+
+struct slab_engine {
+  std::unique_ptr<slab::EngineBase> impl;
+};
+
+extern "C" int slab_version(void) { return 100; }
+
+extern "C" const char* slab_last_error(void) { return slab::last_error(); }
+
+extern "C" int slab_engine_create(slab_engine** out, int p, int n0, int n1, int buf, int precision,
+                                  const double* hD, const double* hDsq, const double* hNx, const double* hinterp,
+                                  const int* hjxr, void* stream) {
+  if (!out || p < 4 || n0 < 1 || n1 < 1 || buf < 1 || n0 % buf != 0 || !hD || !hDsq || !hNx || !hinterp || !hjxr)
+    return slab::set_error(SLAB_ERR_ARG, "slab_engine_create: invalid geometry or null operator");
+  const long long ntot = (long long)(p - 2) * ((long long)n0 * (2 * n1 + 1) + n1);
+  if (ntot >= (1LL << 31)) return slab::set_error(SLAB_ERR_ARG, "slab_engine_create: problem too large for int32 indexing");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  auto e = std::make_unique<slab_engine>();
+  int st = SLAB_OK;
+  if (precision == SLAB_PREC_FP64) {
+    auto im = std::make_unique<slab::EngineImpl<double, double>>(p, n0, n1, buf, s);
+    st = im->init(hD, hDsq, hNx, hinterp, hjxr);
+    e->impl = std::move(im);
+  } else if (precision == SLAB_PREC_MIXED) {
+    auto im = std::make_unique<slab::EngineImpl<float, double>>(p, n0, n1, buf, s);
+    st = im->init(hD, hDsq, hNx, hinterp, hjxr);
+    e->impl = std::move(im);
+  } else if (precision == SLAB_PREC_FP32) {
+    auto im = std::make_unique<slab::EngineImpl<float, float>>(p, n0, n1, buf, s);
+    st = im->init(hD, hDsq, hNx, hinterp, hjxr);
+    e->impl = std::move(im);
+  } else {
+    return slab::set_error(SLAB_ERR_ARG, "slab_engine_create: unknown precision %d", precision);
+  }
+  if (st != SLAB_OK) return st;
+  *out = e.release();
+  return SLAB_OK;
+}
+
+extern "C" int slab_engine_destroy(slab_engine* e) {
+  delete e;
+  return SLAB_OK;
+}
+
+extern "C" long long slab_engine_nfaces(const slab_engine* e) { return e ? e->impl->ntot : -1; }
+extern "C" long long slab_engine_nleaves(const slab_engine* e) { return e ? e->impl->nleaf : -1; }
+extern "C" size_t slab_engine_factor_bytes(const slab_engine* e) { return e ? e->impl->factor_bytes() : 0; }
+
+extern "C" int slab_engine_factor(slab_engine* e, const double* c11, const double* c22, const double* c1,
+                                  const double* c2, const double* c) {
+  if (!e) return slab::set_error(SLAB_ERR_ARG, "slab_engine_factor: null engine");
+  return e->impl->factor(slab::LeafCoeffs{c11, c22, c1, c2, c});
+}
+
+extern "C" int slab_engine_solve(slab_engine* e, int nrhs, const double* bnd, const double* fbody, double tol,
+                                 int max_iter, double* ufaces, double* uleaf, int* iters, double* stats) {
+  if (!e) return slab::set_error(SLAB_ERR_ARG, "slab_engine_solve: null engine");
+  return e->impl->solve(nrhs, bnd, fbody, tol, max_iter, ufaces, uleaf, iters, stats);
+}
+
+extern "C" int slab_engine_residual(slab_engine* e, int nrhs, const double* ufaces, const double* uint,
+                                    const double* fbody, double* rint, double* rfaces) {
+  if (!e) return slab::set_error(SLAB_ERR_ARG, "slab_engine_residual: null engine");
+  return e->impl->residual(nrhs, ufaces, uint, fbody, rint, rfaces);
+}

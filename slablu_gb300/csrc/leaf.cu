@@ -1,0 +1,220 @@
+// Leaf kernels: launchers, FP64 residual, solution assembly, and the
+// standalone batched leaf DtN entry point.
+#include "leaf.cuh"
+
+namespace slab {
+
+template <typename T>
+int leaf_factor(cudaStream_t s, const LeafFactorArgs<T>& a, int nleaf) {
+  if (nleaf <= 0) return SLAB_OK;
+  if (a.nx > 2 * kCT) return set_error(SLAB_ERR_ARG, "leaf_factor: p = %d too large", a.p);
+  const size_t bytes = leaf_factor_smem_bytes(a.p, sizeof(T));
+  if (bytes > smem_limit_bytes())
+    return set_error(SLAB_ERR_ARG, "leaf_factor: p = %d needs %zu bytes of shared memory", a.p, bytes);
+  SLAB_CUDA_TRY(
+      cudaFuncSetAttribute(leaf_factor_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  leaf_factor_kernel<T><<<nleaf, kNT, bytes, s>>>(a);
+  SLAB_CHECK_LAUNCH();
+  return SLAB_OK;
+}
+
+template int leaf_factor<float>(cudaStream_t, const LeafFactorArgs<float>&, int);
+template int leaf_factor<double>(cudaStream_t, const LeafFactorArgs<double>&, int);
+
+__global__ void __launch_bounds__(256) residual_kernel(ResidualArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int p = a.p, q = a.q, n = a.n, nx = a.nx;
+  double* Dsh = reinterpret_cast<double*>(smem_raw);
+  double* Dsqsh = Dsh + p * p;
+  double* u = Dsqsh + p * p;
+  const int leaf = blockIdx.x;
+  const int tid = threadIdx.x;
+  for (int i = tid; i < p * p; i += blockDim.x) {
+    Dsh[i] = a.D[i];
+    Dsqsh[i] = a.Dsq[i];
+  }
+  const int lofs = leaf * p * p;
+  const LeafCoeffs& co = a.co;
+  for (int c = 0; c < a.nrhs; ++c) {
+    __syncthreads();
+    for (int i = tid; i < p * p; i += blockDim.x) u[i] = 0.0;
+    __syncthreads();
+    for (int r = tid; r < n; r += blockDim.x) {
+      int i1, i2;
+      interior_node(r, q, i1, i2);
+      u[i1 * p + i2] = a.uc[((size_t)leaf * a.nrhs + c) * n + r];
+    }
+    for (int s = tid; s < nx; s += blockDim.x) {
+      int j1, j2;
+      face_node(s, p, q, j1, j2);
+      u[j1 * p + j2] = a.ux[a.leafglob[(size_t)leaf * nx + s] + (size_t)c * a.ntot];
+    }
+    __syncthreads();
+    for (int r = tid; r < n; r += blockDim.x) {
+      int i1, i2;
+      interior_node(r, q, i1, i2);
+      const int k = lofs + i1 * p + i2;
+      double t11 = 0, t22 = 0, t1 = 0, t2 = 0;
+      for (int j = 0; j < p; ++j) {
+        const double ux1 = u[j * p + i2], ux2 = u[i1 * p + j];
+        t11 += Dsqsh[i1 * p + j] * ux1;
+        t22 += Dsqsh[i2 * p + j] * ux2;
+        t1 += Dsh[i1 * p + j] * ux1;
+        t2 += Dsh[i2 * p + j] * ux2;
+      }
+      double Au = 0.0;
+      if (co.c11) Au -= co.c11[k] * t11;
+      if (co.c22) Au -= co.c22[k] * t22;
+      if (co.c1) Au -= co.c1[k] * t1;
+      if (co.c2) Au -= co.c2[k] * t2;
+      if (co.c) Au += co.c[k] * u[i1 * p + i2];
+      const double f = a.fbody ? a.fbody[(size_t)k + (size_t)c * a.nleaf * p * p] : 0.0;
+      a.rc[((size_t)leaf * a.nrhs + c) * n + r] = f - Au;
+    }
+    for (int s = tid; s < nx; s += blockDim.x) {
+      const int g = a.leafglob[(size_t)leaf * nx + s];
+      if (a.dirmask[g]) continue;
+      const int f = s / q, t = s % q + 1;
+      double flux = 0.0;
+      // Nx rows: [-D1[Jl]; D1[Jr]; -D2[Jd]; D2[Ju]] with D1 = -kron(D,I), D2 = -kron(I,D)
+      if (f == 0)
+        for (int j = 0; j < p; ++j) flux += Dsh[j] * u[j * p + t];
+      else if (f == 1)
+        for (int j = 0; j < p; ++j) flux -= Dsh[(p - 1) * p + j] * u[j * p + t];
+      else if (f == 2)
+        for (int j = 0; j < p; ++j) flux += Dsh[j] * u[t * p + j];
+      else
+        for (int j = 0; j < p; ++j) flux -= Dsh[(p - 1) * p + j] * u[t * p + j];
+      atomicAdd(&a.rx[g + (size_t)c * a.ntot], -flux);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256) assemble_solution_kernel(AssembleArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double* uxl = reinterpret_cast<double*>(smem_raw);
+  const int p = a.p, q = a.q, n = a.n, nx = a.nx;
+  const int leaf = blockIdx.x, tid = threadIdx.x;
+  const int nr = 4 * (p - 1);
+  const size_t ldo = (size_t)a.nleaf * p * p;
+  for (int c = 0; c < a.nrhs; ++c) {
+    __syncthreads();
+    for (int s = tid; s < nx; s += blockDim.x) uxl[s] = a.ux[a.leafglob[(size_t)leaf * nx + s] + (size_t)c * a.ntot];
+    __syncthreads();
+    double* out = a.out + (size_t)leaf * p * p + c * ldo;
+    for (int t = tid; t < nr; t += blockDim.x) {
+      double v = 0.0;
+      for (int s = 0; s < nx; ++s) v += a.interp[(size_t)t * nx + s] * uxl[s];
+      out[a.jxreorder[t]] = v;
+    }
+    for (int r = tid; r < n; r += blockDim.x) {
+      int i1, i2;
+      interior_node(r, q, i1, i2);
+      out[i1 * p + i2] = a.uc[((size_t)leaf * a.nrhs + c) * n + r];
+    }
+  }
+}
+
+namespace {
+
+__global__ void transpose_out_kernel(const float* in, double* out, int nx, int nleaf) {
+  const long long tot = (long long)nleaf * nx * nx;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < tot; i += (long long)gridDim.x * blockDim.x) {
+    const long long l = i / ((long long)nx * nx);
+    const int rem = (int)(i % ((long long)nx * nx));
+    const int r = rem / nx, c = rem % nx;  // out row-major (r, c)
+    out[i] = (double)in[l * nx * nx + r + (long long)c * nx];
+  }
+}
+__global__ void transpose_out_kernel(const double* in, double* out, int nx, int nleaf) {
+  const long long tot = (long long)nleaf * nx * nx;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < tot; i += (long long)gridDim.x * blockDim.x) {
+    const long long l = i / ((long long)nx * nx);
+    const int rem = (int)(i % ((long long)nx * nx));
+    const int r = rem / nx, c = rem % nx;
+    out[i] = in[l * nx * nx + r + (long long)c * nx];
+  }
+}
+
+// S (column-major n x nx inside G) -> row-major n x nx doubles
+template <typename T>
+__global__ void copy_S_kernel(const T* G, long long strideG, int n, int nx, int nleaf, double* S) {
+  const long long tot = (long long)nleaf * n * nx;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < tot; i += (long long)gridDim.x * blockDim.x) {
+    const long long l = i / ((long long)n * nx);
+    const int rem = (int)(i % ((long long)n * nx));
+    const int r = rem / nx, c = rem % nx;
+    S[i] = (double)G[l * strideG + (long long)n * n + r + (long long)c * n];
+  }
+}
+
+template <typename T>
+size_t leaf_work_bytes(int nleaf, int p) {
+  const int q = p - 2, n = q * q, nx = 4 * q;
+  size_t b = 0;
+  auto add = [&](size_t bytes) { b += (bytes + 255) / 256 * 256; };
+  add((size_t)nleaf * n * (n + nx) * sizeof(T));  // G
+  add((size_t)nleaf * n * sizeof(int));           // pivots
+  add((size_t)nleaf * nx * nx * sizeof(T));       // DtN (T)
+  add((size_t)nx * n * sizeof(T));                // Nxc
+  add((size_t)nx * nx * sizeof(T));               // Nxx
+  return b;
+}
+
+template <typename T>
+int leaf_dtn_impl(int nleaf, int p, const LeafCoeffs& co, const double* D, const double* Dsq, const double* Nx,
+                  void* work, size_t work_bytes, double* dtn_out, double* S_out, int* info, cudaStream_t s) {
+  const int q = p - 2, n = q * q, nx = 4 * q;
+  if (work_bytes < leaf_work_bytes<T>(nleaf, p)) return set_error(SLAB_ERR_ARG, "slab_leaf_dtn: work too small");
+  unsigned char* w = static_cast<unsigned char*>(work);
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    void* ptr = w + off;
+    off += (bytes + 255) / 256 * 256;
+    return ptr;
+  };
+  T* G = static_cast<T*>(take((size_t)nleaf * n * (n + nx) * sizeof(T)));
+  int* piv = static_cast<int*>(take((size_t)nleaf * n * sizeof(int)));
+  T* dtn = static_cast<T*>(take((size_t)nleaf * nx * nx * sizeof(T)));
+  T* Nxc = static_cast<T*>(take((size_t)nx * n * sizeof(T)));
+  T* Nxx = static_cast<T*>(take((size_t)nx * nx * sizeof(T)));
+  split_nx_kernel<T><<<64, 256, 0, s>>>(Nx, p, q, Nxc, Nxx);
+  SLAB_CHECK_LAUNCH();
+  LeafFactorArgs<T> a{};
+  a.p = p; a.q = q; a.n = n; a.nx = nx;
+  a.co = co; a.D = D; a.Dsq = Dsq; a.Nxc = Nxc; a.Nxx = Nxx;
+  a.G = G; a.strideG = (long long)n * (n + nx); a.piv = piv; a.dtn = dtn; a.info = info;
+  a.decouple = 0;
+  SLAB_TRY(leaf_factor<T>(s, a, nleaf));
+  transpose_out_kernel<<<1024, 256, 0, s>>>(dtn, dtn_out, nx, nleaf);
+  SLAB_CHECK_LAUNCH();
+  if (S_out) {
+    copy_S_kernel<T><<<1024, 256, 0, s>>>(G, a.strideG, n, nx, nleaf, S_out);
+    SLAB_CHECK_LAUNCH();
+  }
+  return SLAB_OK;
+}
+
+}  // namespace
+}  // namespace slab
+
+extern "C" size_t slab_leaf_dtn_work_bytes(int nleaf, int p, int precision) {
+  if (nleaf <= 0 || p < 4) return 0;
+  return precision == SLAB_PREC_FP64 ? slab::leaf_work_bytes<double>(nleaf, p)
+                                     : slab::leaf_work_bytes<float>(nleaf, p);
+}
+
+extern "C" int slab_leaf_dtn(int nleaf, int p, const double* c11, const double* c22, const double* c1,
+                             const double* c2, const double* c, const double* D, const double* Dsq,
+                             const double* Nx, int precision, void* work, size_t work_bytes, double* dtn,
+                             double* S, int* info, void* stream) {
+  if (nleaf <= 0 || p < 4 || !D || !Dsq || !Nx || !work || !dtn)
+    return slab::set_error(SLAB_ERR_ARG, "slab_leaf_dtn: invalid argument");
+  if (precision != SLAB_PREC_FP64 && precision != SLAB_PREC_FP32 && precision != SLAB_PREC_MIXED)
+    return slab::set_error(SLAB_ERR_ARG, "slab_leaf_dtn: unknown precision %d", precision);
+  slab::LeafCoeffs co{c11, c22, c1, c2, c};
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (precision == SLAB_PREC_FP64)
+    return slab::leaf_dtn_impl<double>(nleaf, p, co, D, Dsq, Nx, work, work_bytes, dtn, S, info, s);
+  return slab::leaf_dtn_impl<float>(nleaf, p, co, D, Dsq, Nx, work, work_bytes, dtn, S, info, s);
+}

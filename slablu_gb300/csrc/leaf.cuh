@@ -1,0 +1,195 @@
+// Leaf-level kernels of the HPS discretisation (unit-square leaves, c12 = None).
+#pragma once
+
+#include "dense.cuh"
+
+namespace slab {
+
+// Canonical leaf node of interior row r (Jc order) and of face-node column s
+// (Jx = [Jl, Jr, Jd, Ju]); node = i1*p + i2 (src_disc/hps_subdomain_disc.py:105-134).
+__host__ __device__ inline void interior_node(int r, int q, int& i1, int& i2) {
+  i1 = r / q + 1;
+  i2 = r % q + 1;
+}
+__host__ __device__ inline void face_node(int s, int p, int q, int& j1, int& j2) {
+  const int f = s / q, t = s % q + 1;
+  switch (f) {
+    case 0: j1 = 0; j2 = t; break;
+    case 1: j1 = p - 1; j2 = t; break;
+    case 2: j1 = t; j2 = 0; break;
+    default: j1 = t; j2 = p - 1; break;
+  }
+}
+
+struct LeafCoeffs {
+  const double* c11;
+  const double* c22;
+  const double* c1;
+  const double* c2;
+  const double* c;
+};
+
+template <typename T>
+struct LeafFactorArgs {
+  int p, q, n, nx;
+  LeafCoeffs co;            // nleaf*p*p each (offset to the first leaf of the launch) or null
+  const double* D;          // p*p row-major
+  const double* Dsq;        // p*p row-major
+  const T* Nxc;             // nx x n   column-major
+  const T* Nxx;             // nx x nx  column-major
+  T* G;                     // per leaf n x (n+nx) column-major (ld n): LU | S
+  long long strideG;
+  int* piv;                 // per leaf n
+  T* dtn;                   // per leaf nx x nx column-major
+  int* info;                // per leaf
+  int decouple;             // replace Dirichlet-face rows/cols by identity
+  int n0, n1, leaf_begin;   // grid geometry (for decouple)
+};
+
+// Entry (row node k=(i1,i2), column node (j1,j2)) of
+//   Aloc = -c11 D11 - c22 D22 + c1 D1 + c2 D2 + diag(c)
+// accumulated in the reference's term order (src_disc/hps_parallel_leaf_ops.py:17-27).
+__device__ __forceinline__ double aloc_entry(const LeafCoeffs& co, int lofs, int p, int i1, int i2, int j1,
+                                             int j2, const double* D, const double* Dsq) {
+  const int k = lofs + i1 * p + i2;
+  double v = 0.0;
+  if (i2 == j2 && co.c11) v += (-co.c11[k]) * Dsq[i1 * p + j1];
+  if (i1 == j1 && co.c22) v += (-co.c22[k]) * Dsq[i2 * p + j2];
+  if (i2 == j2 && co.c1) v += co.c1[k] * (-D[i1 * p + j1]);
+  if (i1 == j1 && co.c2) v += co.c2[k] * (-D[i2 * p + j2]);
+  if (i1 == j1 && i2 == j2 && co.c) v += co.c[k];
+  return v;
+}
+
+// Dynamic shared memory of leaf_factor_kernel<T> for order p.
+inline size_t leaf_factor_smem_bytes(int p, size_t elem) {
+  const int n = (p - 2) * (p - 2);
+  size_t b = (size_t)getrf_smem_elems(n) * elem;
+  b = (b + 15) / 16 * 16;
+  return b + 2 * (size_t)p * p * sizeof(double);
+}
+
+// One CTA per leaf: assemble [A_cc | A_cx], pivoted LU, S = -A_cc^{-1} A_cx,
+// DtN = Nx[:,Jc] S + Nx[:,Jx] (src_disc/hps_parallel_leaf_ops.py:40-58).
+template <typename T>
+__global__ void __launch_bounds__(kNT) leaf_factor_kernel(LeafFactorArgs<T> a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int tid = threadIdx.x;
+  const int leaf = blockIdx.x;
+  const int p = a.p, q = a.q, n = a.n, nx = a.nx;
+  T* smem = reinterpret_cast<T*>(smem_raw);
+  size_t off = (size_t)getrf_smem_elems(n) * sizeof(T);
+  off = (off + 15) / 16 * 16;
+  double* Dsh = reinterpret_cast<double*>(smem_raw + off);
+  double* Dsqsh = Dsh + p * p;
+  for (int i = tid; i < p * p; i += blockDim.x) {
+    Dsh[i] = a.D[i];
+    Dsqsh[i] = a.Dsq[i];
+  }
+  __syncthreads();
+  T* G = a.G + a.strideG * leaf;
+  const int lofs = leaf * p * p;
+  const int nc = n + nx;
+  for (int idx = tid; idx < n * nc; idx += blockDim.x) {
+    const int r = idx % n, col = idx / n;
+    int i1, i2, j1, j2;
+    interior_node(r, q, i1, i2);
+    if (col < n)
+      interior_node(col, q, j1, j2);
+    else
+      face_node(col - n, p, q, j1, j2);
+    G[idx] = (T)aloc_entry(a.co, lofs, p, i1, i2, j1, j2, Dsh, Dsqsh);
+  }
+  __syncthreads();
+  cta_getrf_aug<T>(G, n, n, nc, a.piv + (size_t)leaf * n, smem, a.info ? a.info + leaf : nullptr);
+  for (int c0 = 0; c0 < nx; c0 += kCT) cta_backsub<T>(G, n, n, n + c0, min(kCT, nx - c0), smem);
+  // DtN = Nxx - Nxc X  (X = A_cc^{-1} A_cx, S = -X)
+  T* dtn = a.dtn + (size_t)leaf * nx * nx;
+  for (int idx = tid; idx < nx * nx; idx += blockDim.x) dtn[idx] = a.Nxx[idx];
+  T* Psm = smem;
+  T* Bt = smem + round_up(n, 4) * kNB + kPad;
+  const int ldq = round_up(nx, 4);
+  const T* X = G + (size_t)n * n;
+  for (int k0 = 0; k0 < n; k0 += kNB) {
+    const int kb = min(kNB, n - k0);
+    __syncthreads();
+    for (int idx = tid; idx < nx * kb; idx += blockDim.x) {
+      const int r = idx % nx, c = idx / nx;
+      Psm[r + c * ldq] = a.Nxc[r + (size_t)(k0 + c) * nx];
+    }
+    for (int idx = tid; idx < kb * nx; idx += blockDim.x) {
+      const int kk = idx % kb, c = idx / kb;
+      Bt[c + kk * kCTLD] = X[(size_t)c * n + k0 + kk];
+    }
+    __syncthreads();
+    cta_gemm_sub(dtn, nx, nx, nx, Psm, ldq, Bt, kCTLD, kb);
+  }
+  __syncthreads();
+  for (int idx = tid; idx < n * nx; idx += blockDim.x) G[(size_t)n * n + idx] = -G[(size_t)n * n + idx];
+  if (a.decouple) {
+    const int gl = a.leaf_begin + leaf;
+    const int I = gl / a.n1, J = gl % a.n1;
+    const bool dir[4] = {I == 0, I == a.n0 - 1, J == 0, J == a.n1 - 1};
+    if (dir[0] || dir[1] || dir[2] || dir[3]) {
+      for (int idx = tid; idx < nx * nx; idx += blockDim.x) {
+        const int r = idx % nx, c = idx / nx;
+        if (dir[r / q] || dir[c / q]) dtn[idx] = r == c ? T(1) : T(0);
+      }
+    }
+  }
+}
+
+template <typename T>
+int leaf_factor(cudaStream_t s, const LeafFactorArgs<T>& a, int nleaf);
+
+// Nx (nx x p^2 row-major, FP64) -> Nxc (nx x n) and Nxx (nx x nx), column-major, in T.
+template <typename T>
+__global__ void split_nx_kernel(const double* Nx, int p, int q, T* Nxc, T* Nxx) {
+  const int nx = 4 * q, n = q * q;
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < nx * (n + nx); idx += gridDim.x * blockDim.x) {
+    const int t = idx % nx, col = idx / nx;
+    int j1, j2;
+    if (col < n) {
+      interior_node(col, q, j1, j2);
+      Nxc[t + (size_t)col * nx] = (T)Nx[(size_t)t * p * p + j1 * p + j2];
+    } else {
+      face_node(col - n, p, q, j1, j2);
+      Nxx[t + (size_t)(col - n) * nx] = (T)Nx[(size_t)t * p * p + j1 * p + j2];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// FP64 residual of the full collocation system, one CTA per leaf.
+struct ResidualArgs {
+  int p, q, n, nx, nleaf, nrhs;
+  long long ntot;
+  LeafCoeffs co;
+  const double* D;
+  const double* Dsq;
+  const int* leafglob;          // nleaf x nx global face-node index of each leaf face node
+  const unsigned char* dirmask; // ntot: 1 on Dirichlet face nodes
+  const double* ux;             // ntot x nrhs
+  const double* uc;             // leaf-major: leaf*n*nrhs + c*n + r
+  const double* fbody;          // (nleaf*p*p) x nrhs column-major, or null
+  double* rc;                   // leaf-major like uc
+  double* rx;                   // ntot x nrhs, accumulated with atomicAdd (caller zeroes)
+};
+
+__global__ void residual_kernel(ResidualArgs a);
+
+// sol_tot assembly: out[(leaf*p*p + k) + c*nleaf*p*p] for every leaf node.
+struct AssembleArgs {
+  int p, q, n, nx, nleaf, nrhs;
+  long long ntot;
+  const int* leafglob;
+  const double* interp;   // 4(p-1) x nx row-major
+  const int* jxreorder;   // 4(p-1)
+  const double* ux;       // ntot x nrhs
+  const double* uc;       // leaf-major
+  double* out;
+};
+
+__global__ void assemble_solution_kernel(AssembleArgs a);
+
+}  // namespace slab

@@ -1,0 +1,138 @@
+"""Python handle on the C-ABI factor-and-solve engine.
+
+Thin ownership wrapper: device arrays are torch tensors (allocation and
+streams only); all arithmetic runs in libslablu_gb300.so.
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+from .hps import Geometry
+
+
+def _col_major(x, rows):
+    """(rows,) or (rows, k) tensor -> storage laid out column-major (k, rows)."""
+    if x.dim() == 1:
+        x = x[:, None]
+    assert x.shape[0] == rows
+    return x.T.contiguous()
+
+
+class SlabEngine:
+    """Factorization of the HPS operator on a ``Geometry`` (see include/slablu_gb300.h)."""
+
+    def __init__(self, geom: Geometry, precision='mixed', stream=None):
+        if precision not in _lib.PREC:
+            raise ValueError(f'precision must be one of {sorted(_lib.PREC)}')
+        if not torch.cuda.is_available():
+            raise RuntimeError('slablu_gb300 needs a CUDA GPU (there is no CPU path)')
+        self.L = _lib.lib()
+        self.geom, self.precision = geom, precision
+        self.stream = stream if stream is not None else torch.cuda.current_stream()
+        ops = geom.ops
+        h = lambda a: np.ascontiguousarray(a, dtype=np.float64)
+        self._host = dict(D=h(ops.D), Dsq=h(ops.Dsq), Nx=h(ops.Nx), interp=h(ops.Interp_mat),
+                          jxr=np.ascontiguousarray(ops.Jxreorder, dtype=np.int32))
+        handle = ctypes.c_void_p()
+        st = self.L.slab_engine_create(ctypes.byref(handle), geom.p, geom.n0, geom.n1, geom.buf,
+                                       _lib.PREC[precision],
+                                       _lib.np_ptr(self._host['D'], ctypes.c_double),
+                                       _lib.np_ptr(self._host['Dsq'], ctypes.c_double),
+                                       _lib.np_ptr(self._host['Nx'], ctypes.c_double),
+                                       _lib.np_ptr(self._host['interp'], ctypes.c_double),
+                                       _lib.np_ptr(self._host['jxr'], ctypes.c_int),
+                                       ctypes.c_void_p(self.stream.cuda_stream))
+        _lib.check(st, 'slab_engine_create')
+        self.h = handle
+        self.ntot = int(self.L.slab_engine_nfaces(self.h))
+        self.nleaf = int(self.L.slab_engine_nleaves(self.h))
+        self.npts = self.nleaf * geom.p * geom.p
+
+    def __del__(self):
+        h = getattr(self, 'h', None)
+        if h is not None and h.value:
+            self.L.slab_engine_destroy(h)
+            self.h = None
+
+    @property
+    def factor_bytes(self):
+        return int(self.L.slab_engine_factor_bytes(self.h))
+
+    def factor(self, c11=None, c22=None, c1=None, c2=None, c=None):
+        """Coefficients: device float64 tensors with nleaf*p*p entries (or None)."""
+        args = []
+        for t in (c11, c22, c1, c2, c):
+            if t is not None:
+                t = t.reshape(-1)
+                assert t.dtype == torch.float64 and t.is_cuda and t.numel() == self.npts and t.is_contiguous()
+            args.append(t)
+        self._coef = args  # keep alive until the factorization has read them
+        st = self.L.slab_engine_factor(self.h, *[_lib.ptr(t) for t in args])
+        return _lib.check(st, 'slab_engine_factor')
+
+    def solve(self, bnd, fbody=None, tol=1e-10, max_iter=20, want_faces=False, allow_noconv=False):
+        """bnd: (ntot,) or (ntot, nrhs) face values (only Dirichlet faces are read).
+
+        Returns (u_leaf (npts, nrhs) device tensor, u_faces or None, iters, stats dict).
+        """
+        dev = bnd.device
+        nrhs = 1 if bnd.dim() == 1 else bnd.shape[1]
+        bnd_cm = _col_major(bnd.to(torch.float64), self.ntot)
+        fb_cm = None if fbody is None else _col_major(fbody.to(torch.float64), self.npts)
+        uleaf = torch.empty(nrhs, self.npts, dtype=torch.float64, device=dev)
+        ufaces = torch.empty(nrhs, self.ntot, dtype=torch.float64, device=dev) if want_faces else None
+        iters = ctypes.c_int(0)
+        stats = (ctypes.c_double * 5)()
+        st = self.L.slab_engine_solve(self.h, nrhs, _lib.ptr(bnd_cm), _lib.ptr(fb_cm), float(tol), int(max_iter),
+                                      _lib.ptr(ufaces), _lib.ptr(uleaf), ctypes.byref(iters), stats)
+        _lib.check(st, 'slab_engine_solve', allow=(_lib.SLAB_ERR_NOCONV,) if allow_noconv else ())
+        info = dict(rel_correction=stats[0], residual=stats[1], residual0=stats[2], resloc=stats[3],
+                    rel_residual=stats[4], converged=(st == _lib.SLAB_OK))
+        return uleaf.T, (None if ufaces is None else ufaces.T), iters.value, info
+
+    def residual(self, ufaces, uint, fbody=None):
+        """FP64 residual of the full collocation system.
+
+        ufaces: (ntot, nrhs); uint: (nleaf, nrhs, (p-2)^2) leaf-major interior values.
+        Returns (r_int like uint, r_faces (ntot, nrhs)).
+        """
+        nrhs = 1 if ufaces.dim() == 1 else ufaces.shape[1]
+        uf = _col_major(ufaces.to(torch.float64), self.ntot)
+        ui = uint.to(torch.float64).contiguous()
+        fb = None if fbody is None else _col_major(fbody.to(torch.float64), self.npts)
+        rint = torch.empty_like(ui)
+        rf = torch.empty_like(uf)
+        st = self.L.slab_engine_residual(self.h, nrhs, _lib.ptr(uf), _lib.ptr(ui), _lib.ptr(fb), _lib.ptr(rint),
+                                         _lib.ptr(rf))
+        _lib.check(st, 'slab_engine_residual')
+        return rint, rf.T
+
+
+def leaf_dtn(coeffs, p, D, Dsq, Nx, precision='fp64', return_S=False):
+    """Batched leaf DtN maps (form_DtNs 'build') through slab_leaf_dtn.
+
+    coeffs: dict of device float64 tensors (nleaf, p*p) for 'c11','c22','c1','c2','c'.
+    Returns DtN (nleaf, 4(p-2), 4(p-2)) float64 on the device (and S if asked).
+    """
+    L = _lib.lib()
+    ref = next(v for v in coeffs.values() if v is not None)
+    nleaf = ref.shape[0]
+    dev = ref.device
+    q = p - 2
+    prec = _lib.PREC[precision]
+    wb = int(L.slab_leaf_dtn_work_bytes(nleaf, p, prec))
+    work = torch.empty(wb, dtype=torch.uint8, device=dev)
+    dtn = torch.empty(nleaf, 4 * q, 4 * q, dtype=torch.float64, device=dev)
+    S = torch.empty(nleaf, q * q, 4 * q, dtype=torch.float64, device=dev) if return_S else None
+    info = torch.zeros(nleaf, dtype=torch.int32, device=dev)
+    t = lambda a: torch.as_tensor(np.ascontiguousarray(a), dtype=torch.float64, device=dev)
+    Dd, Dsqd, Nxd = t(D), t(Dsq), t(Nx)
+    cs = [coeffs.get(k) for k in ('c11', 'c22', 'c1', 'c2', 'c')]
+    cs = [None if c is None else c.to(torch.float64).contiguous() for c in cs]
+    st = L.slab_leaf_dtn(nleaf, p, *[_lib.ptr(c) for c in cs], _lib.ptr(Dd), _lib.ptr(Dsqd), _lib.ptr(Nxd), prec,
+                         _lib.ptr(work), wb, _lib.ptr(dtn), _lib.ptr(S), _lib.ptr(info),
+                         ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    _lib.check(st, 'slab_leaf_dtn')
+    return (dtn, S, info) if return_S else (dtn, info)

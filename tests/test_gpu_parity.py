@@ -1,0 +1,191 @@
+"""GPU parity: the CUDA path (through the C ABI) against the CPU oracle.
+
+Tolerances: FP64 paths agree with the FP64 oracle to 1e-9 relative (different
+but backward-stable pivoted eliminations); mixed/FP32 factorizations are
+refined against the FP64 residual and must reach the same 1e-9.
+"""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import domain as odomain
+from oracle import funcs as ofuncs
+from oracle import leaf as oleaf
+
+pytestmark = pytest.mark.gpu
+
+GOLD = os.path.join(os.path.dirname(__file__), 'golden')
+
+
+@pytest.fixture(scope='module', autouse=True)
+def _gpu():
+    if not torch.cuda.is_available():
+        pytest.fail('GPU tests need CUDA')
+    from slablu_gb300 import build
+    build.build()
+
+
+def _rand_coeffs(nleaf, p, seed, with_first_order=False):
+    rng = np.random.default_rng(seed)
+    n = p * p
+    co = {'c11': 1 + 0.2 * rng.random((nleaf, n)), 'c22': 1 + 0.2 * rng.random((nleaf, n)),
+          'c': -300.0 * (1 + rng.random((nleaf, n)))}
+    if with_first_order:
+        co['c1'] = rng.standard_normal((nleaf, n))
+        co['c2'] = rng.standard_normal((nleaf, n))
+    return co
+
+
+def _dev(co):
+    return {k: (None if v is None else torch.as_tensor(v, device='cuda')) for k, v in co.items()}
+
+
+@pytest.mark.parametrize('p,first_order', [(6, False), (8, True), (12, False), (22, False), (22, True)])
+def test_leaf_dtn_fp64_matches_oracle(p, first_order):
+    from slablu_gb300 import hps, leaf_dtn
+    a = 0.01
+    ops = hps.LeafOps(a, p)
+    ld = oleaf.leaf_disc(a, p)
+    co = _rand_coeffs(37, p, seed=p, with_first_order=first_order)
+    ref, Sref = oleaf.dtn_build(ld, co, return_S=True)
+    dtn, S, info = leaf_dtn(_dev(co), p, ops.D, ops.Dsq, ops.Nx, precision='fp64', return_S=True)
+    assert int(info.abs().sum()) == 0
+    dtn = dtn.cpu().numpy()
+    rel = np.linalg.norm(dtn - ref, axis=(1, 2)) / np.linalg.norm(ref, axis=(1, 2))
+    assert rel.max() < 1e-10, rel.max()
+    relS = np.linalg.norm(S.cpu().numpy() - Sref) / np.linalg.norm(Sref)
+    assert relS < 1e-10
+
+
+def test_leaf_dtn_fp32_accuracy():
+    from slablu_gb300 import hps, leaf_dtn
+    p, a = 22, 0.005
+    ops = hps.LeafOps(a, p)
+    ld = oleaf.leaf_disc(a, p)
+    co = _rand_coeffs(64, p, seed=5)
+    ref = oleaf.dtn_build(ld, co)
+    dtn, info = leaf_dtn(_dev(co), p, ops.D, ops.Dsq, ops.Nx, precision='fp32')
+    rel = np.linalg.norm(dtn.cpu().numpy() - ref, axis=(1, 2)) / np.linalg.norm(ref, axis=(1, 2))
+    assert rel.max() < 2e-4, rel.max()
+
+
+def test_leaf_dtn_matches_reference_golden():
+    """Leaf DtN of the reference's own form_DtNs (p = 22, 32-bump coefficient)."""
+    from slablu_gb300 import hps, leaf_dtn
+    g = np.load(os.path.join(GOLD, 'dtn_p22.npz'))
+    p = int(g['p'])
+    ops = hps.LeafOps(float(g['a']), p)
+    n = g['c'].shape[0]
+    co = {'c11': np.ones((n, p * p)), 'c22': np.ones((n, p * p)), 'c': g['c']}
+    dtn, info = leaf_dtn(_dev(co), p, ops.D, ops.Dsq, ops.Nx, precision='fp64')
+    rel = np.linalg.norm(dtn.cpu().numpy() - g['dtn'], axis=(1, 2)) / np.linalg.norm(g['dtn'], axis=(1, 2))
+    assert rel.max() < 1e-10, rel.max()
+
+
+def _oracle_problem(geom, p, n, kh, bf):
+    a = 1 / (2 * (n / (p - 2)))
+    md = odomain.Multidomain(geom, a, p)
+    part = odomain.SlabPartition(md, 1.0)
+    co = md.coeffs(ofuncs.helmholtz_pdo(lambda x: bf(x, kh)))
+    return a, md, part, co
+
+
+def _engine_solve(geom, p, a, co, bnd_func, precision, xx_active, tol=1e-12):
+    from slablu_gb300 import hps
+    from slablu_gb300.engine import SlabEngine
+    g = hps.Geometry(geom, a, p, 1.0)
+    eng = SlabEngine(g, precision)
+    eng.factor(**{k: (None if v is None else torch.as_tensor(v.ravel(), device='cuda')) for k, v in co.items()})
+    bnd = torch.as_tensor(bnd_func(xx_active), device='cuda')
+    uleaf, ufaces, iters, st = eng.solve(bnd, tol=tol, max_iter=30, want_faces=True)
+    return g, eng, uleaf.cpu().numpy(), ufaces.cpu().numpy(), iters, st
+
+
+CASES = [
+    ([[0, 1], [0, 1]], 8, 48, 30.0),     # 8 x 8 leaves, buf 4, 2 slabs
+    ([[0, 1], [0, 0.5]], 8, 48, 30.0),   # 8 x 4 leaves (rectangle)
+    ([[0, 1], [0, 1]], 6, 28, 20.0),     # 7 x 7 leaves: prime n0 -> buf 7, one slab
+    ([[0, 1], [0, 1]], 8, 72, 45.0),     # 12 x 12 leaves, buf 4, 3 slabs
+]
+
+
+@pytest.mark.parametrize('precision', ['fp64', 'mixed', 'fp32'])
+@pytest.mark.parametrize('case', range(len(CASES)))
+def test_engine_matches_sparse_direct_oracle(case, precision):
+    geom, p, n, kh = CASES[case]
+    a, md, part, co = _oracle_problem(geom, p, n, kh, ofuncs.bfield_gaussian_bumps)
+    ud = lambda x: ofuncs.uu_dir_greens(x, kh)
+    out = odomain.solve_full(md, part, co, ud)
+    _, eng, uleaf, ufaces, iters, st = _engine_solve(geom, p, a, co, ud, precision, md.xx_active)
+    assert st['converged']
+    ref = out['sol_tot'][:, 0]
+    rel = np.linalg.norm(uleaf[:, 0] - ref) / np.linalg.norm(ref)
+    assert rel < 1e-9, (rel, iters, st)
+    relf = np.linalg.norm(ufaces[:, 0] - out['sol_faces'][:, 0]) / np.linalg.norm(out['sol_faces'])
+    assert relf < 1e-9
+    if precision == 'fp64':
+        assert iters <= 3
+
+
+def test_residual_of_oracle_solution_vanishes():
+    geom, p, n, kh = CASES[0]
+    a, md, part, co = _oracle_problem(geom, p, n, kh, ofuncs.bfield_gaussian_bumps)
+    ud = lambda x: ofuncs.uu_dir_greens(x, kh)
+    out = odomain.solve_full(md, part, co, ud)
+    from slablu_gb300 import hps
+    from slablu_gb300.engine import SlabEngine
+    g = hps.Geometry(geom, a, p, 1.0)
+    eng = SlabEngine(g, 'fp64')
+    eng.factor(**{k: (None if v is None else torch.as_tensor(v.ravel(), device='cuda')) for k, v in co.items()})
+    # interior values of the oracle solution, leaf-major
+    uleaf = out['sol_tot'].reshape(md.nboxes, p * p)
+    uint = torch.as_tensor(uleaf[:, md.ld.Jc][:, None, :], device='cuda')
+    uf = torch.as_tensor(out['sol_faces'], device='cuda')
+    rint, rf = eng.residual(uf, uint)
+    A = oleaf.aloc(md.ld, co)
+    scale = np.abs(A).max() * np.abs(uleaf).max()
+    # the reference recovers interiors exactly; faces balance fluxes
+    assert float(rint.abs().max()) < 1e-9 * scale
+    assert float(rf.abs().max()) < 1e-9 * scale
+
+
+@pytest.mark.parametrize('precision', ['fp64', 'mixed'])
+def test_domain_solver_reference_known_answer(precision):
+    """Reference test tests/test_2d.py (square): p=22, n=400, ppw=40, trueres < 2e-5,
+    and the solution vector of the reference run (golden fixture)."""
+    import slablu_gb300 as sg
+    g = np.load(os.path.join(GOLD, 'slablu_p22_n400_ppw40.npz'))
+    p, n, kh = int(g['p']), int(g['n']), float(g['kh'])
+    op = sg.pdo.PDO_2d(sg.pdo.ones, sg.pdo.ones, c=lambda xx: sg.built_in_funcs.bfield_constant(xx, kh))
+    a = 1 / (2 * (n / (p - 2)))
+    dom = sg.Domain_Solver(torch.tensor([[0, 1.0], [0, 1.0]]), op, kh, a, p=p, buf_constant=1.0,
+                           precision=precision)
+    dom.build('reduced_gpu', 'slabLU', verbose=False)
+    uu = lambda xx: sg.built_in_funcs.uu_dir_func_greens(xx, kh)
+    sol, rel, tres, rloc, toc = dom.solve(uu, None, known_sol=True)
+    assert float(tres) < 2e-5
+    assert abs(float(tres) - float(g['trueres'])) < 1e-3 * float(g['trueres'])
+    sol = sol.numpy()
+    stride = int(g['stride'])
+    assert np.linalg.norm(sol[::stride] - g['sol_sub']) / np.linalg.norm(g['sol_sub']) < 1e-8
+    assert float(rel) < 1e-10
+
+
+def test_domain_solver_reference_config1_solution():
+    """p=12, n=400 (40 x 40 leaves, 8 slabs), constant Helmholtz at 10 ppw vs the reference run."""
+    import slablu_gb300 as sg
+    g = np.load(os.path.join(GOLD, 'slablu_p12_n400_ppw10.npz'))
+    p, n, kh = int(g['p']), int(g['n']), float(g['kh'])
+    op = sg.pdo.PDO_2d(sg.pdo.ones, sg.pdo.ones, c=lambda xx: sg.built_in_funcs.bfield_constant(xx, kh))
+    a = 1 / (2 * (n / (p - 2)))
+    dom = sg.Domain_Solver(torch.tensor([[0, 1.0], [0, 1.0]]), op, kh, a, p=p, buf_constant=1.0,
+                           precision='mixed')
+    dom.build('reduced_gpu', 'slabLU', verbose=False)
+    sol, rel, tres, rloc, toc = dom.solve(lambda xx: sg.built_in_funcs.uu_dir_func_greens(xx, kh), None,
+                                          known_sol=True)
+    sol = sol.numpy()
+    stride = int(g['stride'])
+    assert np.linalg.norm(sol[::stride] - g['sol_sub']) / np.linalg.norm(g['sol_sub']) < 1e-8
+    assert abs(float(tres) - float(g['trueres'])) < 1e-4 * float(g['trueres'])
