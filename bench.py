@@ -1,0 +1,332 @@
+"""Benchmark: unknowns/s of SlabLU factor+solve on one GB300.
+
+Workload (our arm): the N = 4,404,000 problem (p = 22, n = 2000: 100 x 100
+leaves, 10 slabs of 10 leaf columns), variable-coefficient Helmholtz with a
+Gaussian-lattice scatterer (spacing 0.04, width 0.005, amplitude 1, seeded
+offset), kh for 10 points per wavelength, Dirichlet u = 1.  One step = build
+(leaf DtN, slab elimination, FP64 interface block LU) + solve with FP64
+iterative refinement, mixed precision (FP32 leaf/slab factors, FP64
+interface).  Validity: the mixed-precision solution must agree with the
+all-FP64 GPU solution to <= 1e-6 relative error (checked every run).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the reference algorithm's CPU implementation (the
+oracle port of src_solver/slablu_solver.py) on the host cores.
+Prints one JSON line.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = 'unknowns/sec factor+solve at N~4M p=22, mixed-prec vs FP64 GPU at 1e-6 rel err'
+P, NSIDE = 22, 2000
+CPU_SAMPLE_N = 400
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=5)
+    ap.add_argument('--warmup', type=int, default=3)
+    ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
+    ap.add_argument('--n', type=int, default=NSIDE, help='points per side (p-2 divides it)')
+    ap.add_argument('--tol', type=float, default=1e-8, help='refinement tolerance (relative correction)')
+    ap.add_argument('--fp64-steps', type=int, default=1, help='timed steps of the all-FP64 path')
+    ap.add_argument('--no-cpu-baseline', action='store_true')
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get('RANK', '0'))
+    world = int(os.environ.get('WORLD_SIZE', '1'))
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    return rank, world, local
+
+
+# ---------------------------------------------------------------------------
+# CPU arm: the reference algorithm (oracle port) on the host cores.
+def cpu_sample(seconds_hint=None):
+    """One factor+solve of the same field at n = 400 (N = 176,800) with the
+    oracle port of the reference slabLU (all host threads)."""
+    import torch
+    from oracle import domain, funcs
+    from slablu_gb300 import problems
+    p, n = P, CPU_SAMPLE_N
+    kh = problems.kh_for(n, 10)
+    a = problems.leaf_half_width(n, p)
+    md = domain.Multidomain([[0, 1], [0, 1]], a, p)
+    part = domain.SlabPartition(md, 1.0)
+    cf = lambda x: (-(kh ** 2) * (1 - problems.lattice_b(torch.as_tensor(x), 0))).numpy()
+    co = md.coeffs(funcs.helmholtz_pdo(cf))
+    _, t = domain.slablu_pipeline(md, part, co, lambda x: np.ones((x.shape[0], 1)))
+    N = (p - 2) * (p * md.n0 * md.n1 + md.n0 + md.n1)
+    return N, t
+
+
+def cpu_threads():
+    try:
+        from threadpoolctl import threadpool_info
+        return max(int(i.get('num_threads', 1)) for i in threadpool_info())
+    except Exception:
+        return os.cpu_count() or 1
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if world > 1 and rank != 0:
+        return
+    times = []
+    N = None
+    for i in range(args.warmup + args.steps):
+        N, t = cpu_sample()
+        if i >= args.warmup:
+            times.append(t['total'])
+    tmean = sum(times) / len(times)
+    val = N / tmean
+    cores = cpu_threads()
+    line = dict(metric=METRIC, value=val, unit='unknowns/s', n_gpus=0, steps=args.steps, warmup=args.warmup,
+                ms_per_step=1e3 * tmean, higher_is_better=True, scaling='weak', vs_baseline=None, dtype='f64',
+                data='synthetic', impl='reference',
+                config=dict(workload=f'oracle port of reference CPU slabLU, p=22, n={CPU_SAMPLE_N} sample of the '
+                                     'Gaussian-lattice Helmholtz field (N=176,800)', parallelism='host threads'),
+                cpu_baseline=dict(value=val, unit='unknowns/s', cores=cores, kind='port',
+                                  sample=f'full factor+solve at n={CPU_SAMPLE_N} (N={N}) per step'),
+                e2e=dict(value=val, unit='unknowns/s', h2d_bytes_per_step=0, d2h_bytes_per_step=0))
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    QUERY = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
+             'clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,'
+             'clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix='.csv')
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(['nvidia-smi', '-i', str(self.index), f'--query-gpu={self.QUERY}',
+                                          '--format=csv,noheader,nounits', '-lms', '200'],
+                                         stdout=open(self.path, 'w'), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        try:
+            for line in open(self.path):
+                f = [x.strip() for x in line.split(',')]
+                if len(f) < 9:
+                    continue
+                try:
+                    sm.append(float(f[1]))
+                    smax = float(f[2])
+                except ValueError:
+                    continue
+                for name, v in zip(('hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap'),
+                                   f[5:9]):
+                    if v.lower() == 'active':
+                        reasons.add(name)
+        except Exception:
+            pass
+        finally:
+            if self.path and os.path.exists(self.path):
+                os.remove(self.path)
+        return dict(sm_mhz=statistics.median(sm) if sm else None, sm_max_mhz=smax, reasons=sorted(reasons),
+                    samples=len(sm))
+
+
+def leaf_flops(p):
+    """Algorithmic flops of one leaf: LU of A_cc, 4(p-2) solves, DtN product."""
+    q = p - 2
+    n, nx = q * q, 4 * q
+    return 2 / 3 * n ** 3 + 2 * n * n * nx + 2 * nx * n * nx
+
+
+def iface_flops(npan, nI):
+    """FP64 interface block LU: per step LU + S^{-1} sup + Schur GEMM."""
+    return npan * (2 / 3 * nI ** 3) + (npan - 1) * (2 * nI ** 3 + 2 * nI ** 3) if npan > 0 else 0
+
+
+def run_ours(args):
+    import torch
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group('nccl')
+    dev = torch.device('cuda', local if world > 1 else 0)
+    from slablu_gb300 import _lib, hps, problems
+    from slablu_gb300.engine import SlabEngine
+    L = _lib.lib()
+    cfg = problems.config3()
+    p, n = cfg['p'], args.n
+    g = hps.Geometry([[0, 1], [0, 1]], problems.leaf_half_width(n, p), p, 1.0)
+    N = g.N_reported
+    xx = torch.as_tensor(g.xx_tot, device=dev)
+    c = cfg['c'](xx).contiguous()
+    one = torch.ones_like(c)
+    bnd = torch.ones(g.ntot, dtype=torch.float64, device=dev)
+
+    # ---- validity and the plain FP64 GPU path --------------------------------
+    e64 = SlabEngine(g, 'fp64')
+    e64.factor(c11=one, c22=one, c=c)
+    u64, _, it64, st64 = e64.solve(bnd, tol=1e-12, max_iter=10, allow_noconv=True)
+    fp64_times = []
+    for _ in range(args.fp64_steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e64.factor(c11=one, c22=one, c=c)
+        e64.solve(bnd, tol=args.tol, max_iter=10, allow_noconv=True)
+        torch.cuda.synchronize()
+        fp64_times.append(time.perf_counter() - t0)
+    tim64 = e64.timings()
+    u64 = u64[:, 0].clone()
+    del e64
+    torch.cuda.empty_cache()
+
+    eng = SlabEngine(g, 'mixed')
+    stream = eng.stream
+
+    def step():
+        eng.factor(c11=one, c22=one, c=c)
+        return eng.solve(bnd, tol=args.tol, max_iter=30)
+
+    for _ in range(args.warmup):
+        u, _, iters, st = step()
+    rel_err = float(torch.linalg.norm(u[:, 0] - u64) / torch.linalg.norm(u64))
+
+    # ---- timed region: K steps, device time with CUDA events ------------------
+    leaf_ms, iface_ms, tree_ms, apply_ms, napply = [], [], [], [], []
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    launches0 = L.slab_launch_count()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(dev.index or 0) as clk:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            u, _, iters, st = step()
+            tm = eng.timings()
+            leaf_ms.append(tm['leaf_ms']); tree_ms.append(tm['tree_ms']); iface_ms.append(tm['interface_ms'])
+            apply_ms.append(tm['apply_ms']); napply.append(tm['n_apply'])
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    launches = L.slab_launch_count() - launches0
+    t_total = ev0.elapsed_time(ev1) / 1e3
+    if world > 1:
+        import torch.distributed as dist
+        tt = torch.tensor([t_total], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_total = float(tt)
+    clocks = clk.summary()
+    value = N * args.steps * world / t_total
+
+    # ---- end-to-end through the C ABI with host buffers -----------------------
+    hc = c.cpu().pin_memory()
+    h1 = one.cpu().pin_memory()
+    hb = bnd.cpu().pin_memory()
+    hout = torch.empty(eng.npts, dtype=torch.float64).pin_memory()
+    e2e_times = []
+    for i in range(2):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        dc, d1, db = hc.to(dev, non_blocking=True), h1.to(dev, non_blocking=True), hb.to(dev, non_blocking=True)
+        eng.factor(c11=d1, c22=d1, c=dc)
+        ue, _, _, _ = eng.solve(db, tol=args.tol, max_iter=30)
+        hout.copy_(ue[:, 0])
+        torch.cuda.synchronize()
+        e2e_times.append(time.perf_counter() - t0)
+    h2d = 3 * hc.numel() * 8 + hb.numel() * 8
+    d2h = hout.numel() * 8
+
+    # ---- roofline of the leaf kernel (one launch per step) --------------------
+    lf = leaf_flops(p) * g.nboxes
+    leaf_avg = sum(leaf_ms) / len(leaf_ms) / 1e3
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, 'MEASURED_PEAKS.json')))
+    except Exception:
+        pass
+    bf16 = peaks.get('bf16_tflops')
+    peak = bf16 if bf16 else 1900.0
+    achieved = lf / leaf_avg / 1e12
+    iface_avg = sum(iface_ms) / len(iface_ms) / 1e3
+    if_fl = iface_flops(g.Npan - 1, g.n1 * g.q)
+
+    line = dict(
+        metric=METRIC, value=value, unit='unknowns/s', n_gpus=world, steps=args.steps, warmup=args.warmup,
+        ms_per_step=1e3 * t_total / args.steps, higher_is_better=True, scaling='weak', vs_baseline=None,
+        dtype='f32+f64', data='synthetic',
+        config=dict(workload=f'HPS SlabLU p={p} n={n} ({g.n0}x{g.n1} leaves, N={N}), Gaussian-lattice Helmholtz '
+                             f'kh={cfg["kh"]:.1f}, u=1 Dirichlet; mixed precision + FP64 refinement to tol '
+                             f'{args.tol:g}', buf=g.buf, Npan=g.Npan, parallelism='replicas' if world > 1 else 'single GPU',
+                    l2='inputs and factors (~17 GB) larger than L2; no flush'),
+        rel_err_vs_fp64=rel_err, refine_iters=int(iters), fp64_iters=int(it64),
+        fp64_value=N / (sum(fp64_times) / len(fp64_times)),
+        speedup_vs_fp64=(N / (t_total / args.steps)) / (N / (sum(fp64_times) / len(fp64_times))),
+        phases_ms=dict(leaf=leaf_avg * 1e3, tree=sum(tree_ms) / len(tree_ms), interface=iface_avg * 1e3,
+                       solve_applications=sum(apply_ms) / len(apply_ms), applications=sum(napply) / len(napply),
+                       fp64_leaf=tim64['leaf_ms'], fp64_tree=tim64['tree_ms'], fp64_interface=tim64['interface_ms']),
+        interface_fp64_tflops=if_fl / iface_avg / 1e12,
+        roofline=dict(kernel='leaf_factor_kernel<float> (one launch per step)', bound='tensor', achieved=achieved,
+                      peak=peak, unit='TFLOP/s', frac=achieved / peak, traffic=None,
+                      peak_source='MEASURED_PEAKS.json bf16_tflops (measured)' if bf16 else 'fallback 1.9 PF bf16',
+                      algorithmic_flops_per_launch=lf),
+        clocks=clocks,
+        e2e=dict(value=N / (sum(e2e_times) / len(e2e_times)), unit='unknowns/s', h2d_bytes_per_step=h2d,
+                 d2h_bytes_per_step=d2h),
+        gpu_launches=int(launches),
+    )
+    if rank == 0 and not args.no_cpu_baseline:
+        Nc, tc = cpu_sample()
+        line['cpu_baseline'] = dict(value=Nc / tc['total'], unit='unknowns/s', cores=cpu_threads(), kind='port',
+                                    sample=f'oracle port of the reference CPU slabLU, full factor+solve of the same '
+                                           f'field at n={CPU_SAMPLE_N} (N={Nc}), {tc["total"]:.1f} s')
+    if rel_err > 1e-6:
+        line['invalid'] = f'mixed vs FP64 relative error {rel_err:.2e} > 1e-6'
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == 'reference':
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == '__main__':
+    main()

@@ -130,6 +130,16 @@ int slab_engine_residual(slab_engine* e, int nrhs, const double* d_ufaces, const
 /* Bytes of device memory held by the engine's factorization. */
 size_t slab_engine_factor_bytes(const slab_engine* e);
 
+/* Device times (CUDA events on the engine stream, milliseconds) of the last
+ * factor and solve: [0] leaf kernel, [1] slab merge tree, [2] interface block
+ * LU, [3] whole solve, [4] sum of the factorization applications inside the
+ * solve, [5] number of those applications.  Writes min(n, 6) values and
+ * returns that count. */
+int slab_engine_timings(const slab_engine* e, double* h_ms, int n);
+
+/* Number of kernel launches issued by the library since it was loaded. */
+long long slab_launch_count(void);
+
 #ifdef __cplusplus
 }
 #endif

@@ -315,3 +315,22 @@ class SlabLU:
         g = fC - self.A[pt.I_slabC][:, pt.I_slabX] @ uX
         uC = np.concatenate([self.slab_solve(s, g[s * nC:(s + 1) * nC]) for s in range(pt.Npan)])
         return np.concatenate((uC, uX))
+
+
+def slablu_pipeline(md, part, co, u_dir_func):
+    """Reference CPU slabLU end to end, timed like the reference driver
+    (argparse_driver.py:169-170, 250-258): leaf DtNs + assembly, two-level slab
+    build, solve with leaf recovery.  Returns (leaf-node solution, timings dict)."""
+    import time
+    t0 = time.perf_counter()
+    A = md.sparse_mat(leafmod.dtn_build(md.ld, co))
+    t1 = time.perf_counter()
+    S = SlabLU(md, part, A)
+    t2 = time.perf_counter()
+    u_dir = np.asarray(u_dir_func(md.xx_active[part.I_Xtot]), dtype=float).reshape(-1, 1)
+    ff = dirichlet_rhs(A, part, u_dir)
+    x = S.solve(ff)
+    sol = assemble_solution(md, part, x, u_dir)
+    u_tot, _ = leaf_recover(md, co, sol)
+    t3 = time.perf_counter()
+    return u_tot, dict(assembly=t1 - t0, build=t2 - t1, solve=t3 - t2, total=t3 - t0)

@@ -35,6 +35,8 @@ _SIGS = {
     'slab_engine_solve': (c_int, [c_void, c_int, c_void, c_void, c_double, c_int, c_void, c_void, P_int, P_double]),
     'slab_engine_residual': (c_int, [c_void, c_int] + [c_void] * 5),
     'slab_engine_factor_bytes': (c_size, [c_void]),
+    'slab_engine_timings': (c_int, [c_void, P_double, c_int]),
+    'slab_launch_count': (c_ll, []),
 }
 
 

@@ -21,7 +21,14 @@ int set_error(int status, const char* fmt, ...);
                                #expr, cudaGetErrorString(e_));                     \
   } while (0)
 
-#define SLAB_CHECK_LAUNCH() SLAB_CUDA_TRY(cudaGetLastError())
+// Every kernel launch of the library is followed by SLAB_CHECK_LAUNCH(), which
+// also counts it (slab_launch_count()).
+void count_launch();
+#define SLAB_CHECK_LAUNCH()            \
+  do {                                 \
+    ::slab::count_launch();            \
+    SLAB_CUDA_TRY(cudaGetLastError()); \
+  } while (0)
 
 #define SLAB_TRY(expr)                 \
   do {                                 \

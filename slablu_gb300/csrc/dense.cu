@@ -1,5 +1,7 @@
 // Host launchers for the dense building blocks (float and double).
+#include <atomic>
 #include <cstdarg>
+#include <map>
 #include <mutex>
 #include <string>
 
@@ -9,7 +11,12 @@ namespace slab {
 
 namespace {
 thread_local std::string g_last_error;
+std::atomic<long long> g_launches{0};
 }
+
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+long long launch_count() { return g_launches.load(std::memory_order_relaxed); }
+void add_launches(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
 int set_error(int status, const char* fmt, ...) {
   char buf[1024];
@@ -32,6 +39,26 @@ size_t smem_limit_bytes() {
     v = optin > 0 ? (size_t)optin : 48 * 1024;
   }
   return v;
+}
+
+size_t allow_dynamic_smem(const void* kernel) {
+  static std::mutex mu;
+  static std::map<const void*, size_t> done;
+  std::lock_guard<std::mutex> lock(mu);
+  auto it = done.find(kernel);
+  if (it != done.end()) return it->second;
+  cudaFuncAttributes fa{};
+  if (cudaFuncGetAttributes(&fa, kernel) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  const size_t lim = smem_limit_bytes() > fa.sharedSizeBytes ? smem_limit_bytes() - fa.sharedSizeBytes : 0;
+  if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lim) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  done[kernel] = lim;
+  return lim;
 }
 
 __global__ void perm_from_ipiv_kernel(const int* ipiv, int n, int* perm) {
@@ -68,6 +95,26 @@ int gemm(cudaStream_t s, int m, int n, int k, T alpha, const T* A, const long lo
     }
     return SLAB_OK;
   }
+  if (n <= 16) {
+    dim3 g(ceil_div(m, 256), 1, batch);
+    const int kk = k < 0 ? 0 : k;
+#define SLAB_NARROW(NC)                                                                                     \
+  gemm_narrow_kernel<T, NC><<<g, 256, 0, s>>>(m, n, kk, alpha, A, offA, strideA, lda, B, offB, strideB, ldb, \
+                                              beta, C, offC, strideC, ldc)
+    if (n <= 1)
+      SLAB_NARROW(1);
+    else if (n <= 2)
+      SLAB_NARROW(2);
+    else if (n <= 4)
+      SLAB_NARROW(4);
+    else if (n <= 8)
+      SLAB_NARROW(8);
+    else
+      SLAB_NARROW(16);
+#undef SLAB_NARROW
+    SLAB_CHECK_LAUNCH();
+    return SLAB_OK;
+  }
   // k == 0 leaves the k loop empty: C = beta*C
   dim3 grid(ceil_div(m, 64), ceil_div(n, 64), batch);
   gemm_kernel<T><<<grid, 256, 0, s>>>(m, n, k < 0 ? 0 : k, alpha, A, offA, strideA, lda, B, offB, strideB, ldb,
@@ -81,10 +128,7 @@ int getrf_batched(cudaStream_t s, int n, int nc, T* A, const long long* offA, lo
                   int* piv, const long long* offP, long long strideP, int* info, int batch) {
   if (n <= 0 || batch <= 0) return SLAB_OK;
   const size_t bytes = (size_t)getrf_smem_elems(n) * sizeof(T);
-  if (bytes > smem_limit_bytes())
-    return set_error(SLAB_ERR_ARG, "getrf_batched: order %d needs %zu bytes of shared memory", n, bytes);
-  SLAB_CUDA_TRY(cudaFuncSetAttribute(getrf_batched_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)bytes));
+  SLAB_TRY(ensure_smem(getrf_batched_kernel<T>, bytes, "getrf_batched"));
   getrf_batched_kernel<T><<<batch, kNT, bytes, s>>>(n, nc, A, offA, strideA, lda, piv, offP, strideP, info);
   SLAB_CHECK_LAUNCH();
   return SLAB_OK;
@@ -95,12 +139,12 @@ int getrs_batched(cudaStream_t s, int n, int nrhs, const T* LU, const long long*
                   int lda, const int* piv, const long long* offP, long long strideP, T* B,
                   const long long* offB, long long strideB, int ldb, int batch, bool lower, bool upper) {
   if (n <= 0 || nrhs <= 0 || batch <= 0) return SLAB_OK;
-  const size_t limit = smem_limit_bytes();
-  const int tile = getrs_tile_cols(n, sizeof(T), limit);
+  const size_t limit = allow_dynamic_smem(reinterpret_cast<const void*>(getrs_batched_kernel<T>));
+  int tile = getrs_tile_cols(n, sizeof(T), limit);
+  if (tile > round_up(nrhs, 4)) tile = round_up(nrhs, 4);  // do not reserve unused columns
   if (tile <= 0) return set_error(SLAB_ERR_ARG, "getrs_batched: order %d too large for shared memory", n);
   const size_t bytes = (size_t)getrs_smem_elems(n, tile) * sizeof(T);
-  SLAB_CUDA_TRY(cudaFuncSetAttribute(getrs_batched_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)bytes));
+  SLAB_TRY(ensure_smem(getrs_batched_kernel<T>, bytes, "getrs_batched"));
   const int ntiles = ceil_div(nrhs, tile);
   if (ntiles > 65535) return set_error(SLAB_ERR_ARG, "getrs_batched: %d right-hand sides is too many", nrhs);
   dim3 grid(batch, ntiles);

@@ -150,6 +150,36 @@ __device__ void cta_gemm_sub(T* C, int ldc, int mrows, int ncols, const T* As, i
   }
 }
 
+// Narrow variant of cta_gemm_sub for few columns (ncols <= 16): one thread per
+// row, no wasted lanes.  Same operand layout; no over-read.
+template <typename T>
+__device__ void cta_gemm_sub_narrow(T* C, int ldc, int mrows, int ncols, const T* As, int lda, const T* Bs,
+                                    int ldb, int kd) {
+  for (int r = threadIdx.x; r < mrows; r += blockDim.x) {
+    T acc[16];
+#pragma unroll
+    for (int c = 0; c < 16; ++c) acc[c] = T(0);
+    for (int kk = 0; kk < kd; ++kk) {
+      const T a = As[r + kk * lda];
+#pragma unroll
+      for (int c = 0; c < 16; ++c)
+        if (c < ncols) acc[c] += a * Bs[c + kk * ldb];
+    }
+#pragma unroll
+    for (int c = 0; c < 16; ++c)
+      if (c < ncols) C[r + (size_t)c * ldc] -= acc[c];
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void cta_update(T* C, int ldc, int mrows, int ncols, const T* As, int lda, const T* Bs,
+                                           int ldb, int kd) {
+  if (ncols <= 16)
+    cta_gemm_sub_narrow(C, ldc, mrows, ncols, As, lda, Bs, ldb, kd);
+  else
+    cta_gemm_sub(C, ldc, mrows, ncols, As, lda, Bs, ldb, kd);
+}
+
 // Shared-memory footprint (elements of T) of cta_getrf_aug / cta_backsub for order n.
 __host__ __device__ inline int getrf_smem_elems(int n) {
   return round_up(n, 4) * kNB + kPad + kCTLD * kNB + kPad;
@@ -266,7 +296,7 @@ __device__ void cta_backsub(T* A, int lda, int n, int c0, int nr, T* smem) {
       const int kk = idx % nb, c = idx / nb;
       Y[(size_t)c * lda + k0 + kk] = Bt[c + kk * kCTLD];
     }
-    if (k0 > 0) cta_gemm_sub(Y, lda, k0, nr, Psm, ldq, Bt, kCTLD, nb);
+    if (k0 > 0) cta_update(Y, lda, k0, nr, Psm, ldq, Bt, kCTLD, nb);
   }
   __syncthreads();
 }
@@ -316,7 +346,7 @@ __device__ void cta_getrs_smem(const T* LU, int lda, int n, const int* ipiv, T* 
           Bt[c + kk * kCTLD] = Bsm[(size_t)c * ldbs + k0 + kk];
         }
         __syncthreads();
-        cta_gemm_sub(Bsm + k0 + nb, ldbs, m - nb, ncols, Psm + nb, ldq, Bt, kCTLD, nb);
+        cta_update(Bsm + k0 + nb, ldbs, m - nb, ncols, Psm + nb, ldq, Bt, kCTLD, nb);
       }
     }
   }
@@ -347,7 +377,7 @@ __device__ void cta_getrs_smem(const T* LU, int lda, int n, const int* ipiv, T* 
           Bt[c + kk * kCTLD] = Bsm[(size_t)c * ldbs + k0 + kk];
         }
         __syncthreads();
-        cta_gemm_sub(Bsm, ldbs, k0, ncols, Psm, ldq, Bt, kCTLD, nb);
+        cta_update(Bsm, ldbs, k0, ncols, Psm, ldq, Bt, kCTLD, nb);
       }
     }
   }
@@ -476,6 +506,52 @@ __global__ void __launch_bounds__(256) gemm_kernel(int m, int n, int k, T alpha,
       if (r >= m) continue;
       T* cp = C + r + (size_t)c * ldc;
       *cp = (beta == T(0) ? T(0) : beta * *cp) + alpha * acc[i][j];
+    }
+  }
+}
+
+// Narrow GEMM (n <= NC columns): one thread per row of C, B staged in shared
+// memory; reads A once (memory-bound shape of the solve phase).
+// grid (ceil(m/256), 1, batch).
+template <typename T, int NC>
+__global__ void __launch_bounds__(256) gemm_narrow_kernel(int m, int n, int k, T alpha, const T* __restrict__ A,
+                                                         const long long* offA, long long strideA, int lda,
+                                                         const T* __restrict__ B, const long long* offB,
+                                                         long long strideB, int ldb, T beta, T* C,
+                                                         const long long* offC, long long strideC, int ldc) {
+  constexpr int KC = 128;
+  __shared__ T Bs[KC * NC];
+  const int bz = blockIdx.z;
+  A += batch_off(offA, strideA, bz);
+  B += batch_off(offB, strideB, bz);
+  C += batch_off(offC, strideC, bz);
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  T acc[NC];
+#pragma unroll
+  for (int c = 0; c < NC; ++c) acc[c] = T(0);
+  for (int k0 = 0; k0 < k; k0 += KC) {
+    const int kc = min(KC, k - k0);
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < KC * NC; idx += blockDim.x) {
+      const int kk = idx % KC, c = idx / KC;
+      Bs[c * KC + kk] = (kk < kc && c < n) ? B[(k0 + kk) + (size_t)c * ldb] : T(0);
+    }
+    __syncthreads();
+    if (r < m) {
+      const T* ap = A + r + (size_t)k0 * lda;
+      for (int kk = 0; kk < kc; ++kk) {
+        const T a = ap[(size_t)kk * lda];
+#pragma unroll
+        for (int c = 0; c < NC; ++c) acc[c] += a * Bs[c * KC + kk];
+      }
+    }
+  }
+  if (r < m) {
+#pragma unroll
+    for (int c = 0; c < NC; ++c) {
+      if (c >= n) break;
+      T* cp = C + r + (size_t)c * ldc;
+      *cp = (beta == T(0) ? T(0) : beta * *cp) + alpha * acc[c];
     }
   }
 }
@@ -636,5 +712,17 @@ int bigtrs(cudaStream_t s, const T* LU, int lda, int n, const int* perm, const T
 int build_perm(cudaStream_t s, const int* ipiv, int n, int* perm);
 
 size_t smem_limit_bytes();
+
+// Raise a kernel's dynamic shared-memory limit to the device maximum (minus its
+// static shared memory), once.  The limit is never lowered: CUDA graphs that
+// captured a larger launch stay valid.  Returns the dynamic bytes allowed.
+size_t allow_dynamic_smem(const void* kernel);
+
+template <typename K>
+int ensure_smem(K* kernel, size_t bytes, const char* what) {
+  const size_t lim = allow_dynamic_smem(reinterpret_cast<const void*>(kernel));
+  if (bytes > lim) return set_error(SLAB_ERR_ARG, "%s needs %zu bytes of shared memory (limit %zu)", what, bytes, lim);
+  return SLAB_OK;
+}
 
 }  // namespace slab

@@ -24,6 +24,7 @@
 // Refinement: FP64 residual of the full collocation system, corrections from
 // the (possibly FP32) factorization, until ||du|| <= tol ||u||.
 #include <algorithm>
+#include <cstdlib>
 #include <cmath>
 #include <map>
 #include <memory>
@@ -35,6 +36,8 @@
 namespace slab {
 
 const char* last_error();
+long long launch_count();
+void add_launches(long long n);
 
 // ---------------------------------------------------------------------------
 // Device memory owner.
@@ -276,13 +279,19 @@ struct EngineBase {
   virtual int residual(int nrhs, const double* ufaces, const double* uint, const double* fbody, double* rint,
                        double* rfaces) = 0;
   virtual size_t factor_bytes() const = 0;
+  virtual double timing(int i) const = 0;
   long long ntot = 0, nleaf = 0;
 };
 
 template <typename T, typename TI>
 struct EngineImpl : EngineBase {
   int p, q, n, nx, n0, n1, buf, npan;
-  cudaStream_t s;
+  cudaStream_t s = nullptr;      // engine-owned stream (captured into graphs)
+  cudaStream_t us = nullptr;     // caller's stream
+  cudaEvent_t join = nullptr;
+  cudaGraphExec_t gfac[3] = {nullptr, nullptr, nullptr}, gapp = nullptr;
+  int gapp_nrhs = 0;
+  bool use_graphs = true;
   DevBuf D, Dsq, Nx, NxcT, NxxT, interp, jxr, leafglob, dirmask;
   DevBuf coef[5];
   bool has[5] = {false, false, false, false, false};
@@ -305,10 +314,76 @@ struct EngineImpl : EngineBase {
   DevBuf wc, flux, gvec, uvec, Ybuf, Zbuf, ifF, ifZ, ux_d, uc_d, rc_d, rx_d, rcT, acc;
   size_t factor_bytes_ = 0;
   bool factored = false;
+  // phase timing (CUDA events on the engine stream), milliseconds
+  cudaEvent_t ev[8] = {};
+  double tms[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+
+  ~EngineImpl() override {
+    if (s) cudaStreamSynchronize(s);
+    for (auto& g : gfac)
+      if (g) cudaGraphExecDestroy(g);
+    if (gapp) cudaGraphExecDestroy(gapp);
+    for (auto& e : ev)
+      if (e) cudaEventDestroy(e);
+    if (join) cudaEventDestroy(join);
+    if (s) cudaStreamDestroy(s);
+  }
+  // order the engine stream after the caller's stream (and back)
+  int enter() {
+    SLAB_CUDA_TRY(cudaEventRecord(join, us));
+    SLAB_CUDA_TRY(cudaStreamWaitEvent(s, join, 0));
+    return SLAB_OK;
+  }
+  int leave() {
+    SLAB_CUDA_TRY(cudaEventRecord(join, s));
+    SLAB_CUDA_TRY(cudaStreamWaitEvent(us, join, 0));
+    return SLAB_OK;
+  }
+  // Run `body` on the engine stream, through a CUDA graph captured on first use.
+  std::map<cudaGraphExec_t, long long> graph_kernels;  // kernels captured per graph
+  template <typename F>
+  int run_graph(cudaGraphExec_t& exec, F body) {
+    if (!use_graphs) return body();
+    if (!exec) {
+      cudaGraph_t g = nullptr;
+      const long long before = launch_count();
+      SLAB_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed));
+      const int st = body();
+      const long long captured = launch_count() - before;
+      add_launches(-captured);  // counted when the graph runs, below
+      const cudaError_t ce = cudaStreamEndCapture(s, &g);
+      if (st != SLAB_OK) {
+        if (g) cudaGraphDestroy(g);
+        return st;
+      }
+      if (ce != cudaSuccess) return set_error(SLAB_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ce));
+      const cudaError_t ie = cudaGraphInstantiate(&exec, g, 0);
+      cudaGraphDestroy(g);
+      if (ie != cudaSuccess) {
+        exec = nullptr;
+        return set_error(SLAB_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ie));
+      }
+      graph_kernels[exec] = captured;
+    }
+    SLAB_CUDA_TRY(cudaGraphLaunch(exec, s));
+    add_launches(graph_kernels[exec]);
+    return SLAB_OK;
+  }
+  float elapsed(int a, int b) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, ev[a], ev[b]) != cudaSuccess) {
+      cudaGetLastError();  // timing is advisory: do not leave the error for the next check
+      return -1.f;
+    }
+    return ms;
+  }
+  double timing(int i) const override { return i >= 0 && i < 8 ? tms[i] : 0.0; }
 
   EngineImpl(int p_, int n0_, int n1_, int buf_, cudaStream_t s_)
       : p(p_), q(p_ - 2), n((p_ - 2) * (p_ - 2)), nx(4 * (p_ - 2)), n0(n0_), n1(n1_), buf(buf_), npan(n0_ / buf_),
-        s(s_) {
+        us(s_) {
+    const char* ng = getenv("SLAB_NO_GRAPHS");
+    use_graphs = !(ng && ng[0] == '1');
     ntot = (long long)q * ((long long)n0 * (2 * n1 + 1) + n1);
     nleaf = (long long)n0 * n1;
   }
@@ -524,6 +599,8 @@ struct EngineImpl : EngineBase {
   }
 
   int init(const double* hD, const double* hDsq, const double* hNx, const double* hinterp, const int* hjxr) {
+    SLAB_CUDA_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    SLAB_CUDA_TRY(cudaEventCreateWithFlags(&join, cudaEventDisableTiming));
     SLAB_TRY(upload(D, std::vector<double>(hD, hD + p * p), s));
     SLAB_TRY(upload(Dsq, std::vector<double>(hDsq, hDsq + p * p), s));
     SLAB_TRY(upload(Nx, std::vector<double>(hNx, hNx + (size_t)nx * p * p), s));
@@ -555,6 +632,8 @@ struct EngineImpl : EngineBase {
       SLAB_TRY(ifInfo.alloc(sizeof(int)));
     }
     SLAB_TRY(acc.alloc(4 * sizeof(double)));
+    for (auto& e : ev) SLAB_CUDA_TRY(cudaEventCreate(&e));
+    SLAB_CUDA_TRY(cudaStreamSynchronize(s));
     factor_bytes_ = G.bytes + piv.bytes + nodepool.bytes + fpool.bytes + pivpool.bytes + ifLU.bytes + ifPiv.bytes +
                     ifPerm.bytes + ifSub.bytes + ifSup.bytes + ifX.bytes;
     return SLAB_OK;
@@ -563,6 +642,13 @@ struct EngineImpl : EngineBase {
   size_t factor_bytes() const override { return factor_bytes_; }
 
   int factor(const LeafCoeffs& co_in) override {
+    SLAB_TRY(enter());
+    const int st = factor_impl(co_in);
+    const int st2 = leave();
+    return st != SLAB_OK ? st : st2;
+  }
+
+  int factor_impl(const LeafCoeffs& co_in) {
     const size_t cbytes = (size_t)nleaf * p * p * sizeof(double);
     const double* src[5] = {co_in.c11, co_in.c22, co_in.c1, co_in.c2, co_in.c};
     for (int i = 0; i < 5; ++i) {
@@ -572,6 +658,28 @@ struct EngineImpl : EngineBase {
         SLAB_CUDA_TRY(cudaMemcpyAsync(coef[i].p, src[i], cbytes, cudaMemcpyDeviceToDevice, s));
       }
     }
+    const bool layout_changed = !factored || has_prev[0] != has[0] || has_prev[1] != has[1] ||
+                                has_prev[2] != has[2] || has_prev[3] != has[3] || has_prev[4] != has[4];
+    if (layout_changed)
+      for (auto& g : gfac)
+        if (g) {
+          cudaGraphExecDestroy(g);
+          g = nullptr;
+        }
+    for (int i = 0; i < 5; ++i) has_prev[i] = has[i];
+    SLAB_CUDA_TRY(cudaEventRecord(ev[0], s));
+    SLAB_TRY(run_graph(gfac[0], [&]() { return factor_leaf(); }));
+    SLAB_CUDA_TRY(cudaEventRecord(ev[1], s));
+    SLAB_TRY(run_graph(gfac[1], [&]() { return factor_tree(); }));
+    SLAB_CUDA_TRY(cudaEventRecord(ev[2], s));
+    if (nbI > 0) SLAB_TRY(run_graph(gfac[2], [&]() { return factor_interface(); }));
+    SLAB_CUDA_TRY(cudaEventRecord(ev[3], s));
+    return factor_check();
+  }
+
+  bool has_prev[5] = {false, false, false, false, false};
+
+  int factor_leaf() {
     LeafCoeffs co = coeffs();
     SLAB_CUDA_TRY(cudaMemsetAsync(leafinfo.p, 0, leafinfo.bytes, s));
     SLAB_CUDA_TRY(cudaMemsetAsync(mergeinfo.p, 0, mergeinfo.bytes, s));
@@ -582,7 +690,10 @@ struct EngineImpl : EngineBase {
     a.G = G.as<T>(); a.strideG = (long long)n * (n + nx); a.piv = piv.as<int>();
     a.dtn = nodepool.as<T>(); a.info = leafinfo.as<int>();
     a.decouple = 1; a.n0 = n0; a.n1 = n1; a.leaf_begin = 0;
-    SLAB_TRY(leaf_factor<T>(s, a, (int)nleaf));
+    return leaf_factor<T>(s, a, (int)nleaf);
+  }
+
+  int factor_tree() {
     // merge tree, level by level
     int info_ofs = 0;
     for (auto& bp : batches) {
@@ -605,7 +716,10 @@ struct EngineImpl : EngineBase {
                        nullptr, (long long)b.nO * b.nO, b.nO, b.count));
       info_ofs += b.count;
     }
-    // interface
+    return SLAB_OK;
+  }
+
+  int factor_interface() {
     if (nbI > 0) {
       const long long blk = (long long)nI * nI;
       SLAB_CUDA_TRY(cudaMemsetAsync(ifInfo.p, 0, sizeof(int), s));
@@ -625,6 +739,10 @@ struct EngineImpl : EngineBase {
         SLAB_TRY(build_perm(s, ifPiv.as<int>() + (long long)nI * j, nI, ifPerm.as<int>() + (long long)nI * j));
       }
     }
+    return SLAB_OK;
+  }
+
+  int factor_check() {
     // breakdown report
     std::vector<int> hinfo((size_t)nleaf);
     SLAB_CUDA_TRY(cudaMemcpyAsync(hinfo.data(), leafinfo.p, leafinfo.bytes, cudaMemcpyDeviceToHost, s));
@@ -633,6 +751,9 @@ struct EngineImpl : EngineBase {
     int iinfo = 0;
     if (nbI > 0) SLAB_CUDA_TRY(cudaMemcpyAsync(&iinfo, ifInfo.p, sizeof(int), cudaMemcpyDeviceToHost, s));
     SLAB_CUDA_TRY(cudaStreamSynchronize(s));
+    tms[0] = elapsed(0, 1);
+    tms[1] = elapsed(1, 2);
+    tms[2] = elapsed(2, 3);
     factored = true;
     for (size_t i = 0; i < hinfo.size(); ++i)
       if (hinfo[i] > 0) {
@@ -659,6 +780,10 @@ struct EngineImpl : EngineBase {
 
   int reserve(int nrhs) {
     if (nrhs <= cap_nrhs) return SLAB_OK;
+    if (gapp) {
+      cudaGraphExecDestroy(gapp);
+      gapp = nullptr;
+    }
     long long ymax = 0, zmax = 0;
     for (auto& b : batches) {
       b->offY0 = ymax;
@@ -810,9 +935,20 @@ struct EngineImpl : EngineBase {
 
   int solve(int nrhs, const double* bnd, const double* fbody, double tol, int max_iter, double* ufaces,
             double* uleaf, int* iters, double* stats) override {
+    SLAB_TRY(enter());
+    const int st = solve_impl(nrhs, bnd, fbody, tol, max_iter, ufaces, uleaf, iters, stats);
+    const int st2 = leave();
+    return st != SLAB_OK ? st : st2;
+  }
+
+  int solve_impl(int nrhs, const double* bnd, const double* fbody, double tol, int max_iter, double* ufaces,
+                 double* uleaf, int* iters, double* stats) {
     if (!factored) return set_error(SLAB_ERR_STATE, "slab_engine_solve: engine not factored");
     if (nrhs <= 0 || !bnd) return set_error(SLAB_ERR_ARG, "slab_engine_solve: invalid arguments");
     SLAB_TRY(reserve(nrhs));
+    SLAB_CUDA_TRY(cudaEventRecord(ev[4], s));
+    tms[4] = 0.0;
+    tms[5] = 0.0;
     const long long nc_el = nleaf * n * nrhs, nf_el = ntot * nrhs;
     init_faces_kernel<<<grid_for(nf_el), 256, 0, s>>>(bnd, dirmask.as<unsigned char>(), ux_d.as<double>(), ntot, nrhs);
     SLAB_CHECK_LAUNCH();
@@ -834,12 +970,21 @@ struct EngineImpl : EngineBase {
       SLAB_CHECK_LAUNCH();
       convert_kernel<T, double><<<grid_for(nf_el), 256, 0, s>>>(rx_d.as<double>(), gvec.as<T>(), nf_el);
       SLAB_CHECK_LAUNCH();
-      SLAB_TRY(apply(nrhs));
+      SLAB_CUDA_TRY(cudaEventRecord(ev[6], s));
+      if (gapp && gapp_nrhs != nrhs) {
+        cudaGraphExecDestroy(gapp);
+        gapp = nullptr;
+      }
+      gapp_nrhs = nrhs;
+      SLAB_TRY(run_graph(gapp, [&]() { return apply(nrhs); }));
+      SLAB_CUDA_TRY(cudaEventRecord(ev[7], s));
       axpy_kernel<T><<<grid_for(nc_el), 256, 0, s>>>(uc_d.as<double>(), wc.as<T>(), nc_el);
       SLAB_CHECK_LAUNCH();
       axpy_kernel<T><<<grid_for(nf_el), 256, 0, s>>>(ux_d.as<double>(), uvec.as<T>(), nf_el);
       SLAB_CHECK_LAUNCH();
       SLAB_TRY(norms(wc.p, false, nc_el, uvec.p, false, nf_el, &dn));
+      tms[4] += elapsed(6, 7);
+      tms[5] += 1;
       SLAB_TRY(norms(uc_d.p, true, nc_el, ux_d.p, true, nf_el, &un));
       rel = un > 0 ? dn / un : 0.0;
       if (rel <= tol) {
@@ -863,6 +1008,9 @@ struct EngineImpl : EngineBase {
       assemble_solution_kernel<<<(unsigned)nleaf, 256, (size_t)nx * sizeof(double), s>>>(aa);
       SLAB_CHECK_LAUNCH();
     }
+    SLAB_CUDA_TRY(cudaEventRecord(ev[5], s));
+    SLAB_CUDA_TRY(cudaEventSynchronize(ev[5]));
+    tms[3] = elapsed(4, 5);
     if (iters) *iters = it;
     if (stats) {
       stats[0] = rel;
@@ -883,9 +1031,10 @@ struct EngineImpl : EngineBase {
                double* rfaces) override {
     if (!factored && !has[0] && !has[1] && !has[4])
       return set_error(SLAB_ERR_STATE, "slab_engine_residual: coefficients not set (call factor first)");
+    SLAB_TRY(enter());
     SLAB_TRY(residual_impl(nrhs, ufaces, uint, fbody, rint, rfaces));
     SLAB_CUDA_TRY(cudaStreamSynchronize(s));
-    return SLAB_OK;
+    return leave();
   }
 };
 
@@ -932,6 +1081,15 @@ extern "C" int slab_engine_create(slab_engine** out, int p, int n0, int n1, int 
 extern "C" int slab_engine_destroy(slab_engine* e) {
   delete e;
   return SLAB_OK;
+}
+
+extern "C" long long slab_launch_count(void) { return slab::launch_count(); }
+
+extern "C" int slab_engine_timings(const slab_engine* e, double* ms, int n) {
+  if (!e || !ms) return slab::set_error(SLAB_ERR_ARG, "slab_engine_timings: null argument");
+  const int m = n < 6 ? n : 6;
+  for (int i = 0; i < m; ++i) ms[i] = e->impl->timing(i);
+  return m;
 }
 
 extern "C" long long slab_engine_nfaces(const slab_engine* e) { return e ? e->impl->ntot : -1; }

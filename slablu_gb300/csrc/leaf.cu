@@ -9,10 +9,7 @@ int leaf_factor(cudaStream_t s, const LeafFactorArgs<T>& a, int nleaf) {
   if (nleaf <= 0) return SLAB_OK;
   if (a.nx > 2 * kCT) return set_error(SLAB_ERR_ARG, "leaf_factor: p = %d too large", a.p);
   const size_t bytes = leaf_factor_smem_bytes(a.p, sizeof(T));
-  if (bytes > smem_limit_bytes())
-    return set_error(SLAB_ERR_ARG, "leaf_factor: p = %d needs %zu bytes of shared memory", a.p, bytes);
-  SLAB_CUDA_TRY(
-      cudaFuncSetAttribute(leaf_factor_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  SLAB_TRY(ensure_smem(leaf_factor_kernel<T>, bytes, "leaf_factor"));
   leaf_factor_kernel<T><<<nleaf, kNT, bytes, s>>>(a);
   SLAB_CHECK_LAUNCH();
   return SLAB_OK;

@@ -56,6 +56,13 @@ class SlabEngine:
             self.L.slab_engine_destroy(h)
             self.h = None
 
+    def timings(self):
+        """Device milliseconds of the last factor/solve phases (slab_engine_timings)."""
+        buf = (ctypes.c_double * 6)()
+        self.L.slab_engine_timings(self.h, buf, 6)
+        keys = ('leaf_ms', 'tree_ms', 'interface_ms', 'solve_ms', 'apply_ms', 'n_apply')
+        return dict(zip(keys, list(buf)))
+
     @property
     def factor_bytes(self):
         return int(self.L.slab_engine_factor_bytes(self.h))
