@@ -163,6 +163,7 @@ def solve_superlu(md, part, A, u_dir):
     ff = dirichlet_rhs(A, part, u_dir)
     lu = spla.splu(A_CC)
     x = lu.solve(ff)
+    x = x.reshape(ff.shape)
     res = np.linalg.norm(A_CC @ x - ff) / np.linalg.norm(ff)
     return x, ff, res
 
@@ -189,7 +190,7 @@ def solve_full(md, part, coeffs, u_dir_func, A=None):
     """
     if A is None:
         A = md.sparse_mat(leafmod.dtn_build(md.ld, coeffs))
-    u_dir = np.asarray(u_dir_func(md.xx_active[part.I_Xtot]), dtype=float).reshape(-1, 1)
+    u_dir = np.asarray(u_dir_func(md.xx_active[part.I_Xtot]), dtype=float).reshape(part.I_Xtot.size, -1)
     x, ff, res = solve_superlu(md, part, A, u_dir)
     sol = assemble_solution(md, part, x, u_dir)
     u_tot, resloc = leaf_recover(md, coeffs, sol)

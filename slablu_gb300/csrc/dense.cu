@@ -74,6 +74,69 @@ __global__ void perm_from_ipiv_kernel(const int* ipiv, int n, int* perm) {
   }
 }
 
+__global__ void perm_batched_kernel(const int* ipiv, long long strideP, int n, int batch, int* perm,
+                                    long long strideQ) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= batch) return;
+  const int* iv = ipiv + strideP * b;
+  int* pm = perm + strideQ * b;
+  for (int i = 0; i < n; ++i) pm[i] = i;
+  for (int j = 0; j < n; ++j) {
+    const int pj = iv[j];
+    if (pj != j && pj >= 0 && pj < n) {
+      const int t = pm[j];
+      pm[j] = pm[pj];
+      pm[pj] = t;
+    }
+  }
+}
+
+int build_perm_batched(cudaStream_t s, const int* ipiv, long long strideP, int n, int batch, int* perm,
+                       long long strideQ) {
+  if (batch <= 0) return SLAB_OK;
+  perm_batched_kernel<<<ceil_div(batch, 128), 128, 0, s>>>(ipiv, strideP, n, batch, perm, strideQ);
+  SLAB_CHECK_LAUNCH();
+  return SLAB_OK;
+}
+
+template <typename T>
+int getrs_small(cudaStream_t s, int n, int nrhs, const T* LU, const long long* offLU, long long strideLU, int lda,
+                const int* perm, const long long* offP, long long strideP, T* B, const long long* offB,
+                long long strideB, int ldb, int batch) {
+  if (n <= 0 || nrhs <= 0 || batch <= 0) return SLAB_OK;
+  if (nrhs > 4) return set_error(SLAB_ERR_ARG, "getrs_small: nrhs %d > 4", nrhs);
+  if (n > 32 * kWarpSlots) return set_error(SLAB_ERR_ARG, "getrs_small: order %d > %d", n, 32 * kWarpSlots);
+  const size_t bytes = (size_t)kWarpSolveWarps * n * nrhs * sizeof(T);
+  SLAB_TRY(ensure_smem(getrs_warp_kernel<T>, bytes, "getrs_small"));
+  getrs_warp_kernel<T><<<ceil_div(batch, kWarpSolveWarps), 32 * kWarpSolveWarps, bytes, s>>>(
+      n, nrhs, LU, offLU, strideLU, lda, perm, offP, strideP, B, offB, strideB, ldb, batch);
+  SLAB_CHECK_LAUNCH();
+  return SLAB_OK;
+}
+
+template <typename T>
+int trsv_coop(cudaStream_t s, const T* LU, int lda, int n, const int* perm, const T* B, int ldb, T* X, int ldx,
+              int nrhs) {
+  if (n <= 0 || nrhs <= 0) return SLAB_OK;
+  if (nrhs > kCoopMaxRhs) return set_error(SLAB_ERR_ARG, "trsv_coop: nrhs %d > %d", nrhs, kCoopMaxRhs);
+  static int max_grid = 0;
+  if (max_grid == 0) {
+    int dev = 0, sms = 0, per_sm = 0;
+    SLAB_CUDA_TRY(cudaGetDevice(&dev));
+    SLAB_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    SLAB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, trsv_coop_kernel<T>, 256, 0));
+    max_grid = sms * (per_sm > 0 ? per_sm : 1);
+  }
+  const int nblk = ceil_div(n, kCoopRows);
+  const int G = nblk < max_grid ? nblk : max_grid;
+  if (ceil_div(nblk, G) > 8) return set_error(SLAB_ERR_ARG, "trsv_coop: order %d too large", n);
+  void* args[] = {(void*)&LU, (void*)&lda, (void*)&n, (void*)&perm, (void*)&B, (void*)&ldb, (void*)&X, (void*)&ldx,
+                  (void*)&nrhs};
+  SLAB_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)trsv_coop_kernel<T>, dim3(G), dim3(256), args, 0, s));
+  SLAB_CHECK_LAUNCH();
+  return SLAB_OK;
+}
+
 int build_perm(cudaStream_t s, const int* ipiv, int n, int* perm) {
   perm_from_ipiv_kernel<<<1, 1, 0, s>>>(ipiv, n, perm);
   SLAB_CHECK_LAUNCH();
@@ -92,6 +155,37 @@ int gemm(cudaStream_t s, int m, int n, int k, T alpha, const T* A, const long lo
       SLAB_TRY(gemm<T>(s, m, n, k, alpha, offA ? A : A + strideA * b0, offA ? offA + b0 : nullptr, strideA, lda,
                        offB ? B : B + strideB * b0, offB ? offB + b0 : nullptr, strideB, ldb, beta,
                        offC ? C : C + strideC * b0, offC ? offC + b0 : nullptr, strideC, ldc, nb));
+    }
+    return SLAB_OK;
+  }
+  if (n <= 16 && batch == 1 && !offA && !offB && !offC && k >= 512 && ceil_div(m, 256) < 64) {
+    // tall-skinny single product: split k over CTAs, accumulate with atomics
+    const int mb = ceil_div(m, 256);
+    int nsplit = ceil_div(256, mb);
+    const int kchunk = 256;
+    nsplit = nsplit < ceil_div(k, kchunk) ? nsplit : ceil_div(k, kchunk);
+    if (beta != T(1)) {
+      scale_kernel<T><<<ceil_div(m * n, 256), 256, 0, s>>>(C, m, n, ldc, beta);
+      SLAB_CHECK_LAUNCH();
+    }
+    for (int ks = 0; ks < k; ks += kchunk * nsplit) {
+      const int kk = k - ks < kchunk * nsplit ? k - ks : kchunk * nsplit;
+      dim3 g(mb, ceil_div(kk, kchunk));
+#define SLAB_SPLIT(NC)                                                                                             \
+  gemm_narrow_splitk_kernel<T, NC><<<g, 256, 0, s>>>(m, n, kk, kchunk, alpha, A + (size_t)ks * lda, lda, B + ks, ldb, \
+                                                     C, ldc)
+      if (n <= 1)
+        SLAB_SPLIT(1);
+      else if (n <= 2)
+        SLAB_SPLIT(2);
+      else if (n <= 4)
+        SLAB_SPLIT(4);
+      else if (n <= 8)
+        SLAB_SPLIT(8);
+      else
+        SLAB_SPLIT(16);
+#undef SLAB_SPLIT
+      SLAB_CHECK_LAUNCH();
     }
     return SLAB_OK;
   }
@@ -228,5 +322,14 @@ int bigtrs(cudaStream_t s, const T* LU, int lda, int n, const int* perm, const T
 
 SLAB_INSTANTIATE(float)
 SLAB_INSTANTIATE(double)
+
+template int getrs_small<float>(cudaStream_t, int, int, const float*, const long long*, long long, int, const int*,
+                                const long long*, long long, float*, const long long*, long long, int, int);
+template int getrs_small<double>(cudaStream_t, int, int, const double*, const long long*, long long, int,
+                                 const int*, const long long*, long long, double*, const long long*, long long, int,
+                                 int);
+template int trsv_coop<float>(cudaStream_t, const float*, int, int, const int*, const float*, int, float*, int, int);
+template int trsv_coop<double>(cudaStream_t, const double*, int, int, const int*, const double*, int, double*, int,
+                               int);
 
 }  // namespace slab

@@ -10,6 +10,8 @@
 
 #include <climits>
 
+#include <cooperative_groups.h>
+
 #include "common.cuh"
 
 namespace slab {
@@ -557,6 +559,258 @@ __global__ void __launch_bounds__(256) gemm_narrow_kernel(int m, int n, int k, T
 }
 
 // ---------------------------------------------------------------------------
+// Batched ipiv -> row permutation (perm[i] = source row of row i), one thread
+// per matrix.
+__global__ void perm_batched_kernel(const int* ipiv, long long strideP, int n, int batch, int* perm,
+                                    long long strideQ);
+
+// Warp-per-matrix X = U^{-1} L^{-1} P B for few right-hand sides (nrhs <= 4),
+// column-oriented substitution: the vector lives in shared memory, each column
+// of L / U is streamed from global memory by the 32 lanes (coalesced).
+// One warp per batch entry, 8 warps per CTA.
+constexpr int kWarpSolveWarps = 8;
+constexpr int kWarpSlots = 16;  // rows per lane: n <= 512
+template <typename T>
+__global__ void __launch_bounds__(32 * kWarpSolveWarps)
+    getrs_warp_kernel(int n, int nrhs, const T* __restrict__ LU, const long long* offLU, long long strideLU, int lda,
+                      const int* __restrict__ perm, const long long* offP, long long strideP, T* B,
+                      const long long* offB, long long strideB, int ldb, int batch) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int b = blockIdx.x * kWarpSolveWarps + warp;
+  if (b >= batch) return;
+  T* xs = reinterpret_cast<T*>(smem_raw) + (size_t)warp * n * nrhs;
+  const T* __restrict__ A = LU + batch_off(offLU, strideLU, b);
+  const int* pv = perm + batch_off(offP, strideP, b);
+  T* Bg = B + batch_off(offB, strideB, b);
+  for (int c = 0; c < nrhs; ++c)
+    for (int i = lane; i < n; i += 32) xs[i + c * n] = Bg[pv[i] + (size_t)c * ldb];
+  __syncwarp();
+  // forward, unit lower: column k updates rows k+1+lane+32t; the next column is
+  // loaded into registers while the current one is applied.
+  T cur[kWarpSlots], nxt[kWarpSlots];
+#pragma unroll
+  for (int t = 0; t < kWarpSlots; ++t) {
+    const int i = 1 + lane + 32 * t;
+    cur[t] = (n > 1 && i < n) ? A[i] : T(0);
+  }
+  for (int k = 0; k < n - 1; ++k) {
+    if (k + 1 < n - 1) {
+      const T* nc = A + (size_t)(k + 1) * lda;
+#pragma unroll
+      for (int t = 0; t < kWarpSlots; ++t) {
+        const int i = k + 2 + lane + 32 * t;
+        nxt[t] = i < n ? nc[i] : T(0);
+      }
+    }
+    for (int c = 0; c < nrhs; ++c) {
+      const T xk = xs[k + c * n];
+#pragma unroll
+      for (int t = 0; t < kWarpSlots; ++t) {
+        const int i = k + 1 + lane + 32 * t;
+        if (i < n) xs[i + c * n] -= cur[t] * xk;
+      }
+    }
+    __syncwarp();
+#pragma unroll
+    for (int t = 0; t < kWarpSlots; ++t) cur[t] = nxt[t];
+  }
+  // backward, upper: column k updates rows lane+32t < k
+  {
+    const T* cc = A + (size_t)(n - 1) * lda;
+#pragma unroll
+    for (int t = 0; t < kWarpSlots; ++t) {
+      const int i = lane + 32 * t;
+      cur[t] = i < n ? cc[i] : T(0);  // includes the diagonal U[k,k] at i = k
+    }
+  }
+  for (int k = n - 1; k >= 0; --k) {
+    if (k > 0) {
+      const T* nc = A + (size_t)(k - 1) * lda;
+#pragma unroll
+      for (int t = 0; t < kWarpSlots; ++t) {
+        const int i = lane + 32 * t;
+        nxt[t] = i < k ? nc[i] : T(0);
+      }
+    }
+    const T d = A[(size_t)k * lda + k];
+    for (int c = 0; c < nrhs; ++c) {
+      const T xk = xs[k + c * n] / d;
+#pragma unroll
+      for (int t = 0; t < kWarpSlots; ++t) {
+        const int i = lane + 32 * t;
+        if (i < k) xs[i + c * n] -= cur[t] * xk;
+      }
+      __syncwarp();
+      if (lane == 0) xs[k + c * n] = xk;
+    }
+    __syncwarp();
+#pragma unroll
+    for (int t = 0; t < kWarpSlots; ++t) cur[t] = nxt[t];
+  }
+  for (int c = 0; c < nrhs; ++c)
+    for (int i = lane; i < n; i += 32) Bg[i + (size_t)c * ldb] = xs[i + c * n];
+}
+
+// Cooperative triangular solves with one large factored matrix (FP64
+// interface blocks), X = U^{-1} L^{-1} P B for nrhs <= 8 columns.
+// CTA j owns the 32-row blocks j, j+G, ...; it applies the contributions of
+// every solved block to its rows and solves its own diagonal blocks
+// (owner computes).  One grid-wide barrier per block.
+constexpr int kCoopRows = 32;
+constexpr int kCoopMaxRhs = 8;
+template <typename T>
+__global__ void __launch_bounds__(256) trsv_coop_kernel(const T* __restrict__ LU, int lda, int n,
+                                                       const int* __restrict__ perm, const T* __restrict__ Bin,
+                                                       int ldb, T* X, int ldx, int nrhs) {
+  namespace cg = cooperative_groups;
+  cg::grid_group grid = cg::this_grid();
+  __shared__ T acc[8][kCoopRows * kCoopMaxRhs];  // owned blocks (up to 8 per CTA)
+  __shared__ T dblk[kCoopRows * (kCoopRows + 1)];
+  __shared__ T xb[kCoopRows * kCoopMaxRhs];
+  const int G = gridDim.x, j = blockIdx.x, tid = threadIdx.x;
+  const int nblk = (n + kCoopRows - 1) / kCoopRows;
+  const int nown = (nblk - j + G - 1) / G;  // blocks j, j+G, ... (<= 8, checked by the launcher)
+  // acc = (P^T B) on owned rows
+  for (int o = 0; o < nown; ++o) {
+    const int r0 = (j + o * G) * kCoopRows;
+    for (int idx = tid; idx < kCoopRows * nrhs; idx += blockDim.x) {
+      const int r = idx % kCoopRows, c = idx / kCoopRows;
+      acc[o][idx] = (r0 + r < n) ? Bin[perm[r0 + r] + (size_t)c * ldb] : T(0);
+    }
+  }
+  __syncthreads();
+  const int lane = tid & 31, warp = tid >> 5;
+  // ---- forward, unit lower
+  for (int b = 0; b < nblk; ++b) {
+    const int k0 = b * kCoopRows, kb = min(kCoopRows, n - k0);
+    if (b % G == j) {
+      const int o = b / G;
+      __syncthreads();
+      for (int idx = tid; idx < kb * kb; idx += blockDim.x) {
+        const int r = idx % kb, c = idx / kb;
+        dblk[r + c * (kCoopRows + 1)] = LU[(size_t)(k0 + c) * lda + k0 + r];
+      }
+      __syncthreads();
+      if (warp < nrhs) {
+        T v = lane < kb ? acc[o][lane + warp * kCoopRows] : T(0);
+        for (int i = 0; i < kb; ++i) {
+          const T xi = __shfl_sync(0xffffffffu, v, i);
+          if (lane > i && lane < kb) v -= dblk[lane + i * (kCoopRows + 1)] * xi;
+        }
+        if (lane < kb) {
+          acc[o][lane + warp * kCoopRows] = v;
+          X[k0 + lane + (size_t)warp * ldx] = v;
+        }
+      }
+    }
+    grid.sync();
+    for (int idx = tid; idx < kb * nrhs; idx += blockDim.x) xb[idx] = X[k0 + idx % kb + (size_t)(idx / kb) * ldx];
+    for (int o = 0; o < nown; ++o) {
+      const int ob = j + o * G;
+      if (ob <= b) continue;
+      const int r0 = ob * kCoopRows;
+      const int rb = min(kCoopRows, n - r0);
+      __syncthreads();
+      for (int idx = tid; idx < rb * kb; idx += blockDim.x) {
+        const int r = idx % rb, k = idx / rb;
+        dblk[r + k * (kCoopRows + 1)] = LU[(size_t)(k0 + k) * lda + r0 + r];
+      }
+      __syncthreads();
+      for (int idx = tid; idx < rb * nrhs; idx += blockDim.x) {
+        const int r = idx % rb, c = idx / rb;
+        T s = T(0);
+        for (int k = 0; k < kb; ++k) s += dblk[r + k * (kCoopRows + 1)] * xb[k + c * kb];
+        acc[o][r + c * kCoopRows] -= s;
+      }
+    }
+    __syncthreads();
+  }
+  // ---- backward, upper (non-unit)
+  for (int b = nblk - 1; b >= 0; --b) {
+    const int k0 = b * kCoopRows, kb = min(kCoopRows, n - k0);
+    if (b % G == j) {
+      const int o = b / G;
+      __syncthreads();
+      for (int idx = tid; idx < kb * kb; idx += blockDim.x) {
+        const int r = idx % kb, c = idx / kb;
+        dblk[r + c * (kCoopRows + 1)] = LU[(size_t)(k0 + c) * lda + k0 + r];
+      }
+      __syncthreads();
+      if (warp < nrhs) {
+        T v = lane < kb ? acc[o][lane + warp * kCoopRows] : T(0);
+        for (int i = kb - 1; i >= 0; --i) {
+          if (lane == i) v /= dblk[i + i * (kCoopRows + 1)];
+          const T xi = __shfl_sync(0xffffffffu, v, i);
+          if (lane < i) v -= dblk[lane + i * (kCoopRows + 1)] * xi;
+        }
+        if (lane < kb) X[k0 + lane + (size_t)warp * ldx] = v;
+      }
+    }
+    grid.sync();
+    for (int idx = tid; idx < kb * nrhs; idx += blockDim.x) xb[idx] = X[k0 + idx % kb + (size_t)(idx / kb) * ldx];
+    for (int o = 0; o < nown; ++o) {
+      const int ob = j + o * G;
+      if (ob >= b) continue;
+      const int r0 = ob * kCoopRows;
+      const int rb = min(kCoopRows, n - r0);
+      __syncthreads();
+      for (int idx = tid; idx < rb * kb; idx += blockDim.x) {
+        const int r = idx % rb, k = idx / rb;
+        dblk[r + k * (kCoopRows + 1)] = LU[(size_t)(k0 + k) * lda + r0 + r];
+      }
+      __syncthreads();
+      for (int idx = tid; idx < rb * nrhs; idx += blockDim.x) {
+        const int r = idx % rb, c = idx / rb;
+        T s = T(0);
+        for (int k = 0; k < kb; ++k) s += dblk[r + k * (kCoopRows + 1)] * xb[k + c * kb];
+        acc[o][r + c * kCoopRows] -= s;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// Split-K narrow GEMM for one tall matrix: C += alpha * A[:, kchunk] B[kchunk, :]
+// accumulated with atomics (C already scaled by beta).  grid (ceil(m/256), nsplit).
+template <typename T, int NC>
+__global__ void __launch_bounds__(256) gemm_narrow_splitk_kernel(int m, int n, int k, int kchunk, T alpha,
+                                                                const T* __restrict__ A, int lda,
+                                                                const T* __restrict__ B, int ldb, T* C, int ldc) {
+  __shared__ T Bs[NC * 256];
+  const int k0 = blockIdx.y * kchunk;
+  const int kc = min(kchunk, k - k0);
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  for (int idx = threadIdx.x; idx < 256 * NC; idx += blockDim.x) {
+    const int kk = idx % 256, c = idx / 256;
+    Bs[c * 256 + kk] = (kk < kc && c < n) ? B[(k0 + kk) + (size_t)c * ldb] : T(0);
+  }
+  __syncthreads();
+  if (r >= m || kc <= 0) return;
+  T acc[NC];
+#pragma unroll
+  for (int c = 0; c < NC; ++c) acc[c] = T(0);
+  const T* ap = A + r + (size_t)k0 * lda;
+  for (int kk = 0; kk < kc; ++kk) {
+    const T a = ap[(size_t)kk * lda];
+#pragma unroll
+    for (int c = 0; c < NC; ++c) acc[c] += a * Bs[c * 256 + kk];
+  }
+#pragma unroll
+  for (int c = 0; c < NC; ++c)
+    if (c < n) atomicAdd(C + r + (size_t)c * ldc, alpha * acc[c]);
+}
+
+template <typename T>
+__global__ void scale_kernel(T* C, int m, int n, int ldc, T beta) {
+  const long long tot = (long long)m * n;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < tot; i += (long long)gridDim.x * blockDim.x) {
+    T* cp = C + (i % m) + (size_t)(i / m) * ldc;
+    *cp = beta == T(0) ? T(0) : beta * *cp;
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Large single-matrix LU (FP64 interface blocks): host loop over panels.
 
 // Panel factorization in global memory: rows [k0, n), columns [k0, k0+nb).
@@ -710,6 +964,20 @@ int bigtrs(cudaStream_t s, const T* LU, int lda, int n, const int* perm, const T
            int nrhs, bool lower = true, bool upper = true);
 
 int build_perm(cudaStream_t s, const int* ipiv, int n, int* perm);
+int build_perm_batched(cudaStream_t s, const int* ipiv, long long strideP, int n, int batch, int* perm,
+                       long long strideQ);
+
+// Batched X = U^{-1} L^{-1} P B with the warp kernel (nrhs <= 4); perm from
+// build_perm_batched.  Returns SLAB_ERR_ARG when the shape does not fit.
+template <typename T>
+int getrs_small(cudaStream_t s, int n, int nrhs, const T* LU, const long long* offLU, long long strideLU, int lda,
+                const int* perm, const long long* offP, long long strideP, T* B, const long long* offB,
+                long long strideB, int ldb, int batch);
+
+// X = U^{-1} L^{-1} P B for one large factored matrix, nrhs <= 8, cooperative launch.
+template <typename T>
+int trsv_coop(cudaStream_t s, const T* LU, int lda, int n, const int* perm, const T* B, int ldb, T* X, int ldx,
+              int nrhs);
 
 size_t smem_limit_bytes();
 

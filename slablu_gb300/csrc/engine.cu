@@ -296,12 +296,12 @@ struct EngineImpl : EngineBase {
   DevBuf coef[5];
   bool has[5] = {false, false, false, false, false};
   // leaf factors
-  DevBuf G, piv, leafinfo;
+  DevBuf G, piv, leafperm, leafinfo;
   // tree
   std::vector<HNode> nodes;
   std::vector<HMerge> merges;
   std::vector<std::unique_ptr<Batch>> batches;
-  DevBuf nodepool, fpool, pivpool, mergeinfo;
+  DevBuf nodepool, fpool, pivpool, permpool, mergeinfo;
   long long nodepool_elems = 0, fpool_elems = 0, pivpool_elems = 0;
   std::vector<int> roots;
   DevBuf rootoff;
@@ -614,10 +614,12 @@ struct EngineImpl : EngineBase {
     // factor storage
     SLAB_TRY(G.alloc((size_t)nleaf * n * (n + nx) * sizeof(T)));
     SLAB_TRY(piv.alloc((size_t)nleaf * n * sizeof(int)));
+    SLAB_TRY(leafperm.alloc((size_t)nleaf * n * sizeof(int)));
     SLAB_TRY(leafinfo.alloc((size_t)nleaf * sizeof(int)));
     SLAB_TRY(nodepool.alloc((size_t)nodepool_elems * sizeof(T)));
     SLAB_TRY(fpool.alloc((size_t)std::max<long long>(fpool_elems, 1) * sizeof(T)));
     SLAB_TRY(pivpool.alloc((size_t)std::max<long long>(pivpool_elems, 1) * sizeof(int)));
+    SLAB_TRY(permpool.alloc((size_t)std::max<long long>(pivpool_elems, 1) * sizeof(int)));
     int ninfo = 0;
     for (auto& b : batches) ninfo += b->count;
     SLAB_TRY(mergeinfo.alloc((size_t)std::max(ninfo, 1) * sizeof(int)));
@@ -690,7 +692,8 @@ struct EngineImpl : EngineBase {
     a.G = G.as<T>(); a.strideG = (long long)n * (n + nx); a.piv = piv.as<int>();
     a.dtn = nodepool.as<T>(); a.info = leafinfo.as<int>();
     a.decouple = 1; a.n0 = n0; a.n1 = n1; a.leaf_begin = 0;
-    return leaf_factor<T>(s, a, (int)nleaf);
+    SLAB_TRY(leaf_factor<T>(s, a, (int)nleaf));
+    return build_perm_batched(s, piv.as<int>(), n, n, (int)nleaf, leafperm.as<int>(), n);
   }
 
   int factor_tree() {
@@ -709,6 +712,7 @@ struct EngineImpl : EngineBase {
       int* pv = pivpool.as<int>() + b.offPiv0;
       SLAB_TRY(getrf_batched<T>(s, b.nE, b.nE, Maug, nullptr, strideM, b.nE, pv, nullptr, b.nE,
                                 mergeinfo.as<int>() + info_ofs, b.count));
+      SLAB_TRY(build_perm_batched(s, pv, b.nE, b.nE, b.count, permpool.as<int>() + b.offPiv0, b.nE));
       SLAB_TRY(getrs_batched<T>(s, b.nE, b.nO, Maug, nullptr, strideM, b.nE, pv, nullptr, b.nE,
                                 Maug + (long long)b.nE * b.nE, nullptr, strideM, b.nE, b.count));
       SLAB_TRY(gemm<T>(s, b.nO, b.nO, b.nE, T(-1), fpool.as<T>() + b.offC0, nullptr, (long long)b.nO * b.nE, b.nO,
@@ -818,8 +822,12 @@ struct EngineImpl : EngineBase {
     T* w = wc.as<T>();
     const long long strideG = (long long)n * (n + nx);
     SLAB_CUDA_TRY(cudaMemcpyAsync(w, rcT.p, (size_t)nleaf * n * nrhs * sizeof(T), cudaMemcpyDeviceToDevice, s));
-    SLAB_TRY(getrs_batched<T>(s, n, nrhs, G.as<T>(), nullptr, strideG, n, piv.as<int>(), nullptr, n, w, nullptr,
+    if (nrhs <= 4 && n <= 32 * kWarpSlots)
+      SLAB_TRY(getrs_small<T>(s, n, nrhs, G.as<T>(), nullptr, strideG, n, leafperm.as<int>(), nullptr, n, w, nullptr,
                               (long long)n * nrhs, n, (int)nleaf));
+    else
+      SLAB_TRY(getrs_batched<T>(s, n, nrhs, G.as<T>(), nullptr, strideG, n, piv.as<int>(), nullptr, n, w, nullptr,
+                                (long long)n * nrhs, n, (int)nleaf));
     SLAB_TRY(gemm<T>(s, nx, nrhs, n, T(1), NxcT.as<T>(), nullptr, 0, nx, w, nullptr, (long long)n * nrhs, n, T(0),
                      flux.as<T>(), nullptr, (long long)nx * nrhs, nx, (int)nleaf));
     scatter_add_kernel<T><<<grid_for(nleaf * nx * nrhs), 256, 0, s>>>(g, ntot, leafglob.as<int>(), nx, (int)nleaf,
@@ -835,8 +843,12 @@ struct EngineImpl : EngineBase {
       gather_kernel<T><<<grid_for((long long)b.count * b.nE * nrhs), 256, 0, s>>>(g, ntot, b.Eglob.as<int>(), b.nE,
                                                                                 b.count, nrhs, Y);
       SLAB_CHECK_LAUNCH();
-      SLAB_TRY(getrs_batched<T>(s, b.nE, nrhs, Maug, nullptr, strideM, b.nE, pivpool.as<int>() + b.offPiv0, nullptr,
-                                b.nE, Y, nullptr, (long long)b.nE * nrhs, b.nE, b.count));
+      if (nrhs <= 4 && b.nE <= 32 * kWarpSlots)
+        SLAB_TRY(getrs_small<T>(s, b.nE, nrhs, Maug, nullptr, strideM, b.nE, permpool.as<int>() + b.offPiv0,
+                                nullptr, b.nE, Y, nullptr, (long long)b.nE * nrhs, b.nE, b.count));
+      else
+        SLAB_TRY(getrs_batched<T>(s, b.nE, nrhs, Maug, nullptr, strideM, b.nE, pivpool.as<int>() + b.offPiv0,
+                                  nullptr, b.nE, Y, nullptr, (long long)b.nE * nrhs, b.nE, b.count));
       SLAB_TRY(gemm<T>(s, b.nO, nrhs, b.nE, T(1), fpool.as<T>() + b.offC0, nullptr, (long long)b.nO * b.nE, b.nO, Y,
                        nullptr, (long long)b.nE * nrhs, b.nE, T(0), Z, nullptr, (long long)b.nO * nrhs, b.nO,
                        b.count));
@@ -861,8 +873,12 @@ struct EngineImpl : EngineBase {
         if (j > 0)
           SLAB_TRY(gemm<TI>(s, nI, nrhs, nI, TI(-1), ifSub.as<TI>() + blk * j, nullptr, 0, nI, Zi + vb * (j - 1),
                             nullptr, 0, nI, TI(1), F + vb * j, nullptr, 0, nI, 1));
-        SLAB_TRY(bigtrs<TI>(s, ifLU.as<TI>() + blk * j, nI, nI, ifPerm.as<int>() + (long long)nI * j, F + vb * j, nI,
-                            Zi + vb * j, nI, nrhs));
+        if (nrhs <= kCoopMaxRhs)
+          SLAB_TRY(trsv_coop<TI>(s, ifLU.as<TI>() + blk * j, nI, nI, ifPerm.as<int>() + (long long)nI * j, F + vb * j,
+                                 nI, Zi + vb * j, nI, nrhs));
+        else
+          SLAB_TRY(bigtrs<TI>(s, ifLU.as<TI>() + blk * j, nI, nI, ifPerm.as<int>() + (long long)nI * j, F + vb * j,
+                              nI, Zi + vb * j, nI, nrhs));
       }
       for (int j = nbI - 2; j >= 0; --j)
         SLAB_TRY(gemm<TI>(s, nI, nrhs, nI, TI(-1), ifX.as<TI>() + blk * j, nullptr, 0, nI, Zi + vb * (j + 1), nullptr,

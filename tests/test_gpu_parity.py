@@ -189,3 +189,18 @@ def test_domain_solver_reference_config1_solution():
     stride = int(g['stride'])
     assert np.linalg.norm(sol[::stride] - g['sol_sub']) / np.linalg.norm(g['sol_sub']) < 1e-8
     assert abs(float(tres) - float(g['trueres'])) < 1e-4 * float(g['trueres'])
+
+
+@pytest.mark.parametrize('nrhs', [3, 6, 12])
+def test_engine_multi_rhs(nrhs):
+    """Several right-hand sides in one solve (warp, tiled and blocked solve kernels)."""
+    geom, p, n, kh = CASES[3]
+    a, md, part, co = _oracle_problem(geom, p, n, kh, ofuncs.bfield_gaussian_bumps)
+    rng = np.random.default_rng(nrhs)
+    B = rng.standard_normal((md.ntot, nrhs))          # face values; only Dirichlet faces are used
+    out = odomain.solve_full(md, part, co, lambda x: B[part.I_Xtot])
+    g, eng, uleaf, ufaces, iters, st = _engine_solve(geom, p, a, co, lambda x: B, 'mixed', md.xx_active)
+    assert st['converged']
+    ref = out['sol_tot']
+    rel = np.linalg.norm(uleaf - ref, axis=0) / np.linalg.norm(ref, axis=0)
+    assert rel.max() < 1e-9, rel
