@@ -69,6 +69,25 @@ int slab_leaf_dtn(int nleaf, int p, const double* d_c11, const double* d_c22, co
                   double* d_S, int* d_info, void* stream);
 
 /*
+ * Allocation-free batched leaf DtN maps.  No counterpart in the reference: it
+ * exists for callers that cannot allocate device memory when they need DtN
+ * maps (inside CUDA stream capture, where cudaMalloc is not allowed, or under
+ * a host application that owns all device memory).  Same arguments and
+ * results as slab_leaf_dtn without the work buffer and without S; the leaf
+ * factors live in a fixed scratch array compiled into the library
+ * (slab_leaf_dtn_noalloc_max_bytes() bytes, held on every device that loads
+ * the library).  Calls whose work would exceed it fail with SLAB_ERR_ARG.
+ * The first call on each device looks up the scratch address
+ * (cudaGetSymbolAddress) and should come before any stream capture.  All
+ * calls share the scratch: calls that overlap on the GPU race.  Allocates
+ * nothing (no cudaMalloc / cudaFree).
+ */
+size_t slab_leaf_dtn_noalloc_max_bytes(void);
+int slab_leaf_dtn_noalloc(int nleaf, int p, const double* d_c11, const double* d_c22, const double* d_c1,
+                          const double* d_c2, const double* d_c, const double* d_D, const double* d_Dsq,
+                          const double* d_Nx, int precision, double* d_dtn, int* d_info, void* stream);
+
+/*
  * Factor-and-solve engine for the unit-square HPS SlabLU path.
  * Replaces Domain_Solver.build (src_solver/slablu_solver.py:440-487: leaf DtN
  * assembly, build_slabLU :297-358, build_Tred_solver :668-687) and

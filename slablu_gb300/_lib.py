@@ -36,6 +36,8 @@ _SIGS = {
     'slab_engine_residual': (c_int, [c_void, c_int] + [c_void] * 5),
     'slab_engine_factor_bytes': (c_size, [c_void]),
     'slab_engine_timings': (c_int, [c_void, P_double, c_int]),
+    'slab_leaf_dtn_noalloc_max_bytes': (c_size, []),
+    'slab_leaf_dtn_noalloc': (c_int, [c_int, c_int] + [c_void] * 8 + [c_int, c_void, c_void, c_void]),
     'slab_launch_count': (c_ll, []),
 }
 

@@ -193,6 +193,16 @@ int leaf_dtn_impl(int nleaf, int p, const LeafCoeffs& co, const double* D, const
 }
 
 }  // namespace
+
+// Leaf DtN maps with a caller-provided work area (no allocation).
+int leaf_dtn_with_work(int nleaf, int p, const LeafCoeffs& co, const double* D, const double* Dsq, const double* Nx,
+                       int precision, void* work, size_t work_bytes, double* dtn_out, double* S_out, int* info,
+                       cudaStream_t s) {
+  if (precision == SLAB_PREC_FP64)
+    return leaf_dtn_impl<double>(nleaf, p, co, D, Dsq, Nx, work, work_bytes, dtn_out, S_out, info, s);
+  return leaf_dtn_impl<float>(nleaf, p, co, D, Dsq, Nx, work, work_bytes, dtn_out, S_out, info, s);
+}
+
 }  // namespace slab
 
 extern "C" size_t slab_leaf_dtn_work_bytes(int nleaf, int p, int precision) {
