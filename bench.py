@@ -291,8 +291,8 @@ def run_ours(args):
                              f'{args.tol:g}', buf=g.buf, Npan=g.Npan, parallelism='replicas' if world > 1 else 'single GPU',
                     l2='inputs and factors (~17 GB) larger than L2; no flush'),
         rel_err_vs_fp64=rel_err, refine_iters=int(iters), fp64_iters=int(it64),
-        fp64_value=N / (sum(fp64_times) / len(fp64_times)),
-        speedup_vs_fp64=(N / (t_total / args.steps)) / (N / (sum(fp64_times) / len(fp64_times))),
+        fp64_value=(N / (sum(fp64_times) / len(fp64_times))) if fp64_times else None,
+        speedup_vs_fp64=((sum(fp64_times) / len(fp64_times)) / (t_total / args.steps)) if fp64_times else None,
         phases_ms=dict(leaf=leaf_avg * 1e3, tree=sum(tree_ms) / len(tree_ms), interface=iface_avg * 1e3,
                        solve_applications=sum(apply_ms) / len(apply_ms), applications=sum(napply) / len(napply),
                        fp64_leaf=tim64['leaf_ms'], fp64_tree=tim64['tree_ms'], fp64_interface=tim64['interface_ms']),

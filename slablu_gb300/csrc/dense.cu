@@ -115,24 +115,24 @@ int getrs_small(cudaStream_t s, int n, int nrhs, const T* LU, const long long* o
 }
 
 template <typename T>
-int trsv_coop(cudaStream_t s, const T* LU, int lda, int n, const int* perm, const T* B, int ldb, T* X, int ldx,
-              int nrhs) {
+int trsv_coop(cudaStream_t s, const T* LU, int lda, int n, const int* perm, const T* Linv, const T* Uinv, int bs,
+              const T* B, int ldb, T* X, int ldx, int nrhs) {
   if (n <= 0 || nrhs <= 0) return SLAB_OK;
   if (nrhs > kCoopMaxRhs) return set_error(SLAB_ERR_ARG, "trsv_coop: nrhs %d > %d", nrhs, kCoopMaxRhs);
-  static int max_grid = 0;
-  if (max_grid == 0) {
-    int dev = 0, sms = 0, per_sm = 0;
-    SLAB_CUDA_TRY(cudaGetDevice(&dev));
-    SLAB_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    SLAB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, trsv_coop_kernel<T>, 256, 0));
-    max_grid = sms * (per_sm > 0 ? per_sm : 1);
-  }
-  const int nblk = ceil_div(n, kCoopRows);
+  const size_t bytes = ((size_t)kCoopMaxOwn * bs * nrhs + (size_t)bs * (bs + 1) + (size_t)bs * nrhs) * sizeof(T);
+  SLAB_TRY(ensure_smem(trsv_coop_kernel<T>, bytes, "trsv_coop"));
+  int dev = 0, sms = 0, per_sm = 0;
+  SLAB_CUDA_TRY(cudaGetDevice(&dev));
+  SLAB_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  SLAB_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, trsv_coop_kernel<T>, 256, bytes));
+  const int max_grid = sms * (per_sm > 0 ? per_sm : 0);
+  const int nblk = ceil_div(n, bs);
   const int G = nblk < max_grid ? nblk : max_grid;
-  if (ceil_div(nblk, G) > 8) return set_error(SLAB_ERR_ARG, "trsv_coop: order %d too large", n);
-  void* args[] = {(void*)&LU, (void*)&lda, (void*)&n, (void*)&perm, (void*)&B, (void*)&ldb, (void*)&X, (void*)&ldx,
-                  (void*)&nrhs};
-  SLAB_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)trsv_coop_kernel<T>, dim3(G), dim3(256), args, 0, s));
+  if (G <= 0 || ceil_div(nblk, G) > kCoopMaxOwn)
+    return set_error(SLAB_ERR_ARG, "trsv_coop: order %d too large for a co-resident grid", n);
+  void* args[] = {(void*)&LU, (void*)&lda, (void*)&n, (void*)&perm, (void*)&Linv, (void*)&Uinv, (void*)&bs,
+                  (void*)&B, (void*)&ldb, (void*)&X, (void*)&ldx, (void*)&nrhs};
+  SLAB_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)trsv_coop_kernel<T>, dim3(G), dim3(256), args, bytes, s));
   SLAB_CHECK_LAUNCH();
   return SLAB_OK;
 }
@@ -248,25 +248,116 @@ int getrs_batched(cudaStream_t s, int n, int nrhs, const T* LU, const long long*
   return SLAB_OK;
 }
 
+namespace {
+constexpr int kPanelCluster = 8;
+
+// Panel factorization: distributed shared memory of one 8-CTA cluster when the
+// panel fits (rows per CTA * nb elements), the global-memory kernel otherwise.
 template <typename T>
-int biglu(cudaStream_t s, T* A, int lda, int n, int* ipiv, int* info) {
+int panel_factor(cudaStream_t s, T* A, int lda, int n, int k0, int nb, int* ipiv, int* info) {
+  const int m = n - k0;
+  const int R = ceil_div(m, kPanelCluster);
+  const size_t bytes = ((size_t)R * nb + nb) * sizeof(T);
+  const size_t lim = allow_dynamic_smem(reinterpret_cast<const void*>(biglu_panel_cluster_kernel<T>));
+  if (bytes <= lim && m >= kPanelCluster) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(kPanelCluster);
+    cfg.blockDim = dim3(256);
+    cfg.dynamicSmemBytes = bytes;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = kPanelCluster;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    SLAB_CUDA_TRY(cudaLaunchKernelEx(&cfg, biglu_panel_cluster_kernel<T>, A, lda, n, k0, nb, R, ipiv, info));
+    SLAB_CHECK_LAUNCH();
+    return SLAB_OK;
+  }
+  biglu_panel_kernel<T><<<1, 1024, 0, s>>>(A, lda, n, k0, nb, ipiv, info);
+  SLAB_CHECK_LAUNCH();
+  return SLAB_OK;
+}
+}  // namespace
+
+template <typename T>
+int tri_inv_blocks(cudaStream_t s, const T* LU, int lda, int n, int bs, T* Linv, T* Uinv) {
+  const int nblk = ceil_div(n, bs);
+  const size_t bytes = 2 * (size_t)bs * (bs + 1) * sizeof(T);
+  SLAB_TRY(ensure_smem(tri_inv_blocks_kernel<T>, bytes, "tri_inv_blocks"));
+  if (Linv) {
+    tri_inv_blocks_kernel<T><<<nblk, 128, bytes, s>>>(LU, lda, n, bs, 0, Linv);
+    SLAB_CHECK_LAUNCH();
+  }
+  if (Uinv) {
+    tri_inv_blocks_kernel<T><<<nblk, 128, bytes, s>>>(LU, lda, n, bs, 1, Uinv);
+    SLAB_CHECK_LAUNCH();
+  }
+  return SLAB_OK;
+}
+
+template <typename T>
+static int trsm_inv(cudaStream_t s, const T* Inv, int bs, int k0, int nb, T* X, int ldx, int ncols) {
+  if (ncols <= 0 || nb <= 0) return SLAB_OK;
+  const size_t bytes = ((size_t)bs * bs + (size_t)bs * 64) * sizeof(T);
+  SLAB_TRY(ensure_smem(trsm_inv_kernel<T>, bytes, "trsm_inv"));
+  trsm_inv_kernel<T><<<ceil_div(ncols, 64), 256, bytes, s>>>(Inv, bs, k0, nb, X, ldx, ncols);
+  SLAB_CHECK_LAUNCH();
+  return SLAB_OK;
+}
+
+template <typename T>
+int biglu(cudaStream_t s, T* A, int lda, int n, int* ipiv, int* info, T* work) {
   for (int k0 = 0; k0 < n; k0 += kNB) {
     const int nb = n - k0 < kNB ? n - k0 : kNB;
-    biglu_panel_kernel<T><<<1, 1024, 0, s>>>(A, lda, n, k0, nb, ipiv, info);
-    SLAB_CHECK_LAUNCH();
+    SLAB_TRY(panel_factor<T>(s, A, lda, n, k0, nb, ipiv, info));
     if (n - nb > 0) {
       biglu_swap_kernel<T><<<ceil_div(n - nb, 256), 256, 0, s>>>(A, lda, n, k0, nb, ipiv);
       SLAB_CHECK_LAUNCH();
     }
     const int rest = n - k0 - nb;
     if (rest > 0) {
-      trsm_block_kernel<T><<<ceil_div(rest, 64), 256, 0, s>>>(A, lda, k0, nb, A + (size_t)(k0 + nb) * lda, lda,
-                                                             rest, 0);
-      SLAB_CHECK_LAUNCH();
+      if (work) {
+        // U12 = L11^{-1} A12 through the explicit inverse of the panel's unit-lower triangle
+        SLAB_TRY(tri_inv_blocks<T>(s, A + (size_t)k0 * lda + k0, lda, nb, kNB, work, nullptr));
+        SLAB_TRY(trsm_inv<T>(s, work, kNB, k0, nb, A + (size_t)(k0 + nb) * lda, lda, rest));
+      } else {
+        trsm_block_kernel<T><<<ceil_div(rest, 64), 256, 0, s>>>(A, lda, k0, nb, A + (size_t)(k0 + nb) * lda, lda,
+                                                               rest, 0);
+        SLAB_CHECK_LAUNCH();
+      }
       SLAB_TRY(gemm<T>(s, rest, rest, nb, T(-1), A + (size_t)k0 * lda + k0 + nb, nullptr, 0, lda,
                        A + (size_t)(k0 + nb) * lda + k0, nullptr, 0, lda, T(1),
                        A + (size_t)(k0 + nb) * lda + k0 + nb, nullptr, 0, lda, 1));
     }
+  }
+  return SLAB_OK;
+}
+
+template <typename T>
+int bigtrs_inv(cudaStream_t s, const T* LU, int lda, int n, const int* perm, const T* Linv, const T* Uinv, int bs,
+               const T* B, int ldb, T* X, int ldx, int nrhs) {
+  if (n <= 0 || nrhs <= 0) return SLAB_OK;
+  const long long tot = (long long)n * nrhs;
+  permute_rows_kernel<T><<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(B, ldb, X, ldx, n, nrhs, perm);
+  SLAB_CHECK_LAUNCH();
+  const int nblk = ceil_div(n, bs);
+  for (int b = 0; b < nblk; ++b) {
+    const int k0 = b * bs, nb = n - k0 < bs ? n - k0 : bs;
+    SLAB_TRY(trsm_inv<T>(s, Linv + (size_t)b * bs * bs, bs, k0, nb, X, ldx, nrhs));
+    const int rest = n - k0 - nb;
+    if (rest > 0)
+      SLAB_TRY(gemm<T>(s, rest, nrhs, nb, T(-1), LU + (size_t)k0 * lda + k0 + nb, nullptr, 0, lda, X + k0, nullptr, 0,
+                       ldx, T(1), X + k0 + nb, nullptr, 0, ldx, 1));
+  }
+  for (int b = nblk - 1; b >= 0; --b) {
+    const int k0 = b * bs, nb = n - k0 < bs ? n - k0 : bs;
+    SLAB_TRY(trsm_inv<T>(s, Uinv + (size_t)b * bs * bs, bs, k0, nb, X, ldx, nrhs));
+    if (k0 > 0)
+      SLAB_TRY(gemm<T>(s, k0, nrhs, nb, T(-1), LU + (size_t)k0 * lda, nullptr, 0, lda, X + k0, nullptr, 0, ldx, T(1), X,
+                       nullptr, 0, ldx, 1));
   }
   return SLAB_OK;
 }
@@ -317,7 +408,10 @@ int bigtrs(cudaStream_t s, const T* LU, int lda, int n, const int* perm, const T
   template int getrs_batched<T>(cudaStream_t, int, int, const T*, const long long*, long long, int,           \
                                 const int*, const long long*, long long, T*, const long long*, long long,     \
                                 int, int, bool, bool);                                                        \
-  template int biglu<T>(cudaStream_t, T*, int, int, int*, int*);                                              \
+  template int biglu<T>(cudaStream_t, T*, int, int, int*, int*, T*);                                          \
+  template int tri_inv_blocks<T>(cudaStream_t, const T*, int, int, int, T*, T*);                              \
+  template int bigtrs_inv<T>(cudaStream_t, const T*, int, int, const int*, const T*, const T*, int, const T*,  \
+                             int, T*, int, int);                                                              \
   template int bigtrs<T>(cudaStream_t, const T*, int, int, const int*, const T*, int, T*, int, int, bool, bool);
 
 SLAB_INSTANTIATE(float)
@@ -328,8 +422,9 @@ template int getrs_small<float>(cudaStream_t, int, int, const float*, const long
 template int getrs_small<double>(cudaStream_t, int, int, const double*, const long long*, long long, int,
                                  const int*, const long long*, long long, double*, const long long*, long long, int,
                                  int);
-template int trsv_coop<float>(cudaStream_t, const float*, int, int, const int*, const float*, int, float*, int, int);
-template int trsv_coop<double>(cudaStream_t, const double*, int, int, const int*, const double*, int, double*, int,
-                               int);
+template int trsv_coop<float>(cudaStream_t, const float*, int, int, const int*, const float*, const float*, int,
+                              const float*, int, float*, int, int);
+template int trsv_coop<double>(cudaStream_t, const double*, int, int, const int*, const double*, const double*, int,
+                               const double*, int, double*, int, int);
 
 }  // namespace slab

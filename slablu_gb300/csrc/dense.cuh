@@ -653,121 +653,86 @@ __global__ void __launch_bounds__(32 * kWarpSolveWarps)
 }
 
 // Cooperative triangular solves with one large factored matrix (FP64
-// interface blocks), X = U^{-1} L^{-1} P B for nrhs <= 8 columns.
-// CTA j owns the 32-row blocks j, j+G, ...; it applies the contributions of
-// every solved block to its rows and solves its own diagonal blocks
-// (owner computes).  One grid-wide barrier per block.
-constexpr int kCoopRows = 32;
+// interface blocks): X = U^{-1} L^{-1} P B for nrhs <= 8 columns, using the
+// precomputed inverses of the bs x bs diagonal triangles (tri_inv_blocks).
+// CTA j owns the row blocks j, j+G, ... (at most kCoopMaxOwn); per block b
+// its owner forms x_b = inv_b acc_b, then after one grid-wide barrier every
+// CTA subtracts the block's contribution from the rows it owns.
 constexpr int kCoopMaxRhs = 8;
+constexpr int kCoopMaxOwn = 4;
 template <typename T>
 __global__ void __launch_bounds__(256) trsv_coop_kernel(const T* __restrict__ LU, int lda, int n,
-                                                       const int* __restrict__ perm, const T* __restrict__ Bin,
-                                                       int ldb, T* X, int ldx, int nrhs) {
+                                                       const int* __restrict__ perm, const T* __restrict__ Linv,
+                                                       const T* __restrict__ Uinv, int bs,
+                                                       const T* __restrict__ Bin, int ldb, T* X, int ldx, int nrhs) {
   namespace cg = cooperative_groups;
   cg::grid_group grid = cg::this_grid();
-  __shared__ T acc[8][kCoopRows * kCoopMaxRhs];  // owned blocks (up to 8 per CTA)
-  __shared__ T dblk[kCoopRows * (kCoopRows + 1)];
-  __shared__ T xb[kCoopRows * kCoopMaxRhs];
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int ldd = bs + 1;
+  T* acc = reinterpret_cast<T*>(smem_raw);          // kCoopMaxOwn x (bs x nrhs)
+  T* dblk = acc + (size_t)kCoopMaxOwn * bs * nrhs;   // bs x bs, ld bs+1
+  T* xb = dblk + (size_t)bs * ldd;                   // bs x nrhs
   const int G = gridDim.x, j = blockIdx.x, tid = threadIdx.x;
-  const int nblk = (n + kCoopRows - 1) / kCoopRows;
-  const int nown = (nblk - j + G - 1) / G;  // blocks j, j+G, ... (<= 8, checked by the launcher)
-  // acc = (P^T B) on owned rows
+  const int nblk = (n + bs - 1) / bs;
+  const int nown = (nblk - j + G - 1) / G;
   for (int o = 0; o < nown; ++o) {
-    const int r0 = (j + o * G) * kCoopRows;
-    for (int idx = tid; idx < kCoopRows * nrhs; idx += blockDim.x) {
-      const int r = idx % kCoopRows, c = idx / kCoopRows;
-      acc[o][idx] = (r0 + r < n) ? Bin[perm[r0 + r] + (size_t)c * ldb] : T(0);
+    const int r0 = (j + o * G) * bs;
+    for (int idx = tid; idx < bs * nrhs; idx += blockDim.x) {
+      const int r = idx % bs, c = idx / bs;
+      acc[(size_t)o * bs * nrhs + idx] = (r0 + r < n) ? Bin[perm[r0 + r] + (size_t)c * ldb] : T(0);
     }
   }
-  __syncthreads();
-  const int lane = tid & 31, warp = tid >> 5;
-  // ---- forward, unit lower
-  for (int b = 0; b < nblk; ++b) {
-    const int k0 = b * kCoopRows, kb = min(kCoopRows, n - k0);
-    if (b % G == j) {
-      const int o = b / G;
-      __syncthreads();
-      for (int idx = tid; idx < kb * kb; idx += blockDim.x) {
-        const int r = idx % kb, c = idx / kb;
-        dblk[r + c * (kCoopRows + 1)] = LU[(size_t)(k0 + c) * lda + k0 + r];
+  for (int pass = 0; pass < 2; ++pass) {
+    const bool lower = pass == 0;
+    const T* Inv = lower ? Linv : Uinv;
+    for (int step = 0; step < nblk; ++step) {
+      const int b = lower ? step : nblk - 1 - step;
+      const int k0 = b * bs, kb = min(bs, n - k0);
+      if (b % G == j) {
+        const int o = b / G;
+        __syncthreads();
+        for (int idx = tid; idx < bs * bs; idx += blockDim.x) dblk[(idx % bs) + (idx / bs) * ldd] = Inv[(size_t)b * bs * bs + idx];
+        __syncthreads();
+        for (int idx = tid; idx < kb * nrhs; idx += blockDim.x) {
+          const int r = idx % kb, c = idx / kb;
+          const T* a = acc + (size_t)o * bs * nrhs + (size_t)c * bs;
+          T sum = T(0);
+          for (int k = 0; k < kb; ++k) sum += dblk[r + k * ldd] * a[k];
+          X[k0 + r + (size_t)c * ldx] = sum;
+        }
       }
+      grid.sync();
       __syncthreads();
-      if (warp < nrhs) {
-        T v = lane < kb ? acc[o][lane + warp * kCoopRows] : T(0);
-        for (int i = 0; i < kb; ++i) {
-          const T xi = __shfl_sync(0xffffffffu, v, i);
-          if (lane > i && lane < kb) v -= dblk[lane + i * (kCoopRows + 1)] * xi;
+      for (int idx = tid; idx < kb * nrhs; idx += blockDim.x) xb[idx] = X[k0 + idx % kb + (size_t)(idx / kb) * ldx];
+      for (int o = 0; o < nown; ++o) {
+        const int ob = j + o * G;
+        if (lower ? ob <= b : ob >= b) continue;
+        const int r0 = ob * bs;
+        const int rb = min(bs, n - r0);
+        __syncthreads();
+        for (int idx = tid; idx < rb * kb; idx += blockDim.x) {
+          const int r = idx % rb, k = idx / rb;
+          dblk[r + k * ldd] = LU[(size_t)(k0 + k) * lda + r0 + r];
         }
-        if (lane < kb) {
-          acc[o][lane + warp * kCoopRows] = v;
-          X[k0 + lane + (size_t)warp * ldx] = v;
+        __syncthreads();
+        for (int idx = tid; idx < rb * nrhs; idx += blockDim.x) {
+          const int r = idx % rb, c = idx / rb;
+          T sum = T(0);
+          for (int k = 0; k < kb; ++k) sum += dblk[r + k * ldd] * xb[k + c * kb];
+          acc[(size_t)o * bs * nrhs + r + (size_t)c * bs] -= sum;
         }
+      }
+    }
+    // second pass starts from the forward result held in X for the owned rows
+    __syncthreads();
+    for (int o = 0; o < nown; ++o) {
+      const int r0 = (j + o * G) * bs;
+      for (int idx = tid; idx < bs * nrhs; idx += blockDim.x) {
+        const int r = idx % bs, c = idx / bs;
+        acc[(size_t)o * bs * nrhs + idx] = (r0 + r < n) ? X[r0 + r + (size_t)c * ldx] : T(0);
       }
     }
     grid.sync();
-    for (int idx = tid; idx < kb * nrhs; idx += blockDim.x) xb[idx] = X[k0 + idx % kb + (size_t)(idx / kb) * ldx];
-    for (int o = 0; o < nown; ++o) {
-      const int ob = j + o * G;
-      if (ob <= b) continue;
-      const int r0 = ob * kCoopRows;
-      const int rb = min(kCoopRows, n - r0);
-      __syncthreads();
-      for (int idx = tid; idx < rb * kb; idx += blockDim.x) {
-        const int r = idx % rb, k = idx / rb;
-        dblk[r + k * (kCoopRows + 1)] = LU[(size_t)(k0 + k) * lda + r0 + r];
-      }
-      __syncthreads();
-      for (int idx = tid; idx < rb * nrhs; idx += blockDim.x) {
-        const int r = idx % rb, c = idx / rb;
-        T s = T(0);
-        for (int k = 0; k < kb; ++k) s += dblk[r + k * (kCoopRows + 1)] * xb[k + c * kb];
-        acc[o][r + c * kCoopRows] -= s;
-      }
-    }
-    __syncthreads();
-  }
-  // ---- backward, upper (non-unit)
-  for (int b = nblk - 1; b >= 0; --b) {
-    const int k0 = b * kCoopRows, kb = min(kCoopRows, n - k0);
-    if (b % G == j) {
-      const int o = b / G;
-      __syncthreads();
-      for (int idx = tid; idx < kb * kb; idx += blockDim.x) {
-        const int r = idx % kb, c = idx / kb;
-        dblk[r + c * (kCoopRows + 1)] = LU[(size_t)(k0 + c) * lda + k0 + r];
-      }
-      __syncthreads();
-      if (warp < nrhs) {
-        T v = lane < kb ? acc[o][lane + warp * kCoopRows] : T(0);
-        for (int i = kb - 1; i >= 0; --i) {
-          if (lane == i) v /= dblk[i + i * (kCoopRows + 1)];
-          const T xi = __shfl_sync(0xffffffffu, v, i);
-          if (lane < i) v -= dblk[lane + i * (kCoopRows + 1)] * xi;
-        }
-        if (lane < kb) X[k0 + lane + (size_t)warp * ldx] = v;
-      }
-    }
-    grid.sync();
-    for (int idx = tid; idx < kb * nrhs; idx += blockDim.x) xb[idx] = X[k0 + idx % kb + (size_t)(idx / kb) * ldx];
-    for (int o = 0; o < nown; ++o) {
-      const int ob = j + o * G;
-      if (ob >= b) continue;
-      const int r0 = ob * kCoopRows;
-      const int rb = min(kCoopRows, n - r0);
-      __syncthreads();
-      for (int idx = tid; idx < rb * kb; idx += blockDim.x) {
-        const int r = idx % rb, k = idx / rb;
-        dblk[r + k * (kCoopRows + 1)] = LU[(size_t)(k0 + k) * lda + r0 + r];
-      }
-      __syncthreads();
-      for (int idx = tid; idx < rb * nrhs; idx += blockDim.x) {
-        const int r = idx % rb, c = idx / rb;
-        T s = T(0);
-        for (int k = 0; k < kb; ++k) s += dblk[r + k * (kCoopRows + 1)] * xb[k + c * kb];
-        acc[o][r + c * kCoopRows] -= s;
-      }
-    }
-    __syncthreads();
   }
 }
 
@@ -859,6 +824,172 @@ __global__ void __launch_bounds__(1024) biglu_panel_kernel(T* A, int lda, int n,
       }
     }
     __syncthreads();
+  }
+}
+
+// Panel factorization held in the distributed shared memory of one thread-block
+// cluster of CL CTAs: CTA r keeps panel rows [r*R, (r+1)*R) of the m x nb
+// panel (rows k0.. of columns k0..k0+nb).  Per column: local argmax, exchange
+// of the CL candidates through DSMEM, row swap through DSMEM, pivot row
+// broadcast, local rank-1 update; two cluster barriers per column.
+// Shared memory: R * nb elements + nb (pivot row).  grid = CL (one cluster).
+template <typename T>
+__global__ void __launch_bounds__(256) biglu_panel_cluster_kernel(T* A, int lda, int n, int k0, int nb, int R,
+                                                                  int* ipiv, int* info) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cluster = cg::this_cluster();
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* P = reinterpret_cast<T*>(smem_raw);  // R x nb, ld R
+  T* prow = P + (size_t)R * nb;            // nb
+  __shared__ T cand_v[1];
+  __shared__ int cand_i[1];
+  __shared__ T sv[33];
+  __shared__ int si[33];
+  const int CL = (int)cluster.num_blocks();
+  const int r = (int)cluster.block_rank();
+  const int tid = threadIdx.x;
+  const int m = n - k0;
+  const int g0 = r * R;                     // first panel row held here
+  const int rows = max(0, min(R, m - g0));  // rows held here
+  for (int idx = tid; idx < rows * nb; idx += blockDim.x) {
+    const int i = idx % rows, c = idx / rows;
+    P[i + (size_t)c * R] = A[(size_t)(k0 + c) * lda + k0 + g0 + i];
+  }
+  cluster.sync();
+  for (int j = 0; j < nb && j < m; ++j) {
+    // local candidate over panel rows >= j
+    T best = T(-1);
+    int bi = INT_MAX;
+    for (int i = tid; i < rows; i += blockDim.x) {
+      if (g0 + i < j) continue;
+      const T a = tabs(P[i + (size_t)j * R]);
+      if (a > best) {
+        best = a;
+        bi = g0 + i;
+      }
+    }
+    const int li = cta_argmax(best, bi, sv, si);
+    if (tid == 0) {
+      cand_i[0] = li;
+      cand_v[0] = li == INT_MAX ? T(-1) : tabs(P[(li - g0) + (size_t)j * R]);
+    }
+    cluster.sync();
+    // winner over the cluster (identical in every CTA)
+    T wv = T(-1);
+    int wi = INT_MAX;
+    for (int q = 0; q < CL; ++q) {
+      const T v = *cluster.map_shared_rank(&cand_v[0], q);
+      const int i = *cluster.map_shared_rank(&cand_i[0], q);
+      if (i != INT_MAX && (v > wv || (v == wv && i < wi))) {
+        wv = v;
+        wi = i;
+      }
+    }
+    const int piv = wi == INT_MAX ? j : wi;
+    const int oj = j / R, op = piv / R;
+    if (r == oj) {
+      if (tid == 0) ipiv[k0 + j] = k0 + piv;
+      if (piv != j) {
+        T* Pj = cluster.map_shared_rank(P, oj);
+        T* Pp = cluster.map_shared_rank(P, op);
+        for (int c = tid; c < nb; c += blockDim.x) {
+          const T a = Pj[(j - oj * R) + (size_t)c * R];
+          Pj[(j - oj * R) + (size_t)c * R] = Pp[(piv - op * R) + (size_t)c * R];
+          Pp[(piv - op * R) + (size_t)c * R] = a;
+        }
+      }
+    }
+    cluster.sync();
+    {
+      const T* Pj = cluster.map_shared_rank(P, oj);
+      for (int c = tid; c < nb; c += blockDim.x) prow[c] = Pj[(j - oj * R) + (size_t)c * R];
+    }
+    __syncthreads();
+    const T d = prow[j];
+    if (d == T(0) || d != d) {
+      if (r == 0 && tid == 0 && info && *info == 0) *info = k0 + j + 1;
+    } else {
+      const T rd = T(1) / d;
+      for (int i = tid; i < rows; i += blockDim.x) {
+        if (g0 + i <= j) continue;
+        const T l = P[i + (size_t)j * R] * rd;
+        P[i + (size_t)j * R] = l;
+        for (int c = j + 1; c < nb; ++c) P[i + (size_t)c * R] -= l * prow[c];
+      }
+    }
+    // the next column's first cluster barrier orders these updates before any remote read
+  }
+  cluster.sync();
+  for (int idx = tid; idx < rows * nb; idx += blockDim.x) {
+    const int i = idx % rows, c = idx / rows;
+    A[(size_t)(k0 + c) * lda + k0 + g0 + i] = P[i + (size_t)c * R];
+  }
+}
+
+// Inverse of the nb x nb diagonal triangle A[k0:k0+nb, k0:k0+nb] (unit lower if
+// upper == 0, upper otherwise), one CTA per block; blocks k0 = blk * bs.
+// out: nblk blocks of bs x bs (column-major, ld bs), zero outside the triangle.
+template <typename T>
+__global__ void __launch_bounds__(128) tri_inv_blocks_kernel(const T* A, int lda, int n, int bs, int upper, T* out) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int ld = bs + 1;
+  T* D = reinterpret_cast<T*>(smem_raw);  // bs x bs, ld bs+1
+  T* Xs = D + (size_t)bs * ld;              // bs x bs, ld bs+1 (column c = thread c)
+  const int blk = blockIdx.x;
+  const int k0 = blk * bs, nb = min(bs, n - k0);
+  T* O = out + (size_t)blk * bs * bs;
+  for (int idx = threadIdx.x; idx < bs * bs; idx += blockDim.x) {
+    const int i = idx % bs, c = idx / bs;
+    D[i + c * ld] = (i < nb && c < nb) ? A[(size_t)(k0 + c) * lda + k0 + i] : T(0);
+    Xs[i + c * ld] = T(0);
+  }
+  __syncthreads();
+  for (int c = threadIdx.x; c < nb; c += blockDim.x) {
+    T* x = Xs + c * ld;
+    if (!upper) {
+      x[c] = T(1);
+      for (int i = c + 1; i < nb; ++i) {
+        T s = T(0);
+        for (int k = c; k < i; ++k) s -= D[i + k * ld] * x[k];
+        x[i] = s;
+      }
+    } else {
+      x[c] = T(1) / D[c + c * ld];
+      for (int i = c - 1; i >= 0; --i) {
+        T s = T(0);
+        for (int k = i + 1; k <= c; ++k) s -= D[i + k * ld] * x[k];
+        x[i] = s / D[i + i * ld];
+      }
+    }
+  }
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < bs * bs; idx += blockDim.x) {
+    const int i = idx % bs, c = idx / bs;
+    O[idx] = Xs[i + c * ld];
+  }
+}
+
+// X[k0:k0+nb, :] = Inv * X[k0:k0+nb, :] with a precomputed nb x nb inverse
+// (ld bs); grid: column tiles of 64.
+template <typename T>
+__global__ void __launch_bounds__(256) trsm_inv_kernel(const T* Inv, int bs, int k0, int nb, T* X, int ldx,
+                                                      int ncols) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* Is = reinterpret_cast<T*>(smem_raw);  // bs x bs
+  T* Xs = Is + bs * bs;                    // bs x 64
+  const int c0 = blockIdx.x * 64;
+  const int nc = min(64, ncols - c0);
+  for (int idx = threadIdx.x; idx < bs * bs; idx += blockDim.x) Is[idx] = Inv[idx];
+  for (int idx = threadIdx.x; idx < nb * nc; idx += blockDim.x) {
+    const int i = idx % nb, c = idx / nb;
+    Xs[i + c * bs] = X[(size_t)(c0 + c) * ldx + k0 + i];
+  }
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < nb * nc; idx += blockDim.x) {
+    const int i = idx % nb, c = idx / nb;
+    T s = T(0);
+    for (int k = 0; k < nb; ++k) s += Is[i + k * bs] * Xs[k + c * bs];
+    X[(size_t)(c0 + c) * ldx + k0 + i] = s;
   }
 }
 
@@ -954,8 +1085,19 @@ int getrs_batched(cudaStream_t s, int n, int nrhs, const T* LU, const long long*
                   bool upper = true);
 
 // Large single-matrix LU in place (n x n, lda); ipiv/info device pointers.
+// work: kNB*kNB elements (inverse of the current panel's unit-lower triangle).
 template <typename T>
-int biglu(cudaStream_t s, T* A, int lda, int n, int* ipiv, int* info);
+int biglu(cudaStream_t s, T* A, int lda, int n, int* ipiv, int* info, T* work = nullptr);
+
+// Inverses of the bs x bs diagonal triangles of a factored matrix:
+// Linv/Uinv hold ceil(n/bs) blocks of bs x bs each.
+template <typename T>
+int tri_inv_blocks(cudaStream_t s, const T* LU, int lda, int n, int bs, T* Linv, T* Uinv);
+
+// bigtrs with precomputed diagonal-block inverses (block size bs).
+template <typename T>
+int bigtrs_inv(cudaStream_t s, const T* LU, int lda, int n, const int* perm, const T* Linv, const T* Uinv, int bs,
+               const T* B, int ldb, T* X, int ldx, int nrhs);
 
 // X = U^{-1} L^{-1} P B for one large factored matrix; B (n x nrhs, ldb) is
 // permuted into X (ldx), then solved in place.  perm from perm_from_ipiv_kernel.
@@ -974,10 +1116,11 @@ int getrs_small(cudaStream_t s, int n, int nrhs, const T* LU, const long long* o
                 const int* perm, const long long* offP, long long strideP, T* B, const long long* offB,
                 long long strideB, int ldb, int batch);
 
-// X = U^{-1} L^{-1} P B for one large factored matrix, nrhs <= 8, cooperative launch.
+// X = U^{-1} L^{-1} P B for one large factored matrix, nrhs <= 8, cooperative
+// launch; Linv/Uinv from tri_inv_blocks with block size bs.
 template <typename T>
-int trsv_coop(cudaStream_t s, const T* LU, int lda, int n, const int* perm, const T* B, int ldb, T* X, int ldx,
-              int nrhs);
+int trsv_coop(cudaStream_t s, const T* LU, int lda, int n, const int* perm, const T* Linv, const T* Uinv, int bs,
+              const T* B, int ldb, T* X, int ldx, int nrhs);
 
 size_t smem_limit_bytes();
 

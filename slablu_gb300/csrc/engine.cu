@@ -308,7 +308,9 @@ struct EngineImpl : EngineBase {
   int nR = 0;
   // interface
   int nI = 0, nbI = 0;
-  DevBuf ifLU, ifPiv, ifPerm, ifX, ifSub, ifSup, ifInfo, ifGlob;
+  DevBuf ifLU, ifPiv, ifPerm, ifX, ifSub, ifSup, ifInfo, ifGlob, ifLinv, ifUinv, ifWork;
+  static constexpr int kInvBs = 64;  // diagonal-block size of the interface triangular inverses
+  int nInvBlk = 0;
   // solve buffers
   int cap_nrhs = 0;
   DevBuf wc, flux, gvec, uvec, Ybuf, Zbuf, ifF, ifZ, ux_d, uc_d, rc_d, rx_d, rcT, acc;
@@ -632,12 +634,17 @@ struct EngineImpl : EngineBase {
       SLAB_TRY(ifSup.alloc(blk * nbI * sizeof(TI)));
       SLAB_TRY(ifX.alloc(blk * nbI * sizeof(TI)));
       SLAB_TRY(ifInfo.alloc(sizeof(int)));
+      nInvBlk = ceil_div(nI, kInvBs);
+      SLAB_TRY(ifLinv.alloc((size_t)nbI * nInvBlk * kInvBs * kInvBs * sizeof(TI)));
+      SLAB_TRY(ifUinv.alloc((size_t)nbI * nInvBlk * kInvBs * kInvBs * sizeof(TI)));
+      SLAB_TRY(ifWork.alloc((size_t)kNB * kNB * sizeof(TI)));
     }
     SLAB_TRY(acc.alloc(4 * sizeof(double)));
     for (auto& e : ev) SLAB_CUDA_TRY(cudaEventCreate(&e));
     SLAB_CUDA_TRY(cudaStreamSynchronize(s));
-    factor_bytes_ = G.bytes + piv.bytes + nodepool.bytes + fpool.bytes + pivpool.bytes + ifLU.bytes + ifPiv.bytes +
-                    ifPerm.bytes + ifSub.bytes + ifSup.bytes + ifX.bytes;
+    factor_bytes_ = G.bytes + piv.bytes + leafperm.bytes + nodepool.bytes + fpool.bytes + pivpool.bytes +
+                    permpool.bytes + ifLU.bytes + ifPiv.bytes + ifPerm.bytes + ifSub.bytes + ifSup.bytes + ifX.bytes +
+                    ifLinv.bytes + ifUinv.bytes;
     return SLAB_OK;
   }
 
@@ -723,6 +730,9 @@ struct EngineImpl : EngineBase {
     return SLAB_OK;
   }
 
+  TI* linv(int j) { return ifLinv.as<TI>() + (size_t)j * nInvBlk * kInvBs * kInvBs; }
+  TI* uinv(int j) { return ifUinv.as<TI>() + (size_t)j * nInvBlk * kInvBs * kInvBs; }
+
   int factor_interface() {
     if (nbI > 0) {
       const long long blk = (long long)nI * nI;
@@ -734,13 +744,14 @@ struct EngineImpl : EngineBase {
         TI* Sj = ifLU.as<TI>() + blk * j;
         if (j > 0) {
           TI* Xprev = ifX.as<TI>() + blk * (j - 1);
-          SLAB_TRY(bigtrs<TI>(s, ifLU.as<TI>() + blk * (j - 1), nI, nI, ifPerm.as<int>() + (long long)nI * (j - 1),
-                              ifSup.as<TI>() + blk * (j - 1), nI, Xprev, nI, nI));
+          SLAB_TRY(bigtrs_inv<TI>(s, ifLU.as<TI>() + blk * (j - 1), nI, nI, ifPerm.as<int>() + (long long)nI * (j - 1),
+                                  linv(j - 1), uinv(j - 1), kInvBs, ifSup.as<TI>() + blk * (j - 1), nI, Xprev, nI, nI));
           SLAB_TRY(gemm<TI>(s, nI, nI, nI, TI(-1), ifSub.as<TI>() + blk * j, nullptr, 0, nI, Xprev, nullptr, 0, nI,
                             TI(1), Sj, nullptr, 0, nI, 1));
         }
-        SLAB_TRY(biglu<TI>(s, Sj, nI, nI, ifPiv.as<int>() + (long long)nI * j, ifInfo.as<int>()));
+        SLAB_TRY(biglu<TI>(s, Sj, nI, nI, ifPiv.as<int>() + (long long)nI * j, ifInfo.as<int>(), ifWork.as<TI>()));
         SLAB_TRY(build_perm(s, ifPiv.as<int>() + (long long)nI * j, nI, ifPerm.as<int>() + (long long)nI * j));
+        SLAB_TRY(tri_inv_blocks<TI>(s, Sj, nI, nI, kInvBs, linv(j), uinv(j)));
       }
     }
     return SLAB_OK;
@@ -874,11 +885,11 @@ struct EngineImpl : EngineBase {
           SLAB_TRY(gemm<TI>(s, nI, nrhs, nI, TI(-1), ifSub.as<TI>() + blk * j, nullptr, 0, nI, Zi + vb * (j - 1),
                             nullptr, 0, nI, TI(1), F + vb * j, nullptr, 0, nI, 1));
         if (nrhs <= kCoopMaxRhs)
-          SLAB_TRY(trsv_coop<TI>(s, ifLU.as<TI>() + blk * j, nI, nI, ifPerm.as<int>() + (long long)nI * j, F + vb * j,
-                                 nI, Zi + vb * j, nI, nrhs));
+          SLAB_TRY(trsv_coop<TI>(s, ifLU.as<TI>() + blk * j, nI, nI, ifPerm.as<int>() + (long long)nI * j, linv(j),
+                                 uinv(j), kInvBs, F + vb * j, nI, Zi + vb * j, nI, nrhs));
         else
-          SLAB_TRY(bigtrs<TI>(s, ifLU.as<TI>() + blk * j, nI, nI, ifPerm.as<int>() + (long long)nI * j, F + vb * j,
-                              nI, Zi + vb * j, nI, nrhs));
+          SLAB_TRY(bigtrs_inv<TI>(s, ifLU.as<TI>() + blk * j, nI, nI, ifPerm.as<int>() + (long long)nI * j, linv(j),
+                                  uinv(j), kInvBs, F + vb * j, nI, Zi + vb * j, nI, nrhs));
       }
       for (int j = nbI - 2; j >= 0; --j)
         SLAB_TRY(gemm<TI>(s, nI, nrhs, nI, TI(-1), ifX.as<TI>() + blk * j, nullptr, 0, nI, Zi + vb * (j + 1), nullptr,
