@@ -33,6 +33,8 @@ sys.path.insert(0, ROOT)
 METRIC = 'unknowns/sec factor+solve at N~4M p=22, mixed-prec vs FP64 GPU at 1e-6 rel err'
 P, NSIDE = 22, 2000
 CPU_SAMPLE_N = 400
+# DRAM bytes per leaf of leaf_factor_kernel<float>, measured with ncu on 1024 leaves
+LEAF_DRAM_BYTES_PER_LEAF = 9.68e9 / 1024
 
 
 def parse():
@@ -42,9 +44,11 @@ def parse():
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
     ap.add_argument('--n', type=int, default=NSIDE, help='points per side (p-2 divides it)')
-    ap.add_argument('--tol', type=float, default=1e-8, help='refinement tolerance (relative correction)')
+    ap.add_argument('--tol', type=float, default=1e-7,
+                    help='refinement tolerance on the relative correction; the error left is ~0.1x this')
     ap.add_argument('--fp64-steps', type=int, default=1, help='timed steps of the all-FP64 path')
     ap.add_argument('--no-cpu-baseline', action='store_true')
+    ap.add_argument('--nrhs', type=int, default=256, help='right-hand sides of the multi-RHS solve (0 = skip)')
     return ap.parse_args()
 
 
@@ -268,6 +272,24 @@ def run_ours(args):
     h2d = 3 * hc.numel() * 8 + hb.numel() * 8
     d2h = hout.numel() * 8
 
+    # ---- 256 right-hand sides on the same factorization (one graph per application)
+    multi = None
+    if args.nrhs > 0:
+        ix = torch.as_tensor(g.I_Xtot, device=dev)
+        B = torch.zeros(g.ntot, args.nrhs, dtype=torch.float64, device=dev)
+        B[ix] = problems.config4_rhs(len(g.I_Xtot), args.nrhs).to(dev)
+        eng.factor(c11=one, c22=one, c=c)
+        eng.solve(B, tol=args.tol, max_iter=30)  # warm-up (captures the nrhs-wide graph)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        um, _, itm, stm = eng.solve(B, tol=args.tol, max_iter=30)
+        torch.cuda.synchronize()
+        tm_ = time.perf_counter() - t0
+        multi = dict(nrhs=args.nrhs, solve_ms=1e3 * tm_, refine_iters=int(itm), rhs_per_s=args.nrhs / tm_,
+                     unknowns_rhs_per_s=N * args.nrhs / tm_, converged=bool(stm['converged']))
+        del B, um
+        torch.cuda.empty_cache()
+
     # ---- roofline of the leaf kernel (one launch per step) --------------------
     lf = leaf_flops(p) * g.nboxes
     leaf_avg = sum(leaf_ms) / len(leaf_ms) / 1e3
@@ -298,13 +320,17 @@ def run_ours(args):
                        fp64_leaf=tim64['leaf_ms'], fp64_tree=tim64['tree_ms'], fp64_interface=tim64['interface_ms']),
         interface_fp64_tflops=if_fl / iface_avg / 1e12,
         roofline=dict(kernel='leaf_factor_kernel<float> (one launch per step)', bound='tensor', achieved=achieved,
-                      peak=peak, unit='TFLOP/s', frac=achieved / peak, traffic=None,
+                      peak=peak, unit='TFLOP/s', frac=achieved / peak,
+                      traffic=LEAF_DRAM_BYTES_PER_LEAF * g.nboxes,
+                      traffic_source='dram read+write per leaf from the 1024-leaf ncu capture '
+                                     '(profiles/leaf_factor_kernel_fp32_1024leaves.md) x leaves per launch',
                       peak_source='MEASURED_PEAKS.json bf16_tflops (measured)' if bf16 else 'fallback 1.9 PF bf16',
                       algorithmic_flops_per_launch=lf),
         clocks=clocks,
         e2e=dict(value=N / (sum(e2e_times) / len(e2e_times)), unit='unknowns/s', h2d_bytes_per_step=h2d,
                  d2h_bytes_per_step=d2h),
         gpu_launches=int(launches),
+        multi_rhs=multi,
     )
     if rank == 0 and not args.no_cpu_baseline:
         Nc, tc = cpu_sample()

@@ -1,0 +1,41 @@
+"""Fixed workloads for profiling single phases on one GPU.
+
+    python -m slablu_gb300.profile_cases factor --n 640 --precision mixed
+    python -m slablu_gb300.profile_cases solve  --n 2000 --precision mixed --iters 1
+
+Both use the Gaussian-lattice Helmholtz field of the benchmark (p = 22) on an
+n x n-point grid ((n/20)^2 leaves).  `factor` runs one factorization; `solve`
+runs one factorization and one refined solve with at most --iters steps.
+"""
+import argparse
+
+import torch
+
+from . import hps, problems
+from .engine import SlabEngine
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument('case', choices=['factor', 'solve'])
+    ap.add_argument('--n', type=int, default=640)
+    ap.add_argument('--precision', default='mixed', choices=['fp64', 'mixed', 'fp32'])
+    ap.add_argument('--iters', type=int, default=1)
+    a = ap.parse_args(argv)
+    cfg = problems.config3()
+    p = cfg['p']
+    g = hps.Geometry([[0, 1], [0, 1]], problems.leaf_half_width(a.n, p), p, 1.0)
+    xx = torch.as_tensor(g.xx_tot, device='cuda')
+    c = cfg['c'](xx).contiguous()
+    one = torch.ones_like(c)
+    eng = SlabEngine(g, a.precision)
+    eng.factor(c11=one, c22=one, c=c)
+    if a.case == 'solve':
+        eng.solve(torch.ones(g.ntot, dtype=torch.float64, device='cuda'), tol=1e-10, max_iter=a.iters,
+                  allow_noconv=True)
+    torch.cuda.synchronize()
+    print('ok', a.case, g.nboxes, 'leaves', eng.timings())
+
+
+if __name__ == '__main__':
+    main()
