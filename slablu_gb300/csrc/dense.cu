@@ -254,10 +254,12 @@ constexpr int kPanelCluster = 8;
 // Panel factorization: distributed shared memory of one 8-CTA cluster when the
 // panel fits (rows per CTA * nb elements), the global-memory kernel otherwise.
 template <typename T>
-int panel_factor(cudaStream_t s, T* A, int lda, int n, int k0, int nb, int* ipiv, int* info) {
+int panel_factor(cudaStream_t s, T* A, int lda, int n, int k0, int nb, int* ipiv, int* info, T* linv,
+                 bool* linv_done) {
+  *linv_done = false;
   const int m = n - k0;
   const int R = ceil_div(m, kPanelCluster);
-  const size_t bytes = ((size_t)R * nb + nb) * sizeof(T);
+  const size_t bytes = ((size_t)R * nb + nb + (size_t)nb * (nb + 1)) * sizeof(T);
   const size_t lim = allow_dynamic_smem(reinterpret_cast<const void*>(biglu_panel_cluster_kernel<T>));
   if (bytes <= lim && m >= kPanelCluster) {
     cudaLaunchConfig_t cfg = {};
@@ -272,8 +274,9 @@ int panel_factor(cudaStream_t s, T* A, int lda, int n, int k0, int nb, int* ipiv
     at[0].val.clusterDim.z = 1;
     cfg.attrs = at;
     cfg.numAttrs = 1;
-    SLAB_CUDA_TRY(cudaLaunchKernelEx(&cfg, biglu_panel_cluster_kernel<T>, A, lda, n, k0, nb, R, ipiv, info));
+    SLAB_CUDA_TRY(cudaLaunchKernelEx(&cfg, biglu_panel_cluster_kernel<T>, A, lda, n, k0, nb, R, ipiv, info, linv));
     SLAB_CHECK_LAUNCH();
+    *linv_done = linv != nullptr && R >= nb;
     return SLAB_OK;
   }
   biglu_panel_kernel<T><<<1, 1024, 0, s>>>(A, lda, n, k0, nb, ipiv, info);
@@ -301,9 +304,9 @@ int tri_inv_blocks(cudaStream_t s, const T* LU, int lda, int n, int bs, T* Linv,
 template <typename T>
 static int trsm_inv(cudaStream_t s, const T* Inv, int bs, int k0, int nb, T* X, int ldx, int ncols) {
   if (ncols <= 0 || nb <= 0) return SLAB_OK;
-  const size_t bytes = ((size_t)bs * bs + (size_t)bs * 64) * sizeof(T);
+  const size_t bytes = ((size_t)bs * bs + (size_t)bs * kTrsmCols) * sizeof(T);
   SLAB_TRY(ensure_smem(trsm_inv_kernel<T>, bytes, "trsm_inv"));
-  trsm_inv_kernel<T><<<ceil_div(ncols, 64), 256, bytes, s>>>(Inv, bs, k0, nb, X, ldx, ncols);
+  trsm_inv_kernel<T><<<ceil_div(ncols, kTrsmCols), 256, bytes, s>>>(Inv, bs, k0, nb, X, ldx, ncols);
   SLAB_CHECK_LAUNCH();
   return SLAB_OK;
 }
@@ -312,7 +315,8 @@ template <typename T>
 int biglu(cudaStream_t s, T* A, int lda, int n, int* ipiv, int* info, T* work) {
   for (int k0 = 0; k0 < n; k0 += kNB) {
     const int nb = n - k0 < kNB ? n - k0 : kNB;
-    SLAB_TRY(panel_factor<T>(s, A, lda, n, k0, nb, ipiv, info));
+    bool linv_done = false;
+    SLAB_TRY(panel_factor<T>(s, A, lda, n, k0, nb, ipiv, info, work, &linv_done));
     if (n - nb > 0) {
       biglu_swap_kernel<T><<<ceil_div(n - nb, 256), 256, 0, s>>>(A, lda, n, k0, nb, ipiv);
       SLAB_CHECK_LAUNCH();
@@ -321,8 +325,8 @@ int biglu(cudaStream_t s, T* A, int lda, int n, int* ipiv, int* info, T* work) {
     if (rest > 0) {
       if (work) {
         // U12 = L11^{-1} A12 through the explicit inverse of the panel's unit-lower triangle
-        SLAB_TRY(tri_inv_blocks<T>(s, A + (size_t)k0 * lda + k0, lda, nb, kNB, work, nullptr));
-        SLAB_TRY(trsm_inv<T>(s, work, kNB, k0, nb, A + (size_t)(k0 + nb) * lda, lda, rest));
+        if (!linv_done) SLAB_TRY(tri_inv_blocks<T>(s, A + (size_t)k0 * lda + k0, lda, nb, kNB, work, nullptr));
+        SLAB_TRY(trsm_inv<T>(s, work, linv_done ? nb : kNB, k0, nb, A + (size_t)(k0 + nb) * lda, lda, rest));
       } else {
         trsm_block_kernel<T><<<ceil_div(rest, 64), 256, 0, s>>>(A, lda, k0, nb, A + (size_t)(k0 + nb) * lda, lda,
                                                                rest, 0);

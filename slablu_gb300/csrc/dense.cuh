@@ -660,6 +660,27 @@ __global__ void __launch_bounds__(32 * kWarpSolveWarps)
 // CTA subtracts the block's contribution from the rows it owns.
 constexpr int kCoopMaxRhs = 8;
 constexpr int kCoopMaxOwn = 4;
+
+// Copy an rb x kb column-major block (ld lds) into shared memory (ld ldd) with
+// every load of a thread issued before its stores (one memory round trip).
+template <typename T>
+__device__ __forceinline__ void stage_block(T* dst, int ldd, const T* src, int lds, int rb, int kb) {
+  constexpr int kPer = 16;  // 64 x 64 / 256 threads
+  const int tot = rb * kb;
+  for (int base = 0; base < tot; base += kPer * blockDim.x) {
+    T v[kPer];
+#pragma unroll
+    for (int t = 0; t < kPer; ++t) {
+      const int idx = base + t * blockDim.x + threadIdx.x;
+      v[t] = idx < tot ? src[(size_t)(idx / rb) * lds + (idx % rb)] : T(0);
+    }
+#pragma unroll
+    for (int t = 0; t < kPer; ++t) {
+      const int idx = base + t * blockDim.x + threadIdx.x;
+      if (idx < tot) dst[(idx % rb) + (idx / rb) * ldd] = v[t];
+    }
+  }
+}
 template <typename T>
 __global__ void __launch_bounds__(256) trsv_coop_kernel(const T* __restrict__ LU, int lda, int n,
                                                        const int* __restrict__ perm, const T* __restrict__ Linv,
@@ -691,7 +712,7 @@ __global__ void __launch_bounds__(256) trsv_coop_kernel(const T* __restrict__ LU
       if (b % G == j) {
         const int o = b / G;
         __syncthreads();
-        for (int idx = tid; idx < bs * bs; idx += blockDim.x) dblk[(idx % bs) + (idx / bs) * ldd] = Inv[(size_t)b * bs * bs + idx];
+        stage_block(dblk, ldd, Inv + (size_t)b * bs * bs, bs, bs, bs);
         __syncthreads();
         for (int idx = tid; idx < kb * nrhs; idx += blockDim.x) {
           const int r = idx % kb, c = idx / kb;
@@ -710,10 +731,7 @@ __global__ void __launch_bounds__(256) trsv_coop_kernel(const T* __restrict__ LU
         const int r0 = ob * bs;
         const int rb = min(bs, n - r0);
         __syncthreads();
-        for (int idx = tid; idx < rb * kb; idx += blockDim.x) {
-          const int r = idx % rb, k = idx / rb;
-          dblk[r + k * ldd] = LU[(size_t)(k0 + k) * lda + r0 + r];
-        }
+        stage_block(dblk, ldd, LU + (size_t)k0 * lda + r0, lda, rb, kb);
         __syncthreads();
         for (int idx = tid; idx < rb * nrhs; idx += blockDim.x) {
           const int r = idx % rb, c = idx / rb;
@@ -832,10 +850,11 @@ __global__ void __launch_bounds__(1024) biglu_panel_kernel(T* A, int lda, int n,
 // panel (rows k0.. of columns k0..k0+nb).  Per column: local argmax, exchange
 // of the CL candidates through DSMEM, row swap through DSMEM, pivot row
 // broadcast, local rank-1 update; two cluster barriers per column.
-// Shared memory: R * nb elements + nb (pivot row).  grid = CL (one cluster).
+// Shared memory: R * nb + nb (pivot row) + nb * (nb + 1) (L11 inverse)
+// elements.  grid = CL (one cluster).
 template <typename T>
 __global__ void __launch_bounds__(256) biglu_panel_cluster_kernel(T* A, int lda, int n, int k0, int nb, int R,
-                                                                  int* ipiv, int* info) {
+                                                                  int* ipiv, int* info, T* linv) {
   namespace cg = cooperative_groups;
   cg::cluster_group cluster = cg::this_cluster();
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -924,6 +943,25 @@ __global__ void __launch_bounds__(256) biglu_panel_cluster_kernel(T* A, int lda,
     const int i = idx % rows, c = idx / rows;
     A[(size_t)(k0 + c) * lda + k0 + g0 + i] = P[i + (size_t)c * R];
   }
+  // inverse of the unit-lower nb x nb triangle (panel rows 0..nb-1, all held by
+  // CTA 0 when R >= nb), column c by thread c, written to linv (ld nb)
+  if (linv && r == 0 && R >= nb) {
+    T* Xs = prow + nb;  // nb x nb, ld nb + 1
+    const int ldx = nb + 1;
+    if (tid < nb) {
+      const int c = tid;
+      T* x = Xs + (size_t)c * ldx;
+      for (int i = 0; i < c; ++i) x[i] = T(0);
+      x[c] = T(1);
+      for (int i = c + 1; i < nb; ++i) {
+        T sum = T(0);
+        for (int k = c; k < i; ++k) sum -= P[i + (size_t)k * R] * x[k];
+        x[i] = sum;
+      }
+    }
+    __syncthreads();
+    for (int idx = tid; idx < nb * nb; idx += blockDim.x) linv[idx] = Xs[(idx % nb) + (idx / nb) * ldx];
+  }
 }
 
 // Inverse of the nb x nb diagonal triangle A[k0:k0+nb, k0:k0+nb] (unit lower if
@@ -970,15 +1008,17 @@ __global__ void __launch_bounds__(128) tri_inv_blocks_kernel(const T* A, int lda
 }
 
 // X[k0:k0+nb, :] = Inv * X[k0:k0+nb, :] with a precomputed nb x nb inverse
-// (ld bs); grid: column tiles of 64.
+// (ld bs); grid: column tiles of kTrsmCols (narrow tiles spread the FP64 work
+// over every SM).
+constexpr int kTrsmCols = 8;
 template <typename T>
 __global__ void __launch_bounds__(256) trsm_inv_kernel(const T* Inv, int bs, int k0, int nb, T* X, int ldx,
                                                       int ncols) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* Is = reinterpret_cast<T*>(smem_raw);  // bs x bs
-  T* Xs = Is + bs * bs;                    // bs x 64
-  const int c0 = blockIdx.x * 64;
-  const int nc = min(64, ncols - c0);
+  T* Xs = Is + bs * bs;                    // bs x kTrsmCols
+  const int c0 = blockIdx.x * kTrsmCols;
+  const int nc = min(kTrsmCols, ncols - c0);
   for (int idx = threadIdx.x; idx < bs * bs; idx += blockDim.x) Is[idx] = Inv[idx];
   for (int idx = threadIdx.x; idx < nb * nc; idx += blockDim.x) {
     const int i = idx % nb, c = idx / nb;
