@@ -146,6 +146,37 @@ int slab_engine_solve(slab_engine* e, int nrhs, const double* d_bnd, const doubl
 int slab_engine_residual(slab_engine* e, int nrhs, const double* d_ufaces, const double* d_uint,
                          const double* d_fbody, double* d_rint, double* d_rfaces);
 
+/* Adjoint (transposed) solve with the stored factors, for the gradient of a
+ * loss L(u) through slab_engine_solve.  Extends Domain_Solver.solve
+ * (src_solver/slablu_solver.py:623-666); the transposed pieces follow
+ * lusolve_sweep_transpose (src_solver/block_tridiag_solver_dense.py:205-222)
+ * and solve_slab(transpose=True) (src_solver/slablu_solver.py:901-943).
+ *   d_gleaf  : dL/du at every leaf node (nleaves*p*p x nrhs column-major), or NULL
+ *   d_gfaces : dL/du_faces (nfaces x nrhs column-major), or NULL
+ * Solves A^T lam = g on the full collocation system with FP64 refinement (same
+ * tol / max_iter meaning as slab_engine_solve) and writes, each optional:
+ *   d_lam_leaf  : multipliers of the interior PDE rows at the leaf nodes
+ *                 (zero on leaf boundary nodes) = dL/d(body load)
+ *   d_lam_faces : multipliers of the face flux rows (zero on Dirichlet faces)
+ *   d_gbnd      : dL/d(Dirichlet data) on Dirichlet faces, zero elsewhere
+ *                 (nfaces x nrhs, the layout of slab_engine_solve's d_bnd).
+ * Leaf order and merge blocks are limited to 512 unknowns (p <= 24 with the
+ * default slab widths).  h_stats as for slab_engine_solve (worst column). */
+int slab_engine_adjoint(slab_engine* e, int nrhs, const double* d_gleaf, const double* d_gfaces, double tol,
+                        int max_iter, double* d_lam_leaf, double* d_lam_faces, double* d_gbnd, int* h_iters,
+                        double* h_stats);
+
+/* Gradient of L with respect to the PDE coefficient fields at the leaf nodes,
+ * summed over the nrhs columns: d_g* (nleaves*p*p each, NULL to skip) from the
+ * forward solution (d_ufaces, d_uleaf of slab_engine_solve) and d_lam_leaf of
+ * slab_engine_adjoint.  dL/dc = -lam*u, dL/dc11 = lam*(D11 u), dL/dc22 =
+ * lam*(D22 u), dL/dc1 = -lam*(D1 u), dL/dc2 = -lam*(D2 u) at interior nodes,
+ * zero at leaf boundary nodes (which carry no PDE row); Aloc as in
+ * src_disc/hps_parallel_leaf_ops.py:17-27. */
+int slab_engine_coeff_grad(slab_engine* e, int nrhs, const double* d_ufaces, const double* d_uleaf,
+                           const double* d_lam_leaf, double* d_gc11, double* d_gc22, double* d_gc1, double* d_gc2,
+                           double* d_gc);
+
 /* Bytes of device memory held by the engine's factorization. */
 size_t slab_engine_factor_bytes(const slab_engine* e);
 

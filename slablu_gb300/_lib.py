@@ -34,6 +34,9 @@ _SIGS = {
     'slab_engine_factor': (c_int, [c_void] * 6),
     'slab_engine_solve': (c_int, [c_void, c_int, c_void, c_void, c_double, c_int, c_void, c_void, P_int, P_double]),
     'slab_engine_residual': (c_int, [c_void, c_int] + [c_void] * 5),
+    'slab_engine_adjoint': (c_int, [c_void, c_int, c_void, c_void, c_double, c_int, c_void, c_void, c_void,
+                                    P_int, P_double]),
+    'slab_engine_coeff_grad': (c_int, [c_void, c_int] + [c_void] * 8),
     'slab_engine_factor_bytes': (c_size, [c_void]),
     'slab_engine_timings': (c_int, [c_void, P_double, c_int]),
     'slab_leaf_dtn_noalloc_max_bytes': (c_size, []),

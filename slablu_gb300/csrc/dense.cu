@@ -116,7 +116,7 @@ int getrs_small(cudaStream_t s, int n, int nrhs, const T* LU, const long long* o
 
 template <typename T>
 int trsv_coop(cudaStream_t s, const T* LU, int lda, int n, const int* perm, const T* Linv, const T* Uinv, int bs,
-              const T* B, int ldb, T* X, int ldx, int nrhs) {
+              const T* B, int ldb, T* X, int ldx, int nrhs, bool trans) {
   if (n <= 0 || nrhs <= 0) return SLAB_OK;
   if (nrhs > kCoopMaxRhs) return set_error(SLAB_ERR_ARG, "trsv_coop: nrhs %d > %d", nrhs, kCoopMaxRhs);
   const size_t bytes = ((size_t)kCoopMaxOwn * bs * nrhs + (size_t)bs * (bs + 1) + (size_t)bs * nrhs) * sizeof(T);
@@ -130,9 +130,66 @@ int trsv_coop(cudaStream_t s, const T* LU, int lda, int n, const int* perm, cons
   const int G = nblk < max_grid ? nblk : max_grid;
   if (G <= 0 || ceil_div(nblk, G) > kCoopMaxOwn)
     return set_error(SLAB_ERR_ARG, "trsv_coop: order %d too large for a co-resident grid", n);
+  int tr = trans ? 1 : 0;
   void* args[] = {(void*)&LU, (void*)&lda, (void*)&n, (void*)&perm, (void*)&Linv, (void*)&Uinv, (void*)&bs,
-                  (void*)&B, (void*)&ldb, (void*)&X, (void*)&ldx, (void*)&nrhs};
+                  (void*)&B, (void*)&ldb, (void*)&X, (void*)&ldx, (void*)&nrhs, (void*)&tr};
   SLAB_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)trsv_coop_kernel<T>, dim3(G), dim3(256), args, bytes, s));
+  SLAB_CHECK_LAUNCH();
+  return SLAB_OK;
+}
+
+template <typename T>
+int getrs_small_t(cudaStream_t s, int n, int nrhs, const T* LU, const long long* offLU, long long strideLU, int lda,
+                  const int* perm, const long long* offP, long long strideP, T* B, const long long* offB,
+                  long long strideB, int ldb, int batch) {
+  if (n <= 0 || nrhs <= 0 || batch <= 0) return SLAB_OK;
+  if (nrhs > 4) return set_error(SLAB_ERR_ARG, "getrs_small_t: nrhs %d > 4", nrhs);
+  if (n > 32 * kWarpSlots) return set_error(SLAB_ERR_ARG, "getrs_small_t: order %d > %d", n, 32 * kWarpSlots);
+  const size_t bytes = (size_t)kWarpSolveWarps * n * nrhs * sizeof(T);
+  SLAB_TRY(ensure_smem(getrs_warp_t_kernel<T>, bytes, "getrs_small_t"));
+  getrs_warp_t_kernel<T><<<ceil_div(batch, kWarpSolveWarps), 32 * kWarpSolveWarps, bytes, s>>>(
+      n, nrhs, LU, offLU, strideLU, lda, perm, offP, strideP, B, offB, strideB, ldb, batch);
+  SLAB_CHECK_LAUNCH();
+  return SLAB_OK;
+}
+
+template <typename T>
+int gemm_tn(cudaStream_t s, int m, int n, int k, T alpha, const T* A, const long long* offA, long long strideA,
+            int lda, const T* B, const long long* offB, long long strideB, int ldb, T beta, T* C,
+            const long long* offC, long long strideC, int ldc, int batch) {
+  if (m <= 0 || n <= 0 || batch <= 0) return SLAB_OK;
+  if (batch > 65535) {
+    for (int b0 = 0; b0 < batch; b0 += 65535) {
+      const int nb = batch - b0 < 65535 ? batch - b0 : 65535;
+      SLAB_TRY(gemm_tn<T>(s, m, n, k, alpha, offA ? A : A + strideA * b0, offA ? offA + b0 : nullptr, strideA, lda,
+                          offB ? B : B + strideB * b0, offB ? offB + b0 : nullptr, strideB, ldb, beta,
+                          offC ? C : C + strideC * b0, offC ? offC + b0 : nullptr, strideC, ldc, nb));
+    }
+    return SLAB_OK;
+  }
+  const int kk = k < 0 ? 0 : k;
+  if (n <= 16) {
+    dim3 g(ceil_div(m, 8), 1, batch);
+#define SLAB_TN(NC)                                                                                           \
+  gemm_tn_narrow_kernel<T, NC><<<g, 256, 0, s>>>(m, n, kk, alpha, A, offA, strideA, lda, B, offB, strideB, ldb, \
+                                                 beta, C, offC, strideC, ldc)
+    if (n <= 1)
+      SLAB_TN(1);
+    else if (n <= 2)
+      SLAB_TN(2);
+    else if (n <= 4)
+      SLAB_TN(4);
+    else if (n <= 8)
+      SLAB_TN(8);
+    else
+      SLAB_TN(16);
+#undef SLAB_TN
+    SLAB_CHECK_LAUNCH();
+    return SLAB_OK;
+  }
+  dim3 grid(ceil_div(m, 64), ceil_div(n, 64), batch);
+  gemm_kernel<T, true><<<grid, 256, 0, s>>>(m, n, kk, alpha, A, offA, strideA, lda, B, offB, strideB, ldb, beta, C,
+                                           offC, strideC, ldc);
   SLAB_CHECK_LAUNCH();
   return SLAB_OK;
 }
@@ -211,7 +268,7 @@ int gemm(cudaStream_t s, int m, int n, int k, T alpha, const T* A, const long lo
   }
   // k == 0 leaves the k loop empty: C = beta*C
   dim3 grid(ceil_div(m, 64), ceil_div(n, 64), batch);
-  gemm_kernel<T><<<grid, 256, 0, s>>>(m, n, k < 0 ? 0 : k, alpha, A, offA, strideA, lda, B, offB, strideB, ldb,
+  gemm_kernel<T, false><<<grid, 256, 0, s>>>(m, n, k < 0 ? 0 : k, alpha, A, offA, strideA, lda, B, offB, strideB, ldb,
                                       beta, C, offC, strideC, ldc);
   SLAB_CHECK_LAUNCH();
   return SLAB_OK;
@@ -427,8 +484,19 @@ template int getrs_small<double>(cudaStream_t, int, int, const double*, const lo
                                  const int*, const long long*, long long, double*, const long long*, long long, int,
                                  int);
 template int trsv_coop<float>(cudaStream_t, const float*, int, int, const int*, const float*, const float*, int,
-                              const float*, int, float*, int, int);
+                              const float*, int, float*, int, int, bool);
 template int trsv_coop<double>(cudaStream_t, const double*, int, int, const int*, const double*, const double*, int,
-                               const double*, int, double*, int, int);
+                               const double*, int, double*, int, int, bool);
+template int getrs_small_t<float>(cudaStream_t, int, int, const float*, const long long*, long long, int, const int*,
+                                  const long long*, long long, float*, const long long*, long long, int, int);
+template int getrs_small_t<double>(cudaStream_t, int, int, const double*, const long long*, long long, int,
+                                   const int*, const long long*, long long, double*, const long long*, long long,
+                                   int, int);
+template int gemm_tn<float>(cudaStream_t, int, int, int, float, const float*, const long long*, long long, int,
+                            const float*, const long long*, long long, int, float, float*, const long long*,
+                            long long, int, int);
+template int gemm_tn<double>(cudaStream_t, int, int, int, double, const double*, const long long*, long long, int,
+                             const double*, const long long*, long long, int, double, double*, const long long*,
+                             long long, int, int);
 
 }  // namespace slab

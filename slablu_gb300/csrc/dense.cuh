@@ -453,7 +453,7 @@ __global__ void __launch_bounds__(kNT) getrs_batched_kernel(int n, int nrhs, int
 // 64 x 64 output tile per CTA, k staged 16 at a time; grid (m/64, n/64, batch).
 constexpr int kGK = 16;
 constexpr int kGLD = 68;
-template <typename T>
+template <typename T, bool TA = false>
 __global__ void __launch_bounds__(256) gemm_kernel(int m, int n, int k, T alpha, const T* __restrict__ A,
                                                   const long long* offA, long long strideA, int lda,
                                                   const T* __restrict__ B, const long long* offB,
@@ -474,11 +474,21 @@ __global__ void __launch_bounds__(256) gemm_kernel(int m, int n, int k, T alpha,
 #pragma unroll
     for (int j = 0; j < 4; ++j) acc[i][j] = T(0);
   for (int k0 = 0; k0 < k; k0 += kGK) {
+    if (!TA) {
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const int r = tid & 63, kk = (tid >> 6) + 4 * q;
-      const int gr = r0 + r, gk = k0 + kk;
-      As[r + kk * kGLD] = (gr < m && gk < k) ? A[gr + (size_t)gk * lda] : T(0);
+      for (int q = 0; q < 4; ++q) {
+        const int r = tid & 63, kk = (tid >> 6) + 4 * q;
+        const int gr = r0 + r, gk = k0 + kk;
+        As[r + kk * kGLD] = (gr < m && gk < k) ? A[gr + (size_t)gk * lda] : T(0);
+      }
+    } else {
+      // op(A)(r, kk) = A[kk + r*lda]; consecutive threads walk kk (contiguous in A)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int kk = tid & 15, r = (tid >> 4) + 16 * q;
+        const int gr = r0 + r, gk = k0 + kk;
+        As[r + kk * kGLD] = (gr < m && gk < k) ? A[gk + (size_t)gr * lda] : T(0);
+      }
     }
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
@@ -652,6 +662,98 @@ __global__ void __launch_bounds__(32 * kWarpSolveWarps)
     for (int i = lane; i < n; i += 32) Bg[i + (size_t)c * ldb] = xs[i + c * n];
 }
 
+// Warp-per-matrix X = A^{-T} B = P^T L^{-T} U^{-T} B (nrhs <= 4): dot-product
+// substitution along the columns of U (forward with U^T) and of L (backward
+// with L^T); each column segment is read by the 32 lanes (coalesced) and
+// reduced with shuffles; the next column is prefetched.
+template <typename T>
+__global__ void __launch_bounds__(32 * kWarpSolveWarps)
+    getrs_warp_t_kernel(int n, int nrhs, const T* __restrict__ LU, const long long* offLU, long long strideLU,
+                        int lda, const int* __restrict__ perm, const long long* offP, long long strideP, T* B,
+                        const long long* offB, long long strideB, int ldb, int batch) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int b = blockIdx.x * kWarpSolveWarps + warp;
+  if (b >= batch) return;
+  T* xs = reinterpret_cast<T*>(smem_raw) + (size_t)warp * n * nrhs;
+  const T* __restrict__ A = LU + batch_off(offLU, strideLU, b);
+  const int* pv = perm + batch_off(offP, strideP, b);
+  T* Bg = B + batch_off(offB, strideB, b);
+  for (int c = 0; c < nrhs; ++c)
+    for (int i = lane; i < n; i += 32) xs[i + c * n] = Bg[i + (size_t)c * ldb];
+  __syncwarp();
+  T cur[kWarpSlots], nxt[kWarpSlots];
+  // forward with U^T: x_k = (b_k - U[0:k, k] . x[0:k]) / U[k, k]
+#pragma unroll
+  for (int t = 0; t < kWarpSlots; ++t) cur[t] = T(0);
+  for (int k = 0; k < n; ++k) {
+    if (k + 1 < n) {
+      const T* nc = A + (size_t)(k + 1) * lda;
+#pragma unroll
+      for (int t = 0; t < kWarpSlots; ++t) {
+        const int i = lane + 32 * t;
+        nxt[t] = i <= k + 1 ? nc[i] : T(0);  // U[0:k+1, k+1] and the diagonal
+      }
+    }
+    const T* ck = A + (size_t)k * lda;
+    const T d = ck[k];
+    for (int c = 0; c < nrhs; ++c) {
+      T part = T(0);
+#pragma unroll
+      for (int t = 0; t < kWarpSlots; ++t) {
+        const int i = lane + 32 * t;
+        if (i < k) part += (k == 0 ? T(0) : cur[t]) * xs[i + c * n];
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+      const T xk = (xs[k + c * n] - part) / d;
+      __syncwarp();
+      if (lane == 0) xs[k + c * n] = xk;
+      __syncwarp();
+    }
+#pragma unroll
+    for (int t = 0; t < kWarpSlots; ++t) cur[t] = nxt[t];
+  }
+  // backward with L^T (unit): x_k = b_k - L[k+1:n, k] . x[k+1:n]
+  {
+    const T* cc = A + (size_t)(n - 1) * lda;
+#pragma unroll
+    for (int t = 0; t < kWarpSlots; ++t) {
+      const int i = lane + 32 * t;
+      cur[t] = (i > n - 1 && i < n) ? cc[i] : T(0);
+    }
+  }
+  for (int k = n - 1; k >= 0; --k) {
+    if (k > 0) {
+      const T* nc = A + (size_t)(k - 1) * lda;
+#pragma unroll
+      for (int t = 0; t < kWarpSlots; ++t) {
+        const int i = lane + 32 * t;
+        nxt[t] = (i > k - 1 && i < n) ? nc[i] : T(0);
+      }
+    }
+    for (int c = 0; c < nrhs; ++c) {
+      T part = T(0);
+#pragma unroll
+      for (int t = 0; t < kWarpSlots; ++t) {
+        const int i = lane + 32 * t;
+        if (i > k && i < n) part += cur[t] * xs[i + c * n];
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+      const T xk = xs[k + c * n] - part;
+      __syncwarp();
+      if (lane == 0) xs[k + c * n] = xk;
+      __syncwarp();
+    }
+#pragma unroll
+    for (int t = 0; t < kWarpSlots; ++t) cur[t] = nxt[t];
+  }
+  // x = P^T z: row perm[i] of x is row i of z
+  for (int c = 0; c < nrhs; ++c)
+    for (int i = lane; i < n; i += 32) Bg[pv[i] + (size_t)c * ldb] = xs[i + c * n];
+}
+
 // Cooperative triangular solves with one large factored matrix (FP64
 // interface blocks): X = U^{-1} L^{-1} P B for nrhs <= 8 columns, using the
 // precomputed inverses of the bs x bs diagonal triangles (tri_inv_blocks).
@@ -660,6 +762,26 @@ __global__ void __launch_bounds__(32 * kWarpSolveWarps)
 // CTA subtracts the block's contribution from the rows it owns.
 constexpr int kCoopMaxRhs = 8;
 constexpr int kCoopMaxOwn = 4;
+
+// Transposed copy: dst(r, k) = src[r * lds + k] for an rb x kb result.
+template <typename T>
+__device__ __forceinline__ void stage_block_t(T* dst, int ldd, const T* src, int lds, int rb, int kb) {
+  constexpr int kPer = 16;
+  const int tot = rb * kb;
+  for (int base = 0; base < tot; base += kPer * blockDim.x) {
+    T v[kPer];
+#pragma unroll
+    for (int t = 0; t < kPer; ++t) {
+      const int idx = base + t * blockDim.x + threadIdx.x;
+      v[t] = idx < tot ? src[(size_t)(idx / kb) * lds + (idx % kb)] : T(0);  // contiguous in k
+    }
+#pragma unroll
+    for (int t = 0; t < kPer; ++t) {
+      const int idx = base + t * blockDim.x + threadIdx.x;
+      if (idx < tot) dst[(idx / kb) + (idx % kb) * ldd] = v[t];
+    }
+  }
+}
 
 // Copy an rb x kb column-major block (ld lds) into shared memory (ld ldd) with
 // every load of a thread issued before its stores (one memory round trip).
@@ -685,7 +807,8 @@ template <typename T>
 __global__ void __launch_bounds__(256) trsv_coop_kernel(const T* __restrict__ LU, int lda, int n,
                                                        const int* __restrict__ perm, const T* __restrict__ Linv,
                                                        const T* __restrict__ Uinv, int bs,
-                                                       const T* __restrict__ Bin, int ldb, T* X, int ldx, int nrhs) {
+                                                       const T* __restrict__ Bin, int ldb, T* X, int ldx, int nrhs,
+                                                       int trans) {
   namespace cg = cooperative_groups;
   cg::grid_group grid = cg::this_grid();
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -696,23 +819,28 @@ __global__ void __launch_bounds__(256) trsv_coop_kernel(const T* __restrict__ LU
   const int G = gridDim.x, j = blockIdx.x, tid = threadIdx.x;
   const int nblk = (n + bs - 1) / bs;
   const int nown = (nblk - j + G - 1) / G;
+  // non-transposed: L U x = P^T b (gather b[perm]); transposed: U^T L^T z = b, x = P z
   for (int o = 0; o < nown; ++o) {
     const int r0 = (j + o * G) * bs;
     for (int idx = tid; idx < bs * nrhs; idx += blockDim.x) {
       const int r = idx % bs, c = idx / bs;
-      acc[(size_t)o * bs * nrhs + idx] = (r0 + r < n) ? Bin[perm[r0 + r] + (size_t)c * ldb] : T(0);
+      acc[(size_t)o * bs * nrhs + idx] =
+          (r0 + r < n) ? Bin[(trans ? r0 + r : perm[r0 + r]) + (size_t)c * ldb] : T(0);
     }
   }
   for (int pass = 0; pass < 2; ++pass) {
-    const bool lower = pass == 0;
-    const T* Inv = lower ? Linv : Uinv;
+    const bool lower = pass == 0;  // the first pass walks the blocks forward
+    const T* Inv = (lower != (trans != 0)) ? Linv : Uinv;
     for (int step = 0; step < nblk; ++step) {
       const int b = lower ? step : nblk - 1 - step;
       const int k0 = b * bs, kb = min(bs, n - k0);
       if (b % G == j) {
         const int o = b / G;
         __syncthreads();
-        stage_block(dblk, ldd, Inv + (size_t)b * bs * bs, bs, bs, bs);
+        if (!trans)
+          stage_block(dblk, ldd, Inv + (size_t)b * bs * bs, bs, bs, bs);
+        else
+          stage_block_t(dblk, ldd, Inv + (size_t)b * bs * bs, bs, bs, bs);
         __syncthreads();
         for (int idx = tid; idx < kb * nrhs; idx += blockDim.x) {
           const int r = idx % kb, c = idx / kb;
@@ -731,7 +859,10 @@ __global__ void __launch_bounds__(256) trsv_coop_kernel(const T* __restrict__ LU
         const int r0 = ob * bs;
         const int rb = min(bs, n - r0);
         __syncthreads();
-        stage_block(dblk, ldd, LU + (size_t)k0 * lda + r0, lda, rb, kb);
+        if (!trans)
+          stage_block(dblk, ldd, LU + (size_t)k0 * lda + r0, lda, rb, kb);
+        else  // op(A)[ob rows, b cols] = A[b rows, ob cols]^T
+          stage_block_t(dblk, ldd, LU + (size_t)r0 * lda + k0, lda, rb, kb);
         __syncthreads();
         for (int idx = tid; idx < rb * nrhs; idx += blockDim.x) {
           const int r = idx % rb, c = idx / rb;
@@ -751,6 +882,16 @@ __global__ void __launch_bounds__(256) trsv_coop_kernel(const T* __restrict__ LU
       }
     }
     grid.sync();
+  }
+  if (trans) {
+    // x = P z: acc holds z on the owned rows; row perm[i] of x is row i of z
+    for (int o = 0; o < nown; ++o) {
+      const int r0 = (j + o * G) * bs;
+      for (int idx = tid; idx < bs * nrhs; idx += blockDim.x) {
+        const int r = idx % bs, c = idx / bs;
+        if (r0 + r < n) X[perm[r0 + r] + (size_t)c * ldx] = acc[(size_t)o * bs * nrhs + idx];
+      }
+    }
   }
 }
 
@@ -782,6 +923,47 @@ __global__ void __launch_bounds__(256) gemm_narrow_splitk_kernel(int m, int n, i
 #pragma unroll
   for (int c = 0; c < NC; ++c)
     if (c < n) atomicAdd(C + r + (size_t)c * ldc, alpha * acc[c]);
+}
+
+// Narrow transposed GEMM: C (m x n, n <= NC) = beta C + alpha A^T B with A k x m.
+// One warp per row of C: the lanes read the column of A and of B (coalesced)
+// and reduce with shuffles.  grid (ceil(m/8), 1, batch), 256 threads.
+template <typename T, int NC>
+__global__ void __launch_bounds__(256) gemm_tn_narrow_kernel(int m, int n, int k, T alpha, const T* __restrict__ A,
+                                                            const long long* offA, long long strideA, int lda,
+                                                            const T* __restrict__ B, const long long* offB,
+                                                            long long strideB, int ldb, T beta, T* C,
+                                                            const long long* offC, long long strideC, int ldc) {
+  const int bz = blockIdx.z;
+  A += batch_off(offA, strideA, bz);
+  B += batch_off(offB, strideB, bz);
+  C += batch_off(offC, strideC, bz);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int r = blockIdx.x * 8 + warp;
+  if (r >= m) return;
+  const T* ac = A + (size_t)r * lda;
+  T acc[NC];
+#pragma unroll
+  for (int c = 0; c < NC; ++c) acc[c] = T(0);
+  for (int kk = lane; kk < k; kk += 32) {
+    const T a = ac[kk];
+#pragma unroll
+    for (int c = 0; c < NC; ++c)
+      if (c < n) acc[c] += a * B[kk + (size_t)c * ldb];
+  }
+#pragma unroll
+  for (int c = 0; c < NC; ++c) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], o);
+  }
+  if (lane == 0) {
+#pragma unroll
+    for (int c = 0; c < NC; ++c) {
+      if (c >= n) break;
+      T* cp = C + r + (size_t)c * ldc;
+      *cp = (beta == T(0) ? T(0) : beta * *cp) + alpha * acc[c];
+    }
+  }
 }
 
 template <typename T>
@@ -1160,7 +1342,19 @@ int getrs_small(cudaStream_t s, int n, int nrhs, const T* LU, const long long* o
 // launch; Linv/Uinv from tri_inv_blocks with block size bs.
 template <typename T>
 int trsv_coop(cudaStream_t s, const T* LU, int lda, int n, const int* perm, const T* Linv, const T* Uinv, int bs,
-              const T* B, int ldb, T* X, int ldx, int nrhs);
+              const T* B, int ldb, T* X, int ldx, int nrhs, bool trans = false);
+
+// C = beta C + alpha A^T B (A is k x m); same batching conventions as gemm.
+template <typename T>
+int gemm_tn(cudaStream_t s, int m, int n, int k, T alpha, const T* A, const long long* offA, long long strideA,
+            int lda, const T* B, const long long* offB, long long strideB, int ldb, T beta, T* C,
+            const long long* offC, long long strideC, int ldc, int batch);
+
+// Batched X = A^{-T} B with the warp kernel (nrhs <= 4).
+template <typename T>
+int getrs_small_t(cudaStream_t s, int n, int nrhs, const T* LU, const long long* offLU, long long strideLU, int lda,
+                  const int* perm, const long long* offP, long long strideP, T* B, const long long* offB,
+                  long long strideB, int ldb, int batch);
 
 size_t smem_limit_bytes();
 

@@ -163,6 +163,34 @@ __global__ void sumsq_kernel(const T* __restrict__ x, long long n, double* __res
   }
 }
 
+// dst = src where the face's Dirichlet flag equals keep_dir, else 0 (ntot x nrhs).
+__global__ void mask_faces_kernel(const double* __restrict__ src, const unsigned char* __restrict__ dir,
+                                  double* __restrict__ dst, long long ntot, int nrhs, int keep_dir) {
+  const long long tot = ntot * nrhs;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < tot; i += (long long)gridDim.x * blockDim.x) {
+    const long long g = i % ntot;
+    dst[i] = ((int)dir[g] == keep_dir && src) ? src[i] : 0.0;
+  }
+}
+
+// Leaf-major interior values -> leaf-node layout (nleaf*p*p x nrhs column-major),
+// zero at the leaf boundary nodes.
+__global__ void interior_to_nodes_kernel(const double* __restrict__ uc, double* __restrict__ out, int p, int nleaf,
+                                         int nrhs) {
+  const int q = p - 2, n = q * q, pp = p * p;
+  const long long tot = (long long)nleaf * pp * nrhs;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < tot; i += (long long)gridDim.x * blockDim.x) {
+    const long long node = i % ((long long)nleaf * pp);
+    const int c = (int)(i / ((long long)nleaf * pp));
+    const int leaf = (int)(node / pp), k = (int)(node % pp);
+    const int i1 = k / p, i2 = k % p;
+    double v = 0.0;
+    if (i1 >= 1 && i1 <= p - 2 && i2 >= 1 && i2 <= p - 2)
+      v = uc[((size_t)leaf * nrhs + c) * n + (size_t)(i1 - 1) * q + (i2 - 1)];
+    out[i] = v;
+  }
+}
+
 static unsigned grid_for(long long n) {
   long long g = (n + 255) / 256;
   if (g > 4096) g = 4096;
@@ -278,6 +306,10 @@ struct EngineBase {
                     double* uleaf, int* iters, double* stats) = 0;
   virtual int residual(int nrhs, const double* ufaces, const double* uint, const double* fbody, double* rint,
                        double* rfaces) = 0;
+  virtual int adjoint(int nrhs, const double* gleaf, const double* gfaces, double tol, int max_iter, double* lam_leaf,
+                      double* lam_faces, double* gbnd, int* iters, double* stats) = 0;
+  virtual int coeff_grad(int nrhs, const double* ufaces, const double* uleaf, const double* lam_leaf, double* g11,
+                         double* g22, double* g1, double* g2, double* g0) = 0;
   virtual size_t factor_bytes() const = 0;
   virtual double timing(int i) const = 0;
   long long ntot = 0, nleaf = 0;
@@ -289,8 +321,8 @@ struct EngineImpl : EngineBase {
   cudaStream_t s = nullptr;      // engine-owned stream (captured into graphs)
   cudaStream_t us = nullptr;     // caller's stream
   cudaEvent_t join = nullptr;
-  cudaGraphExec_t gfac[3] = {nullptr, nullptr, nullptr}, gapp = nullptr;
-  int gapp_nrhs = 0;
+  cudaGraphExec_t gfac[3] = {nullptr, nullptr, nullptr}, gapp = nullptr, gapp_t = nullptr;
+  int gapp_nrhs = 0, gapp_t_nrhs = 0;
   bool use_graphs = true;
   DevBuf D, Dsq, Nx, NxcT, NxxT, interp, jxr, leafglob, dirmask;
   DevBuf coef[5];
@@ -314,6 +346,7 @@ struct EngineImpl : EngineBase {
   // solve buffers
   int cap_nrhs = 0;
   DevBuf wc, flux, gvec, uvec, Ybuf, Zbuf, ifF, ifZ, ux_d, uc_d, rc_d, rx_d, rcT, acc;
+  DevBuf gi_d, gf_d;  // adjoint right-hand side (interior leaf-major, faces)
   size_t factor_bytes_ = 0;
   bool factored = false;
   // phase timing (CUDA events on the engine stream), milliseconds
@@ -325,6 +358,7 @@ struct EngineImpl : EngineBase {
     for (auto& g : gfac)
       if (g) cudaGraphExecDestroy(g);
     if (gapp) cudaGraphExecDestroy(gapp);
+    if (gapp_t) cudaGraphExecDestroy(gapp_t);
     for (auto& e : ev)
       if (e) cudaEventDestroy(e);
     if (join) cudaEventDestroy(join);
@@ -799,6 +833,10 @@ struct EngineImpl : EngineBase {
       cudaGraphExecDestroy(gapp);
       gapp = nullptr;
     }
+    if (gapp_t) {
+      cudaGraphExecDestroy(gapp_t);
+      gapp_t = nullptr;
+    }
     long long ymax = 0, zmax = 0;
     for (auto& b : batches) {
       b->offY0 = ymax;
@@ -923,6 +961,272 @@ struct EngineImpl : EngineBase {
     SLAB_TRY(gemm<T>(s, n, nrhs, nx, T(1), G.as<T>() + (long long)n * n, nullptr, strideG, n, flux.as<T>(), nullptr,
                      (long long)nx * nrhs, nx, T(1), w, nullptr, (long long)n * nrhs, n, (int)nleaf));
     return SLAB_OK;
+  }
+
+  // One application of the transposed factorization, nrhs <= 4: input rcT
+  // (interior, leaf-major) and gvec (faces, zero on Dirichlet faces); output
+  // uvec (face multipliers) and wc (interior multipliers, leaf-major).  Each
+  // step is the transpose of a step of apply(), taken in reverse order:
+  //   K^T = [A_cc^T  N_c^T; A_cx^T  N_x^T]  ->  DtN^T lam_x = g_x + S^T g_c,
+  //   lam_c = A_cc^{-T} (g_c - N_c^T lam_x).
+  int apply_t(int nrhs) {
+    T* g = gvec.as<T>();
+    T* u = uvec.as<T>();
+    T* w = wc.as<T>();
+    const long long strideG = (long long)n * (n + nx);
+    // leaf forward: g_x += S^T g_c
+    SLAB_TRY(gemm_tn<T>(s, nx, nrhs, n, T(1), G.as<T>() + (long long)n * n, nullptr, strideG, n, rcT.as<T>(), nullptr,
+                        (long long)n * nrhs, n, T(0), flux.as<T>(), nullptr, (long long)nx * nrhs, nx, (int)nleaf));
+    scatter_add_kernel<T><<<grid_for(nleaf * nx * nrhs), 256, 0, s>>>(g, ntot, leafglob.as<int>(), nx, (int)nleaf,
+                                                                     nrhs, flux.as<T>(), T(1), dirmask.as<unsigned char>());
+    SLAB_CHECK_LAUNCH();
+    // tree forward (transposed): g_O -= W^T g_E with W = M^{-1} row; g_E kept in Y
+    for (auto& bp : batches) {
+      Batch& b = *bp;
+      T* Y = Ybuf.as<T>() + b.offY0;
+      T* Z = Zbuf.as<T>();
+      const long long strideM = (long long)b.nE * (b.nE + b.nO);
+      T* Maug = fpool.as<T>() + b.offM0;
+      gather_kernel<T><<<grid_for((long long)b.count * b.nE * nrhs), 256, 0, s>>>(g, ntot, b.Eglob.as<int>(), b.nE,
+                                                                                b.count, nrhs, Y);
+      SLAB_CHECK_LAUNCH();
+      SLAB_TRY(gemm_tn<T>(s, b.nO, nrhs, b.nE, T(1), Maug + (long long)b.nE * b.nE, nullptr, strideM, b.nE, Y, nullptr,
+                          (long long)b.nE * nrhs, b.nE, T(0), Z, nullptr, (long long)b.nO * nrhs, b.nO, b.count));
+      scatter_add_kernel<T><<<grid_for((long long)b.count * b.nO * nrhs), 256, 0, s>>>(
+          g, ntot, b.Oglob.as<int>(), b.nO, b.count, nrhs, Z, T(-1), nullptr);
+      SLAB_CHECK_LAUNCH();
+    }
+    SLAB_CUDA_TRY(cudaMemsetAsync(u, 0, (size_t)ntot * nrhs * sizeof(T), s));
+    // interface: T = L U with L = [S_j on the diagonal, sub_j below], U = [I, X_j above];
+    // T^T x = f: y_j = f_j - X_{j-1}^T y_{j-1}, then x_j = S_j^{-T} (y_j - sub_{j+1}^T x_{j+1})
+    if (nbI > 0) {
+      const long long blk = (long long)nI * nI;
+      const long long vb = (long long)nI * nrhs;
+      TI* F = ifF.as<TI>();
+      TI* Zi = ifZ.as<TI>();
+      gather_kernel<T><<<grid_for((long long)nbI * vb), 256, 0, s>>>(g, ntot, ifGlob.as<int>(), nI, nbI, nrhs,
+                                                                    Zbuf.as<T>());
+      SLAB_CHECK_LAUNCH();
+      convert_kernel<TI, T><<<grid_for(nbI * vb), 256, 0, s>>>(Zbuf.as<T>(), F, nbI * vb);
+      SLAB_CHECK_LAUNCH();
+      for (int j = 1; j < nbI; ++j)
+        SLAB_TRY(gemm_tn<TI>(s, nI, nrhs, nI, TI(-1), ifX.as<TI>() + blk * (j - 1), nullptr, 0, nI, F + vb * (j - 1),
+                             nullptr, 0, nI, TI(1), F + vb * j, nullptr, 0, nI, 1));
+      for (int j = nbI - 1; j >= 0; --j) {
+        if (j < nbI - 1)
+          SLAB_TRY(gemm_tn<TI>(s, nI, nrhs, nI, TI(-1), ifSub.as<TI>() + blk * (j + 1), nullptr, 0, nI,
+                               Zi + vb * (j + 1), nullptr, 0, nI, TI(1), F + vb * j, nullptr, 0, nI, 1));
+        SLAB_TRY(trsv_coop<TI>(s, ifLU.as<TI>() + blk * j, nI, nI, ifPerm.as<int>() + (long long)nI * j, linv(j),
+                               uinv(j), kInvBs, F + vb * j, nI, Zi + vb * j, nI, nrhs, true));
+      }
+      convert_kernel<T, TI><<<grid_for(nbI * vb), 256, 0, s>>>(Zi, Zbuf.as<T>(), nbI * vb);
+      SLAB_CHECK_LAUNCH();
+      scatter_set_kernel<T><<<grid_for((long long)nbI * vb), 256, 0, s>>>(u, ntot, ifGlob.as<int>(), nI, nbI, nrhs,
+                                                                         Zbuf.as<T>());
+      SLAB_CHECK_LAUNCH();
+    }
+    // tree backward (transposed): lam_E = M^{-T} (g_E - col^T lam_O)
+    for (auto it = batches.rbegin(); it != batches.rend(); ++it) {
+      Batch& b = **it;
+      T* Y = Ybuf.as<T>() + b.offY0;
+      T* Z = Zbuf.as<T>();
+      const long long strideM = (long long)b.nE * (b.nE + b.nO);
+      T* Maug = fpool.as<T>() + b.offM0;
+      gather_kernel<T><<<grid_for((long long)b.count * b.nO * nrhs), 256, 0, s>>>(u, ntot, b.Oglob.as<int>(), b.nO,
+                                                                                b.count, nrhs, Z);
+      SLAB_CHECK_LAUNCH();
+      SLAB_TRY(gemm_tn<T>(s, b.nE, nrhs, b.nO, T(-1), fpool.as<T>() + b.offC0, nullptr, (long long)b.nO * b.nE, b.nO,
+                          Z, nullptr, (long long)b.nO * nrhs, b.nO, T(1), Y, nullptr, (long long)b.nE * nrhs, b.nE,
+                          b.count));
+      SLAB_TRY(getrs_small_t<T>(s, b.nE, nrhs, Maug, nullptr, strideM, b.nE, permpool.as<int>() + b.offPiv0, nullptr,
+                                b.nE, Y, nullptr, (long long)b.nE * nrhs, b.nE, b.count));
+      scatter_set_kernel<T><<<grid_for((long long)b.count * b.nE * nrhs), 256, 0, s>>>(u, ntot, b.Eglob.as<int>(),
+                                                                                     b.nE, b.count, nrhs, Y);
+      SLAB_CHECK_LAUNCH();
+    }
+    // leaf backward: lam_c = A_cc^{-T} (g_c - N_c^T lam_x)
+    gather_kernel<T><<<grid_for(nleaf * nx * nrhs), 256, 0, s>>>(u, ntot, leafglob.as<int>(), nx, (int)nleaf, nrhs,
+                                                                flux.as<T>());
+    SLAB_CHECK_LAUNCH();
+    SLAB_CUDA_TRY(cudaMemcpyAsync(w, rcT.p, (size_t)nleaf * n * nrhs * sizeof(T), cudaMemcpyDeviceToDevice, s));
+    SLAB_TRY(gemm_tn<T>(s, n, nrhs, nx, T(-1), NxcT.as<T>(), nullptr, 0, nx, flux.as<T>(), nullptr,
+                        (long long)nx * nrhs, nx, T(1), w, nullptr, (long long)n * nrhs, n, (int)nleaf));
+    return getrs_small_t<T>(s, n, nrhs, G.as<T>(), nullptr, strideG, n, leafperm.as<int>(), nullptr, n, w, nullptr,
+                            (long long)n * nrhs, n, (int)nleaf);
+  }
+
+  int residual_t_impl(int nrhs, const double* lx, const double* lc, const double* gint, const double* gfaces,
+                      double* rc, double* rx, bool all_faces) {
+    mask_faces_kernel<<<grid_for(ntot * nrhs), 256, 0, s>>>(gfaces, dirmask.as<unsigned char>(), rx, ntot, nrhs, 0);
+    SLAB_CHECK_LAUNCH();
+    if (all_faces) {
+      // Dirichlet columns start from the direct sensitivity as well
+      SLAB_CUDA_TRY(cudaMemcpyAsync(rx, gfaces, (size_t)ntot * nrhs * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    }
+    ResidualArgs r{};
+    r.p = p; r.q = q; r.n = n; r.nx = nx; r.nleaf = (int)nleaf; r.nrhs = nrhs; r.ntot = ntot;
+    r.co = coeffs(); r.D = D.as<double>(); r.Dsq = Dsq.as<double>();
+    r.leafglob = leafglob.as<int>(); r.dirmask = dirmask.as<unsigned char>();
+    r.ux = lx; r.uc = lc; r.fbody = gint; r.rc = rc; r.rx = rx; r.all_faces = all_faces ? 1 : 0;
+    residual_t_kernel<<<(unsigned)nleaf, 256, (6 * (size_t)p * p + nx) * sizeof(double), s>>>(r);
+    SLAB_CHECK_LAUNCH();
+    return SLAB_OK;
+  }
+
+  int reserve_t(int nrhs) {
+    SLAB_TRY(reserve(nrhs));
+    if (gi_d.bytes < (size_t)nleaf * n * nrhs * sizeof(double)) {
+      SLAB_TRY(gi_d.alloc((size_t)nleaf * n * nrhs * sizeof(double)));
+      SLAB_TRY(gf_d.alloc((size_t)ntot * nrhs * sizeof(double)));
+    }
+    return SLAB_OK;
+  }
+
+  int adjoint(int nrhs, const double* gleaf, const double* gfaces, double tol, int max_iter, double* lam_leaf,
+              double* lam_faces, double* gbnd, int* iters, double* stats) override {
+    SLAB_TRY(enter());
+    int st = SLAB_OK, total_it = 0;
+    double worst[5] = {0, 0, 0, 0, 0};
+    const long long npts = nleaf * p * p;
+    // the transposed solve kernels take up to four right-hand sides at a time
+    for (int c0 = 0; c0 < nrhs && (st == SLAB_OK || st == SLAB_ERR_NOCONV); c0 += 4) {
+      const int k = std::min(4, nrhs - c0);
+      int it = 0;
+      double sv[5] = {0, 0, 0, 0, 0};
+      const int sc = adjoint_impl(k, gleaf ? gleaf + c0 * npts : nullptr, gfaces ? gfaces + c0 * ntot : nullptr, tol,
+                                  max_iter, lam_leaf ? lam_leaf + c0 * npts : nullptr,
+                                  lam_faces ? lam_faces + c0 * ntot : nullptr, gbnd ? gbnd + c0 * ntot : nullptr, &it,
+                                  sv);
+      if (sc != SLAB_OK && st == SLAB_OK) st = sc;
+      total_it = std::max(total_it, it);
+      for (int i = 0; i < 5; ++i) worst[i] = std::max(worst[i], sv[i]);
+      if (sc != SLAB_OK && sc != SLAB_ERR_NOCONV) break;
+    }
+    if (iters) *iters = total_it;
+    if (stats)
+      for (int i = 0; i < 5; ++i) stats[i] = worst[i];
+    const int st2 = leave();
+    if (st == SLAB_ERR_NOCONV) set_error(SLAB_ERR_NOCONV, "adjoint refinement did not reach tol %.1e", tol);
+    return st != SLAB_OK ? st : st2;
+  }
+
+  int adjoint_impl(int nrhs, const double* gleaf, const double* gfaces, double tol, int max_iter, double* lam_leaf,
+                   double* lam_faces, double* gbnd, int* iters, double* stats) {
+    if (!factored) return set_error(SLAB_ERR_STATE, "slab_engine_adjoint: engine not factored");
+    if (nrhs <= 0 || (!gleaf && !gfaces)) return set_error(SLAB_ERR_ARG, "slab_engine_adjoint: invalid arguments");
+    if (n > 32 * kWarpSlots) return set_error(SLAB_ERR_ARG, "slab_engine_adjoint: leaf order p=%d too large", p);
+    for (auto& b : batches)
+      if (b->nE > 32 * kWarpSlots)
+        return set_error(SLAB_ERR_ARG, "slab_engine_adjoint: merge block of order %d > %d", b->nE, 32 * kWarpSlots);
+    SLAB_TRY(reserve_t(nrhs));
+    const long long nc_el = nleaf * n * nrhs, nf_el = ntot * nrhs;
+    double* gi = gi_d.as<double>();
+    double* gf = gf_d.as<double>();
+    if (gfaces)
+      SLAB_CUDA_TRY(cudaMemcpyAsync(gf, gfaces, (size_t)nf_el * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    else
+      SLAB_CUDA_TRY(cudaMemsetAsync(gf, 0, (size_t)nf_el * sizeof(double), s));
+    if (gleaf) {
+      AssembleTArgs at{};
+      at.p = p; at.q = q; at.n = n; at.nx = nx; at.nleaf = (int)nleaf; at.nrhs = nrhs; at.ntot = ntot;
+      at.leafglob = leafglob.as<int>(); at.interp = interp.as<double>(); at.jxreorder = jxr.as<int>();
+      at.dsol = gleaf; at.gint = gi; at.gfaces = gf;
+      assemble_t_kernel<<<(unsigned)nleaf, 256, 0, s>>>(at);
+      SLAB_CHECK_LAUNCH();
+    } else {
+      SLAB_CUDA_TRY(cudaMemsetAsync(gi, 0, (size_t)nc_el * sizeof(double), s));
+    }
+    SLAB_CUDA_TRY(cudaMemsetAsync(uc_d.p, 0, (size_t)nc_el * sizeof(double), s));
+    SLAB_CUDA_TRY(cudaMemsetAsync(ux_d.p, 0, (size_t)nf_el * sizeof(double), s));
+    double r0 = 0, rn = 0, rel = 1.0, dn = 0, un = 0;
+    int it = 0;
+    bool converged = false;
+    for (; it < max_iter; ++it) {
+      SLAB_TRY(residual_t_impl(nrhs, ux_d.as<double>(), uc_d.as<double>(), gi, gf, rc_d.as<double>(),
+                               rx_d.as<double>(), false));
+      SLAB_TRY(norms(rc_d.p, true, nc_el, rx_d.p, true, nf_el, &rn));
+      if (it == 0) r0 = rn;
+      if (rn == 0.0) {
+        converged = true;
+        rel = 0.0;
+        break;
+      }
+      convert_kernel<T, double><<<grid_for(nc_el), 256, 0, s>>>(rc_d.as<double>(), rcT.as<T>(), nc_el);
+      SLAB_CHECK_LAUNCH();
+      convert_kernel<T, double><<<grid_for(nf_el), 256, 0, s>>>(rx_d.as<double>(), gvec.as<T>(), nf_el);
+      SLAB_CHECK_LAUNCH();
+      if (gapp_t && gapp_t_nrhs != nrhs) {
+        cudaGraphExecDestroy(gapp_t);
+        gapp_t = nullptr;
+      }
+      gapp_t_nrhs = nrhs;
+      SLAB_TRY(run_graph(gapp_t, [&]() { return apply_t(nrhs); }));
+      axpy_kernel<T><<<grid_for(nc_el), 256, 0, s>>>(uc_d.as<double>(), wc.as<T>(), nc_el);
+      SLAB_CHECK_LAUNCH();
+      axpy_kernel<T><<<grid_for(nf_el), 256, 0, s>>>(ux_d.as<double>(), uvec.as<T>(), nf_el);
+      SLAB_CHECK_LAUNCH();
+      SLAB_TRY(norms(wc.p, false, nc_el, uvec.p, false, nf_el, &dn));
+      SLAB_TRY(norms(uc_d.p, true, nc_el, ux_d.p, true, nf_el, &un));
+      rel = un > 0 ? dn / un : 0.0;
+      if (rel <= tol) {
+        converged = true;
+        ++it;
+        break;
+      }
+    }
+    // final transposed residual over every face column: the Dirichlet entries
+    // are the sensitivity of the loss to the Dirichlet data
+    SLAB_TRY(residual_t_impl(nrhs, ux_d.as<double>(), uc_d.as<double>(), gi, gf, rc_d.as<double>(), rx_d.as<double>(),
+                             true));
+    SLAB_TRY(norms(rc_d.p, true, nc_el, nullptr, true, 0, &rn));
+    if (gbnd) {
+      mask_faces_kernel<<<grid_for(nf_el), 256, 0, s>>>(rx_d.as<double>(), dirmask.as<unsigned char>(), gbnd, ntot,
+                                                        nrhs, 1);
+      SLAB_CHECK_LAUNCH();
+    }
+    // residual over the unknown rows only, for the report
+    mask_faces_kernel<<<grid_for(nf_el), 256, 0, s>>>(rx_d.as<double>(), dirmask.as<unsigned char>(),
+                                                      rx_d.as<double>(), ntot, nrhs, 0);
+    SLAB_CHECK_LAUNCH();
+    SLAB_TRY(norms(rc_d.p, true, nc_el, rx_d.p, true, nf_el, &rn));
+    if (lam_faces)
+      SLAB_CUDA_TRY(cudaMemcpyAsync(lam_faces, ux_d.p, (size_t)nf_el * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    if (lam_leaf) {
+      interior_to_nodes_kernel<<<grid_for(nleaf * p * p * nrhs), 256, 0, s>>>(uc_d.as<double>(), lam_leaf, p,
+                                                                             (int)nleaf, nrhs);
+      SLAB_CHECK_LAUNCH();
+    }
+    SLAB_CUDA_TRY(cudaStreamSynchronize(s));
+    if (iters) *iters = it;
+    if (stats) {
+      stats[0] = rel;
+      stats[1] = rn;
+      stats[2] = r0;
+      stats[3] = 0.0;
+      stats[4] = r0 > 0 ? rn / r0 : 0.0;
+    }
+    if (!converged) {
+      set_error(SLAB_ERR_NOCONV, "adjoint refinement: relative correction %.3e after %d steps (tol %.1e)", rel, it,
+                tol);
+      return SLAB_ERR_NOCONV;
+    }
+    return SLAB_OK;
+  }
+
+  int coeff_grad(int nrhs, const double* ufaces, const double* uleaf, const double* lam_leaf, double* g11,
+                 double* g22, double* g1, double* g2, double* g0) override {
+    if (nrhs <= 0 || !ufaces || !uleaf || !lam_leaf)
+      return set_error(SLAB_ERR_ARG, "slab_engine_coeff_grad: invalid arguments");
+    if (n > 4 * 256) return set_error(SLAB_ERR_ARG, "slab_engine_coeff_grad: leaf order p=%d too large", p);
+    SLAB_TRY(enter());
+    GradArgs ga{};
+    ga.p = p; ga.q = q; ga.n = n; ga.nx = nx; ga.nleaf = (int)nleaf; ga.nrhs = nrhs; ga.ntot = ntot;
+    ga.D = D.as<double>(); ga.Dsq = Dsq.as<double>(); ga.leafglob = leafglob.as<int>();
+    ga.uleaf = uleaf; ga.ufaces = ufaces; ga.lam = lam_leaf;
+    ga.g11 = g11; ga.g22 = g22; ga.g1 = g1; ga.g2 = g2; ga.g0 = g0;
+    coeff_grad_kernel<<<(unsigned)nleaf, 256, 3 * (size_t)p * p * sizeof(double), s>>>(ga);
+    SLAB_CHECK_LAUNCH();
+    return leave();
   }
 
   int residual_impl(int nrhs, const double* ux, const double* uc, const double* fbody, double* rc, double* rx) {
@@ -1133,6 +1437,20 @@ extern "C" int slab_engine_solve(slab_engine* e, int nrhs, const double* bnd, co
                                  int max_iter, double* ufaces, double* uleaf, int* iters, double* stats) {
   if (!e) return slab::set_error(SLAB_ERR_ARG, "slab_engine_solve: null engine");
   return e->impl->solve(nrhs, bnd, fbody, tol, max_iter, ufaces, uleaf, iters, stats);
+}
+
+extern "C" int slab_engine_adjoint(slab_engine* e, int nrhs, const double* gleaf, const double* gfaces, double tol,
+                                   int max_iter, double* lam_leaf, double* lam_faces, double* gbnd, int* iters,
+                                   double* stats) {
+  if (!e) return slab::set_error(SLAB_ERR_ARG, "slab_engine_adjoint: null engine");
+  return e->impl->adjoint(nrhs, gleaf, gfaces, tol, max_iter, lam_leaf, lam_faces, gbnd, iters, stats);
+}
+
+extern "C" int slab_engine_coeff_grad(slab_engine* e, int nrhs, const double* ufaces, const double* uleaf,
+                                      const double* lam_leaf, double* g11, double* g22, double* g1, double* g2,
+                                      double* g) {
+  if (!e) return slab::set_error(SLAB_ERR_ARG, "slab_engine_coeff_grad: null engine");
+  return e->impl->coeff_grad(nrhs, ufaces, uleaf, lam_leaf, g11, g22, g1, g2, g);
 }
 
 extern "C" int slab_engine_residual(slab_engine* e, int nrhs, const double* ufaces, const double* uint,

@@ -87,6 +87,188 @@ __global__ void __launch_bounds__(256) residual_kernel(ResidualArgs a) {
   }
 }
 
+__global__ void __launch_bounds__(256) residual_t_kernel(ResidualArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int p = a.p, q = a.q, n = a.n, nx = a.nx;
+  double* Dsh = reinterpret_cast<double*>(smem_raw);
+  double* Dsqsh = Dsh + p * p;
+  double* m11 = Dsqsh + p * p;  // -c11 lam, -c22 lam, -c1 lam, -c2 lam on the p x p grid
+  double* m22 = m11 + p * p;
+  double* m1 = m22 + p * p;
+  double* m2 = m1 + p * p;
+  double* lx = m2 + p * p;      // lambda on the leaf's face nodes (0 on Dirichlet faces)
+  const int leaf = blockIdx.x;
+  const int tid = threadIdx.x;
+  for (int i = tid; i < p * p; i += blockDim.x) {
+    Dsh[i] = a.D[i];
+    Dsqsh[i] = a.Dsq[i];
+  }
+  const int lofs = leaf * p * p;
+  const LeafCoeffs& co = a.co;
+  for (int c = 0; c < a.nrhs; ++c) {
+    __syncthreads();
+    for (int i = tid; i < p * p; i += blockDim.x) m11[i] = m22[i] = m1[i] = m2[i] = 0.0;
+    __syncthreads();
+    for (int r = tid; r < n; r += blockDim.x) {
+      int i1, i2;
+      interior_node(r, q, i1, i2);
+      const int k = i1 * p + i2;
+      const double l = a.uc[((size_t)leaf * a.nrhs + c) * n + r];
+      if (co.c11) m11[k] = -co.c11[lofs + k] * l;
+      if (co.c22) m22[k] = -co.c22[lofs + k] * l;
+      if (co.c1) m1[k] = -co.c1[lofs + k] * l;
+      if (co.c2) m2[k] = -co.c2[lofs + k] * l;
+    }
+    for (int s = tid; s < nx; s += blockDim.x) {
+      const int g = a.leafglob[(size_t)leaf * nx + s];
+      lx[s] = a.dirmask[g] ? 0.0 : a.ux[g + (size_t)c * a.ntot];
+    }
+    __syncthreads();
+    // z[l] = sum_k Aloc[k,l] lam_k + sum_s Nx[s,l] lx_s at interior and face nodes l
+    for (int idx = tid; idx < n + nx; idx += blockDim.x) {
+      int l1, l2;
+      if (idx < n)
+        interior_node(idx, q, l1, l2);
+      else
+        face_node(idx - n, p, q, l1, l2);
+      const int l = l1 * p + l2;
+      double z = 0.0;
+      for (int k1 = 0; k1 < p; ++k1) {
+        z += Dsqsh[k1 * p + l1] * m11[k1 * p + l2];
+        z += Dsh[k1 * p + l1] * m1[k1 * p + l2];
+      }
+      for (int k2 = 0; k2 < p; ++k2) {
+        z += Dsqsh[k2 * p + l2] * m22[l1 * p + k2];
+        z += Dsh[k2 * p + l2] * m2[l1 * p + k2];
+      }
+      if (idx < n && co.c) z += co.c[lofs + l] * a.uc[((size_t)leaf * a.nrhs + c) * n + idx];
+      // Nx^T lx: face rows couple the nodes on their normal line
+      if (l2 >= 1 && l2 <= p - 2) {
+        const int sL = l2 - 1, sR = q + l2 - 1;
+        z += Dsh[l1] * lx[sL];                  // left face row (0, l2): D[0, l1]
+        z -= Dsh[(p - 1) * p + l1] * lx[sR];    // right face row (p-1, l2): -D[p-1, l1]
+      }
+      if (l1 >= 1 && l1 <= p - 2) {
+        const int sD = 2 * q + l1 - 1, sU = 3 * q + l1 - 1;
+        z += Dsh[l2] * lx[sD];                  // down face row (l1, 0): D[0, l2]
+        z -= Dsh[(p - 1) * p + l2] * lx[sU];    // up face row (l1, p-1): -D[p-1, l2]
+      }
+      if (idx < n) {
+        const double g = a.fbody ? a.fbody[((size_t)leaf * a.nrhs + c) * n + idx] : 0.0;
+        a.rc[((size_t)leaf * a.nrhs + c) * n + idx] = g - z;
+      } else {
+        const int gf = a.leafglob[(size_t)leaf * nx + (idx - n)];
+        if (a.all_faces || !a.dirmask[gf]) atomicAdd(&a.rx[gf + (size_t)c * a.ntot], -z);
+      }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256) assemble_t_kernel(AssembleTArgs a) {
+  const int p = a.p, q = a.q, n = a.n, nx = a.nx;
+  const int leaf = blockIdx.x, tid = threadIdx.x;
+  const int nr = 4 * (p - 1);
+  const size_t ldo = (size_t)a.nleaf * p * p;
+  for (int c = 0; c < a.nrhs; ++c) {
+    const double* ds = a.dsol + (size_t)leaf * p * p + c * ldo;
+    for (int r = tid; r < n; r += blockDim.x) {
+      int i1, i2;
+      interior_node(r, q, i1, i2);
+      a.gint[((size_t)leaf * a.nrhs + c) * n + r] = ds[i1 * p + i2];
+    }
+    for (int s = tid; s < nx; s += blockDim.x) {
+      const int g = a.leafglob[(size_t)leaf * nx + s];
+      double v = 0.0;
+      for (int t = 0; t < nr; ++t) v += a.interp[(size_t)t * nx + s] * ds[a.jxreorder[t]];
+      atomicAdd(&a.gfaces[g + (size_t)c * a.ntot], v);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256) coeff_grad_kernel(GradArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int p = a.p, q = a.q, n = a.n, nx = a.nx;
+  double* Dsh = reinterpret_cast<double*>(smem_raw);
+  double* Dsqsh = Dsh + p * p;
+  double* u = Dsqsh + p * p;
+  const int leaf = blockIdx.x, tid = threadIdx.x;
+  for (int i = tid; i < p * p; i += blockDim.x) {
+    Dsh[i] = a.D[i];
+    Dsqsh[i] = a.Dsq[i];
+  }
+  const int lofs = leaf * p * p;
+  const size_t ldl = (size_t)a.nleaf * p * p;
+  // boundary nodes of the leaf carry no PDE row: zero gradient there
+  for (int i = tid; i < p * p; i += blockDim.x) {
+    const int i1 = i / p, i2 = i % p;
+    if (i1 == 0 || i1 == p - 1 || i2 == 0 || i2 == p - 1) {
+      if (a.g0) a.g0[lofs + i] = 0.0;
+      if (a.g11) a.g11[lofs + i] = 0.0;
+      if (a.g22) a.g22[lofs + i] = 0.0;
+      if (a.g1) a.g1[lofs + i] = 0.0;
+      if (a.g2) a.g2[lofs + i] = 0.0;
+    }
+  }
+  // each interior node is owned by one thread across all right-hand sides
+  constexpr int kMaxOwn = 4;  // n <= kMaxOwn * blockDim.x (p <= 33 at 256 threads)
+  double acc[kMaxOwn][5];
+#pragma unroll
+  for (int o = 0; o < kMaxOwn; ++o)
+#pragma unroll
+    for (int t = 0; t < 5; ++t) acc[o][t] = 0.0;
+  for (int c = 0; c < a.nrhs; ++c) {
+    __syncthreads();
+    for (int i = tid; i < p * p; i += blockDim.x) u[i] = 0.0;
+    __syncthreads();
+    for (int r = tid; r < n; r += blockDim.x) {
+      int i1, i2;
+      interior_node(r, q, i1, i2);
+      u[i1 * p + i2] = a.uleaf[lofs + i1 * p + i2 + c * ldl];
+    }
+    for (int s = tid; s < nx; s += blockDim.x) {
+      int j1, j2;
+      face_node(s, p, q, j1, j2);
+      u[j1 * p + j2] = a.ufaces[a.leafglob[(size_t)leaf * nx + s] + (size_t)c * a.ntot];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int o = 0; o < kMaxOwn; ++o) {
+      const int r = tid + o * blockDim.x;
+      if (r >= n) break;
+      int i1, i2;
+      interior_node(r, q, i1, i2);
+      const int k = i1 * p + i2;
+      const double l = a.lam[lofs + k + c * ldl];
+      double t11 = 0, t22 = 0, t1 = 0, t2 = 0;
+      for (int j = 0; j < p; ++j) {
+        const double ux1 = u[j * p + i2], ux2 = u[i1 * p + j];
+        t11 += Dsqsh[i1 * p + j] * ux1;
+        t22 += Dsqsh[i2 * p + j] * ux2;
+        t1 += Dsh[i1 * p + j] * ux1;
+        t2 += Dsh[i2 * p + j] * ux2;
+      }
+      acc[o][0] += l * t11;
+      acc[o][1] += l * t22;
+      acc[o][2] += l * t1;
+      acc[o][3] += l * t2;
+      acc[o][4] -= l * u[k];
+    }
+  }
+#pragma unroll
+  for (int o = 0; o < kMaxOwn; ++o) {
+    const int r = tid + o * blockDim.x;
+    if (r >= n) break;
+    int i1, i2;
+    interior_node(r, q, i1, i2);
+    const int k = lofs + i1 * p + i2;
+    if (a.g11) a.g11[k] = acc[o][0];
+    if (a.g22) a.g22[k] = acc[o][1];
+    if (a.g1) a.g1[k] = acc[o][2];
+    if (a.g2) a.g2[k] = acc[o][3];
+    if (a.g0) a.g0[k] = acc[o][4];
+  }
+}
+
 __global__ void __launch_bounds__(256) assemble_solution_kernel(AssembleArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   double* uxl = reinterpret_cast<double*>(smem_raw);

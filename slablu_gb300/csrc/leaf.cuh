@@ -174,9 +174,60 @@ struct ResidualArgs {
   const double* fbody;          // (nleaf*p*p) x nrhs column-major, or null
   double* rc;                   // leaf-major like uc
   double* rx;                   // ntot x nrhs, accumulated with atomicAdd (caller zeroes)
+  int all_faces;                // residual_t_kernel: also accumulate into Dirichlet face columns
 };
 
 __global__ void residual_kernel(ResidualArgs a);
+
+// FP64 residual of the transposed system, one CTA per leaf:
+//   rc = g_int - (A^T lam) at interior columns (leaf-major, like uc),
+//   rx -= (A^T lam) at face columns (caller initialises rx to g_faces),
+// with lam = (uc, ux) holding the multipliers of the interior PDE rows and of
+// the face flux rows (ux is read as zero on Dirichlet faces, which have no
+// row).  fbody holds g_int in the leaf-major interior layout.  Dirichlet face
+// columns are skipped unless all_faces is set; with it, rx there becomes the
+// sensitivity of the loss to the Dirichlet data.
+__global__ void residual_t_kernel(ResidualArgs a);
+
+// Adjoint of the solution assembly (sol_tot from interior and face values):
+// dsol (nleaf*p*p x nrhs, column-major) -> g_int = dsol at interior nodes
+// (leaf-major) and g_faces += Interp^T dsol at the leaf boundary nodes
+// (atomically, every face including Dirichlet ones).
+struct AssembleTArgs {
+  int p, q, n, nx, nleaf, nrhs;
+  long long ntot;
+  const int* leafglob;
+  const double* interp;
+  const int* jxreorder;
+  const double* dsol;
+  double* gint;
+  double* gfaces;
+};
+__global__ void assemble_t_kernel(AssembleTArgs a);
+
+// Coefficient gradients of a loss L(u) where A(c) u = f, from the multipliers
+// lam of the interior PDE rows: with (A u)_k = -c11 t11 - c22 t22 - c1 t1 -
+// c2 t2 + c u_k (t11 = (D11 u)_k, t1 = (-D1 u)_k, ...),
+//   dL/dc_k = -lam_k u_k, dL/dc11_k = lam_k t11, dL/dc22_k = lam_k t22,
+//   dL/dc1_k = lam_k t1,  dL/dc2_k = lam_k t2
+// at interior nodes k (zero at leaf boundary nodes), summed over the
+// right-hand sides.  u: interior values from uleaf, face values from ufaces.
+struct GradArgs {
+  int p, q, n, nx, nleaf, nrhs;
+  long long ntot;
+  const double* D;
+  const double* Dsq;
+  const int* leafglob;
+  const double* uleaf;   // nleaf*p*p x nrhs column-major
+  const double* ufaces;  // ntot x nrhs
+  const double* lam;     // nleaf*p*p x nrhs column-major (interior nodes read)
+  double* g11;
+  double* g22;
+  double* g1;
+  double* g2;
+  double* g0;            // each nleaf*p*p or null
+};
+__global__ void coeff_grad_kernel(GradArgs a);
 
 // sol_tot assembly: out[(leaf*p*p + k) + c*nleaf*p*p] for every leaf node.
 struct AssembleArgs {

@@ -49,6 +49,7 @@ class SlabEngine:
         self.ntot = int(self.L.slab_engine_nfaces(self.h))
         self.nleaf = int(self.L.slab_engine_nleaves(self.h))
         self.npts = self.nleaf * geom.p * geom.p
+        self.generation = 0  # incremented by every factor(); checked by the autograd backward
 
     def __del__(self):
         h = getattr(self, 'h', None)
@@ -76,6 +77,7 @@ class SlabEngine:
                 assert t.dtype == torch.float64 and t.is_cuda and t.numel() == self.npts and t.is_contiguous()
             args.append(t)
         self._coef = args  # keep alive until the factorization has read them
+        self.generation = getattr(self, 'generation', 0) + 1
         st = self.L.slab_engine_factor(self.h, *[_lib.ptr(t) for t in args])
         return _lib.check(st, 'slab_engine_factor')
 
@@ -98,6 +100,52 @@ class SlabEngine:
         info = dict(rel_correction=stats[0], residual=stats[1], residual0=stats[2], resloc=stats[3],
                     rel_residual=stats[4], converged=(st == _lib.SLAB_OK))
         return uleaf.T, (None if ufaces is None else ufaces.T), iters.value, info
+
+    def adjoint(self, gleaf=None, gfaces=None, tol=1e-10, max_iter=20, want_faces=False, want_bnd=True,
+                allow_noconv=False):
+        """Transposed solve with the stored factors (slab_engine_adjoint).
+
+        gleaf: (npts, nrhs) dL/du at the leaf nodes; gfaces: (ntot, nrhs) dL/du_faces.
+        Returns (lam_leaf (npts, nrhs) = dL/dfbody, lam_faces or None,
+        gbnd (ntot, nrhs) = dL/dbnd or None, iters, stats dict).
+        """
+        ref = gleaf if gleaf is not None else gfaces
+        nrhs = 1 if ref.dim() == 1 else ref.shape[1]
+        dev = ref.device
+        gl = None if gleaf is None else _col_major(gleaf.to(torch.float64), self.npts)
+        gf = None if gfaces is None else _col_major(gfaces.to(torch.float64), self.ntot)
+        lam = torch.empty(nrhs, self.npts, dtype=torch.float64, device=dev)
+        lamf = torch.empty(nrhs, self.ntot, dtype=torch.float64, device=dev) if want_faces else None
+        gb = torch.empty(nrhs, self.ntot, dtype=torch.float64, device=dev) if want_bnd else None
+        iters = ctypes.c_int(0)
+        stats = (ctypes.c_double * 5)()
+        st = self.L.slab_engine_adjoint(self.h, nrhs, _lib.ptr(gl), _lib.ptr(gf), float(tol), int(max_iter),
+                                        _lib.ptr(lam), _lib.ptr(lamf), _lib.ptr(gb), ctypes.byref(iters), stats)
+        _lib.check(st, 'slab_engine_adjoint', allow=(_lib.SLAB_ERR_NOCONV,) if allow_noconv else ())
+        info = dict(rel_correction=stats[0], residual=stats[1], residual0=stats[2], rel_residual=stats[4],
+                    converged=(st == _lib.SLAB_OK))
+        t = lambda x: None if x is None else x.T
+        return lam.T, t(lamf), t(gb), iters.value, info
+
+    def coeff_grad(self, ufaces, uleaf, lam_leaf, keys=('c',)):
+        """dL/d(coefficient) at the leaf nodes for each key in keys (slab_engine_coeff_grad).
+
+        ufaces (ntot, nrhs), uleaf (npts, nrhs): forward solution; lam_leaf
+        (npts, nrhs) from adjoint().  Returns {key: (npts,) tensor}, summed over rhs.
+        """
+        nrhs = 1 if uleaf.dim() == 1 else uleaf.shape[1]
+        uf = _col_major(ufaces.to(torch.float64), self.ntot)
+        ul = _col_major(uleaf.to(torch.float64), self.npts)
+        lm = _col_major(lam_leaf.to(torch.float64), self.npts)
+        out = {k: torch.empty(self.npts, dtype=torch.float64, device=ul.device) for k in keys}
+        order = ('c11', 'c22', 'c1', 'c2', 'c')
+        for k in keys:
+            if k not in order:
+                raise ValueError(f'unknown coefficient {k}')
+        st = self.L.slab_engine_coeff_grad(self.h, nrhs, _lib.ptr(uf), _lib.ptr(ul), _lib.ptr(lm),
+                                           *[_lib.ptr(out.get(k)) for k in order])
+        _lib.check(st, 'slab_engine_coeff_grad')
+        return out
 
     def residual(self, ufaces, uint, fbody=None):
         """FP64 residual of the full collocation system.
