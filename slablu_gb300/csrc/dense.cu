@@ -138,6 +138,77 @@ int trsv_coop(cudaStream_t s, const T* LU, int lda, int n, const int* perm, cons
   return SLAB_OK;
 }
 
+namespace {
+// Largest usable cluster for trsv_cluster_kernel<T> (16 when the device allows
+// non-portable cluster sizes at this shared-memory footprint, else 8).
+template <typename T>
+int trsv_cluster_size(size_t bytes) {
+  static std::mutex mu;
+  static std::map<std::pair<int, size_t>, int> cache;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 8;
+  std::lock_guard<std::mutex> lk(mu);
+  auto key = std::make_pair(dev, bytes);
+  auto it = cache.find(key);
+  if (it != cache.end()) return it->second;
+  int best = 8;
+  if (cudaFuncSetAttribute(trsv_cluster_kernel<T>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
+      cudaSuccess) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(16);
+    cfg.blockDim = dim3(256);
+    cfg.dynamicSmemBytes = bytes;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = 16;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int nc = 0;
+    if (cudaOccupancyMaxActiveClusters(&nc, trsv_cluster_kernel<T>, &cfg) == cudaSuccess && nc > 0) best = 16;
+  }
+  cudaGetLastError();  // a refused query leaves no error behind
+  cache[key] = best;
+  return best;
+}
+}  // namespace
+
+template <typename T>
+int trsv_cluster(cudaStream_t s, const T* LU, int lda, int n, const int* perm, const T* Linv, const T* Uinv,
+                 const T* B, int ldb, T* X, int ldx, int nrhs, bool trans) {
+  if (n <= 0 || nrhs <= 0) return SLAB_OK;
+  if (nrhs > kCoopMaxRhs) return set_error(SLAB_ERR_ARG, "trsv_cluster: nrhs %d > %d", nrhs, kCoopMaxRhs);
+  const int nblk = ceil_div(n, kClBs);
+  const size_t lim = allow_dynamic_smem(reinterpret_cast<const void*>(trsv_cluster_kernel<T>));
+  auto bytes_for = [&](int cl) {
+    const int own = ceil_div(nblk, cl);
+    return (size_t)(5 * own + 3) * kClBs * kCoopMaxRhs * sizeof(T);
+  };
+  int CL = trsv_cluster_size<T>(bytes_for(16));
+  if (CL > nblk) CL = nblk < 8 ? nblk : 8;
+  const int own_max = ceil_div(nblk, CL);
+  const size_t bytes = bytes_for(CL);
+  if (bytes > lim) return set_error(SLAB_ERR_ARG, "trsv_cluster: order %d too large", n);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(CL);
+  cfg.blockDim = dim3(256);
+  cfg.dynamicSmemBytes = bytes;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = CL;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  const int tr = trans ? 1 : 0;
+  SLAB_CUDA_TRY(cudaLaunchKernelEx(&cfg, trsv_cluster_kernel<T>, LU, lda, n, perm, Linv, Uinv, B, ldb, X, ldx, nrhs,
+                                   tr, own_max));
+  SLAB_CHECK_LAUNCH();
+  return SLAB_OK;
+}
+
 template <typename T>
 int getrs_small_t(cudaStream_t s, int n, int nrhs, const T* LU, const long long* offLU, long long strideLU, int lda,
                   const int* perm, const long long* offP, long long strideP, T* B, const long long* offB,
@@ -487,6 +558,10 @@ template int trsv_coop<float>(cudaStream_t, const float*, int, int, const int*, 
                               const float*, int, float*, int, int, bool);
 template int trsv_coop<double>(cudaStream_t, const double*, int, int, const int*, const double*, const double*, int,
                                const double*, int, double*, int, int, bool);
+template int trsv_cluster<float>(cudaStream_t, const float*, int, int, const int*, const float*, const float*,
+                                 const float*, int, float*, int, int, bool);
+template int trsv_cluster<double>(cudaStream_t, const double*, int, int, const int*, const double*, const double*,
+                                  const double*, int, double*, int, int, bool);
 template int getrs_small_t<float>(cudaStream_t, int, int, const float*, const long long*, long long, int, const int*,
                                   const long long*, long long, float*, const long long*, long long, int, int);
 template int getrs_small_t<double>(cudaStream_t, int, int, const double*, const long long*, long long, int,

@@ -895,6 +895,168 @@ __global__ void __launch_bounds__(256) trsv_coop_kernel(const T* __restrict__ LU
   }
 }
 
+// Cluster triangular solves with one large factored matrix: same contract as
+// trsv_coop_kernel (X = A^{-1} B or A^{-T} B, nrhs <= kCoopMaxRhs, bs = 64
+// inverted diagonal blocks), run by ONE thread-block cluster.  Row block b is
+// owned by CTA b % CL, which keeps its right-hand-side accumulators in shared
+// memory across both passes.  Per block step: the owner forms x_b = inv_b acc_b
+// into a double-buffered shared array, one cluster barrier publishes it, every
+// CTA reads it through distributed shared memory and subtracts op(A)[own, b] x_b
+// from the blocks it owns.  A cluster barrier is a few hundred cycles, against
+// microseconds for a grid-wide barrier.
+constexpr int kClBs = 64;
+
+// y[r][c] (+)= sum_k op(A)[r][k] x[k][c] for r < rb, k < kb, op(A)[r][k] =
+// A[r + k*lda] (trans 0, rows contiguous) or A[k + r*lda] (trans 1).
+// x: shared, ld kClBs, ZERO beyond row kb.  Non-transposed partials go to
+// red[4][kClBs][nrhs] (summed by cl_reduce after a barrier); transposed
+// results are written to y directly (scaled by sgn, accumulated when acc_mode).
+// The column loop is a runtime loop and the FMA chain has no per-column
+// predicate: GB300 retires about two FP64 FMAs per clock per SM, so issued but
+// predicated-off FP64 instructions cost as much as useful ones.
+template <typename T>
+__device__ __forceinline__ void cl_gemv_n(const T* __restrict__ A, int lda, int rb, int kb, const T* x, int nrhs,
+                                          T* red) {
+  const int tid = threadIdx.x;
+  const int r = tid & (kClBs - 1), kq = tid >> 6;  // 256 threads: 64 rows x 4 k-quarters
+  const int kbeg = kq * (kClBs / 4);
+  T a[kClBs / 4];
+#pragma unroll
+  for (int t = 0; t < kClBs / 4; ++t) a[t] = (r < rb && kbeg + t < kb) ? A[r + (size_t)(kbeg + t) * lda] : T(0);
+  for (int c = 0; c < nrhs; ++c) {
+    const T* xc = x + kbeg + c * kClBs;
+    T part0 = T(0), part1 = T(0);
+#pragma unroll
+    for (int t = 0; t < kClBs / 4; t += 2) {
+      part0 += a[t] * xc[t];
+      part1 += a[t + 1] * xc[t + 1];
+    }
+    red[(kq * kClBs + r) + (size_t)c * 4 * kClBs] = part0 + part1;
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ T cl_reduce(const T* red, int r, int c) {
+  const T* q = red + r + (size_t)c * 4 * kClBs;
+  return (q[0] + q[kClBs]) + (q[2 * kClBs] + q[3 * kClBs]);
+}
+
+template <typename T>
+__device__ __forceinline__ void cl_gemv_t(const T* __restrict__ A, int lda, int rb, int kb, const T* x, int nrhs,
+                                          T* y, T sgn, bool acc_mode) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nw = blockDim.x >> 5;
+  for (int r = warp; r < rb; r += nw) {
+    const T a0 = lane < kb ? A[lane + (size_t)r * lda] : T(0);
+    const T a1 = lane + 32 < kb ? A[lane + 32 + (size_t)r * lda] : T(0);
+    for (int c = 0; c < nrhs; ++c) {
+      T v = a0 * x[lane + c * kClBs] + a1 * x[lane + 32 + c * kClBs];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      if (lane == 0) y[r + c * kClBs] = acc_mode ? y[r + c * kClBs] + sgn * v : sgn * v;
+    }
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) trsv_cluster_kernel(const T* __restrict__ LU, int lda, int n,
+                                                           const int* __restrict__ perm, const T* __restrict__ Linv,
+                                                           const T* __restrict__ Uinv, const T* __restrict__ Bin,
+                                                           int ldb, T* X, int ldx, int nrhs, int trans, int own_max) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cluster = cg::this_cluster();
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int bs = kClBs;
+  const int CL = (int)cluster.num_blocks();
+  const int rank = (int)cluster.block_rank();
+  const int tid = threadIdx.x;
+  const int vb = bs * kCoopMaxRhs;                 // one block of right-hand sides (ld bs)
+  T* acc = reinterpret_cast<T*>(smem_raw);         // own_max x vb
+  T* xbuf = acc + (size_t)own_max * vb;            // 2 x vb (published x_b)
+  T* xloc = xbuf + 2 * (size_t)vb;                 // vb (local copy of the current x_b)
+  T* red = xloc + vb;                              // own_max x 4 x vb
+  const int nblk = (n + bs - 1) / bs;
+  const int nown = rank < nblk ? (nblk - 1 - rank) / CL + 1 : 0;
+  for (int o = 0; o < nown; ++o) {
+    const int r0 = (rank + o * CL) * bs;
+    for (int idx = tid; idx < bs * nrhs; idx += blockDim.x) {
+      const int r = idx % bs, c = idx / bs;
+      acc[(size_t)o * vb + idx] = (r0 + r < n) ? Bin[(trans ? r0 + r : perm[r0 + r]) + (size_t)c * ldb] : T(0);
+    }
+  }
+  int step_all = 0;
+  for (int pass = 0; pass < 2; ++pass) {
+    const bool fwd = pass == 0;
+    const T* Inv = (fwd != (trans != 0)) ? Linv : Uinv;
+    for (int step = 0; step < nblk; ++step, ++step_all) {
+      const int b = fwd ? step : nblk - 1 - step;
+      const int k0 = b * bs, kb = min(bs, n - k0);
+      const int owner = b % CL;
+      T* xb = xbuf + (size_t)(step_all & 1) * vb;
+      if (rank == owner) {
+        const int o = b / CL;
+        T* a = acc + (size_t)o * vb;
+        const T* Ib = Inv + (size_t)b * bs * bs;
+        __syncthreads();
+        if (!trans) {
+          cl_gemv_n(Ib, bs, kb, kb, a, nrhs, red);
+          __syncthreads();
+          for (int idx = tid; idx < kb * nrhs; idx += blockDim.x) {
+            const int r = idx % kb, c = idx / kb;
+            xb[r + c * bs] = cl_reduce(red, r, c);
+          }
+        } else {
+          cl_gemv_t(Ib, bs, kb, kb, a, nrhs, xb, T(1), false);
+        }
+        __syncthreads();
+        // keep x_b: the next pass starts from it; the last pass is the output
+        for (int idx = tid; idx < kb * nrhs; idx += blockDim.x) {
+          const int r = idx % kb, c = idx / kb;
+          const T v = xb[r + c * bs];
+          if (fwd)
+            a[r + c * bs] = v;
+          else if (!trans)
+            X[k0 + r + (size_t)c * ldx] = v;
+          else
+            X[perm[k0 + r] + (size_t)c * ldx] = v;
+        }
+      }
+      cluster.sync();
+      const T* src = cluster.map_shared_rank(xb, owner);
+      for (int idx = tid; idx < bs * nrhs; idx += blockDim.x) {
+        const int r = idx % bs, c = idx / bs;
+        xloc[r + c * bs] = r < kb ? src[r + c * bs] : T(0);
+      }
+      __syncthreads();
+      // blocks still to come in this pass: b+1.. (forward) or ..b-1 (backward)
+      int nupd = 0;
+      for (int o = 0; o < nown; ++o) {
+        const int ob = rank + o * CL;
+        if (fwd ? ob <= b : ob >= b) continue;
+        const int r0 = ob * bs, rb = min(bs, n - r0);
+        if (!trans)
+          cl_gemv_n(LU + (size_t)k0 * lda + r0, lda, rb, kb, xloc, nrhs, red + (size_t)o * 4 * vb);
+        else
+          cl_gemv_t(LU + (size_t)r0 * lda + k0, lda, rb, kb, xloc, nrhs, acc + (size_t)o * vb, T(-1), true);
+        ++nupd;
+      }
+      if (!trans && nupd > 0) {
+        __syncthreads();
+        for (int o = 0; o < nown; ++o) {
+          const int ob = rank + o * CL;
+          if (fwd ? ob <= b : ob >= b) continue;
+          const int rb = min(bs, n - ob * bs);
+          for (int idx = tid; idx < rb * nrhs; idx += blockDim.x) {
+            const int r = idx % rb, c = idx / rb;
+            acc[(size_t)o * vb + r + c * bs] -= cl_reduce(red + (size_t)o * 4 * vb, r, c);
+          }
+        }
+      }
+    }
+  }
+  cluster.sync();  // no CTA leaves while its shared memory may still be read
+}
+
 // Split-K narrow GEMM for one tall matrix: C += alpha * A[:, kchunk] B[kchunk, :]
 // accumulated with atomics (C already scaled by beta).  grid (ceil(m/256), nsplit).
 template <typename T, int NC>
@@ -1343,6 +1505,12 @@ int getrs_small(cudaStream_t s, int n, int nrhs, const T* LU, const long long* o
 template <typename T>
 int trsv_coop(cudaStream_t s, const T* LU, int lda, int n, const int* perm, const T* Linv, const T* Uinv, int bs,
               const T* B, int ldb, T* X, int ldx, int nrhs, bool trans = false);
+
+// Same contract as trsv_coop with bs = 64, run by one thread-block cluster.
+// Returns SLAB_ERR_ARG when the shape does not fit (caller falls back).
+template <typename T>
+int trsv_cluster(cudaStream_t s, const T* LU, int lda, int n, const int* perm, const T* Linv, const T* Uinv,
+                 const T* B, int ldb, T* X, int ldx, int nrhs, bool trans = false);
 
 // C = beta C + alpha A^T B (A is k x m); same batching conventions as gemm.
 template <typename T>

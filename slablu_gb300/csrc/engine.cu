@@ -324,6 +324,7 @@ struct EngineImpl : EngineBase {
   cudaGraphExec_t gfac[3] = {nullptr, nullptr, nullptr}, gapp = nullptr, gapp_t = nullptr;
   int gapp_nrhs = 0, gapp_t_nrhs = 0;
   bool use_graphs = true;
+  bool use_cluster_solve = true;
   DevBuf D, Dsq, Nx, NxcT, NxxT, interp, jxr, leafglob, dirmask;
   DevBuf coef[5];
   bool has[5] = {false, false, false, false, false};
@@ -420,6 +421,8 @@ struct EngineImpl : EngineBase {
         us(s_) {
     const char* ng = getenv("SLAB_NO_GRAPHS");
     use_graphs = !(ng && ng[0] == '1');
+    const char* nc = getenv("SLAB_COOP_SOLVE");  // 1: grid-wide cooperative interface solve instead of the cluster one
+    use_cluster_solve = !(nc && nc[0] == '1');
     ntot = (long long)q * ((long long)n0 * (2 * n1 + 1) + n1);
     nleaf = (long long)n0 * n1;
   }
@@ -791,6 +794,22 @@ struct EngineImpl : EngineBase {
     return SLAB_OK;
   }
 
+  // Z = S_j^{-1} F (or S_j^{-T} F) with the stored interface factors: one
+  // thread-block cluster for up to eight columns, else the cooperative or the
+  // blocked solve.
+  int iface_solve(int j, const TI* F, TI* Z, int nrhs, bool trans) {
+    const long long blk = (long long)nI * nI;
+    const TI* LUj = ifLU.as<TI>() + blk * j;
+    const int* pj = ifPerm.as<int>() + (long long)nI * j;
+    if (nrhs <= kCoopMaxRhs && kInvBs == kClBs && use_cluster_solve) {
+      const int st = trsv_cluster<TI>(s, LUj, nI, nI, pj, linv(j), uinv(j), F, nI, Z, nI, nrhs, trans);
+      if (st != SLAB_ERR_ARG) return st;  // SLAB_ERR_ARG: shape refused before any launch
+    }
+    if (nrhs <= kCoopMaxRhs) return trsv_coop<TI>(s, LUj, nI, nI, pj, linv(j), uinv(j), kInvBs, F, nI, Z, nI, nrhs, trans);
+    if (trans) return set_error(SLAB_ERR_ARG, "interface: transposed solve takes at most %d columns", kCoopMaxRhs);
+    return bigtrs_inv<TI>(s, LUj, nI, nI, pj, linv(j), uinv(j), kInvBs, F, nI, Z, nI, nrhs);
+  }
+
   int factor_check() {
     // breakdown report
     std::vector<int> hinfo((size_t)nleaf);
@@ -922,12 +941,7 @@ struct EngineImpl : EngineBase {
         if (j > 0)
           SLAB_TRY(gemm<TI>(s, nI, nrhs, nI, TI(-1), ifSub.as<TI>() + blk * j, nullptr, 0, nI, Zi + vb * (j - 1),
                             nullptr, 0, nI, TI(1), F + vb * j, nullptr, 0, nI, 1));
-        if (nrhs <= kCoopMaxRhs)
-          SLAB_TRY(trsv_coop<TI>(s, ifLU.as<TI>() + blk * j, nI, nI, ifPerm.as<int>() + (long long)nI * j, linv(j),
-                                 uinv(j), kInvBs, F + vb * j, nI, Zi + vb * j, nI, nrhs));
-        else
-          SLAB_TRY(bigtrs_inv<TI>(s, ifLU.as<TI>() + blk * j, nI, nI, ifPerm.as<int>() + (long long)nI * j, linv(j),
-                                  uinv(j), kInvBs, F + vb * j, nI, Zi + vb * j, nI, nrhs));
+        SLAB_TRY(iface_solve(j, F + vb * j, Zi + vb * j, nrhs, false));
       }
       for (int j = nbI - 2; j >= 0; --j)
         SLAB_TRY(gemm<TI>(s, nI, nrhs, nI, TI(-1), ifX.as<TI>() + blk * j, nullptr, 0, nI, Zi + vb * (j + 1), nullptr,
@@ -1016,8 +1030,7 @@ struct EngineImpl : EngineBase {
         if (j < nbI - 1)
           SLAB_TRY(gemm_tn<TI>(s, nI, nrhs, nI, TI(-1), ifSub.as<TI>() + blk * (j + 1), nullptr, 0, nI,
                                Zi + vb * (j + 1), nullptr, 0, nI, TI(1), F + vb * j, nullptr, 0, nI, 1));
-        SLAB_TRY(trsv_coop<TI>(s, ifLU.as<TI>() + blk * j, nI, nI, ifPerm.as<int>() + (long long)nI * j, linv(j),
-                               uinv(j), kInvBs, F + vb * j, nI, Zi + vb * j, nI, nrhs, true));
+        SLAB_TRY(iface_solve(j, F + vb * j, Zi + vb * j, nrhs, true));
       }
       convert_kernel<T, TI><<<grid_for(nbI * vb), 256, 0, s>>>(Zi, Zbuf.as<T>(), nbI * vb);
       SLAB_CHECK_LAUNCH();

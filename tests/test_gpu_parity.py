@@ -204,3 +204,19 @@ def test_engine_multi_rhs(nrhs):
     ref = out['sol_tot']
     rel = np.linalg.norm(uleaf - ref, axis=0) / np.linalg.norm(ref, axis=0)
     assert rel.max() < 1e-9, rel
+
+
+@pytest.mark.parametrize('nrhs', [1, 5])
+def test_interface_solve_paths_agree(nrhs, monkeypatch):
+    """The cluster interface solve and the grid-wide cooperative one give the same solution."""
+    geom, p, n, kh = CASES[3]
+    a, md, part, co = _oracle_problem(geom, p, n, kh, ofuncs.bfield_gaussian_bumps)
+    rng = np.random.default_rng(40 + nrhs)
+    B = rng.standard_normal((md.ntot, nrhs))
+    out = []
+    for coop in ('0', '1'):
+        monkeypatch.setenv('SLAB_COOP_SOLVE', coop)
+        _, eng, uleaf, _, iters, st = _engine_solve(geom, p, a, co, lambda x: B, 'fp64', md.xx_active)
+        assert st['converged']
+        out.append(uleaf)
+    assert np.linalg.norm(out[0] - out[1]) <= 1e-12 * np.linalg.norm(out[1])
