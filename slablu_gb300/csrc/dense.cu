@@ -4,6 +4,7 @@
 #include <map>
 #include <mutex>
 #include <string>
+#include <tuple>
 
 #include "dense.cuh"
 
@@ -139,24 +140,22 @@ int trsv_coop(cudaStream_t s, const T* LU, int lda, int n, const int* perm, cons
 }
 
 namespace {
-// Largest usable cluster for trsv_cluster_kernel<T> (16 when the device allows
-// non-portable cluster sizes at this shared-memory footprint, else 8).
-template <typename T>
-int trsv_cluster_size(size_t bytes) {
+// Largest usable cluster (16 when the device allows non-portable cluster sizes
+// for this kernel at this shared-memory footprint and block size, else 8).
+int cluster_size_for(const void* kernel, size_t bytes, int threads) {
   static std::mutex mu;
-  static std::map<std::pair<int, size_t>, int> cache;
+  static std::map<std::tuple<const void*, int, size_t, int>, int> cache;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return 8;
   std::lock_guard<std::mutex> lk(mu);
-  auto key = std::make_pair(dev, bytes);
+  auto key = std::make_tuple(kernel, dev, bytes, threads);
   auto it = cache.find(key);
   if (it != cache.end()) return it->second;
   int best = 8;
-  if (cudaFuncSetAttribute(trsv_cluster_kernel<T>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
-      cudaSuccess) {
+  if (cudaFuncSetAttribute(kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == cudaSuccess) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(16);
-    cfg.blockDim = dim3(256);
+    cfg.blockDim = dim3(threads);
     cfg.dynamicSmemBytes = bytes;
     cudaLaunchAttribute at[1];
     at[0].id = cudaLaunchAttributeClusterDimension;
@@ -166,11 +165,29 @@ int trsv_cluster_size(size_t bytes) {
     cfg.attrs = at;
     cfg.numAttrs = 1;
     int nc = 0;
-    if (cudaOccupancyMaxActiveClusters(&nc, trsv_cluster_kernel<T>, &cfg) == cudaSuccess && nc > 0) best = 16;
+    if (cudaOccupancyMaxActiveClusters(&nc, kernel, &cfg) == cudaSuccess && nc > 0) best = 16;
   }
   cudaGetLastError();  // a refused query leaves no error behind
   cache[key] = best;
   return best;
+}
+
+int launch_cluster(const void* kernel, int cl, int threads, size_t bytes, cudaStream_t s, void** args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(cl);
+  cfg.blockDim = dim3(threads);
+  cfg.dynamicSmemBytes = bytes;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = cl;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  SLAB_CUDA_TRY(cudaLaunchKernelExC(&cfg, kernel, args));
+  SLAB_CHECK_LAUNCH();
+  return SLAB_OK;
 }
 }  // namespace
 
@@ -185,28 +202,16 @@ int trsv_cluster(cudaStream_t s, const T* LU, int lda, int n, const int* perm, c
     const int own = ceil_div(nblk, cl);
     return (size_t)(5 * own + 3) * kClBs * kCoopMaxRhs * sizeof(T);
   };
-  int CL = trsv_cluster_size<T>(bytes_for(16));
+  const void* kern = reinterpret_cast<const void*>(trsv_cluster_kernel<T>);
+  int CL = cluster_size_for(kern, bytes_for(16), 256);
   if (CL > nblk) CL = nblk < 8 ? nblk : 8;
-  const int own_max = ceil_div(nblk, CL);
+  int own_max = ceil_div(nblk, CL);
   const size_t bytes = bytes_for(CL);
   if (bytes > lim) return set_error(SLAB_ERR_ARG, "trsv_cluster: order %d too large", n);
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(CL);
-  cfg.blockDim = dim3(256);
-  cfg.dynamicSmemBytes = bytes;
-  cfg.stream = s;
-  cudaLaunchAttribute at[1];
-  at[0].id = cudaLaunchAttributeClusterDimension;
-  at[0].val.clusterDim.x = CL;
-  at[0].val.clusterDim.y = 1;
-  at[0].val.clusterDim.z = 1;
-  cfg.attrs = at;
-  cfg.numAttrs = 1;
-  const int tr = trans ? 1 : 0;
-  SLAB_CUDA_TRY(cudaLaunchKernelEx(&cfg, trsv_cluster_kernel<T>, LU, lda, n, perm, Linv, Uinv, B, ldb, X, ldx, nrhs,
-                                   tr, own_max));
-  SLAB_CHECK_LAUNCH();
-  return SLAB_OK;
+  int tr = trans ? 1 : 0;
+  void* args[] = {(void*)&LU, (void*)&lda, (void*)&n, (void*)&perm, (void*)&Linv, (void*)&Uinv, (void*)&B,
+                  (void*)&ldb, (void*)&X, (void*)&ldx, (void*)&nrhs, (void*)&tr, (void*)&own_max};
+  return launch_cluster(kern, CL, 256, bytes, s, args);
 }
 
 template <typename T>
@@ -377,34 +382,23 @@ int getrs_batched(cudaStream_t s, int n, int nrhs, const T* LU, const long long*
 }
 
 namespace {
-constexpr int kPanelCluster = 8;
-
-// Panel factorization: distributed shared memory of one 8-CTA cluster when the
-// panel fits (rows per CTA * nb elements), the global-memory kernel otherwise.
+// Panel factorization: distributed shared memory of one 16-CTA (or 8-CTA)
+// cluster when the panel and its row maps fit, the global-memory kernel otherwise.
 template <typename T>
 int panel_factor(cudaStream_t s, T* A, int lda, int n, int k0, int nb, int* ipiv, int* info, T* linv,
                  bool* linv_done) {
   *linv_done = false;
   const int m = n - k0;
-  const int R = ceil_div(m, kPanelCluster);
-  const size_t bytes = ((size_t)R * nb + nb + (size_t)nb * (nb + 1)) * sizeof(T);
-  const size_t lim = allow_dynamic_smem(reinterpret_cast<const void*>(biglu_panel_cluster_kernel<T>));
-  if (bytes <= lim && m >= kPanelCluster) {
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(kPanelCluster);
-    cfg.blockDim = dim3(256);
-    cfg.dynamicSmemBytes = bytes;
-    cfg.stream = s;
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeClusterDimension;
-    at[0].val.clusterDim.x = kPanelCluster;
-    at[0].val.clusterDim.y = 1;
-    at[0].val.clusterDim.z = 1;
-    cfg.attrs = at;
-    cfg.numAttrs = 1;
-    SLAB_CUDA_TRY(cudaLaunchKernelEx(&cfg, biglu_panel_cluster_kernel<T>, A, lda, n, k0, nb, R, ipiv, info, linv));
-    SLAB_CHECK_LAUNCH();
-    *linv_done = linv != nullptr && R >= nb;
+  const void* kern = reinterpret_cast<const void*>(biglu_panel_cluster_kernel<T>);
+  const size_t lim = allow_dynamic_smem(kern);
+  int CL = cluster_size_for(kern, panel_cluster_smem_bytes(m, nb, ceil_div(m, 16), sizeof(T)), 256);
+  int R = ceil_div(m, CL);
+  size_t bytes = panel_cluster_smem_bytes(m, nb, R, sizeof(T));
+  if (bytes <= lim && m >= CL && m >= nb) {
+    void* args[] = {(void*)&A, (void*)&lda, (void*)&n, (void*)&k0, (void*)&nb, (void*)&R, (void*)&ipiv,
+                    (void*)&info, (void*)&linv};
+    SLAB_TRY(launch_cluster(kern, CL, 256, bytes, s, args));
+    *linv_done = linv != nullptr;
     return SLAB_OK;
   }
   biglu_panel_kernel<T><<<1, 1024, 0, s>>>(A, lda, n, k0, nb, ipiv, info);

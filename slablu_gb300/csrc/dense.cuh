@@ -23,23 +23,58 @@ constexpr int kCTLD = kCT + 4;  // shared-memory leading dimension of a transpos
 constexpr int kPad = 64;    // slack elements after a staged panel (micro-kernel over-read)
 
 // ---------------------------------------------------------------------------
-// Block-wide argmax of |x| with LAPACK tie-break (smallest index wins).
-// Every thread passes its local best (value, index); all threads get the index.
-// sv/si need 33 slots.  Contains two __syncthreads.
+// Pivot search keys.  |x| is compared through its IEEE bit pattern read as an
+// unsigned integer (same order as the magnitudes for non-negative values);
+// NaN maps to 0, so a NaN never wins (LAPACK i?amax).  Integer compares keep
+// the search off the FP64 pipe, which GB300 runs at a small fraction of the
+// FP32 rate; the key has the size of T, so scratch declared as T[33] holds it.
 template <typename T>
-__device__ __forceinline__ void argmax_merge(T& v, int& i, T v2, int i2) {
+struct MagKey;
+template <>
+struct MagKey<double> {
+  using type = unsigned long long;
+  __device__ __forceinline__ static type of(double x) {
+    const type b = (type)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull;
+    return b > 0x7FF0000000000000ull ? type(0) : b;
+  }
+};
+template <>
+struct MagKey<float> {
+  using type = unsigned int;
+  __device__ __forceinline__ static type of(float x) {
+    const type b = __float_as_uint(x) & 0x7FFFFFFFu;
+    return b > 0x7F800000u ? type(0) : b;
+  }
+};
+template <typename T>
+using mag_t = typename MagKey<T>::type;
+template <typename T>
+__device__ __forceinline__ mag_t<T> mag_key(T x) {
+  return MagKey<T>::of(x);
+}
+
+// Candidate merge with LAPACK tie-break (smallest index wins); "no candidate"
+// is (0, INT_MAX), which every real candidate beats.
+template <typename K>
+__device__ __forceinline__ void argmax_merge(K& v, int& i, K v2, int i2) {
   if (v2 > v || (v2 == v && i2 < i)) {
     v = v2;
     i = i2;
   }
 }
 
+// Block-wide argmax over (key, index) candidates; every thread passes its
+// local best and all threads get the winning index (INT_MAX if none).  sv/si
+// need 33 slots (sv typed as T, reused for the keys).  Two __syncthreads.
 template <typename T>
-__device__ int cta_argmax(T v, int i, T* sv, int* si) {
+__device__ int cta_argmax(mag_t<T> v, int i, T* sv_, int* si) {
+  using K = mag_t<T>;
+  static_assert(sizeof(K) == sizeof(T), "key and value share scratch");
+  K* sv = reinterpret_cast<K*>(sv_);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
-    T v2 = __shfl_down_sync(0xffffffffu, v, o);
-    int i2 = __shfl_down_sync(0xffffffffu, i, o);
+    const K v2 = __shfl_down_sync(0xffffffffu, v, o);
+    const int i2 = __shfl_down_sync(0xffffffffu, i, o);
     argmax_merge(v, i, v2, i2);
   }
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -50,18 +85,27 @@ __device__ int cta_argmax(T v, int i, T* sv, int* si) {
   __syncthreads();
   if (warp == 0) {
     const int nw = blockDim.x >> 5;
-    v = lane < nw ? sv[lane] : T(-1);
+    v = lane < nw ? sv[lane] : K(0);
     i = lane < nw ? si[lane] : INT_MAX;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-      T v2 = __shfl_down_sync(0xffffffffu, v, o);
-      int i2 = __shfl_down_sync(0xffffffffu, i, o);
+      const K v2 = __shfl_down_sync(0xffffffffu, v, o);
+      const int i2 = __shfl_down_sync(0xffffffffu, i, o);
       argmax_merge(v, i, v2, i2);
     }
     if (lane == 0) si[32] = i;
   }
   __syncthreads();
   return si[32];
+}
+
+// 1/d computed by one thread and broadcast through shared memory (slot is a
+// T in shared memory): an FP64 division is a long dependent FP64 sequence.
+template <typename T>
+__device__ __forceinline__ T cta_recip(T d, T* slot) {
+  if (threadIdx.x == 0) *slot = T(1) / d;
+  __syncthreads();
+  return *slot;
 }
 
 // ---------------------------------------------------------------------------
@@ -74,17 +118,17 @@ __device__ void cta_panel_lu(T* P, int ldp, int m, int nb, int* piv, T* sv, int*
                              int col_offset) {
   const int tid = threadIdx.x;
   for (int j = 0; j < nb && j < m; ++j) {
-    T best = T(-1);
+    mag_t<T> best = 0;
     int bi = INT_MAX;
     for (int r = j + tid; r < m; r += blockDim.x) {
-      T a = tabs(P[r + j * ldp]);
-      if (a > best) {
+      const mag_t<T> a = mag_key(P[r + j * ldp]);
+      if (bi == INT_MAX || a > best) {
         best = a;
         bi = r;
       }
     }
-    int pr = cta_argmax(best, bi, sv, si);
-    if (pr == INT_MAX) pr = j;  // whole column NaN: keep the diagonal, flagged below
+    int pr = cta_argmax<T>(best, bi, sv, si);
+    if (pr == INT_MAX) pr = j;
     if (tid == 0) piv[j] = pr;
     if (pr != j) {
       for (int c = tid; c < nb; c += blockDim.x) {
@@ -98,7 +142,7 @@ __device__ void cta_panel_lu(T* P, int ldp, int m, int nb, int* piv, T* sv, int*
     if (d == T(0) || d != d) {
       if (tid == 0 && *info_s == 0) *info_s = col_offset + j + 1;
     } else {
-      const T rd = T(1) / d;
+      const T rd = cta_recip(d, sv + 32);
       for (int r = j + 1 + tid; r < m; r += blockDim.x) {
         const T l = P[r + j * ldp] * rd;
         P[r + j * ldp] = l;
@@ -1150,16 +1194,16 @@ __global__ void __launch_bounds__(1024) biglu_panel_kernel(T* A, int lda, int n,
   for (int j = 0; j < nb; ++j) {
     const int col = k0 + j;
     T* cj = A + (size_t)col * lda;
-    T best = T(-1);
+    mag_t<T> best = 0;
     int bi = INT_MAX;
     for (int r = col + tid; r < n; r += blockDim.x) {
-      const T a = tabs(cj[r]);
-      if (a > best) {
+      const mag_t<T> a = mag_key(cj[r]);
+      if (bi == INT_MAX || a > best) {
         best = a;
         bi = r;
       }
     }
-    int pr = cta_argmax(best, bi, sv, si);
+    int pr = cta_argmax<T>(best, bi, sv, si);
     if (pr == INT_MAX) pr = col;
     if (tid == 0) ipiv[col] = pr;
     if (pr != col) {
@@ -1175,7 +1219,7 @@ __global__ void __launch_bounds__(1024) biglu_panel_kernel(T* A, int lda, int n,
     if (d == T(0) || d != d) {
       if (tid == 0 && info && *info == 0) *info = col + 1;
     } else {
-      const T rd = T(1) / d;
+      const T rd = cta_recip(d, sv + 32);
       for (int r = col + 1 + tid; r < n; r += blockDim.x) {
         const T l = cj[r] * rd;
         cj[r] = l;
@@ -1190,121 +1234,154 @@ __global__ void __launch_bounds__(1024) biglu_panel_kernel(T* A, int lda, int n,
 }
 
 // Panel factorization held in the distributed shared memory of one thread-block
-// cluster of CL CTAs: CTA r keeps panel rows [r*R, (r+1)*R) of the m x nb
-// panel (rows k0.. of columns k0..k0+nb).  Per column: local argmax, exchange
-// of the CL candidates through DSMEM, row swap through DSMEM, pivot row
-// broadcast, local rank-1 update; two cluster barriers per column.
-// Shared memory: R * nb + nb (pivot row) + nb * (nb + 1) (L11 inverse)
-// elements.  grid = CL (one cluster).
+// cluster of CL CTAs: CTA r keeps physical panel rows [r*R, (r+1)*R) of the
+// m x nb panel (rows k0.. of columns k0..k0+nb).  Row interchanges are not
+// moved in memory: every CTA keeps the same logical -> physical row map (and
+// each CTA the logical index of its own rows), so one column costs one
+// cluster barrier: local argmax over rows with logical index >= j, exchange of
+// the CL candidates (double-buffered) through DSMEM, pivot row read from its
+// owner through DSMEM, interchange recorded in the maps, rank-1 update of the
+// local rows below the pivot spread over (row, column) pairs.  The pivot
+// sequence is LAPACK's (largest magnitude, smallest logical index on ties).
+// At the end each CTA writes its rows to their logical positions, and CTA 0
+// gathers the unit-lower nb x nb triangle and writes its inverse to linv.
+// Shared memory: see panel_cluster_smem_bytes.  grid = CL (one cluster).
+__host__ __device__ inline size_t panel_cluster_smem_bytes(int m, int nb, int R, size_t elem) {
+  return ((size_t)R * nb + R + nb + 2 * (size_t)nb * (nb + 1)) * elem + ((size_t)R + m) * sizeof(int);
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256) biglu_panel_cluster_kernel(T* A, int lda, int n, int k0, int nb, int R,
                                                                   int* ipiv, int* info, T* linv) {
   namespace cg = cooperative_groups;
   cg::cluster_group cluster = cg::this_cluster();
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  T* P = reinterpret_cast<T*>(smem_raw);  // R x nb, ld R
-  T* prow = P + (size_t)R * nb;            // nb
-  __shared__ T cand_v[1];
-  __shared__ int cand_i[1];
+  const int m = n - k0;
+  const int ldx = nb + 1;
+  T* P = reinterpret_cast<T*>(smem_raw);  // R x nb, ld R (physical rows)
+  T* lcol = P + (size_t)R * nb;            // R: multipliers of the current column
+  T* prow = lcol + R;                      // nb: pivot row
+  T* Ls = prow + nb;                       // nb x nb, ld nb+1: gathered L11 (CTA 0)
+  T* Xs = Ls + (size_t)nb * ldx;           // nb x nb, ld nb+1: its inverse
+  int* lrow = reinterpret_cast<int*>(Xs + (size_t)nb * ldx);  // R: logical index of each local row
+  int* map = lrow + R;                     // m: logical row -> physical row (rank * R + slot)
+  using K = mag_t<T>;
+  __shared__ K cand_v[2];
+  __shared__ int cand_i[2];
   __shared__ T sv[33];
   __shared__ int si[33];
   const int CL = (int)cluster.num_blocks();
-  const int r = (int)cluster.block_rank();
+  const int rk = (int)cluster.block_rank();
   const int tid = threadIdx.x;
-  const int m = n - k0;
-  const int g0 = r * R;                     // first panel row held here
-  const int rows = max(0, min(R, m - g0));  // rows held here
+  const int g0 = rk * R;
+  const int rows = max(0, min(R, m - g0));
   for (int idx = tid; idx < rows * nb; idx += blockDim.x) {
     const int i = idx % rows, c = idx / rows;
     P[i + (size_t)c * R] = A[(size_t)(k0 + c) * lda + k0 + g0 + i];
   }
-  cluster.sync();
+  for (int i = tid; i < rows; i += blockDim.x) lrow[i] = g0 + i;
+  for (int i = tid; i < m; i += blockDim.x) map[i] = i;
+  __syncthreads();
   for (int j = 0; j < nb && j < m; ++j) {
-    // local candidate over panel rows >= j
-    T best = T(-1);
+    K best = 0;
     int bi = INT_MAX;
     for (int i = tid; i < rows; i += blockDim.x) {
-      if (g0 + i < j) continue;
-      const T a = tabs(P[i + (size_t)j * R]);
-      if (a > best) {
+      const int li = lrow[i];
+      if (li < j) continue;
+      const K a = mag_key(P[i + (size_t)j * R]);
+      if (a > best || (a == best && li < bi)) {
         best = a;
-        bi = g0 + i;
+        bi = li;
       }
     }
-    const int li = cta_argmax(best, bi, sv, si);
+    const int wl = cta_argmax<T>(best, bi, sv, si);
     if (tid == 0) {
-      cand_i[0] = li;
-      cand_v[0] = li == INT_MAX ? T(-1) : tabs(P[(li - g0) + (size_t)j * R]);
+      cand_i[j & 1] = wl;
+      cand_v[j & 1] = wl == INT_MAX ? K(0) : mag_key(P[(map[wl] - g0) + (size_t)j * R]);
     }
-    cluster.sync();
-    // winner over the cluster (identical in every CTA)
-    T wv = T(-1);
-    int wi = INT_MAX;
-    for (int q = 0; q < CL; ++q) {
-      const T v = *cluster.map_shared_rank(&cand_v[0], q);
-      const int i = *cluster.map_shared_rank(&cand_i[0], q);
-      if (i != INT_MAX && (v > wv || (v == wv && i < wi))) {
-        wv = v;
-        wi = i;
+    cluster.sync();  // candidates published; every update of column j-1 is complete
+    if (tid < 32) {  // lane q reads CTA q's candidate: one remote read in flight per lane
+      K v = 0;
+      int i = INT_MAX;
+      if (tid < CL) {
+        i = *cluster.map_shared_rank(&cand_i[j & 1], tid);
+        v = *cluster.map_shared_rank(&cand_v[j & 1], tid);
       }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const K v2 = __shfl_down_sync(0xffffffffu, v, o);
+        const int i2 = __shfl_down_sync(0xffffffffu, i, o);
+        argmax_merge(v, i, v2, i2);
+      }
+      if (tid == 0) si[32] = i;
     }
+    __syncthreads();
+    const int wi = si[32];
     const int piv = wi == INT_MAX ? j : wi;
-    const int oj = j / R, op = piv / R;
-    if (r == oj) {
-      if (tid == 0) ipiv[k0 + j] = k0 + piv;
-      if (piv != j) {
-        T* Pj = cluster.map_shared_rank(P, oj);
-        T* Pp = cluster.map_shared_rank(P, op);
-        for (int c = tid; c < nb; c += blockDim.x) {
-          const T a = Pj[(j - oj * R) + (size_t)c * R];
-          Pj[(j - oj * R) + (size_t)c * R] = Pp[(piv - op * R) + (size_t)c * R];
-          Pp[(piv - op * R) + (size_t)c * R] = a;
-        }
-      }
-    }
-    cluster.sync();
+    const int php = map[piv], phj = map[j];
     {
-      const T* Pj = cluster.map_shared_rank(P, oj);
-      for (int c = tid; c < nb; c += blockDim.x) prow[c] = Pj[(j - oj * R) + (size_t)c * R];
+      const T* src = cluster.map_shared_rank(P, php / R);
+      for (int c = tid; c < nb; c += blockDim.x) prow[c] = src[(php % R) + (size_t)c * R];
+    }
+    __syncthreads();  // map reads and the pivot row are complete
+    if (tid == 0) {
+      map[j] = php;
+      map[piv] = phj;
+      if (rk == php / R) lrow[php % R] = j;
+      if (piv != j && rk == phj / R) lrow[phj % R] = piv;
+      if (rk == 0) ipiv[k0 + j] = k0 + piv;
     }
     __syncthreads();
     const T d = prow[j];
     if (d == T(0) || d != d) {
-      if (r == 0 && tid == 0 && info && *info == 0) *info = k0 + j + 1;
+      if (rk == 0 && tid == 0 && info && *info == 0) *info = k0 + j + 1;
     } else {
-      const T rd = T(1) / d;
+      const T rd = cta_recip(d, sv + 32);
       for (int i = tid; i < rows; i += blockDim.x) {
-        if (g0 + i <= j) continue;
-        const T l = P[i + (size_t)j * R] * rd;
-        P[i + (size_t)j * R] = l;
-        for (int c = j + 1; c < nb; ++c) P[i + (size_t)c * R] -= l * prow[c];
+        T l = T(0);
+        if (lrow[i] > j) {
+          l = P[i + (size_t)j * R] * rd;
+          P[i + (size_t)j * R] = l;
+        }
+        lcol[i] = l;
+      }
+      __syncthreads();
+      const int ncol = nb - j - 1;
+      for (int idx = tid; idx < rows * ncol; idx += blockDim.x) {
+        const int i = idx % rows, c = j + 1 + idx / rows;
+        P[i + (size_t)c * R] -= lcol[i] * prow[c];
       }
     }
-    // the next column's first cluster barrier orders these updates before any remote read
+    __syncthreads();
   }
   cluster.sync();
   for (int idx = tid; idx < rows * nb; idx += blockDim.x) {
     const int i = idx % rows, c = idx / rows;
-    A[(size_t)(k0 + c) * lda + k0 + g0 + i] = P[i + (size_t)c * R];
+    A[(size_t)(k0 + c) * lda + k0 + lrow[i]] = P[i + (size_t)c * R];
   }
-  // inverse of the unit-lower nb x nb triangle (panel rows 0..nb-1, all held by
-  // CTA 0 when R >= nb), column c by thread c, written to linv (ld nb)
-  if (linv && r == 0 && R >= nb) {
-    T* Xs = prow + nb;  // nb x nb, ld nb + 1
-    const int ldx = nb + 1;
-    if (tid < nb) {
-      const int c = tid;
-      T* x = Xs + (size_t)c * ldx;
-      for (int i = 0; i < c; ++i) x[i] = T(0);
-      x[c] = T(1);
-      for (int i = c + 1; i < nb; ++i) {
-        T sum = T(0);
-        for (int k = c; k < i; ++k) sum -= P[i + (size_t)k * R] * x[k];
-        x[i] = sum;
+  if (linv && nb <= m) {
+    if (rk == 0) {
+      for (int idx = tid; idx < nb * nb; idx += blockDim.x) {
+        const int l = idx % nb, c = idx / nb;
+        const int ph = map[l];
+        Ls[l + (size_t)c * ldx] = *(cluster.map_shared_rank(P, ph / R) + (ph % R) + (size_t)c * R);
       }
+      __syncthreads();
+      if (tid < nb) {  // column c of L11^{-1} by thread c
+        const int c = tid;
+        T* x = Xs + (size_t)c * ldx;
+        for (int i = 0; i < c; ++i) x[i] = T(0);
+        x[c] = T(1);
+        for (int i = c + 1; i < nb; ++i) {
+          T sum = T(0);
+          for (int k = c; k < i; ++k) sum -= Ls[i + (size_t)k * ldx] * x[k];
+          x[i] = sum;
+        }
+      }
+      __syncthreads();
+      for (int idx = tid; idx < nb * nb; idx += blockDim.x) linv[idx] = Xs[(idx % nb) + (idx / nb) * ldx];
     }
-    __syncthreads();
-    for (int idx = tid; idx < nb * nb; idx += blockDim.x) linv[idx] = Xs[(idx % nb) + (idx / nb) * ldx];
+    cluster.sync();  // no CTA leaves while CTA 0 may still read its rows
   }
 }
 
