@@ -177,6 +177,19 @@ int slab_engine_coeff_grad(slab_engine* e, int nrhs, const double* d_ufaces, con
                            const double* d_lam_leaf, double* d_gc11, double* d_gc22, double* d_gc1, double* d_gc2,
                            double* d_gc);
 
+/* FP64 matrix product on the BF16 tensor cores (tcgen05) by exact slicing:
+ * C = alpha A B + beta C with A (m x k), B (k x n), C (m x n), column-major
+ * device arrays.  Rows of A and columns of B are scaled by powers of two, cut
+ * into eight 7-bit integer slices and multiplied with exact FP32 accumulation;
+ * the error is bounded by about k 2^-53 max|A(i,:)| max|B(:,j)| per entry.
+ * Non-finite inputs give NaN in the affected rows/columns.  d_work: at least
+ * slab_dgemm_emu_work_bytes(m, n, k) bytes.  Synchronizes the stream to report
+ * failures.  No counterpart in the reference (used inside the interface
+ * factorization, block_tridiag_solver_structured.py:34-76). */
+size_t slab_dgemm_emu_work_bytes(int m, int n, int k);
+int slab_dgemm_emu(int m, int n, int k, double alpha, const double* d_A, int lda, const double* d_B, int ldb,
+                   double beta, double* d_C, int ldc, void* d_work, size_t work_bytes, void* stream);
+
 /* Bytes of device memory held by the engine's factorization. */
 size_t slab_engine_factor_bytes(const slab_engine* e);
 

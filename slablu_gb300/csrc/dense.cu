@@ -424,7 +424,7 @@ int tri_inv_blocks(cudaStream_t s, const T* LU, int lda, int n, int bs, T* Linv,
 }
 
 template <typename T>
-static int trsm_inv(cudaStream_t s, const T* Inv, int bs, int k0, int nb, T* X, int ldx, int ncols) {
+int trsm_inv(cudaStream_t s, const T* Inv, int bs, int k0, int nb, T* X, int ldx, int ncols) {
   if (ncols <= 0 || nb <= 0) return SLAB_OK;
   const size_t bytes = ((size_t)bs * bs + (size_t)bs * kTrsmCols) * sizeof(T);
   SLAB_TRY(ensure_smem(trsm_inv_kernel<T>, bytes, "trsm_inv"));
@@ -552,6 +552,8 @@ template int trsv_coop<float>(cudaStream_t, const float*, int, int, const int*, 
                               const float*, int, float*, int, int, bool);
 template int trsv_coop<double>(cudaStream_t, const double*, int, int, const int*, const double*, const double*, int,
                                const double*, int, double*, int, int, bool);
+template int trsm_inv<float>(cudaStream_t, const float*, int, int, int, float*, int, int);
+template int trsm_inv<double>(cudaStream_t, const double*, int, int, int, double*, int, int);
 template int trsv_cluster<float>(cudaStream_t, const float*, int, int, const int*, const float*, const float*,
                                  const float*, int, float*, int, int, bool);
 template int trsv_cluster<double>(cudaStream_t, const double*, int, int, const int*, const double*, const double*,

@@ -1583,6 +1583,11 @@ template <typename T>
 int trsv_coop(cudaStream_t s, const T* LU, int lda, int n, const int* perm, const T* Linv, const T* Uinv, int bs,
               const T* B, int ldb, T* X, int ldx, int nrhs, bool trans = false);
 
+// X[k0:k0+nb, 0:ncols] = Inv X[k0:k0+nb, 0:ncols] with Inv a bs x bs inverted
+// diagonal triangle (tri_inv_blocks layout, column-major, ld bs).
+template <typename T>
+int trsm_inv(cudaStream_t s, const T* Inv, int bs, int k0, int nb, T* X, int ldx, int ncols);
+
 // Same contract as trsv_coop with bs = 64, run by one thread-block cluster.
 // Returns SLAB_ERR_ARG when the shape does not fit (caller falls back).
 template <typename T>

@@ -27,11 +27,13 @@
 #include <cstdlib>
 #include <cmath>
 #include <map>
+#include <type_traits>
 #include <memory>
 #include <tuple>
 #include <vector>
 
 #include "leaf.cuh"
+#include "ozaki.cuh"
 
 namespace slab {
 
@@ -342,6 +344,8 @@ struct EngineImpl : EngineBase {
   // interface
   int nI = 0, nbI = 0;
   DevBuf ifLU, ifPiv, ifPerm, ifX, ifSub, ifSup, ifInfo, ifGlob, ifLinv, ifUinv, ifWork;
+  DevBuf emuWork, emuErr;  // tensor-core FP64 products of the interface (mixed precision)
+  bool use_emu = false;
   static constexpr int kInvBs = 64;  // diagonal-block size of the interface triangular inverses
   int nInvBlk = 0;
   // solve buffers
@@ -423,6 +427,10 @@ struct EngineImpl : EngineBase {
     use_graphs = !(ng && ng[0] == '1');
     const char* nc = getenv("SLAB_COOP_SOLVE");  // 1: grid-wide cooperative interface solve instead of the cluster one
     use_cluster_solve = !(nc && nc[0] == '1');
+    // FP64 interface products on the tensor cores in the mixed mode (FP32 leaves and
+    // tree, FP64 interface); SLAB_NATIVE_FP64=1 keeps them on the FP64 cores
+    const char* nf = getenv("SLAB_NATIVE_FP64");
+    use_emu = std::is_same<T, float>::value && std::is_same<TI, double>::value && !(nf && nf[0] == '1');
     ntot = (long long)q * ((long long)n0 * (2 * n1 + 1) + n1);
     nleaf = (long long)n0 * n1;
   }
@@ -675,6 +683,11 @@ struct EngineImpl : EngineBase {
       SLAB_TRY(ifLinv.alloc((size_t)nbI * nInvBlk * kInvBs * kInvBs * sizeof(TI)));
       SLAB_TRY(ifUinv.alloc((size_t)nbI * nInvBlk * kInvBs * kInvBs * sizeof(TI)));
       SLAB_TRY(ifWork.alloc((size_t)kNB * kNB * sizeof(TI)));
+      if (use_emu) {
+        SLAB_TRY(emuWork.alloc(dgemm_emu_work_bytes(nI, nI, nI)));
+        SLAB_TRY(emuErr.alloc(sizeof(int)));
+        SLAB_CUDA_TRY(cudaMemsetAsync(emuErr.p, 0, sizeof(int), s));
+      }
     }
     SLAB_TRY(acc.alloc(4 * sizeof(double)));
     for (auto& e : ev) SLAB_CUDA_TRY(cudaEventCreate(&e));
@@ -770,22 +783,40 @@ struct EngineImpl : EngineBase {
   TI* linv(int j) { return ifLinv.as<TI>() + (size_t)j * nInvBlk * kInvBs * kInvBs; }
   TI* uinv(int j) { return ifUinv.as<TI>() + (size_t)j * nInvBlk * kInvBs * kInvBs; }
 
+  // X_{j-1} = S_{j-1}^{-1} sup_{j-1}, then S_j -= sub_j X_{j-1}: on the tensor
+  // cores through exact slicing when use_emu (the FP64 mixed path), else FP64 cores.
+  int iface_schur(int j) {
+    const long long blk = (long long)nI * nI;
+    TI* Sj = ifLU.as<TI>() + blk * j;
+    TI* Xprev = ifX.as<TI>() + blk * (j - 1);
+    const TI* LUp = ifLU.as<TI>() + blk * (j - 1);
+    const int* pp = ifPerm.as<int>() + (long long)nI * (j - 1);
+    if constexpr (std::is_same<TI, double>::value) {
+      if (use_emu) {
+        EmuWork w{emuWork.p, emuWork.bytes, emuErr.as<int>()};
+        SLAB_TRY(bigtrs_inv_emu(s, LUp, nI, nI, pp, linv(j - 1), uinv(j - 1), kInvBs, ifSup.as<TI>() + blk * (j - 1),
+                                nI, Xprev, nI, nI, w));
+        return dgemm_emu(s, nI, nI, nI, -1.0, ifSub.as<TI>() + blk * j, nI, Xprev, nI, 1.0, Sj, nI, w.buf, w.bytes,
+                         w.err);
+      }
+    }
+    SLAB_TRY(bigtrs_inv<TI>(s, LUp, nI, nI, pp, linv(j - 1), uinv(j - 1), kInvBs, ifSup.as<TI>() + blk * (j - 1), nI,
+                            Xprev, nI, nI));
+    return gemm<TI>(s, nI, nI, nI, TI(-1), ifSub.as<TI>() + blk * j, nullptr, 0, nI, Xprev, nullptr, 0, nI, TI(1), Sj,
+                    nullptr, 0, nI, 1);
+  }
+
   int factor_interface() {
     if (nbI > 0) {
       const long long blk = (long long)nI * nI;
       SLAB_CUDA_TRY(cudaMemsetAsync(ifInfo.p, 0, sizeof(int), s));
+      if (use_emu) SLAB_CUDA_TRY(cudaMemsetAsync(emuErr.p, 0, sizeof(int), s));
       iface_gather_kernel<TI, T><<<grid_for(blk * nbI * 3), 256, 0, s>>>(
           nodepool.as<T>(), rootoff.as<long long>(), nR, nI, nbI, ifLU.as<TI>(), ifSub.as<TI>(), ifSup.as<TI>());
       SLAB_CHECK_LAUNCH();
       for (int j = 0; j < nbI; ++j) {
         TI* Sj = ifLU.as<TI>() + blk * j;
-        if (j > 0) {
-          TI* Xprev = ifX.as<TI>() + blk * (j - 1);
-          SLAB_TRY(bigtrs_inv<TI>(s, ifLU.as<TI>() + blk * (j - 1), nI, nI, ifPerm.as<int>() + (long long)nI * (j - 1),
-                                  linv(j - 1), uinv(j - 1), kInvBs, ifSup.as<TI>() + blk * (j - 1), nI, Xprev, nI, nI));
-          SLAB_TRY(gemm<TI>(s, nI, nI, nI, TI(-1), ifSub.as<TI>() + blk * j, nullptr, 0, nI, Xprev, nullptr, 0, nI,
-                            TI(1), Sj, nullptr, 0, nI, 1));
-        }
+        if (j > 0) SLAB_TRY(iface_schur(j));
         SLAB_TRY(biglu<TI>(s, Sj, nI, nI, ifPiv.as<int>() + (long long)nI * j, ifInfo.as<int>(), ifWork.as<TI>()));
         SLAB_TRY(build_perm(s, ifPiv.as<int>() + (long long)nI * j, nI, ifPerm.as<int>() + (long long)nI * j));
         SLAB_TRY(tri_inv_blocks<TI>(s, Sj, nI, nI, kInvBs, linv(j), uinv(j)));
@@ -816,8 +847,9 @@ struct EngineImpl : EngineBase {
     SLAB_CUDA_TRY(cudaMemcpyAsync(hinfo.data(), leafinfo.p, leafinfo.bytes, cudaMemcpyDeviceToHost, s));
     std::vector<int> minfo(mergeinfo.bytes / sizeof(int));
     SLAB_CUDA_TRY(cudaMemcpyAsync(minfo.data(), mergeinfo.p, mergeinfo.bytes, cudaMemcpyDeviceToHost, s));
-    int iinfo = 0;
+    int iinfo = 0, eerr = 0;
     if (nbI > 0) SLAB_CUDA_TRY(cudaMemcpyAsync(&iinfo, ifInfo.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    if (nbI > 0 && use_emu) SLAB_CUDA_TRY(cudaMemcpyAsync(&eerr, emuErr.p, sizeof(int), cudaMemcpyDeviceToHost, s));
     SLAB_CUDA_TRY(cudaStreamSynchronize(s));
     tms[0] = elapsed(0, 1);
     tms[1] = elapsed(1, 2);
@@ -837,6 +869,7 @@ struct EngineImpl : EngineBase {
       set_error(iinfo, "interface block: zero pivot at column %d", iinfo);
       return iinfo;
     }
+    if (eerr != 0) return set_error(SLAB_ERR_CUDA, "interface: tensor-core pipeline wait expired (code %d)", eerr);
     return SLAB_OK;
   }
 

@@ -1,0 +1,486 @@
+// FP64 matrix products on the BF16 tensor cores (tcgen05) by exact slicing.
+//
+// C = alpha A B + beta C with A (m x k), B (k x n), C column-major FP64.
+// Every row of A and column of B is scaled by a power of two so that its
+// largest entry is below 1, read as a 56-bit fixed-point integer (integer
+// operations on the IEEE bit pattern; rounding error <= 2^-57 of the row or
+// column maximum) and cut into eight 7-bit slices, each an integer in
+// [-127, 127] held exactly in BF16:
+//     A = diag(2^e) sum_s 2^(-7s) A_s,   B = sum_t 2^(-7t) B_t diag(2^f).
+// The products A_s B_t with s + t <= 9 (36 of them) run on the tensor cores
+// with FP32 accumulation in tensor memory.  Over a K chunk of 256 a product
+// sum is an integer below 256 * 127^2 < 2^22, and up to four products of the
+// same weight 2^(-7(s+t)) share one accumulator (< 2^24), so every FP32
+// accumulation is exact.  Twelve accumulators per 128 x 32 output tile hold
+// the levels s + t = 2..9 of one chunk; the epilogue warps drain them into two
+// 64-bit integer fixed-point sums per output (levels 2-5 and 6-9), so the
+// FP64 pipe -- a small fraction of the FP32 rate on GB300 -- only does the
+// final combination, scaling and alpha/beta update (about six FP64 operations
+// per output).  The dropped levels s + t >= 10 and the fixed-point rounding
+// bound the error by about k 2^-53 max|A_i.| max|B_.j|, the size of the
+// worst-case bound of an FP64 dot product.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <climits>
+#include <cstdint>
+#include <mutex>
+
+#include "common.cuh"
+#include "dense.cuh"
+#include "ozaki.cuh"
+#include "tc.cuh"
+
+namespace slab {
+
+namespace {
+
+constexpr int kSl = 8;         // slices per operand
+constexpr int kSliceBits = 7;  // bits per slice
+constexpr int kBM = 128, kBN = 32, kBK = 64, kChunk = 256;
+constexpr int kGroups = 12;
+constexpr int kStages = 4;
+constexpr int kAbytes = kBM * kBK * 2;
+constexpr int kBbytes = kBN * kBK * 2;
+constexpr int kStageBytes = kAbytes + kSl * kBbytes;
+constexpr int kNonFinite = INT_MIN;
+constexpr int kTmemCols = 512;
+constexpr size_t kGemmSmem = (size_t)kStages * kStageBytes + 1024 + 256;
+
+static_assert(kGroups * kBN <= kTmemCols, "accumulators must fit tensor memory");
+
+__device__ __forceinline__ int biased_exp(double x) {
+  return (int)((__double_as_longlong(x) >> 52) & 0x7FF);
+}
+
+// Power-of-two scale exponent of a row or column from its largest biased
+// exponent (zeros and subnormals count as exponent 1); kNonFinite for Inf/NaN.
+__device__ __forceinline__ int scale_of(int emax) {
+  if (emax >= 2047) return kNonFinite;
+  return (emax < 1 ? 1 : emax) - 1022;  // |x| < 2^scale for every entry
+}
+
+// 56-bit fixed-point magnitude of x relative to 2^scale (scale from scale_of),
+// rounded to nearest (ties up): |x| 2^(56 - scale) < 2^56, so the result stays
+// below 2^56 for every entry of the row or column.
+__device__ __forceinline__ unsigned long long fixed56(double x, int scale) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const int E = (int)((b >> 52) & 0x7FF);
+  const unsigned long long mant = (b & 0xFFFFFFFFFFFFFull) | (E != 0 ? (1ull << 52) : 0ull);
+  const int shift = (E < 1 ? 1 : E) - (scale + 1022) + 3;  // <= 3
+  if (shift >= 0) return mant << shift;
+  if (-shift > 54) return 0ull;
+  return (mant + (1ull << (-shift - 1))) >> (-shift);
+}
+
+__device__ __forceinline__ __nv_bfloat16 slice_val(unsigned long long q, int s, bool neg) {
+  const int d = (int)((q >> (56 - kSliceBits * (s + 1))) & 127ull);
+  return __float2bfloat16_rn((float)(neg ? -d : d));
+}
+
+__global__ void rowmax_exp_kernel(const double* __restrict__ A, int lda, int m, int k, int* __restrict__ emax) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  const int k0 = blockIdx.y * 64, k1 = min(k, k0 + 64);
+  int e = 0;
+  for (int kk = k0; kk < k1; ++kk) e = max(e, biased_exp(A[i + (size_t)kk * lda]));
+  atomicMax(&emax[i], e);
+}
+
+__global__ void finish_scale_kernel(int* __restrict__ e, int m) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < m) e[i] = scale_of(e[i]);
+}
+
+// A (m x k, column-major) -> slices [s][i][kk] (K contiguous, row length kp),
+// through a 32 x 32 shared-memory transpose.  Columns k..kp-1 are zero.
+__global__ void __launch_bounds__(256) slice_a_kernel(const double* __restrict__ A, int lda, int m, int k, int kp,
+                                                      const int* __restrict__ ea, __nv_bfloat16* __restrict__ out) {
+  __shared__ __nv_bfloat16 t[kSl][32][33];
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  const int i0 = blockIdx.x * 32, kk0 = blockIdx.y * 32;
+  for (int r = ty; r < 32; r += 8) {
+    const int i = i0 + tx, kk = kk0 + r;
+    double x = 0.0;
+    int sc = 0;
+    if (i < m) {
+      sc = ea[i];
+      if (kk < k) x = A[i + (size_t)kk * lda];
+    }
+    const bool bad = sc == kNonFinite;
+    const unsigned long long q = bad ? 0ull : fixed56(x, sc);
+    const bool neg = x < 0.0;
+#pragma unroll
+    for (int s = 0; s < kSl; ++s) t[s][r][tx] = slice_val(q, s, neg);
+  }
+  __syncthreads();
+  for (int r = ty; r < 32; r += 8) {
+    const int i = i0 + r, kk = kk0 + tx;
+    if (i >= m || kk >= kp) continue;
+#pragma unroll
+    for (int s = 0; s < kSl; ++s) out[((size_t)s * m + i) * kp + kk] = t[s][tx][r];
+  }
+}
+
+// B (k x n, column-major) -> slices [t][j][kk]; one warp per column, which also
+// computes the column's scale exponent.
+__global__ void __launch_bounds__(256) slice_b_kernel(const double* __restrict__ B, int ldb, int n, int k, int kp,
+                                                      int* __restrict__ fb, __nv_bfloat16* __restrict__ out) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp >= n) return;
+  const double* col = B + (size_t)warp * ldb;
+  int e = 0;
+  for (int kk = lane; kk < k; kk += 32) e = max(e, biased_exp(col[kk]));
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) e = max(e, __shfl_xor_sync(0xffffffffu, e, o));
+  const int sc = scale_of(e);
+  if (lane == 0) fb[warp] = sc;
+  for (int kk = lane; kk < kp; kk += 32) {
+    const double x = kk < k ? col[kk] : 0.0;
+    const unsigned long long q = sc == kNonFinite ? 0ull : fixed56(x, sc);
+    const bool neg = x < 0.0;
+#pragma unroll
+    for (int s = 0; s < kSl; ++s) out[((size_t)s * n + warp) * kp + kk] = slice_val(q, s, neg);
+  }
+}
+
+struct EmuArgs {
+  int m, n, kp;
+  double alpha, beta;
+  double* C;
+  int ldc;
+  const int* ea;
+  const int* fb;
+  int* err;
+};
+
+__device__ __forceinline__ double pow2i(int e) {  // e in [-1022, 1023]
+  return __longlong_as_double((long long)(e + 1023) << 52);
+}
+
+// Wait used on the way out: only the time limit ends it.
+__device__ __forceinline__ void final_wait(uint64_t* bar, uint32_t parity, int* err) {
+  const unsigned long long t0 = tc::globaltimer();
+  while (!tc::mbar_try_wait(bar, parity)) {
+    if (tc::globaltimer() - t0 > tc::kWaitNs) {
+      atomicCAS(err, 0, 9);
+      return;
+    }
+  }
+}
+
+// Level group of the product of slices s0 + 1 and t0 + 1 (0-based indices).
+__host__ __device__ constexpr int group_of(int s0, int t0) {
+  return (s0 + t0 + 2) <= 5 ? (s0 + t0) : 4 + 2 * (s0 + t0 + 2 - 6) + (s0 >= 4 ? 1 : 0);
+}
+__host__ __device__ constexpr int group_first_s0(int s0, int t0) { return (s0 + t0 + 2) >= 6 && s0 >= 4 ? 4 : 0; }
+
+// grid (ceil(m/128), ceil(n/32)), 192 threads: warp 0 TMA producer, warp 1
+// tensor-memory owner and MMA issuer, warps 2-5 epilogue (one output row per thread).
+__global__ void __launch_bounds__(192, 1) ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA,
+                                                            const __grid_constant__ CUtensorMap tmB, EmuArgs a) {
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char* stages =
+      reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint64_t* full = reinterpret_cast<uint64_t*>(stages + (size_t)kStages * kStageBytes);
+  uint64_t* empty = full + kStages;
+  uint64_t* accf = empty + kStages;
+  uint64_t* acce = accf + 1;
+  uint64_t* fin = acce + 1;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(fin + 1);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int i0 = blockIdx.x * kBM, j0 = blockIdx.y * kBN;
+  const int nchunk = (a.kp + kChunk - 1) / kChunk;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kStages; ++s) {
+      tc::mbar_init(&full[s], 1);
+      tc::mbar_init(&empty[s], 1);
+    }
+    tc::mbar_init(accf, 1);
+    tc::mbar_init(acce, 128);
+    tc::mbar_init(fin, 1);
+    tc::fence_mbar_init();
+  }
+  if (warp == 1) tc::tmem_alloc(tmem_slot, kTmemCols);
+  if (warp == 0 && lane == 0) {
+    tc::prefetch_tmap(&tmA);
+    tc::prefetch_tmap(&tmB);
+  }
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::tc_fence_after();
+  const uint32_t tbase = *tmem_slot;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      int last_round[kStages];
+#pragma unroll
+      for (int s = 0; s < kStages; ++s) last_round[s] = -1;
+      int it = 0;
+      bool ok = true;
+      for (int c = 0; c < nchunk && ok; ++c) {
+        const int nkb = min(kChunk, a.kp - c * kChunk + kBK - 1) / kBK;
+        for (int s0 = 0; s0 < kSl && ok; ++s0) {
+          for (int kb = 0; kb < nkb; ++kb) {
+            const int st = it % kStages, round = it / kStages;
+            if (!tc::mbar_wait(&empty[st], (uint32_t)((round & 1) ^ 1), a.err, 1)) {
+              ok = false;
+              break;
+            }
+            const int ntile = kSl - s0;
+            tc::mbar_arrive_expect_tx(&full[st], (uint32_t)(kAbytes + ntile * kBbytes));
+            unsigned char* sp = stages + (size_t)st * kStageBytes;
+            const int kx = c * kChunk + kb * kBK;
+            tc::tma_load_3d(sp, &tmA, &full[st], kx, i0, s0);
+            for (int t0 = 0; t0 < ntile; ++t0) tc::tma_load_3d(sp + kAbytes + t0 * kBbytes, &tmB, &full[st], kx, j0, t0);
+            last_round[st] = round;
+            ++it;
+          }
+        }
+      }
+      // no copy may still be in flight when the CTA leaves
+      for (int s = 0; s < kStages; ++s)
+        if (last_round[s] >= 0) final_wait(&full[s], (uint32_t)(last_round[s] & 1), a.err);
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      const uint32_t idesc = tc::idesc_bf16_f32(kBM, kBN);
+      int it = 0;
+      bool ok = true;
+      for (int c = 0; c < nchunk && ok; ++c) {
+        if (c > 0) {
+          if (!tc::mbar_wait(acce, (uint32_t)((c - 1) & 1), a.err, 3)) break;
+          tc::tc_fence_after();
+        }
+        const int nkb = min(kChunk, a.kp - c * kChunk + kBK - 1) / kBK;
+        for (int s0 = 0; s0 < kSl && ok; ++s0) {
+          for (int kb = 0; kb < nkb; ++kb) {
+            const int st = it % kStages, round = it / kStages;
+            if (!tc::mbar_wait(&full[st], (uint32_t)(round & 1), a.err, 4)) {
+              ok = false;
+              break;
+            }
+            tc::tc_fence_after();
+            const uint32_t sa = tc::smem_u32(stages + (size_t)st * kStageBytes);
+            for (int t0 = 0; t0 < kSl - s0; ++t0) {
+              const int g = group_of(s0, t0);
+              const int first = group_first_s0(s0, t0);
+              const uint32_t sb = sa + kAbytes + t0 * kBbytes;
+#pragma unroll
+              for (int kk = 0; kk < kBK / 16; ++kk) {
+                const uint32_t acc = (kb == 0 && kk == 0 && s0 == first) ? 0u : 1u;
+                tc::mma_bf16(tbase + (uint32_t)(g * kBN), tc::sdesc_kmajor_sw128(sa + kk * 32),
+                             tc::sdesc_kmajor_sw128(sb + kk * 32), idesc, acc);
+              }
+            }
+            tc::mma_commit(&empty[st]);  // the stage is free once these products complete
+            ++it;
+          }
+        }
+        if (ok) tc::mma_commit(accf);
+      }
+      tc::mma_commit(fin);  // every product issued has completed before tensor memory is released
+      final_wait(fin, 0, a.err);
+    }
+  } else {
+    const int q = warp & 3;  // tensor-memory lane quarter of this warp
+    const int row = q * 32 + lane;
+    long long hi[kBN], lo[kBN];
+#pragma unroll
+    for (int j = 0; j < kBN; ++j) hi[j] = lo[j] = 0;
+    bool ok = true;
+    for (int c = 0; c < nchunk; ++c) {
+      if (!tc::mbar_wait(accf, (uint32_t)(c & 1), a.err, 5)) {
+        ok = false;
+        break;
+      }
+      tc::tc_fence_after();
+#pragma unroll 1
+      for (int g = 0; g < kGroups; ++g) {
+        uint32_t r[32];
+        tc::tmem_ld_32x32b_x32(tbase + ((uint32_t)(q * 32) << 16) + (uint32_t)(g * kBN), r);
+        tc::tmem_ld_wait();
+        const int L = g < 4 ? g + 2 : 6 + (g - 4) / 2;
+        if (g < 4) {
+          const int sh = 7 * (5 - L);
+#pragma unroll
+          for (int j = 0; j < kBN; ++j) hi[j] += (long long)__float2int_rz(__uint_as_float(r[j])) << sh;
+        } else {
+          const int sh = 7 * (9 - L);
+#pragma unroll
+          for (int j = 0; j < kBN; ++j) lo[j] += (long long)__float2int_rz(__uint_as_float(r[j])) << sh;
+        }
+      }
+      tc::tc_fence_before();
+      tc::mbar_arrive(acce);
+    }
+    if (ok && *reinterpret_cast<volatile int*>(a.err) == 0) {
+      const int i = i0 + row;
+      if (i < a.m) {
+        const int ei = a.ea[i];
+        const double w_hi = pow2i(-35), w_lo = pow2i(-63);
+#pragma unroll
+        for (int j = 0; j < kBN; ++j) {
+          const int jj = j0 + j;
+          if (jj >= a.n) break;
+          const int fj = a.fb[jj];
+          double v;
+          if (ei == kNonFinite || fj == kNonFinite) {
+            v = __longlong_as_double(0x7FF8000000000000ll);
+          } else {
+            v = (double)hi[j] * w_hi + (double)lo[j] * w_lo;
+            const int e = ei + fj, e1 = e / 2;
+            v = v * pow2i(e1) * pow2i(e - e1);
+          }
+          double* cp = a.C + i + (size_t)jj * a.ldc;
+          *cp = a.beta == 0.0 ? a.alpha * v : a.alpha * v + a.beta * *cp;
+        }
+      }
+    }
+  }
+  tc::tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc::tc_fence_after();
+    tc::tmem_dealloc(tbase, kTmemCols);
+  }
+}
+
+using EncodeFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                              const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                              CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeFn encode_fn() {
+  static std::once_flag once;
+  static EncodeFn fn = nullptr;
+  std::call_once(once, []() {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeFn>(p);
+    cudaGetLastError();
+  });
+  return fn;
+}
+
+// 3-D map over slices [S][rows][kp] (bf16), box {64, box_rows, 1}, 128-byte swizzle.
+int make_slice_map(CUtensorMap* map, const void* base, int kp, int rows, int box_rows) {
+  EncodeFn fn = encode_fn();
+  if (!fn) return set_error(SLAB_ERR_CUDA, "tensor-map encoder unavailable");
+  const cuuint64_t dims[3] = {(cuuint64_t)kp, (cuuint64_t)rows, (cuuint64_t)kSl};
+  const cuuint64_t strides[2] = {(cuuint64_t)kp * 2, (cuuint64_t)rows * kp * 2};
+  const cuuint32_t box[3] = {(cuuint32_t)kBK, (cuuint32_t)box_rows, 1};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  const CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(base), dims, strides, box, estr,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return set_error(SLAB_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+  return SLAB_OK;
+}
+
+size_t al256(size_t b) { return (b + 255) / 256 * 256; }
+
+}  // namespace
+
+size_t dgemm_emu_work_bytes(int m, int n, int k) {
+  if (m <= 0 || n <= 0 || k <= 0) return 256;
+  const size_t kp = (size_t)round_up(k, 8);
+  return al256(sizeof(int)) + al256((size_t)kSl * m * kp * 2) + al256((size_t)kSl * n * kp * 2) +
+         al256((size_t)m * sizeof(int)) + al256((size_t)n * sizeof(int));
+}
+
+int dgemm_emu(cudaStream_t s, int m, int n, int k, double alpha, const double* A, int lda, const double* B, int ldb,
+              double beta, double* C, int ldc, void* work, size_t work_bytes, int* err) {
+  if (m <= 0 || n <= 0) return SLAB_OK;
+  if (k <= 0 || !A || !B || !C || !work || !err || lda < m || ldb < k || ldc < m)
+    return set_error(SLAB_ERR_ARG, "dgemm_emu: invalid arguments");
+  if (work_bytes < dgemm_emu_work_bytes(m, n, k)) return set_error(SLAB_ERR_ARG, "dgemm_emu: work buffer too small");
+  const int kp = round_up(k, 8);
+  unsigned char* w = static_cast<unsigned char*>(work);
+  w += al256(sizeof(int));  // first slot reserved for the caller's use
+  __nv_bfloat16* Asl = reinterpret_cast<__nv_bfloat16*>(w);
+  w += al256((size_t)kSl * m * kp * 2);
+  __nv_bfloat16* Bsl = reinterpret_cast<__nv_bfloat16*>(w);
+  w += al256((size_t)kSl * n * kp * 2);
+  int* ea = reinterpret_cast<int*>(w);
+  w += al256((size_t)m * sizeof(int));
+  int* fb = reinterpret_cast<int*>(w);
+  SLAB_CUDA_TRY(cudaMemsetAsync(ea, 0, (size_t)m * sizeof(int), s));
+  rowmax_exp_kernel<<<dim3(ceil_div(m, 256), ceil_div(k, 64)), 256, 0, s>>>(A, lda, m, k, ea);
+  SLAB_CHECK_LAUNCH();
+  finish_scale_kernel<<<ceil_div(m, 256), 256, 0, s>>>(ea, m);
+  SLAB_CHECK_LAUNCH();
+  slice_a_kernel<<<dim3(ceil_div(m, 32), ceil_div(kp, 32)), 256, 0, s>>>(A, lda, m, k, kp, ea, Asl);
+  SLAB_CHECK_LAUNCH();
+  slice_b_kernel<<<ceil_div(n * 32, 256), 256, 0, s>>>(B, ldb, n, k, kp, fb, Bsl);
+  SLAB_CHECK_LAUNCH();
+  CUtensorMap tmA, tmB;
+  SLAB_TRY(make_slice_map(&tmA, Asl, kp, m, kBM));
+  SLAB_TRY(make_slice_map(&tmB, Bsl, kp, n, kBN));
+  SLAB_TRY(ensure_smem(ozaki_gemm_kernel, kGemmSmem, "dgemm_emu"));
+  EmuArgs ea_{m, n, kp, alpha, beta, C, ldc, ea, fb, err};
+  ozaki_gemm_kernel<<<dim3(ceil_div(m, kBM), ceil_div(n, kBN)), 192, kGemmSmem, s>>>(tmA, tmB, ea_);
+  SLAB_CHECK_LAUNCH();
+  return SLAB_OK;
+}
+
+int bigtrs_inv_emu(cudaStream_t s, const double* LU, int lda, int n, const int* perm, const double* Linv,
+                   const double* Uinv, int bs, const double* B, int ldb, double* X, int ldx, int nrhs,
+                   const EmuWork& w) {
+  if (n <= 0 || nrhs <= 0) return SLAB_OK;
+  if (kEmuOuter % bs != 0) return set_error(SLAB_ERR_ARG, "bigtrs_inv_emu: block size %d does not divide %d", bs, kEmuOuter);
+  const long long tot = (long long)n * nrhs;
+  permute_rows_kernel<double><<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(B, ldb, X, ldx, n, nrhs, perm);
+  SLAB_CHECK_LAUNCH();
+  for (int ob0 = 0; ob0 < n; ob0 += kEmuOuter) {
+    const int obe = n - ob0 < kEmuOuter ? n : ob0 + kEmuOuter;
+    for (int k0 = ob0; k0 < obe; k0 += bs) {
+      const int nb = obe - k0 < bs ? obe - k0 : bs;
+      SLAB_TRY(trsm_inv<double>(s, Linv + (size_t)(k0 / bs) * bs * bs, bs, k0, nb, X, ldx, nrhs));
+      const int inner = obe - k0 - nb;
+      if (inner > 0)
+        SLAB_TRY(gemm<double>(s, inner, nrhs, nb, -1.0, LU + (size_t)k0 * lda + k0 + nb, nullptr, 0, lda, X + k0,
+                              nullptr, 0, ldx, 1.0, X + k0 + nb, nullptr, 0, ldx, 1));
+    }
+    const int rest = n - obe;
+    if (rest > 0)
+      SLAB_TRY(dgemm_emu(s, rest, nrhs, obe - ob0, -1.0, LU + (size_t)ob0 * lda + obe, lda, X + ob0, ldx, 1.0,
+                         X + obe, ldx, w.buf, w.bytes, w.err));
+  }
+  for (int ob0 = ((n - 1) / kEmuOuter) * kEmuOuter; ob0 >= 0; ob0 -= kEmuOuter) {
+    const int obe = n - ob0 < kEmuOuter ? n : ob0 + kEmuOuter;
+    for (int k0 = ((obe - 1 - ob0) / bs) * bs + ob0; k0 >= ob0; k0 -= bs) {
+      const int nb = obe - k0 < bs ? obe - k0 : bs;
+      SLAB_TRY(trsm_inv<double>(s, Uinv + (size_t)(k0 / bs) * bs * bs, bs, k0, nb, X, ldx, nrhs));
+      const int inner = k0 - ob0;
+      if (inner > 0)
+        SLAB_TRY(gemm<double>(s, inner, nrhs, nb, -1.0, LU + (size_t)k0 * lda + ob0, nullptr, 0, lda, X + k0, nullptr,
+                              0, ldx, 1.0, X + ob0, nullptr, 0, ldx, 1));
+    }
+    if (ob0 > 0)
+      SLAB_TRY(dgemm_emu(s, ob0, nrhs, obe - ob0, -1.0, LU + (size_t)ob0 * lda, lda, X + ob0, ldx, 1.0, X, ldx, w.buf,
+                         w.bytes, w.err));
+  }
+  return SLAB_OK;
+}
+
+}  // namespace slab
+
+extern "C" size_t slab_dgemm_emu_work_bytes(int m, int n, int k) { return slab::dgemm_emu_work_bytes(m, n, k); }
+
+extern "C" int slab_dgemm_emu(int m, int n, int k, double alpha, const double* A, int lda, const double* B, int ldb,
+                              double beta, double* C, int ldc, void* work, size_t work_bytes, void* stream) {
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (!work || work_bytes < slab::dgemm_emu_work_bytes(m, n, k))
+    return slab::set_error(SLAB_ERR_ARG, "slab_dgemm_emu: work buffer too small");
+  int* err = static_cast<int*>(work);  // the reserved first slot
+  SLAB_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), s));
+  SLAB_TRY(slab::dgemm_emu(s, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, work, work_bytes, err));
+  int h = 0;
+  SLAB_CUDA_TRY(cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, s));
+  SLAB_CUDA_TRY(cudaStreamSynchronize(s));
+  if (h != 0) return slab::set_error(SLAB_ERR_CUDA, "slab_dgemm_emu: tensor-core pipeline wait expired (code %d)", h);
+  return SLAB_OK;
+}

@@ -1,0 +1,37 @@
+// FP64 matrix products on the BF16 tensor cores by exact slicing (ozaki.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+
+namespace slab {
+
+// Work bytes of dgemm_emu for an (m x k) (k x n) product.
+size_t dgemm_emu_work_bytes(int m, int n, int k);
+
+// C = alpha A B + beta C (column-major FP64) on the tensor cores; asynchronous
+// on stream s.  work: dgemm_emu_work_bytes(m, n, k) bytes whose first 256 are
+// left to the caller; err: device int, set nonzero if a pipeline wait expired
+// (C is then not written).
+int dgemm_emu(cudaStream_t s, int m, int n, int k, double alpha, const double* A, int lda, const double* B, int ldb,
+              double beta, double* C, int ldc, void* work, size_t work_bytes, int* err);
+
+// Workspace of the blocked routines below: dgemm_emu work plus its error flag.
+struct EmuWork {
+  void* buf = nullptr;
+  size_t bytes = 0;
+  int* err = nullptr;
+};
+
+// Outer block of the blocked routines: products of this depth go to dgemm_emu,
+// the work inside an outer block stays on the FP64 cores.
+constexpr int kEmuOuter = 256;
+
+// bigtrs_inv (X = U^{-1} L^{-1} P B, inverted bs x bs diagonal triangles) with
+// the updates between outer blocks of kEmuOuter rows done by dgemm_emu.
+int bigtrs_inv_emu(cudaStream_t s, const double* LU, int lda, int n, const int* perm, const double* Linv,
+                   const double* Uinv, int bs, const double* B, int ldb, double* X, int ldx, int nrhs,
+                   const EmuWork& w);
+
+}  // namespace slab
