@@ -434,6 +434,19 @@ int trsm_inv(cudaStream_t s, const T* Inv, int bs, int k0, int nb, T* X, int ldx
 }
 
 template <typename T>
+int biglu_panel_swap(cudaStream_t s, T* A, int lda, int n, int k0, int nb, int* ipiv, int* info, T* linv,
+                     bool* linv_done) {
+  SLAB_TRY(panel_factor<T>(s, A, lda, n, k0, nb, ipiv, info, linv, linv_done));
+  if (n - nb > 0) {
+    biglu_swap_kernel<T><<<ceil_div(n - nb, 256), 256, 0, s>>>(A, lda, n, k0, nb, ipiv);
+    SLAB_CHECK_LAUNCH();
+  }
+  return SLAB_OK;
+}
+template int biglu_panel_swap<float>(cudaStream_t, float*, int, int, int, int, int*, int*, float*, bool*);
+template int biglu_panel_swap<double>(cudaStream_t, double*, int, int, int, int, int*, int*, double*, bool*);
+
+template <typename T>
 int biglu(cudaStream_t s, T* A, int lda, int n, int* ipiv, int* info, T* work) {
   for (int k0 = 0; k0 < n; k0 += kNB) {
     const int nb = n - k0 < kNB ? n - k0 : kNB;

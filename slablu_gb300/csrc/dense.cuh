@@ -1583,6 +1583,14 @@ template <typename T>
 int trsv_coop(cudaStream_t s, const T* LU, int lda, int n, const int* perm, const T* Linv, const T* Uinv, int bs,
               const T* B, int ldb, T* X, int ldx, int nrhs, bool trans = false);
 
+// One panel step of biglu: factor columns k0..k0+nb (rows k0..n) with partial
+// pivoting and apply its interchanges to every other column.  linv (nb x nb,
+// may be null) receives the inverse of the unit-lower panel triangle when
+// *linv_done comes back true.
+template <typename T>
+int biglu_panel_swap(cudaStream_t s, T* A, int lda, int n, int k0, int nb, int* ipiv, int* info, T* linv,
+                     bool* linv_done);
+
 // X[k0:k0+nb, 0:ncols] = Inv X[k0:k0+nb, 0:ncols] with Inv a bs x bs inverted
 // diagonal triangle (tri_inv_blocks layout, column-major, ld bs).
 template <typename T>

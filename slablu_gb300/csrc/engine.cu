@@ -344,7 +344,12 @@ struct EngineImpl : EngineBase {
   // interface
   int nI = 0, nbI = 0;
   DevBuf ifLU, ifPiv, ifPerm, ifX, ifSub, ifSup, ifInfo, ifGlob, ifLinv, ifUinv, ifWork;
-  DevBuf emuWork, emuErr;  // tensor-core FP64 products of the interface (mixed precision)
+  DevBuf emuWork, emuErr, emuLinv;  // tensor-core FP64 products of the interface (mixed precision)
+  // Solve-phase copies of the interface factors in the leaf/tree type T (mixed
+  // precision: FP32 copies of the FP64 factors; every correction is applied
+  // through FP32 leaf and tree factors anyway, and the residual stays FP64).
+  DevBuf sLU, sLinv, sUinv, sX, sSub;
+  static constexpr bool kSplitSolve = !std::is_same<T, TI>::value;
   bool use_emu = false;
   static constexpr int kInvBs = 64;  // diagonal-block size of the interface triangular inverses
   int nInvBlk = 0;
@@ -683,9 +688,17 @@ struct EngineImpl : EngineBase {
       SLAB_TRY(ifLinv.alloc((size_t)nbI * nInvBlk * kInvBs * kInvBs * sizeof(TI)));
       SLAB_TRY(ifUinv.alloc((size_t)nbI * nInvBlk * kInvBs * kInvBs * sizeof(TI)));
       SLAB_TRY(ifWork.alloc((size_t)kNB * kNB * sizeof(TI)));
+      if (kSplitSolve) {
+        SLAB_TRY(sLU.alloc(blk * nbI * sizeof(T)));
+        SLAB_TRY(sX.alloc(blk * nbI * sizeof(T)));
+        SLAB_TRY(sSub.alloc(blk * nbI * sizeof(T)));
+        SLAB_TRY(sLinv.alloc((size_t)nbI * nInvBlk * kInvBs * kInvBs * sizeof(T)));
+        SLAB_TRY(sUinv.alloc((size_t)nbI * nInvBlk * kInvBs * kInvBs * sizeof(T)));
+      }
       if (use_emu) {
         SLAB_TRY(emuWork.alloc(dgemm_emu_work_bytes(nI, nI, nI)));
         SLAB_TRY(emuErr.alloc(sizeof(int)));
+        SLAB_TRY(emuLinv.alloc((size_t)kEmuOuter * 64 * sizeof(double)));
         SLAB_CUDA_TRY(cudaMemsetAsync(emuErr.p, 0, sizeof(int), s));
       }
     }
@@ -694,7 +707,7 @@ struct EngineImpl : EngineBase {
     SLAB_CUDA_TRY(cudaStreamSynchronize(s));
     factor_bytes_ = G.bytes + piv.bytes + leafperm.bytes + nodepool.bytes + fpool.bytes + pivpool.bytes +
                     permpool.bytes + ifLU.bytes + ifPiv.bytes + ifPerm.bytes + ifSub.bytes + ifSup.bytes + ifX.bytes +
-                    ifLinv.bytes + ifUinv.bytes;
+                    ifLinv.bytes + ifUinv.bytes + sLU.bytes + sX.bytes + sSub.bytes + sLinv.bytes + sUinv.bytes;
     return SLAB_OK;
   }
 
@@ -782,6 +795,39 @@ struct EngineImpl : EngineBase {
 
   TI* linv(int j) { return ifLinv.as<TI>() + (size_t)j * nInvBlk * kInvBs * kInvBs; }
   TI* uinv(int j) { return ifUinv.as<TI>() + (size_t)j * nInvBlk * kInvBs * kInvBs; }
+  // solve-phase views (type T)
+  size_t inv_elems() const { return (size_t)nInvBlk * kInvBs * kInvBs; }
+  T* sv_of(DevBuf& split, DevBuf& full, size_t off) {
+    if constexpr (kSplitSolve) return split.as<T>() + off;
+    else return full.as<T>() + off;
+  }
+  T* luS(int j) { return sv_of(sLU, ifLU, (size_t)nI * nI * j); }
+  T* xS(int j) { return sv_of(sX, ifX, (size_t)nI * nI * j); }
+  T* subS(int j) { return sv_of(sSub, ifSub, (size_t)nI * nI * j); }
+  T* linvS(int j) { return sv_of(sLinv, ifLinv, inv_elems() * j); }
+  T* uinvS(int j) { return sv_of(sUinv, ifUinv, inv_elems() * j); }
+
+  // FP32 copies of the FP64 interface factors for the solve phase (mixed precision).
+  int split_solve_copies() {
+    if constexpr (kSplitSolve) {
+      const long long blk = (long long)nI * nI;
+      convert_kernel<T, TI><<<grid_for(blk * nbI), 256, 0, s>>>(ifLU.as<TI>(), sLU.as<T>(), blk * nbI);
+      SLAB_CHECK_LAUNCH();
+      const long long ni = (long long)inv_elems() * nbI;
+      convert_kernel<T, TI><<<grid_for(ni), 256, 0, s>>>(ifLinv.as<TI>(), sLinv.as<T>(), ni);
+      SLAB_CHECK_LAUNCH();
+      convert_kernel<T, TI><<<grid_for(ni), 256, 0, s>>>(ifUinv.as<TI>(), sUinv.as<T>(), ni);
+      SLAB_CHECK_LAUNCH();
+      if (nbI > 1) {
+        convert_kernel<T, TI><<<grid_for(blk * (nbI - 1)), 256, 0, s>>>(ifX.as<TI>(), sX.as<T>(), blk * (nbI - 1));
+        SLAB_CHECK_LAUNCH();
+        convert_kernel<T, TI><<<grid_for(blk * (nbI - 1)), 256, 0, s>>>(ifSub.as<TI>() + blk, sSub.as<T>() + blk,
+                                                                       blk * (nbI - 1));
+        SLAB_CHECK_LAUNCH();
+      }
+    }
+    return SLAB_OK;
+  }
 
   // X_{j-1} = S_{j-1}^{-1} sup_{j-1}, then S_j -= sub_j X_{j-1}: on the tensor
   // cores through exact slicing when use_emu (the FP64 mixed path), else FP64 cores.
@@ -817,10 +863,21 @@ struct EngineImpl : EngineBase {
       for (int j = 0; j < nbI; ++j) {
         TI* Sj = ifLU.as<TI>() + blk * j;
         if (j > 0) SLAB_TRY(iface_schur(j));
-        SLAB_TRY(biglu<TI>(s, Sj, nI, nI, ifPiv.as<int>() + (long long)nI * j, ifInfo.as<int>(), ifWork.as<TI>()));
+        bool done = false;
+        if constexpr (std::is_same<TI, double>::value) {
+          if (use_emu) {
+            EmuWork w{emuWork.p, emuWork.bytes, emuErr.as<int>()};
+            SLAB_TRY(biglu_emu(s, Sj, nI, nI, ifPiv.as<int>() + (long long)nI * j, ifInfo.as<int>(), ifWork.as<TI>(),
+                               emuLinv.as<double>(), w));
+            done = true;
+          }
+        }
+        if (!done)
+          SLAB_TRY(biglu<TI>(s, Sj, nI, nI, ifPiv.as<int>() + (long long)nI * j, ifInfo.as<int>(), ifWork.as<TI>()));
         SLAB_TRY(build_perm(s, ifPiv.as<int>() + (long long)nI * j, nI, ifPerm.as<int>() + (long long)nI * j));
         SLAB_TRY(tri_inv_blocks<TI>(s, Sj, nI, nI, kInvBs, linv(j), uinv(j)));
       }
+      SLAB_TRY(split_solve_copies());
     }
     return SLAB_OK;
   }
@@ -828,17 +885,16 @@ struct EngineImpl : EngineBase {
   // Z = S_j^{-1} F (or S_j^{-T} F) with the stored interface factors: one
   // thread-block cluster for up to eight columns, else the cooperative or the
   // blocked solve.
-  int iface_solve(int j, const TI* F, TI* Z, int nrhs, bool trans) {
-    const long long blk = (long long)nI * nI;
-    const TI* LUj = ifLU.as<TI>() + blk * j;
+  int iface_solve(int j, const T* F, T* Z, int nrhs, bool trans) {
+    const T* LUj = luS(j);
     const int* pj = ifPerm.as<int>() + (long long)nI * j;
     if (nrhs <= kCoopMaxRhs && kInvBs == kClBs && use_cluster_solve) {
-      const int st = trsv_cluster<TI>(s, LUj, nI, nI, pj, linv(j), uinv(j), F, nI, Z, nI, nrhs, trans);
+      const int st = trsv_cluster<T>(s, LUj, nI, nI, pj, linvS(j), uinvS(j), F, nI, Z, nI, nrhs, trans);
       if (st != SLAB_ERR_ARG) return st;  // SLAB_ERR_ARG: shape refused before any launch
     }
-    if (nrhs <= kCoopMaxRhs) return trsv_coop<TI>(s, LUj, nI, nI, pj, linv(j), uinv(j), kInvBs, F, nI, Z, nI, nrhs, trans);
+    if (nrhs <= kCoopMaxRhs) return trsv_coop<T>(s, LUj, nI, nI, pj, linvS(j), uinvS(j), kInvBs, F, nI, Z, nI, nrhs, trans);
     if (trans) return set_error(SLAB_ERR_ARG, "interface: transposed solve takes at most %d columns", kCoopMaxRhs);
-    return bigtrs_inv<TI>(s, LUj, nI, nI, pj, linv(j), uinv(j), kInvBs, F, nI, Z, nI, nrhs);
+    return bigtrs_inv<T>(s, LUj, nI, nI, pj, linvS(j), uinvS(j), kInvBs, F, nI, Z, nI, nrhs);
   }
 
   int factor_check() {
@@ -902,8 +958,8 @@ struct EngineImpl : EngineBase {
     SLAB_TRY(Ybuf.alloc((size_t)std::max<long long>(ymax, 1) * sizeof(T)));
     SLAB_TRY(Zbuf.alloc((size_t)std::max<long long>(zmax, (long long)nleaf * nx * nrhs) * sizeof(T)));
     if (nbI > 0) {
-      SLAB_TRY(ifF.alloc((size_t)nbI * nI * nrhs * sizeof(TI)));
-      SLAB_TRY(ifZ.alloc((size_t)nbI * nI * nrhs * sizeof(TI)));
+      SLAB_TRY(ifF.alloc((size_t)nbI * nI * nrhs * sizeof(T)));
+      SLAB_TRY(ifZ.alloc((size_t)nbI * nI * nrhs * sizeof(T)));
     }
     SLAB_TRY(ux_d.alloc((size_t)ntot * nrhs * sizeof(double)));
     SLAB_TRY(uc_d.alloc((size_t)nleaf * n * nrhs * sizeof(double)));
@@ -962,27 +1018,21 @@ struct EngineImpl : EngineBase {
     if (nbI > 0) {
       const long long blk = (long long)nI * nI;
       const long long vb = (long long)nI * nrhs;
-      TI* F = ifF.as<TI>();
-      TI* Zi = ifZ.as<TI>();
-      // gather with conversion through the T-typed Zbuf
-      gather_kernel<T><<<grid_for((long long)nbI * vb), 256, 0, s>>>(g, ntot, ifGlob.as<int>(), nI, nbI, nrhs,
-                                                                    Zbuf.as<T>());
-      SLAB_CHECK_LAUNCH();
-      convert_kernel<TI, T><<<grid_for(nbI * vb), 256, 0, s>>>(Zbuf.as<T>(), F, nbI * vb);
+      T* F = ifF.as<T>();
+      T* Zi = ifZ.as<T>();
+      gather_kernel<T><<<grid_for((long long)nbI * vb), 256, 0, s>>>(g, ntot, ifGlob.as<int>(), nI, nbI, nrhs, F);
       SLAB_CHECK_LAUNCH();
       for (int j = 0; j < nbI; ++j) {
         if (j > 0)
-          SLAB_TRY(gemm<TI>(s, nI, nrhs, nI, TI(-1), ifSub.as<TI>() + blk * j, nullptr, 0, nI, Zi + vb * (j - 1),
-                            nullptr, 0, nI, TI(1), F + vb * j, nullptr, 0, nI, 1));
+          SLAB_TRY(gemm<T>(s, nI, nrhs, nI, T(-1), subS(j), nullptr, 0, nI, Zi + vb * (j - 1), nullptr, 0, nI, T(1),
+                           F + vb * j, nullptr, 0, nI, 1));
         SLAB_TRY(iface_solve(j, F + vb * j, Zi + vb * j, nrhs, false));
       }
       for (int j = nbI - 2; j >= 0; --j)
-        SLAB_TRY(gemm<TI>(s, nI, nrhs, nI, TI(-1), ifX.as<TI>() + blk * j, nullptr, 0, nI, Zi + vb * (j + 1), nullptr,
-                          0, nI, TI(1), Zi + vb * j, nullptr, 0, nI, 1));
-      convert_kernel<T, TI><<<grid_for(nbI * vb), 256, 0, s>>>(Zi, Zbuf.as<T>(), nbI * vb);
-      SLAB_CHECK_LAUNCH();
+        SLAB_TRY(gemm<T>(s, nI, nrhs, nI, T(-1), xS(j), nullptr, 0, nI, Zi + vb * (j + 1), nullptr, 0, nI, T(1),
+                         Zi + vb * j, nullptr, 0, nI, 1));
       scatter_set_kernel<T><<<grid_for((long long)nbI * vb), 256, 0, s>>>(u, ntot, ifGlob.as<int>(), nI, nbI, nrhs,
-                                                                         Zbuf.as<T>());
+                                                                         Zi);
       SLAB_CHECK_LAUNCH();
     }
     // tree backward
@@ -1049,26 +1099,21 @@ struct EngineImpl : EngineBase {
     if (nbI > 0) {
       const long long blk = (long long)nI * nI;
       const long long vb = (long long)nI * nrhs;
-      TI* F = ifF.as<TI>();
-      TI* Zi = ifZ.as<TI>();
-      gather_kernel<T><<<grid_for((long long)nbI * vb), 256, 0, s>>>(g, ntot, ifGlob.as<int>(), nI, nbI, nrhs,
-                                                                    Zbuf.as<T>());
-      SLAB_CHECK_LAUNCH();
-      convert_kernel<TI, T><<<grid_for(nbI * vb), 256, 0, s>>>(Zbuf.as<T>(), F, nbI * vb);
+      T* F = ifF.as<T>();
+      T* Zi = ifZ.as<T>();
+      gather_kernel<T><<<grid_for((long long)nbI * vb), 256, 0, s>>>(g, ntot, ifGlob.as<int>(), nI, nbI, nrhs, F);
       SLAB_CHECK_LAUNCH();
       for (int j = 1; j < nbI; ++j)
-        SLAB_TRY(gemm_tn<TI>(s, nI, nrhs, nI, TI(-1), ifX.as<TI>() + blk * (j - 1), nullptr, 0, nI, F + vb * (j - 1),
-                             nullptr, 0, nI, TI(1), F + vb * j, nullptr, 0, nI, 1));
+        SLAB_TRY(gemm_tn<T>(s, nI, nrhs, nI, T(-1), xS(j - 1), nullptr, 0, nI, F + vb * (j - 1), nullptr, 0, nI, T(1),
+                            F + vb * j, nullptr, 0, nI, 1));
       for (int j = nbI - 1; j >= 0; --j) {
         if (j < nbI - 1)
-          SLAB_TRY(gemm_tn<TI>(s, nI, nrhs, nI, TI(-1), ifSub.as<TI>() + blk * (j + 1), nullptr, 0, nI,
-                               Zi + vb * (j + 1), nullptr, 0, nI, TI(1), F + vb * j, nullptr, 0, nI, 1));
+          SLAB_TRY(gemm_tn<T>(s, nI, nrhs, nI, T(-1), subS(j + 1), nullptr, 0, nI, Zi + vb * (j + 1), nullptr, 0, nI,
+                              T(1), F + vb * j, nullptr, 0, nI, 1));
         SLAB_TRY(iface_solve(j, F + vb * j, Zi + vb * j, nrhs, true));
       }
-      convert_kernel<T, TI><<<grid_for(nbI * vb), 256, 0, s>>>(Zi, Zbuf.as<T>(), nbI * vb);
-      SLAB_CHECK_LAUNCH();
       scatter_set_kernel<T><<<grid_for((long long)nbI * vb), 256, 0, s>>>(u, ntot, ifGlob.as<int>(), nI, nbI, nrhs,
-                                                                         Zbuf.as<T>());
+                                                                         Zi);
       SLAB_CHECK_LAUNCH();
     }
     // tree backward (transposed): lam_E = M^{-T} (g_E - col^T lam_O)

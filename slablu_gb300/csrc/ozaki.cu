@@ -466,6 +466,45 @@ int bigtrs_inv_emu(cudaStream_t s, const double* LU, int lda, int n, const int* 
   return SLAB_OK;
 }
 
+int biglu_emu(cudaStream_t s, double* A, int lda, int n, int* ipiv, int* info, double* panel_linv, double* blk_linv,
+              const EmuWork& w) {
+  constexpr int kB = 64;  // diagonal blocks of the outer triangular solve
+  for (int ob0 = 0; ob0 < n; ob0 += kEmuOuter) {
+    const int obe = n - ob0 < kEmuOuter ? n : ob0 + kEmuOuter;
+    for (int k0 = ob0; k0 < obe; k0 += kNB) {
+      const int nb = obe - k0 < kNB ? obe - k0 : kNB;
+      bool linv_done = false;
+      SLAB_TRY(biglu_panel_swap<double>(s, A, lda, n, k0, nb, ipiv, info, panel_linv, &linv_done));
+      const int inner = obe - k0 - nb;
+      if (inner > 0) {
+        if (!linv_done) SLAB_TRY(tri_inv_blocks<double>(s, A + (size_t)k0 * lda + k0, lda, nb, kNB, panel_linv, nullptr));
+        SLAB_TRY(trsm_inv<double>(s, panel_linv, linv_done ? nb : kNB, k0, nb, A + (size_t)(k0 + nb) * lda, lda,
+                                  inner));
+        SLAB_TRY(gemm<double>(s, n - k0 - nb, inner, nb, -1.0, A + (size_t)k0 * lda + k0 + nb, nullptr, 0, lda,
+                              A + (size_t)(k0 + nb) * lda + k0, nullptr, 0, lda, 1.0,
+                              A + (size_t)(k0 + nb) * lda + k0 + nb, nullptr, 0, lda, 1));
+      }
+    }
+    const int rest = n - obe;
+    if (rest > 0) {
+      // U12 = L11^{-1} A12 over the outer block's rows, then A22 -= A21 U12 on the tensor cores
+      SLAB_TRY(tri_inv_blocks<double>(s, A + (size_t)ob0 * lda + ob0, lda, obe - ob0, kB, blk_linv, nullptr));
+      double* A12 = A + (size_t)obe * lda;
+      for (int b0 = ob0; b0 < obe; b0 += kB) {
+        const int bn = obe - b0 < kB ? obe - b0 : kB;
+        SLAB_TRY(trsm_inv<double>(s, blk_linv + (size_t)((b0 - ob0) / kB) * kB * kB, kB, b0, bn, A12, lda, rest));
+        const int below = obe - b0 - bn;
+        if (below > 0)
+          SLAB_TRY(gemm<double>(s, below, rest, bn, -1.0, A + (size_t)b0 * lda + b0 + bn, nullptr, 0, lda, A12 + b0,
+                                nullptr, 0, lda, 1.0, A12 + b0 + bn, nullptr, 0, lda, 1));
+      }
+      SLAB_TRY(dgemm_emu(s, rest, rest, obe - ob0, -1.0, A + (size_t)ob0 * lda + obe, lda, A12 + ob0, lda, 1.0,
+                         A12 + obe, lda, w.buf, w.bytes, w.err));
+    }
+  }
+  return SLAB_OK;
+}
+
 }  // namespace slab
 
 extern "C" size_t slab_dgemm_emu_work_bytes(int m, int n, int k) { return slab::dgemm_emu_work_bytes(m, n, k); }

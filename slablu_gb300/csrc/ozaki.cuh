@@ -34,4 +34,11 @@ int bigtrs_inv_emu(cudaStream_t s, const double* LU, int lda, int n, const int* 
                    const double* Uinv, int bs, const double* B, int ldb, double* X, int ldx, int nrhs,
                    const EmuWork& w);
 
+// biglu with the trailing update between outer blocks of kEmuOuter columns
+// done by dgemm_emu (the panels and the updates inside an outer block stay on
+// the FP64 cores).  Same pivots, factors and info as biglu.  panel_linv: kNB x
+// kNB doubles; blk_linv: kEmuOuter * 64 doubles.
+int biglu_emu(cudaStream_t s, double* A, int lda, int n, int* ipiv, int* info, double* panel_linv, double* blk_linv,
+              const EmuWork& w);
+
 }  // namespace slab
