@@ -263,7 +263,8 @@ __device__ void cta_getrf_aug(T* A, int lda, int n, int nc, int* ipiv, T* smem, 
       A[(size_t)(k0 + c) * lda + k0 + r] = Psm[r + c * ldq];
     }
     if (tid < nb) ipiv[k0 + tid] = k0 + piv_s[tid];
-    // row interchanges on every column outside the panel
+    // row interchanges on every column outside the panel (one thread per
+    // column; a register-light loop keeps three leaves resident per SM)
     for (int c = tid; c < nc - nb; c += blockDim.x) {
       const int col = c < k0 ? c : c + nb;
       T* cp = A + (size_t)col * lda;

@@ -327,6 +327,7 @@ struct EngineImpl : EngineBase {
   int gapp_nrhs = 0, gapp_t_nrhs = 0;
   bool use_graphs = true;
   bool use_cluster_solve = true;
+  int leaf_ctas = 0;  // resident leaves per SM in the leaf kernel (0: as many as fit)
   DevBuf D, Dsq, Nx, NxcT, NxxT, interp, jxr, leafglob, dirmask;
   DevBuf coef[5];
   bool has[5] = {false, false, false, false, false};
@@ -432,6 +433,8 @@ struct EngineImpl : EngineBase {
     use_graphs = !(ng && ng[0] == '1');
     const char* nc = getenv("SLAB_COOP_SOLVE");  // 1: grid-wide cooperative interface solve instead of the cluster one
     use_cluster_solve = !(nc && nc[0] == '1');
+    const char* lc = getenv("SLAB_LEAF_CTAS");
+    if (lc) leaf_ctas = atoi(lc);
     // FP64 interface products on the tensor cores in the mixed mode (FP32 leaves and
     // tree, FP64 interface); SLAB_NATIVE_FP64=1 keeps them on the FP64 cores
     const char* nf = getenv("SLAB_NATIVE_FP64");
@@ -762,7 +765,7 @@ struct EngineImpl : EngineBase {
     a.G = G.as<T>(); a.strideG = (long long)n * (n + nx); a.piv = piv.as<int>();
     a.dtn = nodepool.as<T>(); a.info = leafinfo.as<int>();
     a.decouple = 1; a.n0 = n0; a.n1 = n1; a.leaf_begin = 0;
-    SLAB_TRY(leaf_factor<T>(s, a, (int)nleaf));
+    SLAB_TRY(leaf_factor<T>(s, a, (int)nleaf, leaf_ctas));
     return build_perm_batched(s, piv.as<int>(), n, n, (int)nleaf, leafperm.as<int>(), n);
   }
 

@@ -5,18 +5,39 @@
 namespace slab {
 
 template <typename T>
-int leaf_factor(cudaStream_t s, const LeafFactorArgs<T>& a, int nleaf) {
+int leaf_factor(cudaStream_t s, const LeafFactorArgs<T>& a, int nleaf, int ctas_per_sm) {
   if (nleaf <= 0) return SLAB_OK;
   if (a.nx > 2 * kCT) return set_error(SLAB_ERR_ARG, "leaf_factor: p = %d too large", a.p);
-  const size_t bytes = leaf_factor_smem_bytes(a.p, sizeof(T));
+  const size_t bytes = leaf_smem_for_occupancy(reinterpret_cast<const void*>(leaf_factor_kernel<T>),
+                                               leaf_factor_smem_bytes(a.p, sizeof(T)), ctas_per_sm);
   SLAB_TRY(ensure_smem(leaf_factor_kernel<T>, bytes, "leaf_factor"));
   leaf_factor_kernel<T><<<nleaf, kNT, bytes, s>>>(a);
   SLAB_CHECK_LAUNCH();
   return SLAB_OK;
 }
 
-template int leaf_factor<float>(cudaStream_t, const LeafFactorArgs<float>&, int);
-template int leaf_factor<double>(cudaStream_t, const LeafFactorArgs<double>&, int);
+size_t leaf_smem_for_occupancy(const void* kernel, size_t need, int ctas_per_sm) {
+  if (ctas_per_sm <= 0) return need;
+  int dev = 0, per_sm = 0, reserved = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev) != cudaSuccess) {
+    cudaGetLastError();
+    return need;
+  }
+  cudaFuncAttributes fa{};
+  if (cudaFuncGetAttributes(&fa, kernel) != cudaSuccess) {
+    cudaGetLastError();
+    return need;
+  }
+  // the largest dynamic size with which at most ctas_per_sm blocks fit one SM
+  const long long cap = (long long)per_sm / ctas_per_sm - reserved - (long long)fa.sharedSizeBytes;
+  const long long b = cap / 128 * 128;
+  return b > (long long)need ? (size_t)b : need;
+}
+
+template int leaf_factor<float>(cudaStream_t, const LeafFactorArgs<float>&, int, int);
+template int leaf_factor<double>(cudaStream_t, const LeafFactorArgs<double>&, int, int);
 
 __global__ void __launch_bounds__(256) residual_kernel(ResidualArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];

@@ -139,8 +139,15 @@ __global__ void __launch_bounds__(kNT) leaf_factor_kernel(LeafFactorArgs<T> a) {
   }
 }
 
+// ctas_per_sm > 0 sizes the dynamic shared memory so that at most that many
+// leaves are resident per SM (fewer resident leaves keep more of each leaf's
+// trailing matrix in L2); 0 uses the minimum size.
 template <typename T>
-int leaf_factor(cudaStream_t s, const LeafFactorArgs<T>& a, int nleaf);
+int leaf_factor(cudaStream_t s, const LeafFactorArgs<T>& a, int nleaf, int ctas_per_sm = 0);
+
+// Dynamic shared-memory bytes (at least `need`) that allow at most ctas_per_sm
+// resident blocks of `kernel` per SM; `need` itself when ctas_per_sm <= 0.
+size_t leaf_smem_for_occupancy(const void* kernel, size_t need, int ctas_per_sm);
 
 // Nx (nx x p^2 row-major, FP64) -> Nxc (nx x n) and Nxx (nx x nx), column-major, in T.
 template <typename T>
