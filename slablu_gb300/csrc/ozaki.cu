@@ -262,17 +262,18 @@ __global__ void __launch_bounds__(192, 1) ozaki_gemm_kernel(const __grid_constan
               break;
             }
             tc::tc_fence_after();
+            // descriptors are built once per stage; a 32-byte K step and a B
+            // tile step only add to the start-address field (address >> 4)
             const uint32_t sa = tc::smem_u32(stages + (size_t)st * kStageBytes);
-            for (int t0 = 0; t0 < kSl - s0; ++t0) {
-              const int g = group_of(s0, t0);
-              const int first = group_first_s0(s0, t0);
-              const uint32_t sb = sa + kAbytes + t0 * kBbytes;
+            const uint64_t adesc = tc::sdesc_kmajor_sw128(sa);
+            uint64_t bdesc = tc::sdesc_kmajor_sw128(sa + kAbytes);
+            for (int t0 = 0; t0 < kSl - s0; ++t0, bdesc += (uint64_t)(kBbytes >> 4)) {
+              const uint32_t dcol = tbase + (uint32_t)(group_of(s0, t0) * kBN);
+              const uint32_t acc0 = (kb == 0 && s0 == group_first_s0(s0, t0)) ? 0u : 1u;
+              tc::mma_bf16(dcol, adesc, bdesc, idesc, acc0);
 #pragma unroll
-              for (int kk = 0; kk < kBK / 16; ++kk) {
-                const uint32_t acc = (kb == 0 && kk == 0 && s0 == first) ? 0u : 1u;
-                tc::mma_bf16(tbase + (uint32_t)(g * kBN), tc::sdesc_kmajor_sw128(sa + kk * 32),
-                             tc::sdesc_kmajor_sw128(sb + kk * 32), idesc, acc);
-              }
+              for (int kk = 1; kk < kBK / 16; ++kk)
+                tc::mma_bf16(dcol, adesc + (uint64_t)(2 * kk), bdesc + (uint64_t)(2 * kk), idesc, 1u);
             }
             tc::mma_commit(&empty[st]);  // the stage is free once these products complete
             ++it;

@@ -2,10 +2,13 @@
 
     python -m slablu_gb300.profile_cases factor --n 640 --precision mixed
     python -m slablu_gb300.profile_cases solve  --n 2000 --precision mixed --iters 1
+    python -m slablu_gb300.profile_cases dgemm  --n 2000 --reps 2
 
-Both use the Gaussian-lattice Helmholtz field of the benchmark (p = 22) on an
-n x n-point grid ((n/20)^2 leaves).  `factor` runs one factorization; `solve`
-runs one factorization and one refined solve with at most --iters steps.
+`factor` and `solve` use the Gaussian-lattice Helmholtz field of the benchmark
+(p = 22) on an n x n-point grid ((n/20)^2 leaves): one factorization, and for
+`solve` one refined solve with at most --iters steps.  `dgemm` runs --reps
+tensor-core FP64 products C = A B of n x n random matrices (the shape of the
+interface Schur update at n = 2000).
 """
 import argparse
 
@@ -17,11 +20,22 @@ from .engine import SlabEngine
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument('case', choices=['factor', 'solve'])
+    ap.add_argument('case', choices=['factor', 'solve', 'dgemm'])
     ap.add_argument('--n', type=int, default=640)
     ap.add_argument('--precision', default='mixed', choices=['fp64', 'mixed', 'fp32'])
     ap.add_argument('--iters', type=int, default=1)
+    ap.add_argument('--reps', type=int, default=2)
     a = ap.parse_args(argv)
+    if a.case == 'dgemm':
+        from .dgemm import dgemm_emu
+        gen = torch.Generator(device='cuda').manual_seed(1)
+        A = torch.randn(a.n, a.n, dtype=torch.float64, device='cuda', generator=gen)
+        B = torch.randn(a.n, a.n, dtype=torch.float64, device='cuda', generator=gen)
+        for _ in range(a.reps):
+            C = dgemm_emu(A, B)
+        torch.cuda.synchronize()
+        print('ok dgemm', a.n, float(C.abs().max()))
+        return
     cfg = problems.config3()
     p = cfg['p']
     g = hps.Geometry([[0, 1], [0, 1]], problems.leaf_half_width(a.n, p), p, 1.0)
