@@ -5,6 +5,7 @@
 #include <mutex>
 #include <string>
 #include <tuple>
+#include <type_traits>
 
 #include "dense.cuh"
 
@@ -276,6 +277,27 @@ int build_perm(cudaStream_t s, const int* ipiv, int n, int* perm) {
   return SLAB_OK;
 }
 
+// Multiprocessor count of the current device (queried once per device).
+static int sm_count() {
+  static std::mutex mu;
+  static std::map<int, int> cache;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    return 152;
+  }
+  std::lock_guard<std::mutex> lk(mu);
+  auto it = cache.find(dev);
+  if (it != cache.end()) return it->second;
+  int sms = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) {
+    cudaGetLastError();
+    sms = 152;
+  }
+  cache[dev] = sms;
+  return sms;
+}
+
 template <typename T>
 int gemm(cudaStream_t s, int m, int n, int k, T alpha, const T* A, const long long* offA, long long strideA,
          int lda, const T* B, const long long* offB, long long strideB, int ldb, T beta, T* C,
@@ -343,6 +365,13 @@ int gemm(cudaStream_t s, int m, int n, int k, T alpha, const T* A, const long lo
     return SLAB_OK;
   }
   // k == 0 leaves the k loop empty: C = beta*C
+  if (std::is_same<T, double>::value && (long long)ceil_div(m, 64) * ceil_div(n, 64) * batch < 2LL * sm_count()) {
+    dim3 g32(ceil_div(m, 32), ceil_div(n, 32), batch);
+    gemm32_kernel<T><<<g32, 256, 0, s>>>(m, n, k < 0 ? 0 : k, alpha, A, offA, strideA, lda, B, offB, strideB, ldb,
+                                         beta, C, offC, strideC, ldc);
+    SLAB_CHECK_LAUNCH();
+    return SLAB_OK;
+  }
   dim3 grid(ceil_div(m, 64), ceil_div(n, 64), batch);
   gemm_kernel<T, false><<<grid, 256, 0, s>>>(m, n, k < 0 ? 0 : k, alpha, A, offA, strideA, lda, B, offB, strideB, ldb,
                                       beta, C, offC, strideC, ldc);

@@ -99,6 +99,27 @@ __device__ int cta_argmax(mag_t<T> v, int i, T* sv_, int* si) {
   return si[32];
 }
 
+// Reciprocal of a normal double by Newton's method for 1/d, x <- x (2 - d x),
+// started from the FP32 reciprocal of d's mantissa (relative error < 2^-22, so
+// two steps reach the FP64 rounding level).  The exponent is handled on the bit
+// pattern.  Used where a full FP64 division would sit on a latency-critical
+// chain; within an ulp or two of 1/d (not correctly rounded).  Zero, subnormal,
+// huge, infinite and NaN inputs take the ordinary division.
+__device__ __forceinline__ double recip_newton(double d) {
+  const long long b = __double_as_longlong(d);
+  const int e = (int)((b >> 52) & 0x7FF);
+  if (e < 3 || e > 2044) return 1.0 / d;
+  const double m = __longlong_as_double((b & 0x800FFFFFFFFFFFFFll) | (1023ll << 52));  // d / 2^(e-1023), in [1, 2)
+  double x = (double)__frcp_rn((float)m);
+  double r = fma(-m, x, 1.0);
+  x = fma(x, r, x);
+  r = fma(-m, x, 1.0);
+  x = fma(x, r, x);
+  // 1/d = x * 2^-(e-1023); the scale 2^(2046-e) is a normal power of two for e in [3, 2044]
+  return x * __longlong_as_double((long long)(2046 - e) << 52);
+}
+__device__ __forceinline__ float recip_newton(float d) { return 1.0f / d; }
+
 // 1/d computed by one thread and broadcast through shared memory (slot is a
 // T in shared memory): an FP64 division is a long dependent FP64 sequence.
 template <typename T>
@@ -560,6 +581,63 @@ __global__ void __launch_bounds__(256) gemm_kernel(int m, int n, int k, T alpha,
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
       const int r = r0 + 4 * tr + i;
+      if (r >= m) continue;
+      T* cp = C + r + (size_t)c * ldc;
+      *cp = (beta == T(0) ? T(0) : beta * *cp) + alpha * acc[i][j];
+    }
+  }
+}
+
+// Same product with 32 x 32 output tiles (2 x 2 outputs per thread), for FP64
+// shapes whose 64 x 64 grid would leave SMs idle: GB300 retires about two FP64
+// FMAs per clock per SM, so FP64 products want every SM busy.
+template <typename T>
+__global__ void __launch_bounds__(256) gemm32_kernel(int m, int n, int k, T alpha, const T* __restrict__ A,
+                                                    const long long* offA, long long strideA, int lda,
+                                                    const T* __restrict__ B, const long long* offB,
+                                                    long long strideB, int ldb, T beta, T* C,
+                                                    const long long* offC, long long strideC, int ldc) {
+  constexpr int kLD = 34;
+  __shared__ __align__(16) T As[kGK * kLD];
+  __shared__ __align__(16) T Bs[kGK * kLD];
+  const int bz = blockIdx.z;
+  A += batch_off(offA, strideA, bz);
+  B += batch_off(offB, strideB, bz);
+  C += batch_off(offC, strideC, bz);
+  const int r0 = blockIdx.x * 32, c0 = blockIdx.y * 32;
+  const int tid = threadIdx.x;
+  const int tr = tid & 15, tc = tid >> 4;
+  T acc[2][2] = {{T(0), T(0)}, {T(0), T(0)}};
+  for (int k0 = 0; k0 < k; k0 += kGK) {
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const int idx = tid + 256 * q;  // 512 elements of each tile
+      const int r = idx & 31, kk = idx >> 5;
+      const int gr = r0 + r, gk = k0 + kk;
+      As[r + kk * kLD] = (gr < m && gk < k) ? A[gr + (size_t)gk * lda] : T(0);
+      const int kb = idx & 15, c = idx >> 4;
+      const int gc = c0 + c, gkb = k0 + kb;
+      Bs[c + kb * kLD] = (gc < n && gkb < k) ? B[gkb + (size_t)gc * ldb] : T(0);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < kGK; ++kk) {
+      const T a0 = As[2 * tr + kk * kLD], a1 = As[2 * tr + 1 + kk * kLD];
+      const T b0 = Bs[2 * tc + kk * kLD], b1 = Bs[2 * tc + 1 + kk * kLD];
+      acc[0][0] += a0 * b0;
+      acc[0][1] += a0 * b1;
+      acc[1][0] += a1 * b0;
+      acc[1][1] += a1 * b1;
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int j = 0; j < 2; ++j) {
+    const int c = c0 + 2 * tc + j;
+    if (c >= n) continue;
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+      const int r = r0 + 2 * tr + i;
       if (r >= m) continue;
       T* cp = C + r + (size_t)c * ldc;
       *cp = (beta == T(0) ? T(0) : beta * *cp) + alpha * acc[i][j];
@@ -1283,7 +1361,14 @@ __global__ void __launch_bounds__(256) biglu_panel_cluster_kernel(T* A, int lda,
   for (int i = tid; i < rows; i += blockDim.x) lrow[i] = g0 + i;
   for (int i = tid; i < m; i += blockDim.x) map[i] = i;
   __syncthreads();
+  __shared__ K wk[32];
+  __shared__ int wi_s[32];
+  __shared__ T rd_s;
+  const int lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
   for (int j = 0; j < nb && j < m; ++j) {
+    // local candidate: rows of this CTA with logical index >= j.  The thread
+    // scanning row i is the one that updated P[i, j] in the previous column
+    // (pair index i below), so no barrier is needed before the scan.
     K best = 0;
     int bi = INT_MAX;
     for (int i = tid; i < rows; i += blockDim.x) {
@@ -1295,36 +1380,56 @@ __global__ void __launch_bounds__(256) biglu_panel_cluster_kernel(T* A, int lda,
         bi = li;
       }
     }
-    const int wl = cta_argmax<T>(best, bi, sv, si);
-    if (tid == 0) {
-      cand_i[j & 1] = wl;
-      cand_v[j & 1] = wl == INT_MAX ? K(0) : mag_key(P[(map[wl] - g0) + (size_t)j * R]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const K v2 = __shfl_down_sync(0xffffffffu, best, o);
+      const int i2 = __shfl_down_sync(0xffffffffu, bi, o);
+      argmax_merge(best, bi, v2, i2);
     }
-    cluster.sync();  // candidates published; every update of column j-1 is complete
-    if (tid < 32) {  // lane q reads CTA q's candidate: one remote read in flight per lane
-      K v = 0;
-      int i = INT_MAX;
-      if (tid < CL) {
-        i = *cluster.map_shared_rank(&cand_i[j & 1], tid);
-        v = *cluster.map_shared_rank(&cand_v[j & 1], tid);
-      }
+    if (lane == 0) {
+      wk[warp] = best;
+      wi_s[warp] = bi;
+    }
+    __syncthreads();  // (1) warp candidates; also orders lrow updates of the previous column
+    if (warp == 0) {
+      K v = lane < nwarps ? wk[lane] : K(0);
+      int i = lane < nwarps ? wi_s[lane] : INT_MAX;
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
         const K v2 = __shfl_down_sync(0xffffffffu, v, o);
         const int i2 = __shfl_down_sync(0xffffffffu, i, o);
         argmax_merge(v, i, v2, i2);
       }
-      if (tid == 0) si[32] = i;
+      if (lane == 0) {
+        cand_i[j & 1] = i;
+        cand_v[j & 1] = v;
+      }
     }
-    __syncthreads();
-    const int wi = si[32];
+    cluster.sync();  // candidates published; every update of column j-1 is complete
+    // every warp reduces the CL candidates itself (lane q reads CTA q's)
+    K v = 0;
+    int wi = INT_MAX;
+    if (lane < CL) {
+      wi = *cluster.map_shared_rank(&cand_i[j & 1], lane);
+      v = *cluster.map_shared_rank(&cand_v[j & 1], lane);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const K v2 = __shfl_xor_sync(0xffffffffu, v, o);
+      const int i2 = __shfl_xor_sync(0xffffffffu, wi, o);
+      argmax_merge(v, wi, v2, i2);
+    }
     const int piv = wi == INT_MAX ? j : wi;
     const int php = map[piv], phj = map[j];
     {
       const T* src = cluster.map_shared_rank(P, php / R);
-      for (int c = tid; c < nb; c += blockDim.x) prow[c] = src[(php % R) + (size_t)c * R];
+      for (int c = tid; c < nb; c += blockDim.x) {
+        const T x = src[(php % R) + (size_t)c * R];
+        prow[c] = x;
+        if (c == j) rd_s = mag_key(x) == 0 ? T(0) : recip_newton(x);
+      }
     }
-    __syncthreads();  // map reads and the pivot row are complete
+    __syncthreads();  // (2) pivot row and its reciprocal; every map read of this column done
     if (tid == 0) {
       map[j] = php;
       map[piv] = phj;
@@ -1332,28 +1437,29 @@ __global__ void __launch_bounds__(256) biglu_panel_cluster_kernel(T* A, int lda,
       if (piv != j && rk == phj / R) lrow[phj % R] = piv;
       if (rk == 0) ipiv[k0 + j] = k0 + piv;
     }
-    __syncthreads();
-    const T d = prow[j];
-    if (d == T(0) || d != d) {
+    if (mag_key(prow[j]) == 0) {  // zero or NaN pivot (integer test: no FP64 compare)
       if (rk == 0 && tid == 0 && info && *info == 0) *info = k0 + j + 1;
+      __syncthreads();  // uniform branch: keeps the barrier count of the other path
     } else {
-      const T rd = cta_recip(d, sv + 32);
+      const T rd = rd_s;
+      // logical index after this column's interchange, without waiting for thread 0
       for (int i = tid; i < rows; i += blockDim.x) {
+        const int ph = g0 + i;
+        const int li = ph == php ? j : (ph == phj ? piv : lrow[i]);
         T l = T(0);
-        if (lrow[i] > j) {
+        if (li > j) {
           l = P[i + (size_t)j * R] * rd;
           P[i + (size_t)j * R] = l;
         }
         lcol[i] = l;
       }
-      __syncthreads();
+      __syncthreads();  // (3) multipliers
       const int ncol = nb - j - 1;
       for (int idx = tid; idx < rows * ncol; idx += blockDim.x) {
         const int i = idx % rows, c = j + 1 + idx / rows;
         P[i + (size_t)c * R] -= lcol[i] * prow[c];
       }
     }
-    __syncthreads();
   }
   cluster.sync();
   for (int idx = tid; idx < rows * nb; idx += blockDim.x) {
@@ -1368,15 +1474,26 @@ __global__ void __launch_bounds__(256) biglu_panel_cluster_kernel(T* A, int lda,
         Ls[l + (size_t)c * ldx] = *(cluster.map_shared_rank(P, ph / R) + (ph % R) + (size_t)c * R);
       }
       __syncthreads();
-      if (tid < nb) {  // column c of L11^{-1} by thread c
-        const int c = tid;
-        T* x = Xs + (size_t)c * ldx;
-        for (int i = 0; i < c; ++i) x[i] = T(0);
-        x[c] = T(1);
-        for (int i = c + 1; i < nb; ++i) {
-          T sum = T(0);
-          for (int k = c; k < i; ++k) sum -= Ls[i + (size_t)k * ldx] * x[k];
-          x[i] = sum;
+      // L11^{-1} by forward substitution, one warp per group of columns and one
+      // lane per row (nb <= 32): step k broadcasts x[k] and updates rows i > k,
+      // so the dependent chain is nb steps long for all the warp's columns at once.
+      {
+        constexpr int kCols = 4;
+        for (int c0 = warp * kCols; c0 < nb; c0 += nwarps * kCols) {
+          T x[kCols];
+#pragma unroll
+          for (int q = 0; q < kCols; ++q) x[q] = lane == c0 + q ? T(1) : T(0);
+          for (int k = c0; k < nb - 1; ++k) {
+            const T lik = lane > k && lane < nb ? Ls[lane + (size_t)k * ldx] : T(0);
+#pragma unroll
+            for (int q = 0; q < kCols; ++q) {
+              const T xk = __shfl_sync(0xffffffffu, x[q], k);
+              x[q] -= lik * xk;
+            }
+          }
+#pragma unroll
+          for (int q = 0; q < kCols; ++q)
+            if (c0 + q < nb && lane < nb) Xs[lane + (size_t)(c0 + q) * ldx] = x[q];
         }
       }
       __syncthreads();
