@@ -8,12 +8,16 @@
 // [-127, 127] held exactly in BF16:
 //     A = diag(2^e) sum_s 2^(-7s) A_s,   B = sum_t 2^(-7t) B_t diag(2^f).
 // The products A_s B_t with s + t <= 9 (36 of them) run on the tensor cores
-// with FP32 accumulation in tensor memory.  Over a K chunk of 256 a product
-// sum is an integer below 256 * 127^2 < 2^22, and up to four products of the
-// same weight 2^(-7(s+t)) share one accumulator (< 2^24), so every FP32
-// accumulation is exact.  Twelve accumulators per 128 x 32 output tile hold
-// the levels s + t = 2..9 of one chunk; the epilogue warps drain them into two
-// 64-bit integer fixed-point sums per output (levels 2-5 and 6-9), so the
+// with FP32 accumulation in tensor memory.  Over a K chunk of 128 a product
+// sum is an integer below 128 * 127^2 < 2^21, and the (at most eight)
+// products of one weight 2^(-7(s+t)) share one accumulator (< 2^24), so every
+// FP32 accumulation is exact.  The eight level accumulators of a 128 x 32
+// output tile sit in consecutive tensor-memory columns, level s + t at
+// columns 32 (s + t - 2): with the eight B slices stacked in shared memory,
+// one MMA of width N = 32 (9 - s) computes A_s B_t for every t <= 9 - s at
+// once, each 32-column block landing on its own level.  The epilogue warps
+// drain the levels into two 64-bit integer fixed-point sums per output
+// (levels 2-5 and 6-9), so the
 // FP64 pipe -- a small fraction of the FP32 rate on GB300 -- only does the
 // final combination, scaling and alpha/beta update (about six FP64 operations
 // per output).  The dropped levels s + t >= 10 and the fixed-point rounding
@@ -38,17 +42,22 @@ namespace {
 
 constexpr int kSl = 8;         // slices per operand
 constexpr int kSliceBits = 7;  // bits per slice
-constexpr int kBM = 128, kBN = 32, kBK = 64, kChunk = 256;
-constexpr int kGroups = 12;
-constexpr int kStages = 4;
+constexpr int kBM = 128, kBN = 32, kBK = 64, kChunk = 128;
+constexpr int kGroups = 8;  // one accumulator per level s + t = 2..9
+// Shared-memory rings: one A slice tile per (K step, slice) and all eight B
+// slice tiles of a K step together, so each B slice is loaded once per K step
+// (not once per A slice it pairs with).
+constexpr int kAStages = 6;
+constexpr int kBStages = 3;
 constexpr int kAbytes = kBM * kBK * 2;
 constexpr int kBbytes = kBN * kBK * 2;
-constexpr int kStageBytes = kAbytes + kSl * kBbytes;
+constexpr int kBStageBytes = kSl * kBbytes;
 constexpr int kNonFinite = INT_MIN;
-constexpr int kTmemCols = 512;
-constexpr size_t kGemmSmem = (size_t)kStages * kStageBytes + 1024 + 256;
+constexpr int kTmemCols = 256;
+constexpr size_t kGemmSmem = (size_t)kAStages * kAbytes + (size_t)kBStages * kBStageBytes + 1024 + 256;
 
 static_assert(kGroups * kBN <= kTmemCols, "accumulators must fit tensor memory");
+static_assert(kSl * kBN <= 256, "one MMA covers all B slices of an A slice (N <= 256)");
 
 __device__ __forceinline__ int biased_exp(double x) {
   return (int)((__double_as_longlong(x) >> 52) & 0x7FF);
@@ -170,22 +179,19 @@ __device__ __forceinline__ void final_wait(uint64_t* bar, uint32_t parity, int* 
   }
 }
 
-// Level group of the product of slices s0 + 1 and t0 + 1 (0-based indices).
-__host__ __device__ constexpr int group_of(int s0, int t0) {
-  return (s0 + t0 + 2) <= 5 ? (s0 + t0) : 4 + 2 * (s0 + t0 + 2 - 6) + (s0 >= 4 ? 1 : 0);
-}
-__host__ __device__ constexpr int group_first_s0(int s0, int t0) { return (s0 + t0 + 2) >= 6 && s0 >= 4 ? 4 : 0; }
-
 // grid (ceil(m/128), ceil(n/32)), 192 threads: warp 0 TMA producer, warp 1
 // tensor-memory owner and MMA issuer, warps 2-5 epilogue (one output row per thread).
 __global__ void __launch_bounds__(192, 1) ozaki_gemm_kernel(const __grid_constant__ CUtensorMap tmA,
                                                             const __grid_constant__ CUtensorMap tmB, EmuArgs a) {
   extern __shared__ unsigned char smem_raw[];
-  unsigned char* stages =
+  unsigned char* aring =
       reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  uint64_t* full = reinterpret_cast<uint64_t*>(stages + (size_t)kStages * kStageBytes);
-  uint64_t* empty = full + kStages;
-  uint64_t* accf = empty + kStages;
+  unsigned char* bring = aring + (size_t)kAStages * kAbytes;
+  uint64_t* fullA = reinterpret_cast<uint64_t*>(bring + (size_t)kBStages * kBStageBytes);
+  uint64_t* emptyA = fullA + kAStages;
+  uint64_t* fullB = emptyA + kAStages;
+  uint64_t* emptyB = fullB + kBStages;
+  uint64_t* accf = emptyB + kBStages;
   uint64_t* acce = accf + 1;
   uint64_t* fin = acce + 1;
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(fin + 1);
@@ -193,9 +199,13 @@ __global__ void __launch_bounds__(192, 1) ozaki_gemm_kernel(const __grid_constan
   const int i0 = blockIdx.x * kBM, j0 = blockIdx.y * kBN;
   const int nchunk = (a.kp + kChunk - 1) / kChunk;
   if (threadIdx.x == 0) {
-    for (int s = 0; s < kStages; ++s) {
-      tc::mbar_init(&full[s], 1);
-      tc::mbar_init(&empty[s], 1);
+    for (int s = 0; s < kAStages; ++s) {
+      tc::mbar_init(&fullA[s], 1);
+      tc::mbar_init(&emptyA[s], 1);
+    }
+    for (int s = 0; s < kBStages; ++s) {
+      tc::mbar_init(&fullB[s], 1);
+      tc::mbar_init(&emptyB[s], 1);
     }
     tc::mbar_init(accf, 1);
     tc::mbar_init(acce, 128);
@@ -212,41 +222,55 @@ __global__ void __launch_bounds__(192, 1) ozaki_gemm_kernel(const __grid_constan
   tc::tc_fence_after();
   const uint32_t tbase = *tmem_slot;
 
+  // Order of work, shared by the producer and the MMA issuer: chunk c, K step
+  // kb: the B block of (c, kb), then the A slices s0 = 0..7 of (c, kb).
   if (warp == 0) {
     if (lane == 0) {
-      int last_round[kStages];
+      int lastA[kAStages], lastB[kBStages];
 #pragma unroll
-      for (int s = 0; s < kStages; ++s) last_round[s] = -1;
-      int it = 0;
+      for (int s = 0; s < kAStages; ++s) lastA[s] = -1;
+#pragma unroll
+      for (int s = 0; s < kBStages; ++s) lastB[s] = -1;
+      int itA = 0, itB = 0;
       bool ok = true;
       for (int c = 0; c < nchunk && ok; ++c) {
         const int nkb = min(kChunk, a.kp - c * kChunk + kBK - 1) / kBK;
-        for (int s0 = 0; s0 < kSl && ok; ++s0) {
-          for (int kb = 0; kb < nkb; ++kb) {
-            const int st = it % kStages, round = it / kStages;
-            if (!tc::mbar_wait(&empty[st], (uint32_t)((round & 1) ^ 1), a.err, 1)) {
+        for (int kb = 0; kb < nkb && ok; ++kb) {
+          const int kx = c * kChunk + kb * kBK;
+          {
+            const int st = itB % kBStages, round = itB / kBStages;
+            if (!tc::mbar_wait(&emptyB[st], (uint32_t)((round & 1) ^ 1), a.err, 1)) {
               ok = false;
               break;
             }
-            const int ntile = kSl - s0;
-            tc::mbar_arrive_expect_tx(&full[st], (uint32_t)(kAbytes + ntile * kBbytes));
-            unsigned char* sp = stages + (size_t)st * kStageBytes;
-            const int kx = c * kChunk + kb * kBK;
-            tc::tma_load_3d(sp, &tmA, &full[st], kx, i0, s0);
-            for (int t0 = 0; t0 < ntile; ++t0) tc::tma_load_3d(sp + kAbytes + t0 * kBbytes, &tmB, &full[st], kx, j0, t0);
-            last_round[st] = round;
-            ++it;
+            tc::mbar_arrive_expect_tx(&fullB[st], (uint32_t)kBStageBytes);
+            unsigned char* bp = bring + (size_t)st * kBStageBytes;
+            for (int t0 = 0; t0 < kSl; ++t0) tc::tma_load_3d(bp + t0 * kBbytes, &tmB, &fullB[st], kx, j0, t0);
+            lastB[st] = round;
+            ++itB;
+          }
+          for (int s0 = 0; s0 < kSl; ++s0) {
+            const int st = itA % kAStages, round = itA / kAStages;
+            if (!tc::mbar_wait(&emptyA[st], (uint32_t)((round & 1) ^ 1), a.err, 1)) {
+              ok = false;
+              break;
+            }
+            tc::mbar_arrive_expect_tx(&fullA[st], (uint32_t)kAbytes);
+            tc::tma_load_3d(aring + (size_t)st * kAbytes, &tmA, &fullA[st], kx, i0, s0);
+            lastA[st] = round;
+            ++itA;
           }
         }
       }
       // no copy may still be in flight when the CTA leaves
-      for (int s = 0; s < kStages; ++s)
-        if (last_round[s] >= 0) final_wait(&full[s], (uint32_t)(last_round[s] & 1), a.err);
+      for (int s = 0; s < kAStages; ++s)
+        if (lastA[s] >= 0) final_wait(&fullA[s], (uint32_t)(lastA[s] & 1), a.err);
+      for (int s = 0; s < kBStages; ++s)
+        if (lastB[s] >= 0) final_wait(&fullB[s], (uint32_t)(lastB[s] & 1), a.err);
     }
   } else if (warp == 1) {
     if (lane == 0) {
-      const uint32_t idesc = tc::idesc_bf16_f32(kBM, kBN);
-      int it = 0;
+      int itA = 0, itB = 0;
       bool ok = true;
       for (int c = 0; c < nchunk && ok; ++c) {
         if (c > 0) {
@@ -254,30 +278,37 @@ __global__ void __launch_bounds__(192, 1) ozaki_gemm_kernel(const __grid_constan
           tc::tc_fence_after();
         }
         const int nkb = min(kChunk, a.kp - c * kChunk + kBK - 1) / kBK;
-        for (int s0 = 0; s0 < kSl && ok; ++s0) {
-          for (int kb = 0; kb < nkb; ++kb) {
-            const int st = it % kStages, round = it / kStages;
-            if (!tc::mbar_wait(&full[st], (uint32_t)(round & 1), a.err, 4)) {
+        for (int kb = 0; kb < nkb && ok; ++kb) {
+          const int stB = itB % kBStages, roundB = itB / kBStages;
+          if (!tc::mbar_wait(&fullB[stB], (uint32_t)(roundB & 1), a.err, 4)) {
+            ok = false;
+            break;
+          }
+          // descriptors are built once per stage; a 32-byte K step and a B
+          // tile step only add to the start-address field (address >> 4)
+          const uint64_t bdesc0 = tc::sdesc_kmajor_sw128(tc::smem_u32(bring + (size_t)stB * kBStageBytes));
+          for (int s0 = 0; s0 < kSl; ++s0) {
+            const int stA = itA % kAStages, roundA = itA / kAStages;
+            if (!tc::mbar_wait(&fullA[stA], (uint32_t)(roundA & 1), a.err, 4)) {
               ok = false;
               break;
             }
             tc::tc_fence_after();
-            // descriptors are built once per stage; a 32-byte K step and a B
-            // tile step only add to the start-address field (address >> 4)
-            const uint32_t sa = tc::smem_u32(stages + (size_t)st * kStageBytes);
-            const uint64_t adesc = tc::sdesc_kmajor_sw128(sa);
-            uint64_t bdesc = tc::sdesc_kmajor_sw128(sa + kAbytes);
-            for (int t0 = 0; t0 < kSl - s0; ++t0, bdesc += (uint64_t)(kBbytes >> 4)) {
-              const uint32_t dcol = tbase + (uint32_t)(group_of(s0, t0) * kBN);
-              const uint32_t acc0 = (kb == 0 && s0 == group_first_s0(s0, t0)) ? 0u : 1u;
-              tc::mma_bf16(dcol, adesc, bdesc, idesc, acc0);
+            const uint64_t adesc = tc::sdesc_kmajor_sw128(tc::smem_u32(aring + (size_t)stA * kAbytes));
+            // A_s0 against B slices 0 .. 7-s0 (rows 0 .. 32 (8-s0) - 1 of the B block):
+            // block t0 of the result is level s0 + t0 + 2, at column 32 (s0 + t0)
+            const uint32_t idesc = tc::idesc_bf16_f32(kBM, kBN * (kSl - s0));
+            const uint32_t dcol = tbase + (uint32_t)(kBN * s0);
+            // the chunk's first MMA (s0 = 0 spans every level) starts the accumulators
+            tc::mma_bf16(dcol, adesc, bdesc0, idesc, (kb == 0 && s0 == 0) ? 0u : 1u);
 #pragma unroll
-              for (int kk = 1; kk < kBK / 16; ++kk)
-                tc::mma_bf16(dcol, adesc + (uint64_t)(2 * kk), bdesc + (uint64_t)(2 * kk), idesc, 1u);
-            }
-            tc::mma_commit(&empty[st]);  // the stage is free once these products complete
-            ++it;
+            for (int kk = 1; kk < kBK / 16; ++kk)
+              tc::mma_bf16(dcol, adesc + (uint64_t)(2 * kk), bdesc0 + (uint64_t)(2 * kk), idesc, 1u);
+            tc::mma_commit(&emptyA[stA]);  // the A slot is free once these products complete
+            ++itA;
           }
+          if (ok) tc::mma_commit(&emptyB[stB]);  // and the B block after the last slice of this step
+          ++itB;
         }
         if (ok) tc::mma_commit(accf);
       }
@@ -302,7 +333,7 @@ __global__ void __launch_bounds__(192, 1) ozaki_gemm_kernel(const __grid_constan
         uint32_t r[32];
         tc::tmem_ld_32x32b_x32(tbase + ((uint32_t)(q * 32) << 16) + (uint32_t)(g * kBN), r);
         tc::tmem_ld_wait();
-        const int L = g < 4 ? g + 2 : 6 + (g - 4) / 2;
+        const int L = g + 2;
         if (g < 4) {
           const int sh = 7 * (5 - L);
 #pragma unroll
