@@ -88,6 +88,15 @@ def cpu_threads():
         return os.cpu_count() or 1
 
 
+def reference_workload(args):
+    """The workload string of our arm, so both arms name the same configuration."""
+    from slablu_gb300 import hps, problems
+    cfg = problems.config3()
+    p = cfg['p']
+    g = hps.Geometry([[0, 1], [0, 1]], problems.leaf_half_width(args.n, p), p, 1.0)
+    return workload_name(p, args.n, g, cfg, args.tol)
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if world > 1 and rank != 0:
@@ -104,8 +113,10 @@ def run_reference(args):
     line = dict(metric=METRIC, value=val, unit='unknowns/s', n_gpus=0, steps=args.steps, warmup=args.warmup,
                 ms_per_step=1e3 * tmean, higher_is_better=True, scaling='weak', vs_baseline=None, dtype='f64',
                 data='synthetic', impl='reference',
-                config=dict(workload=f'oracle port of reference CPU slabLU, p=22, n={CPU_SAMPLE_N} sample of the '
-                                     'Gaussian-lattice Helmholtz field (N=176,800)', parallelism='host threads'),
+                config=dict(workload=reference_workload(args), parallelism='host threads',
+                            sample=f'each step: the oracle port of the reference CPU slabLU, full factor+solve of '
+                                   f'the same field at n={CPU_SAMPLE_N} (N={N}); unknowns/s is size-independent '
+                                   f'to within ~15 % for the reference'),
                 cpu_baseline=dict(value=val, unit='unknowns/s', cores=cores, kind='port',
                                   sample=f'full factor+solve at n={CPU_SAMPLE_N} (N={N}) per step'),
                 e2e=dict(value=val, unit='unknowns/s', h2d_bytes_per_step=0, d2h_bytes_per_step=0))
@@ -180,6 +191,26 @@ def iface_flops(npan, nI):
     return npan * (2 / 3 * nI ** 3) + (npan - 1) * (2 * nI ** 3 + 2 * nI ** 3) if npan > 0 else 0
 
 
+def combine_ranks(t_local, units_local, world, device):
+    """Whole-job throughput of `world` replicas: a barrier after the timed
+    region, the maximum of the per-rank times, and the units of all ranks over
+    it.  Returns (t_max, units per second)."""
+    if world <= 1:
+        return t_local, units_local / t_local
+    import torch
+    import torch.distributed as dist
+    dist.barrier()
+    tt = torch.tensor([t_local], dtype=torch.float64, device=device)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    t_max = float(tt)
+    return t_max, units_local * world / t_max
+
+
+def workload_name(p, n, g, cfg, tol):
+    return (f'HPS SlabLU p={p} n={n} ({g.n0}x{g.n1} leaves, N={g.N_reported}), Gaussian-lattice Helmholtz '
+            f'kh={cfg["kh"]:.1f}, u=1 Dirichlet; mixed precision + FP64 refinement to tol {tol:g}')
+
+
 def run_ours(args):
     import torch
     rank, world, local = dist_env()
@@ -246,14 +277,8 @@ def run_ours(args):
         ev1.record(stream)
         torch.cuda.synchronize()
     launches = L.slab_launch_count() - launches0
-    t_total = ev0.elapsed_time(ev1) / 1e3
-    if world > 1:
-        import torch.distributed as dist
-        tt = torch.tensor([t_total], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_total = float(tt)
+    t_total, value = combine_ranks(ev0.elapsed_time(ev1) / 1e3, N * args.steps, world, dev)
     clocks = clk.summary()
-    value = N * args.steps * world / t_total
 
     # ---- end-to-end through the C ABI with host buffers -----------------------
     hc = c.cpu().pin_memory()
@@ -309,9 +334,8 @@ def run_ours(args):
         metric=METRIC, value=value, unit='unknowns/s', n_gpus=world, steps=args.steps, warmup=args.warmup,
         ms_per_step=1e3 * t_total / args.steps, higher_is_better=True, scaling='weak', vs_baseline=None,
         dtype='f32+f64', data='synthetic',
-        config=dict(workload=f'HPS SlabLU p={p} n={n} ({g.n0}x{g.n1} leaves, N={N}), Gaussian-lattice Helmholtz '
-                             f'kh={cfg["kh"]:.1f}, u=1 Dirichlet; mixed precision + FP64 refinement to tol '
-                             f'{args.tol:g}', buf=g.buf, Npan=g.Npan, parallelism='replicas' if world > 1 else 'single GPU',
+        config=dict(workload=workload_name(p, n, g, cfg, args.tol), buf=g.buf, Npan=g.Npan,
+                    parallelism='replicas' if world > 1 else 'single GPU',
                     l2='inputs and factors (~17 GB) larger than L2; no flush'),
         rel_err_vs_fp64=rel_err, refine_iters=int(iters), fp64_iters=int(it64),
         fp64_value=(N / (sum(fp64_times) / len(fp64_times))) if fp64_times else None,
