@@ -190,6 +190,17 @@ size_t slab_dgemm_emu_work_bytes(int m, int n, int k);
 int slab_dgemm_emu(int m, int n, int k, double alpha, const double* d_A, int lda, const double* d_B, int ldb,
                    double beta, double* d_C, int ldc, void* d_work, size_t work_bytes, void* stream);
 
+/* Tunable launch choices of an engine (slablu_gb300/autotune.py times them):
+ *   SLAB_OPT_LEAF_CTAS   resident leaves per SM in the leaf kernel, 0 = as many
+ *                        as fit (fewer keep more of each leaf matrix in L2)
+ *   SLAB_OPT_IFACE_SOLVE interface triangular solves: 0 one thread-block cluster,
+ *                        1 grid-wide cooperative kernel
+ * set returns a status; get returns the value (or a negative status). */
+#define SLAB_OPT_LEAF_CTAS 1
+#define SLAB_OPT_IFACE_SOLVE 2
+int slab_engine_set_option(slab_engine* e, int key, int value);
+int slab_engine_get_option(const slab_engine* e, int key);
+
 /* Bytes of device memory held by the engine's factorization. */
 size_t slab_engine_factor_bytes(const slab_engine* e);
 

@@ -43,9 +43,15 @@ _SIGS = {
     'slab_leaf_dtn_noalloc': (c_int, [c_int, c_int] + [c_void] * 8 + [c_int, c_void, c_void, c_void]),
     'slab_launch_count': (c_ll, []),
     'slab_dgemm_emu_work_bytes': (c_size, [c_int, c_int, c_int]),
+    'slab_engine_set_option': (c_int, [c_void, c_int, c_int]),
+    'slab_engine_get_option': (c_int, [c_void, c_int]),
     'slab_dgemm_emu': (c_int, [c_int, c_int, c_int, c_double, c_void, c_int, c_void, c_int, c_double, c_void, c_int,
                                c_void, c_size, c_void]),
 }
+
+
+SLAB_OPT_LEAF_CTAS = 1
+SLAB_OPT_IFACE_SOLVE = 2
 
 
 class SlabError(RuntimeError):

@@ -314,6 +314,8 @@ struct EngineBase {
                          double* g22, double* g1, double* g2, double* g0) = 0;
   virtual size_t factor_bytes() const = 0;
   virtual double timing(int i) const = 0;
+  virtual int set_option(int key, int value) = 0;
+  virtual int get_option(int key) const = 0;
   long long ntot = 0, nleaf = 0;
 };
 
@@ -425,6 +427,39 @@ struct EngineImpl : EngineBase {
     return ms;
   }
   double timing(int i) const override { return i >= 0 && i < 8 ? tms[i] : 0.0; }
+
+  // Tunable launch choices (see include/slablu_gb300.h); a change drops the CUDA
+  // graphs that captured the old choice.
+  int set_option(int key, int value) override {
+    if (key == SLAB_OPT_LEAF_CTAS) {
+      if (value < 0 || value > 32) return set_error(SLAB_ERR_ARG, "leaf_ctas %d out of range", value);
+      if (value != leaf_ctas && gfac[0]) {
+        cudaGraphExecDestroy(gfac[0]);
+        gfac[0] = nullptr;
+      }
+      leaf_ctas = value;
+      return SLAB_OK;
+    }
+    if (key == SLAB_OPT_IFACE_SOLVE) {
+      if (value != 0 && value != 1) return set_error(SLAB_ERR_ARG, "iface_solve %d not 0 or 1", value);
+      const bool cl = value == 0;
+      if (cl != use_cluster_solve) {
+        for (cudaGraphExec_t* gp : {&gapp, &gapp_t})
+          if (*gp) {
+            cudaGraphExecDestroy(*gp);
+            *gp = nullptr;
+          }
+      }
+      use_cluster_solve = cl;
+      return SLAB_OK;
+    }
+    return set_error(SLAB_ERR_ARG, "unknown option %d", key);
+  }
+  int get_option(int key) const override {
+    if (key == SLAB_OPT_LEAF_CTAS) return leaf_ctas;
+    if (key == SLAB_OPT_IFACE_SOLVE) return use_cluster_solve ? 0 : 1;
+    return set_error(SLAB_ERR_ARG, "unknown option %d", key);
+  }
 
   EngineImpl(int p_, int n0_, int n1_, int buf_, cudaStream_t s_)
       : p(p_), q(p_ - 2), n((p_ - 2) * (p_ - 2)), nx(4 * (p_ - 2)), n0(n0_), n1(n1_), buf(buf_), npan(n0_ / buf_),
@@ -1515,6 +1550,16 @@ extern "C" int slab_engine_timings(const slab_engine* e, double* ms, int n) {
   const int m = n < 6 ? n : 6;
   for (int i = 0; i < m; ++i) ms[i] = e->impl->timing(i);
   return m;
+}
+
+extern "C" int slab_engine_set_option(slab_engine* e, int key, int value) {
+  if (!e) return slab::set_error(SLAB_ERR_ARG, "slab_engine_set_option: null engine");
+  return e->impl->set_option(key, value);
+}
+
+extern "C" int slab_engine_get_option(const slab_engine* e, int key) {
+  if (!e) return slab::set_error(SLAB_ERR_ARG, "slab_engine_get_option: null engine");
+  return e->impl->get_option(key);
 }
 
 extern "C" long long slab_engine_nfaces(const slab_engine* e) { return e ? e->impl->ntot : -1; }
