@@ -109,9 +109,18 @@ int getrs_small(cudaStream_t s, int n, int nrhs, const T* LU, const long long* o
   if (nrhs > 4) return set_error(SLAB_ERR_ARG, "getrs_small: nrhs %d > 4", nrhs);
   if (n > 32 * kWarpSlots) return set_error(SLAB_ERR_ARG, "getrs_small: order %d > %d", n, 32 * kWarpSlots);
   const size_t bytes = (size_t)kWarpSolveWarps * n * nrhs * sizeof(T);
-  SLAB_TRY(ensure_smem(getrs_warp_kernel<T>, bytes, "getrs_small"));
-  getrs_warp_kernel<T><<<ceil_div(batch, kWarpSolveWarps), 32 * kWarpSolveWarps, bytes, s>>>(
-      n, nrhs, LU, offLU, strideLU, lda, perm, offP, strideP, B, offB, strideB, ldb, batch);
+  auto launch = [&](auto kern) -> int {
+    SLAB_TRY(ensure_smem(kern, bytes, "getrs_small"));
+    kern<<<ceil_div(batch, kWarpSolveWarps), 32 * kWarpSolveWarps, bytes, s>>>(n, LU, offLU, strideLU, lda, perm, offP,
+                                                                               strideP, B, offB, strideB, ldb, batch);
+    return SLAB_OK;
+  };
+  switch (nrhs) {
+    case 1: SLAB_TRY(launch(getrs_warp_blocked_kernel<T, 1>)); break;
+    case 2: SLAB_TRY(launch(getrs_warp_blocked_kernel<T, 2>)); break;
+    case 3: SLAB_TRY(launch(getrs_warp_blocked_kernel<T, 3>)); break;
+    default: SLAB_TRY(launch(getrs_warp_blocked_kernel<T, 4>)); break;
+  }
   SLAB_CHECK_LAUNCH();
   return SLAB_OK;
 }

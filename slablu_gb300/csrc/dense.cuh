@@ -697,93 +697,10 @@ __global__ void __launch_bounds__(256) gemm_narrow_kernel(int m, int n, int k, T
 __global__ void perm_batched_kernel(const int* ipiv, long long strideP, int n, int batch, int* perm,
                                     long long strideQ);
 
-// Warp-per-matrix X = U^{-1} L^{-1} P B for few right-hand sides (nrhs <= 4),
-// column-oriented substitution: the vector lives in shared memory, each column
-// of L / U is streamed from global memory by the 32 lanes (coalesced).
-// One warp per batch entry, 8 warps per CTA.
+// Warp-per-matrix X = U^{-1} L^{-1} P B for few right-hand sides (nrhs <= 4):
+// one warp per batch entry, 8 warps per CTA, the vector in shared memory.
 constexpr int kWarpSolveWarps = 8;
 constexpr int kWarpSlots = 16;  // rows per lane: n <= 512
-template <typename T>
-__global__ void __launch_bounds__(32 * kWarpSolveWarps)
-    getrs_warp_kernel(int n, int nrhs, const T* __restrict__ LU, const long long* offLU, long long strideLU, int lda,
-                      const int* __restrict__ perm, const long long* offP, long long strideP, T* B,
-                      const long long* offB, long long strideB, int ldb, int batch) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int b = blockIdx.x * kWarpSolveWarps + warp;
-  if (b >= batch) return;
-  T* xs = reinterpret_cast<T*>(smem_raw) + (size_t)warp * n * nrhs;
-  const T* __restrict__ A = LU + batch_off(offLU, strideLU, b);
-  const int* pv = perm + batch_off(offP, strideP, b);
-  T* Bg = B + batch_off(offB, strideB, b);
-  for (int c = 0; c < nrhs; ++c)
-    for (int i = lane; i < n; i += 32) xs[i + c * n] = Bg[pv[i] + (size_t)c * ldb];
-  __syncwarp();
-  // forward, unit lower: column k updates rows k+1+lane+32t; the next column is
-  // loaded into registers while the current one is applied.
-  T cur[kWarpSlots], nxt[kWarpSlots];
-#pragma unroll
-  for (int t = 0; t < kWarpSlots; ++t) {
-    const int i = 1 + lane + 32 * t;
-    cur[t] = (n > 1 && i < n) ? A[i] : T(0);
-  }
-  for (int k = 0; k < n - 1; ++k) {
-    if (k + 1 < n - 1) {
-      const T* nc = A + (size_t)(k + 1) * lda;
-#pragma unroll
-      for (int t = 0; t < kWarpSlots; ++t) {
-        const int i = k + 2 + lane + 32 * t;
-        nxt[t] = i < n ? nc[i] : T(0);
-      }
-    }
-    for (int c = 0; c < nrhs; ++c) {
-      const T xk = xs[k + c * n];
-#pragma unroll
-      for (int t = 0; t < kWarpSlots; ++t) {
-        const int i = k + 1 + lane + 32 * t;
-        if (i < n) xs[i + c * n] -= cur[t] * xk;
-      }
-    }
-    __syncwarp();
-#pragma unroll
-    for (int t = 0; t < kWarpSlots; ++t) cur[t] = nxt[t];
-  }
-  // backward, upper: column k updates rows lane+32t < k
-  {
-    const T* cc = A + (size_t)(n - 1) * lda;
-#pragma unroll
-    for (int t = 0; t < kWarpSlots; ++t) {
-      const int i = lane + 32 * t;
-      cur[t] = i < n ? cc[i] : T(0);  // includes the diagonal U[k,k] at i = k
-    }
-  }
-  for (int k = n - 1; k >= 0; --k) {
-    if (k > 0) {
-      const T* nc = A + (size_t)(k - 1) * lda;
-#pragma unroll
-      for (int t = 0; t < kWarpSlots; ++t) {
-        const int i = lane + 32 * t;
-        nxt[t] = i < k ? nc[i] : T(0);
-      }
-    }
-    const T d = A[(size_t)k * lda + k];
-    for (int c = 0; c < nrhs; ++c) {
-      const T xk = xs[k + c * n] / d;
-#pragma unroll
-      for (int t = 0; t < kWarpSlots; ++t) {
-        const int i = lane + 32 * t;
-        if (i < k) xs[i + c * n] -= cur[t] * xk;
-      }
-      __syncwarp();
-      if (lane == 0) xs[k + c * n] = xk;
-    }
-    __syncwarp();
-#pragma unroll
-    for (int t = 0; t < kWarpSlots; ++t) cur[t] = nxt[t];
-  }
-  for (int c = 0; c < nrhs; ++c)
-    for (int i = lane; i < n; i += 32) Bg[i + (size_t)c * ldb] = xs[i + c * n];
-}
 
 // Warp-per-matrix X = A^{-T} B = P^T L^{-T} U^{-T} B (nrhs <= 4): dot-product
 // substitution along the columns of U (forward with U^T) and of L (backward
@@ -875,6 +792,115 @@ __global__ void __launch_bounds__(32 * kWarpSolveWarps)
   // x = P^T z: row perm[i] of x is row i of z
   for (int c = 0; c < nrhs; ++c)
     for (int i = lane; i < n; i += 32) Bg[pv[i] + (size_t)c * ldb] = xs[i + c * n];
+}
+
+// Blocked warp-per-matrix solve (NR = nrhs <= 4, n <= 32 * kWarpSlots), in the
+// elimination order of an unblocked substitution: rows in blocks of 32.
+// The diagonal triangle of a block is solved with one lane per row (the
+// block's solution stays in registers and is broadcast by shuffles), and the
+// update of the other rows runs one 32-row group at a time over all 32
+// columns of the block, so each lane has 32 independent loads of the factor in
+// flight: about n^2 / 2048 memory round trips per pass instead of n.
+template <typename T, int NR>
+__device__ __forceinline__ void warp_block_update(const T* __restrict__ A, int lda, int kb, int nb, int rbeg, int rend,
+                                                  const T (&x)[NR], T* xs, int n, int lane) {
+#pragma unroll 1
+  for (int r = rbeg + lane; r - lane < rend; r += 32) {
+    const bool ok = r < rend;
+    T a[32];
+    const T* pc = A + (size_t)kb * lda + (ok ? r : 0);
+#pragma unroll
+    for (int k = 0; k < 32; ++k) {
+      a[k] = (ok && k < nb) ? *pc : T(0);
+      pc += lda;
+    }
+    T acc[NR];
+#pragma unroll
+    for (int c = 0; c < NR; ++c) acc[c] = T(0);
+#pragma unroll
+    for (int k = 0; k < 32; ++k)
+#pragma unroll
+      for (int c = 0; c < NR; ++c) acc[c] += a[k] * __shfl_sync(0xffffffffu, x[c], k);
+    if (ok)
+#pragma unroll
+      for (int c = 0; c < NR; ++c) xs[r + c * n] -= acc[c];
+  }
+}
+
+template <typename T, int NR>
+__global__ void __launch_bounds__(32 * kWarpSolveWarps)
+    getrs_warp_blocked_kernel(int n, const T* __restrict__ LU, const long long* offLU, long long strideLU, int lda,
+                              const int* __restrict__ perm, const long long* offP, long long strideP, T* B,
+                              const long long* offB, long long strideB, int ldb, int batch) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int b = blockIdx.x * kWarpSolveWarps + warp;
+  if (b >= batch) return;
+  T* xs = reinterpret_cast<T*>(smem_raw) + (size_t)warp * n * NR;
+  const T* __restrict__ A = LU + batch_off(offLU, strideLU, b);
+  const int* pv = perm + batch_off(offP, strideP, b);
+  T* Bg = B + batch_off(offB, strideB, b);
+  for (int c = 0; c < NR; ++c)
+    for (int i = lane; i < n; i += 32) xs[i + c * n] = Bg[pv[i] + (size_t)c * ldb];
+  __syncwarp();
+  // forward, unit lower
+  for (int kb = 0; kb < n; kb += 32) {
+    const int nb = min(32, n - kb);
+    T x[NR];
+#pragma unroll
+    for (int c = 0; c < NR; ++c) x[c] = lane < nb ? xs[kb + lane + c * n] : T(0);
+    {
+      T lrow[32];
+      const T* pc = A + (size_t)kb * lda + kb + (lane < nb ? lane : 0);
+#pragma unroll
+      for (int k = 0; k < 32; ++k) {
+        lrow[k] = (k < lane && lane < nb) ? *pc : T(0);
+        pc += lda;
+      }
+#pragma unroll
+      for (int k = 0; k < 31; ++k)
+#pragma unroll
+        for (int c = 0; c < NR; ++c) x[c] -= lrow[k] * __shfl_sync(0xffffffffu, x[c], k);
+    }
+#pragma unroll
+    for (int c = 0; c < NR; ++c)
+      if (lane < nb) xs[kb + lane + c * n] = x[c];
+    warp_block_update<T, NR>(A, lda, kb, nb, kb + nb, n, x, xs, n, lane);
+    __syncwarp();
+  }
+  // backward, upper (non-unit)
+  for (int kb = ((n - 1) / 32) * 32; kb >= 0; kb -= 32) {
+    const int nb = min(32, n - kb);
+    T x[NR];
+#pragma unroll
+    for (int c = 0; c < NR; ++c) x[c] = lane < nb ? xs[kb + lane + c * n] : T(0);
+    {
+      T urow[32];
+      const T* pc = A + (size_t)kb * lda + kb + (lane < nb ? lane : 0);
+#pragma unroll
+      for (int k = 0; k < 32; ++k) {
+        urow[k] = (k > lane && k < nb) ? *pc : T(0);
+        pc += lda;
+      }
+      const T d = lane < nb ? A[(kb + lane) + (size_t)(kb + lane) * lda] : T(1);
+#pragma unroll
+      for (int k = 31; k >= 0; --k) {
+        if (k >= nb) continue;
+#pragma unroll
+        for (int c = 0; c < NR; ++c) {
+          if (lane == k) x[c] = x[c] / d;
+          x[c] -= urow[k] * __shfl_sync(0xffffffffu, x[c], k);
+        }
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < NR; ++c)
+      if (lane < nb) xs[kb + lane + c * n] = x[c];
+    warp_block_update<T, NR>(A, lda, kb, nb, 0, kb, x, xs, n, lane);
+    __syncwarp();
+  }
+  for (int c = 0; c < NR; ++c)
+    for (int i = lane; i < n; i += 32) Bg[i + (size_t)c * ldb] = xs[i + c * n];
 }
 
 // Cooperative triangular solves with one large factored matrix (FP64
