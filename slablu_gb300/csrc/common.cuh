@@ -52,6 +52,17 @@ __device__ __forceinline__ vec4<double> ld4(const double* p) {
   return {a.x, a.y, b.x, b.y};
 }
 
+// Asynchronous copy of one 4- or 8-byte element from global to shared memory
+// (cp.async, no register staging: a CTA can keep all of a tile's loads in
+// flight).  Completed by cp_async_wait_all() followed by a block barrier.
+template <typename T>
+__device__ __forceinline__ void cp_async_elem(T* sdst, const T* gsrc) {
+  static_assert(sizeof(T) == 4 || sizeof(T) == 8, "cp.async element must be 4 or 8 bytes");
+  const unsigned sa = static_cast<unsigned>(__cvta_generic_to_shared(sdst));
+  asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(sa), "l"(gsrc), "n"(sizeof(T)) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
 template <typename T>
 __device__ __forceinline__ T tabs(T v) {
   return v < T(0) ? -v : v;

@@ -180,7 +180,9 @@ __device__ void cta_panel_lu(T* P, int ldp, int m, int nb, int* piv, T* sv, int*
 // readable up to 63 rows past mrows); B transposed in shared memory
 // (element (c,k) at Bs[c + k*ldb], ldb % 4 == 0, readable up to 63 columns past
 // ncols).  C is a generic pointer (global or shared), leading dimension ldc.
-// Requires blockDim.x == 256 (16 x 16 threads, 4 x 4 outputs each).
+// Requires blockDim.x == 256 (16 x 16 threads, 4 x 4 outputs each).  Each
+// thread loads its 16 C values before the k loop, so their latency overlaps the
+// products instead of being paid once per element after it.
 template <typename T>
 __device__ void cta_gemm_sub(T* C, int ldc, int mrows, int ncols, const T* As, int lda, const T* Bs,
                              int ldb, int kd) {
@@ -203,6 +205,16 @@ __device__ void cta_gemm_sub(T* C, int ldc, int mrows, int ncols, const T* As, i
         acc[2][0] += a.z * b.x; acc[2][1] += a.z * b.y; acc[2][2] += a.z * b.z; acc[2][3] += a.z * b.w;
         acc[3][0] += a.w * b.x; acc[3][1] += a.w * b.y; acc[3][2] += a.w * b.z; acc[3][3] += a.w * b.w;
       }
+      T cv[4][4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int c = cb + 4 * tc + j;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const int r = rb + 4 * tr + i;
+          cv[i][j] = (c < ncols && r < mrows) ? C[r + (size_t)c * ldc] : T(0);
+        }
+      }
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
         const int c = cb + 4 * tc + j;
@@ -210,7 +222,7 @@ __device__ void cta_gemm_sub(T* C, int ldc, int mrows, int ncols, const T* As, i
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
           const int r = rb + 4 * tr + i;
-          if (r < mrows) C[r + (size_t)c * ldc] -= acc[i][j];
+          if (r < mrows) C[r + (size_t)c * ldc] = cv[i][j] - acc[i][j];
         }
       }
     }
@@ -218,7 +230,8 @@ __device__ void cta_gemm_sub(T* C, int ldc, int mrows, int ncols, const T* As, i
 }
 
 // Narrow variant of cta_gemm_sub for few columns (ncols <= 16): one thread per
-// row, no wasted lanes.  Same operand layout; no over-read.
+// row, no wasted lanes.  Same operand layout; no over-read.  C is loaded ahead
+// of the products, as in cta_gemm_sub.
 template <typename T>
 __device__ void cta_gemm_sub_narrow(T* C, int ldc, int mrows, int ncols, const T* As, int lda, const T* Bs,
                                     int ldb, int kd) {
@@ -254,9 +267,10 @@ __host__ __device__ inline int getrf_smem_elems(int n) {
 
 // ---------------------------------------------------------------------------
 // Blocked right-looking LU with partial pivoting of the leading n x n block of
-// the column-major n x nc matrix A (global memory, lda), applying the same row
-// operations to all nc columns.  On return A[:, :n] holds L (unit, strictly
-// lower) and U; A[:, n:] holds L^{-1} P A[:, n:]; ipiv[0..n) the pivots.
+// the column-major n x nc matrix A (global memory, lda: it is staged into
+// shared memory with cp.async), applying the same row operations to all nc
+// columns.  On return A[:, :n] holds L (unit, strictly lower) and U; A[:, n:]
+// holds L^{-1} P A[:, n:]; ipiv[0..n) the pivots.
 // *info_out = 0 or the LAPACK info of the first zero pivot.
 template <typename T>
 __device__ void cta_getrf_aug(T* A, int lda, int n, int nc, int* ipiv, T* smem, int* info_out) {
@@ -273,10 +287,9 @@ __device__ void cta_getrf_aug(T* A, int lda, int n, int nc, int* ipiv, T* smem, 
     const int m = n - k0;
     const int ldq = round_up(m, 4);
     __syncthreads();
-    for (int idx = tid; idx < m * nb; idx += blockDim.x) {
-      const int r = idx % m, c = idx / m;
-      Psm[r + c * ldq] = A[(size_t)(k0 + c) * lda + k0 + r];
-    }
+    for (int c = 0; c < nb; ++c)
+      for (int r = tid; r < m; r += blockDim.x) cp_async_elem(&Psm[r + c * ldq], &A[(size_t)(k0 + c) * lda + k0 + r]);
+    cp_async_wait_all();
     __syncthreads();
     cta_panel_lu(Psm, ldq, m, nb, piv_s, sv, si, &info_s, k0);
     for (int idx = tid; idx < m * nb; idx += blockDim.x) {
@@ -304,8 +317,9 @@ __device__ void cta_getrf_aug(T* A, int lda, int n, int nc, int* ipiv, T* smem, 
       const int ct = min(kCT, nc - c0);
       for (int idx = tid; idx < nb * ct; idx += blockDim.x) {
         const int kk = idx % nb, c = idx / nb;
-        Bt[c + kk * kCTLD] = A[(size_t)(c0 + c) * lda + k0 + kk];
+        cp_async_elem(&Bt[c + kk * kCTLD], &A[(size_t)(c0 + c) * lda + k0 + kk]);
       }
+      cp_async_wait_all();
       __syncthreads();
       // U12 = L11^{-1} A12 (unit lower), one thread per column
       for (int c = tid; c < ct; c += blockDim.x) {
@@ -330,7 +344,8 @@ __device__ void cta_getrf_aug(T* A, int lda, int n, int nc, int* ipiv, T* smem, 
 
 // ---------------------------------------------------------------------------
 // Back substitution U X = Y in place for the nr (<= kCT) columns Y = A[:, c0 : c0+nr]
-// where U is the upper triangle of A[:, :n] (global, lda).  smem as cta_getrf_aug.
+// where U is the upper triangle of A[:, :n] (global, lda; staged with cp.async).
+// smem as cta_getrf_aug.
 template <typename T>
 __device__ void cta_backsub(T* A, int lda, int n, int c0, int nr, T* smem) {
   const int tid = threadIdx.x;
@@ -343,14 +358,13 @@ __device__ void cta_backsub(T* A, int lda, int n, int c0, int nr, T* smem) {
     const int rows = k0 + nb;  // stage U[0 : k0+nb, k0 : k0+nb]
     const int ldq = round_up(rows, 4);
     __syncthreads();
-    for (int idx = tid; idx < rows * nb; idx += blockDim.x) {
-      const int r = idx % rows, c = idx / rows;
-      Psm[r + c * ldq] = A[(size_t)(k0 + c) * lda + r];
-    }
+    for (int c = 0; c < nb; ++c)
+      for (int r = tid; r < rows; r += blockDim.x) cp_async_elem(&Psm[r + c * ldq], &A[(size_t)(k0 + c) * lda + r]);
     for (int idx = tid; idx < nb * nr; idx += blockDim.x) {
       const int kk = idx % nb, c = idx / nb;
-      Bt[c + kk * kCTLD] = Y[(size_t)c * lda + k0 + kk];
+      cp_async_elem(&Bt[c + kk * kCTLD], &Y[(size_t)c * lda + k0 + kk]);
     }
+    cp_async_wait_all();
     __syncthreads();
     for (int c = tid; c < nr; c += blockDim.x) {
       for (int i = nb - 1; i >= 0; --i) {
@@ -574,6 +588,17 @@ __global__ void __launch_bounds__(256) gemm_kernel(int m, int n, int k, T alpha,
     }
     __syncthreads();
   }
+  // every C load of the thread is issued before any store (one latency, not 16)
+  T cv[4][4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const int c = c0 + 4 * tc + j;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int r = r0 + 4 * tr + i;
+      cv[i][j] = (beta != T(0) && c < n && r < m) ? C[r + (size_t)c * ldc] : T(0);
+    }
+  }
 #pragma unroll
   for (int j = 0; j < 4; ++j) {
     const int c = c0 + 4 * tc + j;
@@ -582,8 +607,7 @@ __global__ void __launch_bounds__(256) gemm_kernel(int m, int n, int k, T alpha,
     for (int i = 0; i < 4; ++i) {
       const int r = r0 + 4 * tr + i;
       if (r >= m) continue;
-      T* cp = C + r + (size_t)c * ldc;
-      *cp = (beta == T(0) ? T(0) : beta * *cp) + alpha * acc[i][j];
+      C[r + (size_t)c * ldc] = (beta == T(0) ? T(0) : beta * cv[i][j]) + alpha * acc[i][j];
     }
   }
 }
@@ -631,6 +655,16 @@ __global__ void __launch_bounds__(256) gemm32_kernel(int m, int n, int k, T alph
     }
     __syncthreads();
   }
+  T cv[2][2];
+#pragma unroll
+  for (int j = 0; j < 2; ++j) {
+    const int c = c0 + 2 * tc + j;
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+      const int r = r0 + 2 * tr + i;
+      cv[i][j] = (beta != T(0) && c < n && r < m) ? C[r + (size_t)c * ldc] : T(0);
+    }
+  }
 #pragma unroll
   for (int j = 0; j < 2; ++j) {
     const int c = c0 + 2 * tc + j;
@@ -639,8 +673,7 @@ __global__ void __launch_bounds__(256) gemm32_kernel(int m, int n, int k, T alph
     for (int i = 0; i < 2; ++i) {
       const int r = r0 + 2 * tr + i;
       if (r >= m) continue;
-      T* cp = C + r + (size_t)c * ldc;
-      *cp = (beta == T(0) ? T(0) : beta * *cp) + alpha * acc[i][j];
+      C[r + (size_t)c * ldc] = (beta == T(0) ? T(0) : beta * cv[i][j]) + alpha * acc[i][j];
     }
   }
 }

@@ -61,12 +61,20 @@ __device__ __forceinline__ double aloc_entry(const LeafCoeffs& co, int lofs, int
   return v;
 }
 
+// Shared-memory bytes of the assembly stage of leaf_factor_kernel: D and Dsq
+// (FP64) and the (i1, i2) node indices of every interior row.  They occupy
+// the start of the dynamic region, which the LU reuses once assembly is done.
+inline size_t leaf_assembly_smem_bytes(int p) {
+  const int n = (p - 2) * (p - 2);
+  return 2 * (size_t)p * p * sizeof(double) + 2 * (size_t)n;
+}
+
 // Dynamic shared memory of leaf_factor_kernel<T> for order p.
 inline size_t leaf_factor_smem_bytes(int p, size_t elem) {
   const int n = (p - 2) * (p - 2);
-  size_t b = (size_t)getrf_smem_elems(n) * elem;
-  b = (b + 15) / 16 * 16;
-  return b + 2 * (size_t)p * p * sizeof(double);
+  const size_t b = (size_t)getrf_smem_elems(n) * elem;
+  const size_t asm_b = leaf_assembly_smem_bytes(p);
+  return b > asm_b ? b : asm_b;
 }
 
 // One CTA per leaf: assemble [A_cc | A_cx], pivoted LU, S = -A_cc^{-1} A_cx,
@@ -78,27 +86,42 @@ __global__ void __launch_bounds__(kNT) leaf_factor_kernel(LeafFactorArgs<T> a) {
   const int leaf = blockIdx.x;
   const int p = a.p, q = a.q, n = a.n, nx = a.nx;
   T* smem = reinterpret_cast<T*>(smem_raw);
-  size_t off = (size_t)getrf_smem_elems(n) * sizeof(T);
-  off = (off + 15) / 16 * 16;
-  double* Dsh = reinterpret_cast<double*>(smem_raw + off);
+  double* Dsh = reinterpret_cast<double*>(smem_raw);
   double* Dsqsh = Dsh + p * p;
+  unsigned char* ri1 = reinterpret_cast<unsigned char*>(Dsqsh + p * p);  // x index of interior row r
+  unsigned char* ri2 = ri1 + n;                                          // y index
   for (int i = tid; i < p * p; i += blockDim.x) {
     Dsh[i] = a.D[i];
     Dsqsh[i] = a.Dsq[i];
+  }
+  for (int r = tid; r < n; r += blockDim.x) {
+    int i1, i2;
+    interior_node(r, q, i1, i2);
+    ri1[r] = (unsigned char)i1;
+    ri2[r] = (unsigned char)i2;
   }
   __syncthreads();
   T* G = a.G + a.strideG * leaf;
   const int lofs = leaf * p * p;
   const int nc = n + nx;
-  for (int idx = tid; idx < n * nc; idx += blockDim.x) {
-    const int r = idx % n, col = idx / n;
-    int i1, i2, j1, j2;
-    interior_node(r, q, i1, i2);
-    if (col < n)
-      interior_node(col, q, j1, j2);
-    else
-      face_node(col - n, p, q, j1, j2);
-    G[idx] = (T)aloc_entry(a.co, lofs, p, i1, i2, j1, j2, Dsh, Dsqsh);
+  // one warp per column: Aloc[Jc, col] is nonzero only on the rows that share
+  // the column node's x or y line
+  {
+    const int lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
+    for (int col = warp; col < nc; col += nwarps) {
+      int j1, j2;
+      if (col < n)
+        interior_node(col, q, j1, j2);
+      else
+        face_node(col - n, p, q, j1, j2);
+      T* gc = G + (size_t)col * n;
+      for (int r = lane; r < n; r += 32) {
+        const int i1 = ri1[r], i2 = ri2[r];
+        double v = 0.0;
+        if (i1 == j1 || i2 == j2) v = aloc_entry(a.co, lofs, p, i1, i2, j1, j2, Dsh, Dsqsh);
+        gc[r] = (T)v;
+      }
+    }
   }
   __syncthreads();
   cta_getrf_aug<T>(G, n, n, nc, a.piv + (size_t)leaf * n, smem, a.info ? a.info + leaf : nullptr);
@@ -113,14 +136,13 @@ __global__ void __launch_bounds__(kNT) leaf_factor_kernel(LeafFactorArgs<T> a) {
   for (int k0 = 0; k0 < n; k0 += kNB) {
     const int kb = min(kNB, n - k0);
     __syncthreads();
-    for (int idx = tid; idx < nx * kb; idx += blockDim.x) {
-      const int r = idx % nx, c = idx / nx;
-      Psm[r + c * ldq] = a.Nxc[r + (size_t)(k0 + c) * nx];
-    }
+    for (int c = 0; c < kb; ++c)
+      for (int r = tid; r < nx; r += blockDim.x) cp_async_elem(&Psm[r + c * ldq], &a.Nxc[r + (size_t)(k0 + c) * nx]);
     for (int idx = tid; idx < kb * nx; idx += blockDim.x) {
       const int kk = idx % kb, c = idx / kb;
-      Bt[c + kk * kCTLD] = X[(size_t)c * n + k0 + kk];
+      cp_async_elem(&Bt[c + kk * kCTLD], &X[(size_t)c * n + k0 + kk]);
     }
+    cp_async_wait_all();
     __syncthreads();
     cta_gemm_sub(dtn, nx, nx, nx, Psm, ldq, Bt, kCTLD, kb);
   }
