@@ -132,46 +132,84 @@ __device__ __forceinline__ T cta_recip(T d, T* slot) {
 // ---------------------------------------------------------------------------
 // Unblocked LU with partial pivoting of an m x nb panel held in shared memory
 // (column-major, leading dimension ldp).  piv[j] receives the panel-local row
-// swapped with row j.  The first exactly-zero (or NaN) pivot is recorded in
-// *info_s as col_offset + j + 1 (LAPACK info); elimination continues.
+// swapped with row j (largest magnitude, smallest index on ties, as LAPACK).
+// The first exactly-zero (or NaN) pivot is recorded in *info_s as
+// col_offset + j + 1 (LAPACK info); elimination continues.
+// Two block barriers per column: thread t owns the rows r = t (mod blockDim),
+// so the pivot search of column j+1 reads only values its own thread updated
+// in column j; every warp reduces the warp candidates itself; and the
+// interchange is applied inside the update from copies of the pivot row
+// (prow) and of row j (orow), each nb elements of shared memory.
 template <typename T>
-__device__ void cta_panel_lu(T* P, int ldp, int m, int nb, int* piv, T* sv, int* si, int* info_s,
-                             int col_offset) {
-  const int tid = threadIdx.x;
+__device__ void cta_panel_lu(T* P, int ldp, int m, int nb, int* piv, T* sv, int* si, T* prow, T* orow,
+                             int* info_s, int col_offset) {
+  using K = mag_t<T>;
+  static_assert(sizeof(K) == sizeof(T), "key and value share scratch");
+  K* wk = reinterpret_cast<K*>(sv);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
   for (int j = 0; j < nb && j < m; ++j) {
-    mag_t<T> best = 0;
+    K best = 0;
     int bi = INT_MAX;
-    for (int r = j + tid; r < m; r += blockDim.x) {
-      const mag_t<T> a = mag_key(P[r + j * ldp]);
+    for (int r = tid; r < m; r += blockDim.x) {
+      if (r < j) continue;
+      const K a = mag_key(P[r + j * ldp]);
       if (bi == INT_MAX || a > best) {
         best = a;
         bi = r;
       }
     }
-    int pr = cta_argmax<T>(best, bi, sv, si);
-    if (pr == INT_MAX) pr = j;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const K v2 = __shfl_xor_sync(0xffffffffu, best, o);
+      const int i2 = __shfl_xor_sync(0xffffffffu, bi, o);
+      argmax_merge(best, bi, v2, i2);
+    }
+    if (lane == 0) {
+      wk[warp] = best;
+      si[warp] = bi;
+    }
+    __syncthreads();  // (1) warp candidates; every update of column j-1 is complete
+    K v = lane < nw ? wk[lane] : K(0);
+    int wi = lane < nw ? si[lane] : INT_MAX;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const K v2 = __shfl_xor_sync(0xffffffffu, v, o);
+      const int i2 = __shfl_xor_sync(0xffffffffu, wi, o);
+      argmax_merge(v, wi, v2, i2);
+    }
+    const int pr = wi == INT_MAX ? j : wi;
     if (tid == 0) piv[j] = pr;
-    if (pr != j) {
-      for (int c = tid; c < nb; c += blockDim.x) {
-        T t = P[j + c * ldp];
-        P[j + c * ldp] = P[pr + c * ldp];
-        P[pr + c * ldp] = t;
-      }
+    for (int c = tid; c < nb; c += blockDim.x) {
+      prow[c] = P[pr + c * ldp];
+      orow[c] = P[j + c * ldp];
     }
-    __syncthreads();
-    const T d = P[j + j * ldp];
-    if (d == T(0) || d != d) {
-      if (tid == 0 && *info_s == 0) *info_s = col_offset + j + 1;
-    } else {
-      const T rd = cta_recip(d, sv + 32);
-      for (int r = j + 1 + tid; r < m; r += blockDim.x) {
-        const T l = P[r + j * ldp] * rd;
-        P[r + j * ldp] = l;
-        for (int c = j + 1; c < nb; ++c) P[r + c * ldp] -= l * P[j + c * ldp];
+    __syncthreads();  // (2) pivot row and row j copied
+    const T d = prow[j];
+    const bool ok = !(d == T(0) || d != d);
+    if (!ok && tid == 0 && *info_s == 0) *info_s = col_offset + j + 1;
+    for (int c = tid; c < nb; c += blockDim.x) P[j + c * ldp] = prow[c];
+    if (ok) {
+      const T rd = T(1) / d;
+      for (int r = tid; r < m; r += blockDim.x) {
+        if (r <= j) continue;
+        if (r == pr) {  // receives old row j, then is eliminated like the others
+          for (int c = 0; c < j; ++c) P[r + c * ldp] = orow[c];
+          const T l = orow[j] * rd;
+          P[r + j * ldp] = l;
+          for (int c = j + 1; c < nb; ++c) P[r + c * ldp] = orow[c] - l * prow[c];
+        } else {
+          const T l = P[r + j * ldp] * rd;
+          P[r + j * ldp] = l;
+          for (int c = j + 1; c < nb; ++c) P[r + c * ldp] -= l * prow[c];
+        }
       }
+    } else if (pr != j) {
+      for (int r = tid; r < m; r += blockDim.x)
+        if (r == pr)
+          for (int c = 0; c < nb; ++c) P[r + c * ldp] = orow[c];
     }
-    __syncthreads();
   }
+  __syncthreads();
 }
 
 // ---------------------------------------------------------------------------
@@ -262,7 +300,72 @@ __device__ __forceinline__ void cta_update(T* C, int ldc, int mrows, int ncols, 
 
 // Shared-memory footprint (elements of T) of cta_getrf_aug / cta_backsub for order n.
 __host__ __device__ inline int getrf_smem_elems(int n) {
-  return round_up(n, 4) * kNB + kPad + kCTLD * kNB + kPad;
+  return round_up(n, 4) * kNB + kPad + kCTLD * kNB + kPad + kNB * (kNB + 1);
+}
+
+// Inverse of the unit lower-triangular nb x nb block L11 = P[0:nb, 0:nb] of a
+// factored panel (P column-major, ldp), written to Ls[i + k*(kNB+1)] for the
+// full kNB x kNB tile (identity outside nb, zeros above the diagonal).  Lane c
+// computes column c by forward substitution, x_i = -sum_{k=c}^{i-1} L[i][k] x_k,
+// with L11 first copied row-wise into Lt (kNB x (kNB+1) scratch) so that the
+// lanes' reads fall in distinct banks.  Called by the 32 threads of one warp.
+template <typename T>
+__device__ void warp_unit_lower_inverse(const T* P, int ldp, int nb, T* Ls, T* Lt) {
+  constexpr int ld = kNB + 1;
+  const int lane = threadIdx.x & 31;
+  for (int k = 0; k < nb; ++k)
+    if (lane < nb) Lt[k + lane * ld] = P[lane + k * ldp];
+  __syncwarp();
+  const int c = lane;
+  for (int i = 0; i < kNB; ++i) {
+    T v = i == c ? T(1) : T(0);
+    if (i > c && i < nb) {
+      T s0 = T(0), s1 = T(0);
+      int k = c;
+      for (; k + 1 < i; k += 2) {
+        s0 += Lt[k + i * ld] * Ls[k + c * ld];
+        s1 += Lt[k + 1 + i * ld] * Ls[k + 1 + c * ld];
+      }
+      if (k < i) s0 += Lt[k + i * ld] * Ls[k + c * ld];
+      v = -(s0 + s1);
+    }
+    Ls[i + c * ld] = v;
+  }
+  __syncwarp();
+}
+
+// U12 = L11^{-1} B in place for the nb x ct tile B held transposed in Bt
+// (element (k, c) at Bt[c + k*kCTLD], ct <= kCT), with L11^{-1} from
+// warp_unit_lower_inverse in Ls.  8 x 32 threads own 4 x 4 output blocks; two
+// block barriers (all reads of Bt before any write).  Requires blockDim.x == 256.
+template <typename T>
+__device__ void cta_trmm_lower(const T* Ls, T* Bt, int nb, int ct) {
+  constexpr int ld = kNB + 1;
+  const int i0 = 4 * (threadIdx.x & 7), cc0 = 4 * (threadIdx.x >> 3);
+  T acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = T(0);
+  const int kend = min(nb, i0 + 4);
+  for (int k = 0; k < kend; ++k) {
+    const T l0 = Ls[i0 + k * ld], l1 = Ls[i0 + 1 + k * ld], l2 = Ls[i0 + 2 + k * ld], l3 = Ls[i0 + 3 + k * ld];
+    const vec4<T> b = ld4(Bt + cc0 + k * kCTLD);
+    acc[0][0] += l0 * b.x; acc[0][1] += l0 * b.y; acc[0][2] += l0 * b.z; acc[0][3] += l0 * b.w;
+    acc[1][0] += l1 * b.x; acc[1][1] += l1 * b.y; acc[1][2] += l1 * b.z; acc[1][3] += l1 * b.w;
+    acc[2][0] += l2 * b.x; acc[2][1] += l2 * b.y; acc[2][2] += l2 * b.z; acc[2][3] += l2 * b.w;
+    acc[3][0] += l3 * b.x; acc[3][1] += l3 * b.y; acc[3][2] += l3 * b.z; acc[3][3] += l3 * b.w;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const int c = cc0 + j;
+    if (c >= ct) continue;
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+      if (i0 + i < nb) Bt[c + (i0 + i) * kCTLD] = acc[i][j];
+  }
+  __syncthreads();
 }
 
 // ---------------------------------------------------------------------------
@@ -277,11 +380,14 @@ __device__ void cta_getrf_aug(T* A, int lda, int n, int nc, int* ipiv, T* smem, 
   __shared__ int piv_s[kNB];
   __shared__ T sv[33];
   __shared__ int si[33];
+  __shared__ T prow_s[kNB];
+  __shared__ T orow_s[kNB];
   __shared__ int info_s;
   const int tid = threadIdx.x;
   if (tid == 0) info_s = 0;
   T* Psm = smem;
   T* Bt = smem + round_up(n, 4) * kNB + kPad;
+  T* Ls = Bt + kCTLD * kNB + kPad;  // L11^{-1} of the current panel
   for (int k0 = 0; k0 < n; k0 += kNB) {
     const int nb = min(kNB, n - k0);
     const int m = n - k0;
@@ -291,7 +397,9 @@ __device__ void cta_getrf_aug(T* A, int lda, int n, int nc, int* ipiv, T* smem, 
       for (int r = tid; r < m; r += blockDim.x) cp_async_elem(&Psm[r + c * ldq], &A[(size_t)(k0 + c) * lda + k0 + r]);
     cp_async_wait_all();
     __syncthreads();
-    cta_panel_lu(Psm, ldq, m, nb, piv_s, sv, si, &info_s, k0);
+    cta_panel_lu(Psm, ldq, m, nb, piv_s, sv, si, prow_s, orow_s, &info_s, k0);
+    if (tid < 32 && k0 + nb < nc) warp_unit_lower_inverse(Psm, ldq, nb, Ls, Bt);  // Bt is free until the tile loop
+    __syncthreads();
     for (int idx = tid; idx < m * nb; idx += blockDim.x) {
       const int r = idx % m, c = idx / m;
       A[(size_t)(k0 + c) * lda + k0 + r] = Psm[r + c * ldq];
@@ -321,15 +429,7 @@ __device__ void cta_getrf_aug(T* A, int lda, int n, int nc, int* ipiv, T* smem, 
       }
       cp_async_wait_all();
       __syncthreads();
-      // U12 = L11^{-1} A12 (unit lower), one thread per column
-      for (int c = tid; c < ct; c += blockDim.x) {
-        for (int i = 1; i < nb; ++i) {
-          T s = Bt[c + i * kCTLD];
-          for (int k = 0; k < i; ++k) s -= Psm[i + k * ldq] * Bt[c + k * kCTLD];
-          Bt[c + i * kCTLD] = s;
-        }
-      }
-      __syncthreads();
+      cta_trmm_lower(Ls, Bt, nb, ct);  // U12 = L11^{-1} A12
       for (int idx = tid; idx < nb * ct; idx += blockDim.x) {
         const int kk = idx % nb, c = idx / nb;
         A[(size_t)(c0 + c) * lda + k0 + kk] = Bt[c + kk * kCTLD];

@@ -61,12 +61,13 @@ __device__ __forceinline__ double aloc_entry(const LeafCoeffs& co, int lofs, int
   return v;
 }
 
-// Shared-memory bytes of the assembly stage of leaf_factor_kernel: D and Dsq
-// (FP64) and the (i1, i2) node indices of every interior row.  They occupy
-// the start of the dynamic region, which the LU reuses once assembly is done.
+// Shared-memory bytes of the assembly stage of leaf_factor_kernel: D, Dsq and
+// the leaf's five coefficient fields (FP64, p*p each) and the (i1, i2) node
+// indices of every interior row.  They occupy the start of the dynamic region,
+// which the LU reuses once assembly is done.
 inline size_t leaf_assembly_smem_bytes(int p) {
   const int n = (p - 2) * (p - 2);
-  return 2 * (size_t)p * p * sizeof(double) + 2 * (size_t)n;
+  return 7 * (size_t)p * p * sizeof(double) + 2 * (size_t)n;
 }
 
 // Dynamic shared memory of leaf_factor_kernel<T> for order p.
@@ -86,11 +87,28 @@ __global__ void __launch_bounds__(kNT) leaf_factor_kernel(LeafFactorArgs<T> a) {
   const int leaf = blockIdx.x;
   const int p = a.p, q = a.q, n = a.n, nx = a.nx;
   T* smem = reinterpret_cast<T*>(smem_raw);
+  const int pp = p * p;
   double* Dsh = reinterpret_cast<double*>(smem_raw);
-  double* Dsqsh = Dsh + p * p;
-  unsigned char* ri1 = reinterpret_cast<unsigned char*>(Dsqsh + p * p);  // x index of interior row r
-  unsigned char* ri2 = ri1 + n;                                          // y index
-  for (int i = tid; i < p * p; i += blockDim.x) {
+  double* Dsqsh = Dsh + pp;
+  // the leaf's coefficients in shared memory: the assembly reads each of them
+  // many times, and from global memory every read would be a dependent round trip
+  double* csh = Dsqsh + pp;
+  const int lofs = leaf * pp;
+  LeafCoeffs cs{};
+  {
+    const double* src[5] = {a.co.c11, a.co.c22, a.co.c1, a.co.c2, a.co.c};
+    const double** dst[5] = {&cs.c11, &cs.c22, &cs.c1, &cs.c2, &cs.c};
+#pragma unroll
+    for (int f = 0; f < 5; ++f) {
+      if (!src[f]) continue;
+      double* d = csh + f * pp;
+      for (int i = tid; i < pp; i += blockDim.x) cp_async_elem(&d[i], &src[f][lofs + i]);
+      *dst[f] = d;
+    }
+  }
+  unsigned char* ri1 = reinterpret_cast<unsigned char*>(csh + 5 * pp);  // x index of interior row r
+  unsigned char* ri2 = ri1 + n;                                         // y index
+  for (int i = tid; i < pp; i += blockDim.x) {
     Dsh[i] = a.D[i];
     Dsqsh[i] = a.Dsq[i];
   }
@@ -100,9 +118,9 @@ __global__ void __launch_bounds__(kNT) leaf_factor_kernel(LeafFactorArgs<T> a) {
     ri1[r] = (unsigned char)i1;
     ri2[r] = (unsigned char)i2;
   }
+  cp_async_wait_all();
   __syncthreads();
   T* G = a.G + a.strideG * leaf;
-  const int lofs = leaf * p * p;
   const int nc = n + nx;
   // one warp per column: Aloc[Jc, col] is nonzero only on the rows that share
   // the column node's x or y line
@@ -117,9 +135,11 @@ __global__ void __launch_bounds__(kNT) leaf_factor_kernel(LeafFactorArgs<T> a) {
       T* gc = G + (size_t)col * n;
       for (int r = lane; r < n; r += 32) {
         const int i1 = ri1[r], i2 = ri2[r];
-        double v = 0.0;
-        if (i1 == j1 || i2 == j2) v = aloc_entry(a.co, lofs, p, i1, i2, j1, j2, Dsh, Dsqsh);
-        gc[r] = (T)v;
+        // zeros are stored as T directly: an FP64 -> FP32 conversion runs at
+        // the FP64 rate, which is 1/64 of FP32 on this GPU
+        T v = T(0);
+        if (i1 == j1 || i2 == j2) v = (T)aloc_entry(cs, 0, p, i1, i2, j1, j2, Dsh, Dsqsh);
+        gc[r] = v;
       }
     }
   }
