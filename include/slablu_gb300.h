@@ -195,9 +195,14 @@ int slab_dgemm_emu(int m, int n, int k, double alpha, const double* d_A, int lda
  *                        as fit (fewer keep more of each leaf matrix in L2)
  *   SLAB_OPT_IFACE_SOLVE interface triangular solves: 0 one thread-block cluster,
  *                        1 grid-wide cooperative kernel
+ *   SLAB_OPT_IFACE_LOOKAHEAD interface block LU (mixed precision): 1 overlaps
+ *                        each outer block's update of the columns beyond the next
+ *                        block with that block's panels (second stream), 0 serial;
+ *                        both give the same factors
  * set returns a status; get returns the value (or a negative status). */
 #define SLAB_OPT_LEAF_CTAS 1
 #define SLAB_OPT_IFACE_SOLVE 2
+#define SLAB_OPT_IFACE_LOOKAHEAD 3
 int slab_engine_set_option(slab_engine* e, int key, int value);
 int slab_engine_get_option(const slab_engine* e, int key);
 

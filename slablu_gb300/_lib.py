@@ -52,6 +52,7 @@ _SIGS = {
 
 SLAB_OPT_LEAF_CTAS = 1
 SLAB_OPT_IFACE_SOLVE = 2
+SLAB_OPT_IFACE_LOOKAHEAD = 3
 
 
 class SlabError(RuntimeError):

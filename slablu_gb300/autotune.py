@@ -20,6 +20,7 @@ from . import _lib
 TUNABLES = {
     'leaf_ctas': (_lib.SLAB_OPT_LEAF_CTAS, (0, 2, 1)),
     'iface_solve': (_lib.SLAB_OPT_IFACE_SOLVE, (0, 1)),
+    'iface_lookahead': (_lib.SLAB_OPT_IFACE_LOOKAHEAD, (1, 0)),
 }
 
 
@@ -79,6 +80,14 @@ def _time_leaf(engine, coeffs, reps):
     return best
 
 
+def _time_interface(engine, coeffs, reps):
+    best = float('inf')
+    for _ in range(reps):
+        engine.factor(**coeffs)
+        best = min(best, engine.timings()['interface_ms'])
+    return best
+
+
 def _time_apply(engine, bnd, reps):
     best = float('inf')
     for _ in range(reps):
@@ -109,6 +118,15 @@ def tune(engine, coeffs, bnd, reps=2, use_cache=True, path=None):
     picks['leaf_ctas'] = min(cands, key=lambda v: (t_leaf[v], cands.index(v)))
     timings['leaf_ms'] = {str(v): t for v, t in t_leaf.items()}
     _lib.check(engine.L.slab_engine_set_option(engine.h, key, picks['leaf_ctas']), 'slab_engine_set_option')
+    if engine.geom.Npan > 1 and engine.precision == 'mixed':
+        key, cands = TUNABLES['iface_lookahead']
+        t_if = {}
+        for v in cands:
+            _lib.check(engine.L.slab_engine_set_option(engine.h, key, v), 'slab_engine_set_option')
+            t_if[v] = _time_interface(engine, coeffs, reps)
+        picks['iface_lookahead'] = min(cands, key=lambda v: (t_if[v], cands.index(v)))
+        timings['interface_ms'] = {str(v): t for v, t in t_if.items()}
+        _lib.check(engine.L.slab_engine_set_option(engine.h, key, picks['iface_lookahead']), 'slab_engine_set_option')
     engine.factor(**coeffs)
     key, cands = TUNABLES['iface_solve']
     if engine.geom.Npan > 1:

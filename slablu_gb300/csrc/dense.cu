@@ -421,7 +421,8 @@ int getrs_batched(cudaStream_t s, int n, int nrhs, const T* LU, const long long*
 
 namespace {
 // Panel factorization: distributed shared memory of one 16-CTA (or 8-CTA)
-// cluster when the panel and its row maps fit, the global-memory kernel otherwise.
+// cluster (one panel row per thread) when the panel fits, the global-memory
+// kernel otherwise.
 template <typename T>
 int panel_factor(cudaStream_t s, T* A, int lda, int n, int k0, int nb, int* ipiv, int* info, T* linv,
                  bool* linv_done) {
@@ -432,7 +433,7 @@ int panel_factor(cudaStream_t s, T* A, int lda, int n, int k0, int nb, int* ipiv
   int CL = cluster_size_for(kern, panel_cluster_smem_bytes(m, nb, ceil_div(m, 16), sizeof(T)), 256);
   int R = ceil_div(m, CL);
   size_t bytes = panel_cluster_smem_bytes(m, nb, R, sizeof(T));
-  if (bytes <= lim && m >= CL && m >= nb) {
+  if (bytes <= lim && m >= CL && m >= nb && R <= 256 && CL <= 16 && nb <= kNB) {
     void* args[] = {(void*)&A, (void*)&lda, (void*)&n, (void*)&k0, (void*)&nb, (void*)&R, (void*)&ipiv,
                     (void*)&info, (void*)&linv};
     SLAB_TRY(launch_cluster(kern, CL, 256, bytes, s, args));
@@ -481,6 +482,68 @@ int biglu_panel_swap(cudaStream_t s, T* A, int lda, int n, int k0, int nb, int* 
   }
   return SLAB_OK;
 }
+template <typename T>
+int biglu_panel_swap_range(cudaStream_t s, T* A, int lda, int n, int k0, int nb, int c_lo, int c_hi, int* ipiv,
+                           int* info, T* linv, bool* linv_done) {
+  SLAB_TRY(panel_factor<T>(s, A, lda, n, k0, nb, ipiv, info, linv, linv_done));
+  const int ncols = (c_hi - c_lo) - nb;  // the panel lies inside [c_lo, c_hi)
+  if (ncols > 0) {
+    swap_cols_kernel<T><<<ceil_div(ncols, 128), 128, 0, s>>>(A, lda, c_lo, c_hi, k0, nb, ipiv);
+    SLAB_CHECK_LAUNCH();
+  }
+  return SLAB_OK;
+}
+template int biglu_panel_swap_range<double>(cudaStream_t, double*, int, int, int, int, int, int, int*, int*, double*,
+                                            bool*);
+
+__global__ void rowperm_build_kernel(const int* ipiv, int k0, int npiv, int n, int* out) {
+  extern __shared__ int src[];  // src[i]: source row of row k0 + i
+  __shared__ int cnt;
+  const int m = n - k0;
+  for (int i = threadIdx.x; i < m; i += blockDim.x) src[i] = k0 + i;
+  if (threadIdx.x == 0) cnt = 0;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int j = 0; j < npiv; ++j) {
+      const int a = j, b = ipiv[k0 + j] - k0;
+      if (b != a && b >= 0 && b < m) {
+        const int t = src[a];
+        src[a] = src[b];
+        src[b] = t;
+      }
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < m; i += blockDim.x) {
+    if (src[i] != k0 + i) {
+      const int t = atomicAdd(&cnt, 1);
+      if (t < kRowpermMax) {
+        out[1 + 2 * t] = k0 + i;
+        out[2 + 2 * t] = src[i];
+      }
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) out[0] = cnt < kRowpermMax ? cnt : kRowpermMax;
+}
+
+template <typename T>
+int laswp_gather(cudaStream_t s, T* A, int lda, int n, int k0, int npiv, const int* ipiv, int lo1, int hi1, int lo2,
+                 int hi2, int* perm) {
+  if (npiv <= 0) return SLAB_OK;
+  if (2 * npiv > kRowpermMax) return set_error(SLAB_ERR_ARG, "laswp_gather: %d interchanges exceed %d", npiv, kRowpermMax / 2);
+  const int ncols = max(0, hi1 - lo1) + max(0, hi2 - lo2);
+  if (ncols <= 0) return SLAB_OK;
+  const size_t bytes = (size_t)(n - k0) * sizeof(int);
+  SLAB_TRY(ensure_smem(rowperm_build_kernel, bytes, "laswp_gather"));
+  rowperm_build_kernel<<<1, 256, bytes, s>>>(ipiv, k0, npiv, n, perm);
+  SLAB_CHECK_LAUNCH();
+  rowperm_apply_kernel<T><<<ceil_div(ncols, kRowpermCols), 256, 0, s>>>(A, lda, lo1, hi1, lo2, hi2, perm);
+  SLAB_CHECK_LAUNCH();
+  return SLAB_OK;
+}
+template int laswp_gather<double>(cudaStream_t, double*, int, int, int, int, const int*, int, int, int, int, int*);
+
 template int biglu_panel_swap<float>(cudaStream_t, float*, int, int, int, int, int*, int*, float*, bool*);
 template int biglu_panel_swap<double>(cudaStream_t, double*, int, int, int, int, int*, int*, double*, bool*);
 

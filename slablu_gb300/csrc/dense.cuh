@@ -1473,19 +1473,49 @@ __global__ void __launch_bounds__(1024) biglu_panel_kernel(T* A, int lda, int n,
 
 // Panel factorization held in the distributed shared memory of one thread-block
 // cluster of CL CTAs: CTA r keeps physical panel rows [r*R, (r+1)*R) of the
-// m x nb panel (rows k0.. of columns k0..k0+nb).  Row interchanges are not
-// moved in memory: every CTA keeps the same logical -> physical row map (and
-// each CTA the logical index of its own rows), so one column costs one
-// cluster barrier: local argmax over rows with logical index >= j, exchange of
-// the CL candidates (double-buffered) through DSMEM, pivot row read from its
-// owner through DSMEM, interchange recorded in the maps, rank-1 update of the
-// local rows below the pivot spread over (row, column) pairs.  The pivot
-// sequence is LAPACK's (largest magnitude, smallest logical index on ties).
-// At the end each CTA writes its rows to their logical positions, and CTA 0
-// gathers the unit-lower nb x nb triangle and writes its inverse to linv.
+// m x nb panel (rows k0.. of columns k0..k0+nb), one row per thread (R <= 256).
+// Rows never move: each thread keeps the logical index of its row in a
+// register.  One column j costs one cluster barrier, split into arrive and wait:
+//   1. every CTA finds its best candidate (largest magnitude, smallest logical
+//      index on ties) among its rows with logical index >= j and pushes it --
+//      key, logical index, physical row and the row's nb values -- into a
+//      mailbox slot of every CTA of the cluster (DSMEM stores);
+//   2. arrive; while the barrier completes, each thread applies the previous
+//      pivot's update to columns j+1.. of its row (the update is deferred by
+//      one column: only column j has to be current for the search);
+//   3. wait; every warp reduces the CL candidates from its own CTA's mailbox,
+//      so the pivot row is read from local shared memory; each thread relabels
+//      its row for the interchange, forms its multiplier and updates column j+1.
+// The pushed candidate row already includes the deferred update, computed by
+// the pusher from the owner's multiplier.  Mailboxes are triple-buffered: a
+// CTA pushes column j+1 only after the barrier of column j, which every thread
+// reaches only after the deferred update that still reads the pivot row of
+// column j-1.  The pivot sequence is LAPACK's.  At the end each thread writes
+// its row to its logical position, and CTA 0 gathers the unit-lower nb x nb
+// triangle (pushed by the owners) and writes its inverse to linv.
 // Shared memory: see panel_cluster_smem_bytes.  grid = CL (one cluster).
 __host__ __device__ inline size_t panel_cluster_smem_bytes(int m, int nb, int R, size_t elem) {
-  return ((size_t)R * nb + R + nb + 2 * (size_t)nb * (nb + 1)) * elem + ((size_t)R + m) * sizeof(int);
+  (void)m;
+  constexpr int kCLMax = 16;
+  return ((size_t)R * nb + R + 3 * (size_t)kCLMax * nb + 2 * (size_t)nb * (nb + 1)) * elem +
+         3 * (size_t)kCLMax * (elem + 2 * sizeof(int));
+}
+
+__device__ __forceinline__ void cluster_arrive_release() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n" ::: "memory");
+}
+__device__ __forceinline__ void cluster_wait_acquire() {
+  asm volatile("barrier.cluster.wait.acquire.aligned;\n" ::: "memory");
+}
+
+// (key, logical index, slot) candidate merge with the LAPACK tie-break.
+template <typename K>
+__device__ __forceinline__ void argmax_merge3(K& v, int& i, int& sl, K v2, int i2, int s2) {
+  if (v2 > v || (v2 == v && i2 < i)) {
+    v = v2;
+    i = i2;
+    sl = s2;
+  }
 }
 
 template <typename T>
@@ -1493,172 +1523,158 @@ __global__ void __launch_bounds__(256) biglu_panel_cluster_kernel(T* A, int lda,
                                                                   int* ipiv, int* info, T* linv) {
   namespace cg = cooperative_groups;
   cg::cluster_group cluster = cg::this_cluster();
+  using K = mag_t<T>;
+  constexpr int kCLMax = 16;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int m = n - k0;
   const int ldx = nb + 1;
-  T* P = reinterpret_cast<T*>(smem_raw);  // R x nb, ld R (physical rows)
-  T* lcol = P + (size_t)R * nb;            // R: multipliers of the current column
-  T* prow = lcol + R;                      // nb: pivot row
-  T* Ls = prow + nb;                       // nb x nb, ld nb+1: gathered L11 (CTA 0)
-  T* Xs = Ls + (size_t)nb * ldx;           // nb x nb, ld nb+1: its inverse
-  int* lrow = reinterpret_cast<int*>(Xs + (size_t)nb * ldx);  // R: logical index of each local row
-  int* map = lrow + R;                     // m: logical row -> physical row (rank * R + slot)
-  using K = mag_t<T>;
-  __shared__ K cand_v[2];
-  __shared__ int cand_i[2];
-  __shared__ T sv[33];
-  __shared__ int si[33];
+  T* P = reinterpret_cast<T*>(smem_raw);    // R x nb, ld R (physical rows)
+  T* lcol = P + (size_t)R * nb;              // R: each row's multiplier of the previous column
+  T* mrow = lcol + R;                        // [3][kCLMax][nb] pushed candidate rows
+  T* Ls = mrow + 3 * kCLMax * nb;            // nb x nb, ld nb+1: gathered L11 (CTA 0)
+  T* Xs = Ls + (size_t)nb * ldx;             // nb x nb, ld nb+1: its inverse
+  K* mkey = reinterpret_cast<K*>(Xs + (size_t)nb * ldx);  // [3][kCLMax]
+  int* mli = reinterpret_cast<int*>(mkey + 3 * kCLMax);    // [3][kCLMax] logical index
+  int* mph = mli + 3 * kCLMax;                              // [3][kCLMax] physical row
+  __shared__ K wk[8];
+  __shared__ int wi[8];
+  __shared__ int ws[8];
   const int CL = (int)cluster.num_blocks();
   const int rk = (int)cluster.block_rank();
-  const int tid = threadIdx.x;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
   const int g0 = rk * R;
   const int rows = max(0, min(R, m - g0));
-  for (int idx = tid; idx < rows * nb; idx += blockDim.x) {
-    const int i = idx % rows, c = idx / rows;
-    P[i + (size_t)c * R] = A[(size_t)(k0 + c) * lda + k0 + g0 + i];
-  }
-  for (int i = tid; i < rows; i += blockDim.x) lrow[i] = g0 + i;
-  for (int i = tid; i < m; i += blockDim.x) map[i] = i;
-  __syncthreads();
-  __shared__ K wk[32];
-  __shared__ int wi_s[32];
-  __shared__ T rd_s;
-  const int lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
+  const bool own = tid < rows;
+  for (int c = 0; c < nb; ++c)
+    for (int i = tid; i < rows; i += blockDim.x) cp_async_elem(&P[i + (size_t)c * R], &A[(size_t)(k0 + c) * lda + k0 + g0 + i]);
+  cp_async_wait_all();
+  int my_li = own ? g0 + tid : INT_MAX;
+  T l_prev = T(0);              // this row's multiplier of the previous pivot (0: none)
+  const T* prow_prev = nullptr;  // previous pivot row (mailbox)
+  cluster.sync();  // every CTA of the cluster runs before the first DSMEM store
   for (int j = 0; j < nb && j < m; ++j) {
-    // local candidate: rows of this CTA with logical index >= j.  The thread
-    // scanning row i is the one that updated P[i, j] in the previous column
-    // (pair index i below), so no barrier is needed before the scan.
+    const int buf = j % 3;
+    // (a) local candidate among this thread's row, then the warp's and the CTA's
     K best = 0;
-    int bi = INT_MAX;
-    for (int i = tid; i < rows; i += blockDim.x) {
-      const int li = lrow[i];
-      if (li < j) continue;
-      const K a = mag_key(P[i + (size_t)j * R]);
-      if (a > best || (a == best && li < bi)) {
-        best = a;
-        bi = li;
-      }
+    int bi = INT_MAX, bs = -1;
+    if (own && my_li >= j) {
+      best = mag_key(P[tid + (size_t)j * R]);
+      bi = my_li;
+      bs = tid;
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-      const K v2 = __shfl_down_sync(0xffffffffu, best, o);
-      const int i2 = __shfl_down_sync(0xffffffffu, bi, o);
-      argmax_merge(best, bi, v2, i2);
+      const K v2 = __shfl_xor_sync(0xffffffffu, best, o);
+      const int i2 = __shfl_xor_sync(0xffffffffu, bi, o);
+      const int s2 = __shfl_xor_sync(0xffffffffu, bs, o);
+      argmax_merge3(best, bi, bs, v2, i2, s2);
     }
     if (lane == 0) {
       wk[warp] = best;
-      wi_s[warp] = bi;
+      wi[warp] = bi;
+      ws[warp] = bs;
     }
-    __syncthreads();  // (1) warp candidates; also orders lrow updates of the previous column
+    if (own) lcol[tid] = l_prev;
+    __syncthreads();  // (1) warp candidates and multipliers
     if (warp == 0) {
       K v = lane < nwarps ? wk[lane] : K(0);
-      int i = lane < nwarps ? wi_s[lane] : INT_MAX;
+      int i = lane < nwarps ? wi[lane] : INT_MAX;
+      int sl = lane < nwarps ? ws[lane] : -1;
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
-        const K v2 = __shfl_down_sync(0xffffffffu, v, o);
-        const int i2 = __shfl_down_sync(0xffffffffu, i, o);
-        argmax_merge(v, i, v2, i2);
+        const K v2 = __shfl_xor_sync(0xffffffffu, v, o);
+        const int i2 = __shfl_xor_sync(0xffffffffu, i, o);
+        const int s2 = __shfl_xor_sync(0xffffffffu, sl, o);
+        argmax_merge3(v, i, sl, v2, i2, s2);
       }
-      if (lane == 0) {
-        cand_i[j & 1] = i;
-        cand_v[j & 1] = v;
+      // push the candidate to slot rk of every CTA's mailbox
+      if (i != INT_MAX && lane < nb) {
+        T x = P[sl + (size_t)lane * R];
+        if (prow_prev && lane > j) x -= lcol[sl] * prow_prev[lane];
+        for (int q = 0; q < CL; ++q) *cluster.map_shared_rank(&mrow[(buf * kCLMax + rk) * nb + lane], q) = x;
+      }
+      if (lane < CL) {
+        *cluster.map_shared_rank(&mkey[buf * kCLMax + rk], lane) = v;
+        *cluster.map_shared_rank(&mli[buf * kCLMax + rk], lane) = i;
+        *cluster.map_shared_rank(&mph[buf * kCLMax + rk], lane) = i == INT_MAX ? -1 : g0 + sl;
       }
     }
-    cluster.sync();  // candidates published; every update of column j-1 is complete
-    // every warp reduces the CL candidates itself (lane q reads CTA q's)
-    K v = 0;
-    int wi = INT_MAX;
-    if (lane < CL) {
-      wi = *cluster.map_shared_rank(&cand_i[j & 1], lane);
-      v = *cluster.map_shared_rank(&cand_v[j & 1], lane);
-    }
+    __syncthreads();  // (2) the candidate row is read before its owner updates it below
+    cluster_arrive_release();
+    // (b) deferred update of the previous pivot on columns j+1.. of this row
+    if (own && l_prev != T(0))
+      for (int c = j + 1; c < nb; ++c) P[tid + (size_t)c * R] -= l_prev * prow_prev[c];
+    cluster_wait_acquire();
+    // (c) every warp reduces the CL candidates of its own mailbox
+    K v = lane < CL ? mkey[buf * kCLMax + lane] : K(0);
+    int wli = lane < CL ? mli[buf * kCLMax + lane] : INT_MAX;
+    int wq = lane;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
       const K v2 = __shfl_xor_sync(0xffffffffu, v, o);
-      const int i2 = __shfl_xor_sync(0xffffffffu, wi, o);
-      argmax_merge(v, wi, v2, i2);
+      const int i2 = __shfl_xor_sync(0xffffffffu, wli, o);
+      const int s2 = __shfl_xor_sync(0xffffffffu, wq, o);
+      argmax_merge3(v, wli, wq, v2, i2, s2);
     }
-    const int piv = wi == INT_MAX ? j : wi;
-    const int php = map[piv], phj = map[j];
-    {
-      const T* src = cluster.map_shared_rank(P, php / R);
-      for (int c = tid; c < nb; c += blockDim.x) {
-        const T x = src[(php % R) + (size_t)c * R];
-        prow[c] = x;
-        if (c == j) rd_s = mag_key(x) == 0 ? T(0) : recip_newton(x);
+    const int piv = wli == INT_MAX ? j : wli;
+    const T* prow = &mrow[(buf * kCLMax + (wli == INT_MAX ? 0 : wq)) * nb];
+    const int php = wli == INT_MAX ? -1 : mph[buf * kCLMax + wq];
+    if (rk == 0 && tid == 0) ipiv[k0 + j] = k0 + piv;
+    const bool ok = wli != INT_MAX && mag_key(prow[j]) != 0;  // zero or NaN pivot: integer test
+    if (!ok && rk == 0 && tid == 0 && info && *info == 0) *info = k0 + j + 1;
+    T rd = T(0);
+    if (ok) {
+      if (lane == 0) rd = recip_newton(prow[j]);
+      rd = __shfl_sync(0xffffffffu, rd, 0);
+    }
+    // (d) interchange (labels only), multiplier, update of column j+1
+    l_prev = T(0);
+    if (own) {
+      if (g0 + tid == php)
+        my_li = j;
+      else if (my_li == j)
+        my_li = piv;
+      if (ok && my_li > j) {
+        const T l = P[tid + (size_t)j * R] * rd;
+        P[tid + (size_t)j * R] = l;
+        if (j + 1 < nb) P[tid + (size_t)(j + 1) * R] -= l * prow[j + 1];
+        l_prev = l;
       }
     }
-    __syncthreads();  // (2) pivot row and its reciprocal; every map read of this column done
-    if (tid == 0) {
-      map[j] = php;
-      map[piv] = phj;
-      if (rk == php / R) lrow[php % R] = j;
-      if (piv != j && rk == phj / R) lrow[phj % R] = piv;
-      if (rk == 0) ipiv[k0 + j] = k0 + piv;
-    }
-    if (mag_key(prow[j]) == 0) {  // zero or NaN pivot (integer test: no FP64 compare)
-      if (rk == 0 && tid == 0 && info && *info == 0) *info = k0 + j + 1;
-      __syncthreads();  // uniform branch: keeps the barrier count of the other path
-    } else {
-      const T rd = rd_s;
-      // logical index after this column's interchange, without waiting for thread 0
-      for (int i = tid; i < rows; i += blockDim.x) {
-        const int ph = g0 + i;
-        const int li = ph == php ? j : (ph == phj ? piv : lrow[i]);
-        T l = T(0);
-        if (li > j) {
-          l = P[i + (size_t)j * R] * rd;
-          P[i + (size_t)j * R] = l;
-        }
-        lcol[i] = l;
-      }
-      __syncthreads();  // (3) multipliers
-      const int ncol = nb - j - 1;
-      for (int idx = tid; idx < rows * ncol; idx += blockDim.x) {
-        const int i = idx % rows, c = j + 1 + idx / rows;
-        P[i + (size_t)c * R] -= lcol[i] * prow[c];
-      }
-    }
+    prow_prev = prow;
   }
-  cluster.sync();
-  for (int idx = tid; idx < rows * nb; idx += blockDim.x) {
-    const int i = idx % rows, c = idx / rows;
-    A[(size_t)(k0 + c) * lda + k0 + lrow[i]] = P[i + (size_t)c * R];
-  }
+  // every update of this thread's row is its own: write it back
+  if (own)
+    for (int c = 0; c < nb; ++c) A[(size_t)(k0 + c) * lda + k0 + my_li] = P[tid + (size_t)c * R];
   if (linv && nb <= m) {
+    // owners of logical rows 0..nb-1 push their first nb values to CTA 0
+    if (own && my_li < nb)
+      for (int c = 0; c < nb; ++c) *cluster.map_shared_rank(&Ls[my_li + (size_t)c * ldx], 0) = P[tid + (size_t)c * R];
+    cluster.sync();
     if (rk == 0) {
-      for (int idx = tid; idx < nb * nb; idx += blockDim.x) {
-        const int l = idx % nb, c = idx / nb;
-        const int ph = map[l];
-        Ls[l + (size_t)c * ldx] = *(cluster.map_shared_rank(P, ph / R) + (ph % R) + (size_t)c * R);
-      }
-      __syncthreads();
       // L11^{-1} by forward substitution, one warp per group of columns and one
       // lane per row (nb <= 32): step k broadcasts x[k] and updates rows i > k,
       // so the dependent chain is nb steps long for all the warp's columns at once.
-      {
-        constexpr int kCols = 4;
-        for (int c0 = warp * kCols; c0 < nb; c0 += nwarps * kCols) {
-          T x[kCols];
+      constexpr int kCols = 4;
+      for (int c0 = warp * kCols; c0 < nb; c0 += nwarps * kCols) {
+        T x[kCols];
 #pragma unroll
-          for (int q = 0; q < kCols; ++q) x[q] = lane == c0 + q ? T(1) : T(0);
-          for (int k = c0; k < nb - 1; ++k) {
-            const T lik = lane > k && lane < nb ? Ls[lane + (size_t)k * ldx] : T(0);
+        for (int q = 0; q < kCols; ++q) x[q] = lane == c0 + q ? T(1) : T(0);
+        for (int k = c0; k < nb - 1; ++k) {
+          const T lik = lane > k && lane < nb ? Ls[lane + (size_t)k * ldx] : T(0);
 #pragma unroll
-            for (int q = 0; q < kCols; ++q) {
-              const T xk = __shfl_sync(0xffffffffu, x[q], k);
-              x[q] -= lik * xk;
-            }
+          for (int q = 0; q < kCols; ++q) {
+            const T xk = __shfl_sync(0xffffffffu, x[q], k);
+            x[q] -= lik * xk;
           }
-#pragma unroll
-          for (int q = 0; q < kCols; ++q)
-            if (c0 + q < nb && lane < nb) Xs[lane + (size_t)(c0 + q) * ldx] = x[q];
         }
+#pragma unroll
+        for (int q = 0; q < kCols; ++q)
+          if (c0 + q < nb && lane < nb) Xs[lane + (size_t)(c0 + q) * ldx] = x[q];
       }
       __syncthreads();
       for (int idx = tid; idx < nb * nb; idx += blockDim.x) linv[idx] = Xs[(idx % nb) + (idx / nb) * ldx];
     }
-    cluster.sync();  // no CTA leaves while CTA 0 may still read its rows
   }
 }
 
@@ -1746,6 +1762,58 @@ __global__ void biglu_swap_kernel(T* A, int lda, int ncols_total, int k0, int nb
       cp[k0 + j] = cp[pr];
       cp[pr] = t;
     }
+  }
+}
+
+// Row interchanges ipiv[k0 .. k0+nb) of one panel applied to the columns
+// [c_lo, k0) and [k0+nb, c_hi) (one thread per column).
+template <typename T>
+__global__ void swap_cols_kernel(T* A, int lda, int c_lo, int c_hi, int k0, int nb, const int* ipiv) {
+  const int c = c_lo + blockIdx.x * blockDim.x + threadIdx.x;
+  const int col = c < k0 ? c : c + nb;
+  if (col >= c_hi) return;
+  T* cp = A + (size_t)col * lda;
+  for (int j = 0; j < nb; ++j) {
+    const int pr = ipiv[k0 + j];
+    if (pr != k0 + j) {
+      T t = cp[k0 + j];
+      cp[k0 + j] = cp[pr];
+      cp[pr] = t;
+    }
+  }
+}
+
+// Net effect of the interchanges ipiv[k0 .. k0+npiv) (LAPACK order, rows of an
+// n-row matrix) as a gather: out[0] = count, then count (destination, source)
+// row pairs at out[1 + 2t], out[2 + 2t] (count <= 2 npiv).  One CTA; dynamic
+// shared memory (n - k0) ints.
+__global__ void rowperm_build_kernel(const int* ipiv, int k0, int npiv, int n, int* out);
+
+// Applies a gather from rowperm_build_kernel to the columns [lo1, hi1) and
+// [lo2, hi2) of A: every value of a column is read before any is written.
+// kRowpermCols columns per CTA.
+constexpr int kRowpermCols = 8;
+constexpr int kRowpermMax = 2 * 256;
+template <typename T>
+__global__ void __launch_bounds__(256) rowperm_apply_kernel(T* A, int lda, int lo1, int hi1, int lo2, int hi2,
+                                                            const int* perm) {
+  __shared__ T vals[kRowpermMax * kRowpermCols];
+  const int cnt = min(perm[0], kRowpermMax);
+  const int n1 = max(0, hi1 - lo1);
+  const int ncols = n1 + max(0, hi2 - lo2);
+  const int cbase = blockIdx.x * kRowpermCols;
+  const int nc = min(kRowpermCols, ncols - cbase);
+  if (nc <= 0) return;
+  for (int idx = threadIdx.x; idx < cnt * nc; idx += blockDim.x) {
+    const int t = idx % cnt, ci = cbase + idx / cnt;
+    const int col = ci < n1 ? lo1 + ci : lo2 + (ci - n1);
+    vals[idx] = A[(size_t)col * lda + perm[2 + 2 * t]];
+  }
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < cnt * nc; idx += blockDim.x) {
+    const int t = idx % cnt, ci = cbase + idx / cnt;
+    const int col = ci < n1 ? lo1 + ci : lo2 + (ci - n1);
+    A[(size_t)col * lda + perm[1 + 2 * t]] = vals[idx];
   }
 }
 
@@ -1867,6 +1935,19 @@ int trsv_coop(cudaStream_t s, const T* LU, int lda, int n, const int* perm, cons
 template <typename T>
 int biglu_panel_swap(cudaStream_t s, T* A, int lda, int n, int k0, int nb, int* ipiv, int* info, T* linv,
                      bool* linv_done);
+
+// Panel factorization of columns [k0, k0+nb) (as biglu_panel_swap) with the
+// interchanges applied only to the columns [c_lo, c_hi) outside the panel.
+template <typename T>
+int biglu_panel_swap_range(cudaStream_t s, T* A, int lda, int n, int k0, int nb, int c_lo, int c_hi, int* ipiv,
+                           int* info, T* linv, bool* linv_done);
+
+// Interchanges ipiv[k0 .. k0+npiv) (npiv <= 256) applied to the columns
+// [lo1, hi1) and [lo2, hi2) of the n-row matrix A through a gather; perm:
+// 1 + 2 * kRowpermMax ints of scratch.
+template <typename T>
+int laswp_gather(cudaStream_t s, T* A, int lda, int n, int k0, int npiv, const int* ipiv, int lo1, int hi1, int lo2,
+                 int hi2, int* perm);
 
 // X[k0:k0+nb, 0:ncols] = Inv X[k0:k0+nb, 0:ncols] with Inv a bs x bs inverted
 // diagonal triangle (tri_inv_blocks layout, column-major, ld bs).

@@ -322,9 +322,15 @@ struct EngineBase {
 template <typename T, typename TI>
 struct EngineImpl : EngineBase {
   int p, q, n, nx, n0, n1, buf, npan;
-  cudaStream_t s = nullptr;      // engine-owned stream (captured into graphs)
+  cudaStream_t s = nullptr;      // engine-owned stream (captured into graphs), high priority
   cudaStream_t us = nullptr;     // caller's stream
   cudaEvent_t join = nullptr;
+  // interface LU lookahead: updates beyond the next outer block on a second,
+  // low-priority stream (forked from and joined back into s)
+  cudaStream_t side = nullptr;
+  cudaEvent_t la_fork = nullptr, la_join = nullptr;
+  DevBuf laPerm;
+  bool use_lookahead = true;
   cudaGraphExec_t gfac[3] = {nullptr, nullptr, nullptr}, gapp = nullptr, gapp_t = nullptr;
   int gapp_nrhs = 0, gapp_t_nrhs = 0;
   bool use_graphs = true;
@@ -375,6 +381,12 @@ struct EngineImpl : EngineBase {
     for (auto& e : ev)
       if (e) cudaEventDestroy(e);
     if (join) cudaEventDestroy(join);
+    if (la_fork) cudaEventDestroy(la_fork);
+    if (la_join) cudaEventDestroy(la_join);
+    if (side) {
+      cudaStreamSynchronize(side);
+      cudaStreamDestroy(side);
+    }
     if (s) cudaStreamDestroy(s);
   }
   // order the engine stream after the caller's stream (and back)
@@ -406,7 +418,8 @@ struct EngineImpl : EngineBase {
         return st;
       }
       if (ce != cudaSuccess) return set_error(SLAB_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ce));
-      const cudaError_t ie = cudaGraphInstantiate(&exec, g, 0);
+      // node priorities: the lookahead's side-stream work yields SMs to the panels
+      const cudaError_t ie = cudaGraphInstantiate(&exec, g, cudaGraphInstantiateFlagUseNodePriority);
       cudaGraphDestroy(g);
       if (ie != cudaSuccess) {
         exec = nullptr;
@@ -440,6 +453,15 @@ struct EngineImpl : EngineBase {
       leaf_ctas = value;
       return SLAB_OK;
     }
+    if (key == SLAB_OPT_IFACE_LOOKAHEAD) {
+      if (value != 0 && value != 1) return set_error(SLAB_ERR_ARG, "iface_lookahead %d not 0 or 1", value);
+      if ((value == 1) != use_lookahead && gfac[2]) {
+        cudaGraphExecDestroy(gfac[2]);
+        gfac[2] = nullptr;
+      }
+      use_lookahead = value == 1;
+      return SLAB_OK;
+    }
     if (key == SLAB_OPT_IFACE_SOLVE) {
       if (value != 0 && value != 1) return set_error(SLAB_ERR_ARG, "iface_solve %d not 0 or 1", value);
       const bool cl = value == 0;
@@ -458,6 +480,7 @@ struct EngineImpl : EngineBase {
   int get_option(int key) const override {
     if (key == SLAB_OPT_LEAF_CTAS) return leaf_ctas;
     if (key == SLAB_OPT_IFACE_SOLVE) return use_cluster_solve ? 0 : 1;
+    if (key == SLAB_OPT_IFACE_LOOKAHEAD) return use_lookahead ? 1 : 0;
     return set_error(SLAB_ERR_ARG, "unknown option %d", key);
   }
 
@@ -689,8 +712,13 @@ struct EngineImpl : EngineBase {
   }
 
   int init(const double* hD, const double* hDsq, const double* hNx, const double* hinterp, const int* hjxr) {
-    SLAB_CUDA_TRY(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    int prio_lo = 0, prio_hi = 0;
+    SLAB_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi));
+    SLAB_CUDA_TRY(cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, prio_hi));
+    SLAB_CUDA_TRY(cudaStreamCreateWithPriority(&side, cudaStreamNonBlocking, prio_lo));
     SLAB_CUDA_TRY(cudaEventCreateWithFlags(&join, cudaEventDisableTiming));
+    SLAB_CUDA_TRY(cudaEventCreateWithFlags(&la_fork, cudaEventDisableTiming));
+    SLAB_CUDA_TRY(cudaEventCreateWithFlags(&la_join, cudaEventDisableTiming));
     SLAB_TRY(upload(D, std::vector<double>(hD, hD + p * p), s));
     SLAB_TRY(upload(Dsq, std::vector<double>(hDsq, hDsq + p * p), s));
     SLAB_TRY(upload(Nx, std::vector<double>(hNx, hNx + (size_t)nx * p * p), s));
@@ -737,6 +765,7 @@ struct EngineImpl : EngineBase {
         SLAB_TRY(emuWork.alloc(dgemm_emu_work_bytes(nI, nI, nI)));
         SLAB_TRY(emuErr.alloc(sizeof(int)));
         SLAB_TRY(emuLinv.alloc((size_t)kEmuOuter * 64 * sizeof(double)));
+        SLAB_TRY(laPerm.alloc((size_t)(1 + 2 * kRowpermMax) * sizeof(int)));
         SLAB_CUDA_TRY(cudaMemsetAsync(emuErr.p, 0, sizeof(int), s));
       }
     }
@@ -905,8 +934,9 @@ struct EngineImpl : EngineBase {
         if constexpr (std::is_same<TI, double>::value) {
           if (use_emu) {
             EmuWork w{emuWork.p, emuWork.bytes, emuErr.as<int>()};
+            Lookahead la{use_lookahead ? side : nullptr, la_fork, la_join, laPerm.as<int>()};
             SLAB_TRY(biglu_emu(s, Sj, nI, nI, ifPiv.as<int>() + (long long)nI * j, ifInfo.as<int>(), ifWork.as<TI>(),
-                               emuLinv.as<double>(), w));
+                               emuLinv.as<double>(), w, &la));
             done = true;
           }
         }

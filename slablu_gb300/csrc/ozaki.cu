@@ -498,15 +498,42 @@ int bigtrs_inv_emu(cudaStream_t s, const double* LU, int lda, int n, const int* 
   return SLAB_OK;
 }
 
+namespace {
+// U12 = L11^{-1} A12 for the rows [ob0, obe) of the columns [c0, c0 + nc),
+// then A22 -= A21 U12 below them on the tensor cores (blk_linv: inverted
+// 64 x 64 diagonal triangles of the outer block's unit-lower L11).
+int outer_update(cudaStream_t s, double* A, int lda, int n, int ob0, int obe, int c0, int nc, const double* blk_linv,
+                 const EmuWork& w) {
+  constexpr int kB = 64;
+  if (nc <= 0) return SLAB_OK;
+  double* A12 = A + (size_t)c0 * lda;
+  for (int b0 = ob0; b0 < obe; b0 += kB) {
+    const int bn = obe - b0 < kB ? obe - b0 : kB;
+    SLAB_TRY(trsm_inv<double>(s, blk_linv + (size_t)((b0 - ob0) / kB) * kB * kB, kB, b0, bn, A12, lda, nc));
+    const int below = obe - b0 - bn;
+    if (below > 0)
+      SLAB_TRY(gemm<double>(s, below, nc, bn, -1.0, A + (size_t)b0 * lda + b0 + bn, nullptr, 0, lda, A12 + b0,
+                            nullptr, 0, lda, 1.0, A12 + b0 + bn, nullptr, 0, lda, 1));
+  }
+  return dgemm_emu(s, n - obe, nc, obe - ob0, -1.0, A + (size_t)ob0 * lda + obe, lda, A12 + ob0, lda, 1.0,
+                   A12 + obe, lda, w.buf, w.bytes, w.err);
+}
+}  // namespace
+
 int biglu_emu(cudaStream_t s, double* A, int lda, int n, int* ipiv, int* info, double* panel_linv, double* blk_linv,
-              const EmuWork& w) {
+              const EmuWork& w, const Lookahead* la) {
   constexpr int kB = 64;  // diagonal blocks of the outer triangular solve
+  const bool look = la && la->side && la->fork && la->join && la->perm;
+  bool side_busy = false;
   for (int ob0 = 0; ob0 < n; ob0 += kEmuOuter) {
     const int obe = n - ob0 < kEmuOuter ? n : ob0 + kEmuOuter;
     for (int k0 = ob0; k0 < obe; k0 += kNB) {
       const int nb = obe - k0 < kNB ? obe - k0 : kNB;
       bool linv_done = false;
-      SLAB_TRY(biglu_panel_swap<double>(s, A, lda, n, k0, nb, ipiv, info, panel_linv, &linv_done));
+      if (look)
+        SLAB_TRY(biglu_panel_swap_range<double>(s, A, lda, n, k0, nb, ob0, obe, ipiv, info, panel_linv, &linv_done));
+      else
+        SLAB_TRY(biglu_panel_swap<double>(s, A, lda, n, k0, nb, ipiv, info, panel_linv, &linv_done));
       const int inner = obe - k0 - nb;
       if (inner > 0) {
         if (!linv_done) SLAB_TRY(tri_inv_blocks<double>(s, A + (size_t)k0 * lda + k0, lda, nb, kNB, panel_linv, nullptr));
@@ -518,22 +545,29 @@ int biglu_emu(cudaStream_t s, double* A, int lda, int n, int* ipiv, int* info, d
       }
     }
     const int rest = n - obe;
+    if (look) {
+      // the side stream's update of the previous outer block reads the columns
+      // left of ob0 and writes those right of obe: it finishes before this
+      // block's interchanges reach them
+      if (side_busy) SLAB_CUDA_TRY(cudaStreamWaitEvent(s, la->join, 0));
+      side_busy = false;
+      SLAB_TRY(laswp_gather<double>(s, A, lda, n, ob0, obe - ob0, ipiv, 0, ob0, obe, n, la->perm));
+    }
     if (rest > 0) {
       // U12 = L11^{-1} A12 over the outer block's rows, then A22 -= A21 U12 on the tensor cores
       SLAB_TRY(tri_inv_blocks<double>(s, A + (size_t)ob0 * lda + ob0, lda, obe - ob0, kB, blk_linv, nullptr));
-      double* A12 = A + (size_t)obe * lda;
-      for (int b0 = ob0; b0 < obe; b0 += kB) {
-        const int bn = obe - b0 < kB ? obe - b0 : kB;
-        SLAB_TRY(trsm_inv<double>(s, blk_linv + (size_t)((b0 - ob0) / kB) * kB * kB, kB, b0, bn, A12, lda, rest));
-        const int below = obe - b0 - bn;
-        if (below > 0)
-          SLAB_TRY(gemm<double>(s, below, rest, bn, -1.0, A + (size_t)b0 * lda + b0 + bn, nullptr, 0, lda, A12 + b0,
-                                nullptr, 0, lda, 1.0, A12 + b0 + bn, nullptr, 0, lda, 1));
+      const int now = look ? (rest < kEmuOuter ? rest : kEmuOuter) : rest;  // columns the next outer block needs
+      SLAB_TRY(outer_update(s, A, lda, n, ob0, obe, obe, now, blk_linv, w));
+      if (now < rest) {
+        SLAB_CUDA_TRY(cudaEventRecord(la->fork, s));
+        SLAB_CUDA_TRY(cudaStreamWaitEvent(la->side, la->fork, 0));
+        SLAB_TRY(outer_update(la->side, A, lda, n, ob0, obe, obe + now, rest - now, blk_linv, w));
+        SLAB_CUDA_TRY(cudaEventRecord(la->join, la->side));
+        side_busy = true;
       }
-      SLAB_TRY(dgemm_emu(s, rest, rest, obe - ob0, -1.0, A + (size_t)ob0 * lda + obe, lda, A12 + ob0, lda, 1.0,
-                         A12 + obe, lda, w.buf, w.bytes, w.err));
     }
   }
+  if (side_busy) SLAB_CUDA_TRY(cudaStreamWaitEvent(s, la->join, 0));
   return SLAB_OK;
 }
 

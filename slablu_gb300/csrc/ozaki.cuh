@@ -34,11 +34,23 @@ int bigtrs_inv_emu(cudaStream_t s, const double* LU, int lda, int n, const int* 
                    const double* Uinv, int bs, const double* B, int ldb, double* X, int ldx, int nrhs,
                    const EmuWork& w);
 
+// Second stream for the lookahead of biglu_emu.  side == null: serial.
+struct Lookahead {
+  cudaStream_t side = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
+  int* perm = nullptr;  // 1 + 2 * kRowpermMax ints (row-interchange gather)
+};
+
 // biglu with the trailing update between outer blocks of kEmuOuter columns
 // done by dgemm_emu (the panels and the updates inside an outer block stay on
 // the FP64 cores).  Same pivots, factors and info as biglu.  panel_linv: kNB x
 // kNB doubles; blk_linv: kEmuOuter * 64 doubles.
+// With la->side, each outer block's update of the columns beyond the next
+// outer block runs on the side stream while the next outer block's panels
+// are factored on s: panel interchanges are applied inside the outer block at
+// once and to the other columns after the block (as one gather), once the
+// side stream no longer reads them.  The result is the same.
 int biglu_emu(cudaStream_t s, double* A, int lda, int n, int* ipiv, int* info, double* panel_linv, double* blk_linv,
-              const EmuWork& w);
+              const EmuWork& w, const Lookahead* la = nullptr);
 
 }  // namespace slab
