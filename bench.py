@@ -34,7 +34,7 @@ METRIC = 'unknowns/sec factor+solve at N~4M p=22, mixed-prec vs FP64 GPU at 1e-6
 P, NSIDE = 22, 2000
 CPU_SAMPLE_N = 400
 # DRAM bytes per leaf of leaf_factor_kernel<float>, measured with ncu on 1024 leaves
-LEAF_DRAM_BYTES_PER_LEAF = 9.68e9 / 1024
+LEAF_DRAM_BYTES_PER_LEAF = 9.82e9 / 1024
 
 
 def parse():

@@ -449,7 +449,7 @@ int panel_factor(cudaStream_t s, T* A, int lda, int n, int k0, int nb, int* ipiv
 template <typename T>
 int tri_inv_blocks(cudaStream_t s, const T* LU, int lda, int n, int bs, T* Linv, T* Uinv) {
   const int nblk = ceil_div(n, bs);
-  const size_t bytes = 2 * (size_t)bs * (bs + 1) * sizeof(T);
+  const size_t bytes = (2 * (size_t)bs * (bs + 1) + bs) * sizeof(T);
   SLAB_TRY(ensure_smem(tri_inv_blocks_kernel<T>, bytes, "tri_inv_blocks"));
   if (Linv) {
     tri_inv_blocks_kernel<T><<<nblk, 128, bytes, s>>>(LU, lda, n, bs, 0, Linv);

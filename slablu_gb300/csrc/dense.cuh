@@ -1690,27 +1690,47 @@ __global__ void __launch_bounds__(128) tri_inv_blocks_kernel(const T* A, int lda
   const int blk = blockIdx.x;
   const int k0 = blk * bs, nb = min(bs, n - k0);
   T* O = out + (size_t)blk * bs * bs;
+  T* rdiag = Xs + (size_t)bs * ld;           // bs: reciprocals of the diagonal (upper)
   for (int idx = threadIdx.x; idx < bs * bs; idx += blockDim.x) {
     const int i = idx % bs, c = idx / bs;
     D[i + c * ld] = (i < nb && c < nb) ? A[(size_t)(k0 + c) * lda + k0 + i] : T(0);
     Xs[i + c * ld] = T(0);
   }
   __syncthreads();
+  if (upper)
+    for (int i = threadIdx.x; i < nb; i += blockDim.x) rdiag[i] = T(1) / D[i + i * ld];
+  __syncthreads();
+  // one thread per column; each dot product is split over four partial sums,
+  // which cuts the dependent chain of the substitution (FP64 latency) by four
   for (int c = threadIdx.x; c < nb; c += blockDim.x) {
     T* x = Xs + c * ld;
     if (!upper) {
       x[c] = T(1);
       for (int i = c + 1; i < nb; ++i) {
-        T s = T(0);
-        for (int k = c; k < i; ++k) s -= D[i + k * ld] * x[k];
-        x[i] = s;
+        T s0 = T(0), s1 = T(0), s2 = T(0), s3 = T(0);
+        int k = c;
+        for (; k + 3 < i; k += 4) {
+          s0 -= D[i + k * ld] * x[k];
+          s1 -= D[i + (k + 1) * ld] * x[k + 1];
+          s2 -= D[i + (k + 2) * ld] * x[k + 2];
+          s3 -= D[i + (k + 3) * ld] * x[k + 3];
+        }
+        for (; k < i; ++k) s0 -= D[i + k * ld] * x[k];
+        x[i] = (s0 + s1) + (s2 + s3);
       }
     } else {
-      x[c] = T(1) / D[c + c * ld];
+      x[c] = rdiag[c];
       for (int i = c - 1; i >= 0; --i) {
-        T s = T(0);
-        for (int k = i + 1; k <= c; ++k) s -= D[i + k * ld] * x[k];
-        x[i] = s / D[i + i * ld];
+        T s0 = T(0), s1 = T(0), s2 = T(0), s3 = T(0);
+        int k = i + 1;
+        for (; k + 3 <= c; k += 4) {
+          s0 -= D[i + k * ld] * x[k];
+          s1 -= D[i + (k + 1) * ld] * x[k + 1];
+          s2 -= D[i + (k + 2) * ld] * x[k + 2];
+          s3 -= D[i + (k + 3) * ld] * x[k + 3];
+        }
+        for (; k <= c; ++k) s0 -= D[i + k * ld] * x[k];
+        x[i] = ((s0 + s1) + (s2 + s3)) * rdiag[i];
       }
     }
   }
