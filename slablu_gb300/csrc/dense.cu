@@ -356,9 +356,19 @@ int gemm(cudaStream_t s, int m, int n, int k, T alpha, const T* A, const long lo
   if (n <= 16) {
     dim3 g(ceil_div(m, 256), 1, batch);
     const int kk = k < 0 ? 0 : k;
-#define SLAB_NARROW(NC)                                                                                     \
-  gemm_narrow_kernel<T, NC><<<g, 256, 0, s>>>(m, n, kk, alpha, A, offA, strideA, lda, B, offB, strideB, ldb, \
-                                              beta, C, offC, strideC, ldc)
+    // a grid of few CTAs with long rows (the top merge levels: ten slabs, thousands of
+    // columns): split k over the warps of a CTA, 32 rows per CTA
+    const bool ks = (long long)ceil_div(m, 256) * batch < 2LL * sm_count() && kk >= 128;
+    if (ks) g = dim3(ceil_div(m, 32), 1, batch);
+#define SLAB_NARROW(NC)                                                                                        \
+  do {                                                                                                         \
+    if (ks)                                                                                                    \
+      gemm_narrow_ks_kernel<T, NC><<<g, 256, 0, s>>>(m, n, kk, alpha, A, offA, strideA, lda, B, offB, strideB, \
+                                                     ldb, beta, C, offC, strideC, ldc);                       \
+    else                                                                                                       \
+      gemm_narrow_kernel<T, NC><<<g, 256, 0, s>>>(m, n, kk, alpha, A, offA, strideA, lda, B, offB, strideB,    \
+                                                  ldb, beta, C, offC, strideC, ldc);                          \
+  } while (0)
     if (n <= 1)
       SLAB_NARROW(1);
     else if (n <= 2)

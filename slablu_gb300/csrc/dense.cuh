@@ -824,6 +824,61 @@ __global__ void __launch_bounds__(256) gemm_narrow_kernel(int m, int n, int k, T
   }
 }
 
+// The same product for grids of few CTAs: 32 rows per CTA, k split over the 8
+// warps (warp w takes k = w, w+8, ...; each load is one coalesced 32-row
+// segment of a column of A), partial sums reduced in a fixed order through
+// shared memory (deterministic).  grid (ceil(m/32), 1, batch).
+template <typename T, int NC>
+__global__ void __launch_bounds__(256) gemm_narrow_ks_kernel(int m, int n, int k, T alpha, const T* __restrict__ A,
+                                                            const long long* offA, long long strideA, int lda,
+                                                            const T* __restrict__ B, const long long* offB,
+                                                            long long strideB, int ldb, T beta, T* C,
+                                                            const long long* offC, long long strideC, int ldc) {
+  constexpr int KC = 256, KG = 8;
+  __shared__ T Bs[KC * NC];  // B chunk; then the warps' partial sums (KG x 32 x NC <= KC x NC)
+  const int bz = blockIdx.z;
+  A += batch_off(offA, strideA, bz);
+  B += batch_off(offB, strideB, bz);
+  C += batch_off(offC, strideC, bz);
+  const int lr = threadIdx.x & 31, kg = threadIdx.x >> 5;
+  const int r = blockIdx.x * 32 + lr;
+  T acc[NC];
+#pragma unroll
+  for (int c = 0; c < NC; ++c) acc[c] = T(0);
+  for (int k0 = 0; k0 < k; k0 += KC) {
+    const int kc = min(KC, k - k0);
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < KC * NC; idx += blockDim.x) {
+      const int kk = idx % KC, c = idx / KC;
+      Bs[c * KC + kk] = (kk < kc && c < n) ? B[(k0 + kk) + (size_t)c * ldb] : T(0);
+    }
+    __syncthreads();
+    if (r < m) {
+      const T* ap = A + r + (size_t)k0 * lda;
+#pragma unroll 4
+      for (int kk = kg; kk < kc; kk += KG) {
+        const T a = ap[(size_t)kk * lda];
+#pragma unroll
+        for (int c = 0; c < NC; ++c) acc[c] += a * Bs[c * KC + kk];
+      }
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int c = 0; c < NC; ++c) Bs[(kg * 32 + lr) * NC + c] = acc[c];
+  __syncthreads();
+  if (kg == 0 && r < m) {
+#pragma unroll
+    for (int c = 0; c < NC; ++c) {
+      if (c >= n) break;
+      T sum = Bs[lr * NC + c];
+      for (int w = 1; w < KG; ++w) sum += Bs[(w * 32 + lr) * NC + c];
+      T* cp = C + r + (size_t)c * ldc;
+      *cp = (beta == T(0) ? T(0) : beta * *cp) + alpha * sum;
+    }
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Batched ipiv -> row permutation (perm[i] = source row of row i), one thread
 // per matrix.
