@@ -324,9 +324,10 @@ int gemm(cudaStream_t s, int m, int n, int k, T alpha, const T* A, const long lo
   }
   if (n <= 16 && batch == 1 && !offA && !offB && !offC && k >= 512 && ceil_div(m, 256) < 64) {
     // tall-skinny single product: split k over CTAs, accumulate with atomics
+    // (chunks of 64: a 2000 x 2000 matrix-vector product spreads over 256 CTAs)
     const int mb = ceil_div(m, 256);
     int nsplit = ceil_div(256, mb);
-    const int kchunk = 256;
+    const int kchunk = 64;
     nsplit = nsplit < ceil_div(k, kchunk) ? nsplit : ceil_div(k, kchunk);
     if (beta != T(1)) {
       scale_kernel<T><<<ceil_div(m * n, 256), 256, 0, s>>>(C, m, n, ldc, beta);
