@@ -222,13 +222,14 @@ __global__ void merge_gather_kernel(MergeGatherArgs a, const T* __restrict__ poo
   T* M = fpool + a.offM0 + (long long)e * a.nE * (a.nE + a.nO);
   T* C = fpool + a.offC0 + (long long)e * a.nO * a.nE;
   const int nE = a.nE, nO = a.nO;
-  const long long totP = (long long)nO * nO;
-  const long long totM = (long long)nE * (nE + nO);
-  const long long totC = (long long)nO * nE;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < totP + totM + totC;
-       i += (long long)gridDim.x * blockDim.x) {
+  // per merge the element count is below 2^31 (checked by the launcher): 32-bit
+  // index arithmetic, whose divisions cost a fraction of 64-bit ones
+  const int totP = nO * nO;
+  const int totM = nE * (nE + nO);
+  const int totC = nO * nE;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < totP + totM + totC; i += gridDim.x * blockDim.x) {
     if (i < totP) {
-      const int r = (int)(i % nO), c = (int)(i / nO);
+      const int r = i % nO, c = i / nO;
       const int cr = a.oChild[r], cc = a.oChild[c];
       T v = T(0);
       if (cr == cc) {
@@ -239,8 +240,8 @@ __global__ void merge_gather_kernel(MergeGatherArgs a, const T* __restrict__ poo
       }
       P[i] = v;
     } else if (i < totP + totM) {
-      const long long j = i - totP;
-      const int r = (int)(j % nE), c = (int)(j / nE);
+      const int j = i - totP;
+      const int r = j % nE, c = j / nE;
       T v;
       if (c < nE) {
         v = A[a.eA[r] + (long long)a.eA[c] * a.nA] + B[a.eB[r] + (long long)a.eB[c] * a.nB];
@@ -250,8 +251,8 @@ __global__ void merge_gather_kernel(MergeGatherArgs a, const T* __restrict__ poo
       }
       M[j] = v;
     } else {
-      const long long j = i - totP - totM;
-      const int r = (int)(j % nO), c = (int)(j / nO);
+      const int j = i - totP - totM;
+      const int r = j % nO, c = j / nO;
       C[j] = a.oChild[r] == 0 ? A[a.oPos[r] + (long long)a.eA[c] * a.nA] : B[a.oPos[r] + (long long)a.eB[c] * a.nB];
     }
   }
@@ -841,6 +842,8 @@ struct EngineImpl : EngineBase {
       MergeGatherArgs g{b.nA, b.nB, b.nE, b.nO, b.count, b.eA.as<int>(), b.eB.as<int>(), b.oChild.as<int>(),
                         b.oPos.as<int>(), b.offA.as<long long>(), b.offB.as<long long>(), b.offP0, b.offM0, b.offC0};
       const long long per = (long long)b.nO * b.nO + (long long)b.nE * (b.nE + b.nO) + (long long)b.nO * b.nE;
+      if (per + 1024LL * 256 >= (1LL << 31))
+        return set_error(SLAB_ERR_ARG, "merge of %d + %d unknowns too large", b.nE, b.nO);
       dim3 grid((unsigned)std::min<long long>((per + 255) / 256, 1024), b.count);
       merge_gather_kernel<T><<<grid, 256, 0, s>>>(g, nodepool.as<T>(), nodepool.as<T>(), fpool.as<T>());
       SLAB_CHECK_LAUNCH();
