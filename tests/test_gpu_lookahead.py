@@ -3,7 +3,7 @@
 The lookahead moves each outer block's update of the far columns to a second
 stream and applies the panels' row interchanges to those columns later, as
 one gather; the arithmetic is unchanged, so both orders give the same
-solution.  The interface block here has 520 unknowns (130 leaves of p = 6 per
+factors and, after refinement, the same solution.  The interface block here has 520 unknowns (130 leaves of p = 6 per
 slab interface), so the first outer block forks work to the second stream.
 """
 import numpy as np
@@ -48,7 +48,10 @@ def test_lookahead_matches_serial_order_and_oracle():
         u, _, iters, st = eng.solve(bnd, tol=1e-12, max_iter=40)
         assert st['converged'], (la, iters, st)
         sols[la] = u[:, 0].cpu().numpy()
+    # both are refined to a relative correction of 1e-12; the split-k products of
+    # the solve accumulate with atomics, so the two runs agree to the refinement
+    # level, not bit for bit
     diff = np.linalg.norm(sols[1] - sols[0]) / np.linalg.norm(sols[0])
-    assert diff < 1e-13, diff
+    assert diff < 1e-11, diff
     rel = np.linalg.norm(sols[1] - ref) / np.linalg.norm(ref)
     assert rel < 1e-9, rel
