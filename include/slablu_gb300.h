@@ -190,6 +190,26 @@ size_t slab_dgemm_emu_work_bytes(int m, int n, int k);
 int slab_dgemm_emu(int m, int n, int k, double alpha, const double* d_A, int lda, const double* d_B, int ldb,
                    double beta, double* d_C, int ldc, void* d_work, size_t work_bytes, void* stream);
 
+/*
+ * Reduced sparse operator on the device (CSR, FP64).
+ * Replaces the COO -> CSR assembly of HPS_Multidomain.sparse_mat
+ * (src_disc/hps_multidomain_disc.py:53-109: the leaf DtN maps summed over the
+ * reduced face unknowns) and the sparse applies of the right-hand-side
+ * formation (src_solver/slablu_solver.py:48-57 apply_sparse_lowmem, :489-507
+ * get_rhs).  The pattern depends only on the leaf grid and is built on the host
+ * (slablu_gb300/sparse.py); d_dest maps every leaf DtN entry (leaf-major,
+ * row-major within a leaf) to its CSR slot.
+ *   slab_csr_assemble: d_vals[0..nnz) = 0, then d_vals[d_dest[i]] += d_src[i]
+ *                      for i < count (at most two terms per slot: the sum is
+ *                      independent of their order).
+ *   slab_csr_spmv:     d_y = alpha A d_x + beta d_y for the nrows x ncols CSR
+ *                      matrix (d_indptr nrows+1 64-bit offsets, d_indices int32).
+ */
+int slab_csr_assemble(long long count, const double* d_src, const long long* d_dest, long long nnz,
+                      double* d_vals, void* stream);
+int slab_csr_spmv(int nrows, const long long* d_indptr, const int* d_indices, const double* d_vals,
+                  const double* d_x, double alpha, double beta, double* d_y, void* stream);
+
 /* Tunable launch choices of an engine (slablu_gb300/autotune.py times them):
  *   SLAB_OPT_LEAF_CTAS   resident leaves per SM in the leaf kernel, 0 = as many
  *                        as fit (fewer keep more of each leaf matrix in L2)

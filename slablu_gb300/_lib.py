@@ -47,6 +47,8 @@ _SIGS = {
     'slab_engine_get_option': (c_int, [c_void, c_int]),
     'slab_dgemm_emu': (c_int, [c_int, c_int, c_int, c_double, c_void, c_int, c_void, c_int, c_double, c_void, c_int,
                                c_void, c_size, c_void]),
+    'slab_csr_assemble': (c_int, [c_ll, c_void, c_void, c_ll, c_void, c_void]),
+    'slab_csr_spmv': (c_int, [c_int, c_void, c_void, c_void, c_void, c_double, c_double, c_void, c_void]),
 }
 
 

@@ -16,6 +16,9 @@ Differences from the reference, by design:
     is below ``tol``.
   * ``rel_err`` returned by ``solve`` is that FP64 relative residual (the
     reference reports the residual of its reduced sparse system).
+  * the reduced sparse operator is not needed by the solver; ``hps.sparse_mat``
+    and ``get_rhs`` assemble and apply it on the GPU for callers of the
+    reference's sparse interface (slablu_gb300/sparse.py).
 Out of scope (raise NotImplementedError): finite differences (p = 0),
 periodic boundary conditions, mixed second derivatives (c12).
 """
@@ -30,16 +33,47 @@ from .hps import Geometry
 
 
 class _HPSView:
-    """The subset of HPS_Multidomain the reference driver reads (n, xx_tot, xx_active)."""
+    """The subset of HPS_Multidomain the reference driver reads (n, xx_tot,
+    xx_active), and its reduced sparse operator (sparse_mat)."""
 
-    def __init__(self, geom):
+    def __init__(self, geom, coeff_fn=None):
         self.geom = geom
+        self._coeff_fn = coeff_fn
         self.p, self.a = geom.p, geom.a
         self.n = torch.tensor([geom.n0, geom.n1], dtype=torch.int32)
         self.nboxes = geom.nboxes
         self.xx_tot = torch.as_tensor(geom.xx_tot)
         self.xx_active = torch.as_tensor(geom.xx_active)
         self.grid_xx = torch.as_tensor(geom.xx)
+
+    def sparse_mat(self, device='cuda', verbose=False):
+        """Reduced operator: leaf DtN maps (FP64, slab_leaf_dtn) summed on the GPU
+        (hps_multidomain_disc.py:53-109).  Returns (A as a torch sparse CSR tensor on
+        ``device``, timing dict), like the reference's (scipy CSR, t_dict)."""
+        from . import sparse
+        from .engine import leaf_dtn
+        dev = torch.device(device)
+        if dev.type != 'cuda':
+            raise ValueError('sparse_mat is assembled on the GPU (device must be cuda)')
+        if self._coeff_fn is None:
+            raise RuntimeError('this view has no coefficients (use Domain_Solver.hps)')
+        g = self.geom
+        torch.cuda.synchronize()
+        tic = time.time()
+        co = {k: (None if v is None else v.reshape(g.nboxes, g.p * g.p)) for k, v in self._coeff_fn().items()}
+        dtn, info = leaf_dtn(co, g.p, g.ops.D, g.ops.Dsq, g.ops.Nx, precision='fp64')
+        if int(info.abs().sum()) != 0:
+            raise RuntimeError('leaf DtN: zero pivot in a leaf interior block')
+        torch.cuda.synchronize()
+        toc_dtn = time.time() - tic
+        tic = time.time()
+        A = sparse.assemble(g, dtn)
+        torch.cuda.synchronize()
+        t = dict(toc_DtN=toc_dtn, toc_forloop=0.0, toc_sparse=time.time() - tic)
+        if verbose:
+            print(f'\t--time to assemble sparse HPS (DtN ops, csr on the GPU) ({toc_dtn:5.2f},{t["toc_sparse"]:5.2f})')
+        self._A = A
+        return A.to_torch(), t
 
 
 class Domain_Solver:
@@ -61,7 +95,7 @@ class Domain_Solver:
         self.geom = Geometry(bg, h, p, buf_constant)
         g = self.geom
         self.disc = 'hps'
-        self.hps = _HPSView(g)
+        self.hps = _HPSView(g, self._coeffs)
         self.buf_pans, self.Npan, self.Npan_loc = g.buf, g.Npan, g.n1
         self.ntot = g.ntot
         lt = lambda a: torch.as_tensor(a, dtype=torch.long)
@@ -113,6 +147,25 @@ class Domain_Solver:
             print(f'SLABLU GB300 BUILD ({self.precision}): {toc_build:.3f} s, factors {info["mem_build"]:.2f} GB, '
                   f'buf={self.buf_pans} Npan={self.Npan}')
         return info
+
+    def get_rhs(self, uu_dir_func, ff_body_func=None, sum_body_load=True):
+        """Right-hand side of the reduced system on I_Ctot, ff = -A[I_Ctot, I_Xtot] uu_dir
+        (slablu_solver.py:489-507), with A assembled on the GPU; a device tensor
+        (len(I_Ctot), nrhs).  Body loads enter through solve(ff_body_func=...) instead:
+        the reference's reduction of a body load to the faces (reduce_body,
+        hps_parallel_leaf_ops.py:94-100) does not run."""
+        if ff_body_func is not None:
+            raise NotImplementedError('body loads: pass ff_body_func to solve()')
+        if getattr(self.hps, '_A', None) is None:
+            self.hps.sparse_mat(self.device)
+        A = self.hps._A
+        XX = self.hps.xx_active
+        ud = torch.as_tensor(uu_dir_func(XX[self.I_Xtot]), dtype=torch.float64)
+        if ud.dim() == 1:
+            ud = ud[:, None]
+        x = torch.zeros(self.ntot, ud.shape[1], dtype=torch.float64, device=self.device)
+        x[self.I_Xtot.to(self.device)] = ud.to(self.device)
+        return -A.matvec(x)[self.I_Ctot.to(self.device)]
 
     def get_rhs_boundary(self, uu_dir_func):
         """Face vector carrying Dirichlet data at I_Xtot (slablu_solver.py:504)."""

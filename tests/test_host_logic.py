@@ -74,3 +74,22 @@ def test_library_exports_every_declared_symbol():
     assert b'invalid' in lib.slab_last_error()
     assert lib.slab_leaf_dtn_work_bytes(0, 22, 0) == 0
     assert lib.slab_leaf_dtn_work_bytes(10, 22, 0) > 10 * 400 * 480 * 8
+
+
+@pytest.mark.parametrize('geom,p,n', [([[0, 1], [0, 1]], 8, 48), ([[0, 1], [0, 0.5]], 6, 28)])
+def test_reduced_pattern_matches_oracle_csr(geom, p, n):
+    """The device assembly's CSR pattern and slot map reproduce SciPy's COO -> CSR sum of
+    the leaf DtN maps (hps_multidomain_disc.py:84-95), here with random DtN values."""
+    from slablu_gb300 import sparse
+    a = 1 / (2 * (n / (p - 2)))
+    md = odomain.Multidomain(geom, a, p)
+    g = hps.Geometry(geom, a, p, 1.0)
+    indptr, indices, dest = sparse.reduced_pattern(g)
+    rng = np.random.default_rng(3)
+    dtn = rng.standard_normal((md.nboxes, 4 * md.q, 4 * md.q))
+    ref = md.sparse_mat(dtn)
+    ref.sort_indices()
+    assert np.array_equal(indptr, ref.indptr) and np.array_equal(indices, ref.indices)
+    vals = np.zeros(len(indices))
+    np.add.at(vals, dest, dtn.ravel())
+    assert np.array_equal(vals, ref.data)
