@@ -7,7 +7,7 @@ Restates, in NumPy and FP64,
   src_disc/hps_subdomain_disc.py:83-100   HPS_Disc.get_diff_ops (2-D branch)
   src_disc/hps_subdomain_disc.py:105-152  leaf_discretization_2d, cheb_2d
   src_disc/hps_parallel_leaf_ops.py:10-37 get_Aloc_2d / Aloc_acc
-  src_disc/hps_parallel_leaf_ops.py:40-92 form_DtNs ('build' and 'solve', c12 = None)
+  src_disc/hps_parallel_leaf_ops.py:40-92 form_DtNs ('build' and 'solve', with and without c12)
 """
 from dataclasses import dataclass
 
@@ -130,11 +130,12 @@ def leaf_disc(a, p):
 def aloc(ld, coeffs):
     """Dense leaf operators for a batch of leaves (hps_parallel_leaf_ops.py:10-37).
 
-    ``coeffs`` maps 'c11', 'c22', 'c1', 'c2', 'c' to arrays (nleaf, p^2) of
-    coefficient values at the leaf nodes (absent keys are zero terms; c12 is
-    out of scope).  Returns (nleaf, p^2, p^2).
+    ``coeffs`` maps 'c11', 'c22', 'c12', 'c1', 'c2', 'c' to arrays (nleaf, p^2)
+    of coefficient values at the leaf nodes (absent keys are zero terms), added
+    in the reference's order with its factors (-1, -1, -2, 1, 1).  Returns
+    (nleaf, p^2, p^2).
     """
-    terms = [('c11', ld.D11, -1.0), ('c22', ld.D22, -1.0), ('c1', ld.D1, 1.0),
+    terms = [('c11', ld.D11, -1.0), ('c22', ld.D22, -1.0), ('c12', ld.D12, -2.0), ('c1', ld.D1, 1.0),
              ('c2', ld.D2, 1.0)]
     nleaf = next(iter(coeffs.values())).shape[0]
     n = ld.p * ld.p
@@ -148,14 +149,19 @@ def aloc(ld, coeffs):
 
 
 def dtn_build(ld, coeffs, return_S=False):
-    """Leaf DtN maps (form_DtNs 'build', hps_parallel_leaf_ops.py:50-58).
+    """Leaf DtN maps (form_DtNs 'build', hps_parallel_leaf_ops.py:50-65).
 
-    S = -A_cc^{-1} A_cx ; DtN = Nx[:, Jc] S + Nx[:, Jx].
+    S = -A_cc^{-1} A_cx ; DtN = Nx[:, Jc] S + Nx[:, Jx].  With a mixed
+    derivative (c12), the interior couples to the corners too: the columns are
+    the 4(p-1) nodes Jxreorder and S = -A_cc^{-1} A_c,Jxreorder Interp_mat
+    (:59-65).
     """
     A = aloc(ld, coeffs)
     Acc = A[:, ld.Jc][:, :, ld.Jc]
-    Acx = A[:, ld.Jc][:, :, ld.Jx]
-    S = -np.linalg.solve(Acc, Acx)
+    if coeffs.get('c12') is None:
+        S = -np.linalg.solve(Acc, A[:, ld.Jc][:, :, ld.Jx])
+    else:
+        S = -np.linalg.solve(Acc, A[:, ld.Jc][:, :, ld.Jxreorder]) @ ld.Interp_mat[None]
     DtN = ld.Nx[:, ld.Jc][None] @ S + ld.Nx[:, ld.Jx][None]
     return (DtN, S) if return_S else DtN
 
@@ -171,11 +177,13 @@ def dtn_solve(ld, coeffs, u_face, f_body=None):
     nleaf, _, nrhs = u_face.shape
     n = ld.p * ld.p
     Acc = A[:, ld.Jc][:, :, ld.Jc]
-    Acx = A[:, ld.Jc][:, :, ld.Jx]
     fb = np.zeros((nleaf, ld.Jc.size, nrhs)) if f_body is None else f_body
     u = np.zeros((nleaf, n, nrhs))
     u[:, ld.Jxreorder] = ld.Interp_mat[None] @ u_face
-    u[:, ld.Jc] = np.linalg.solve(Acc, fb - Acx @ u_face)
+    if coeffs.get('c12') is None:
+        u[:, ld.Jc] = np.linalg.solve(Acc, fb - A[:, ld.Jc][:, :, ld.Jx] @ u_face)
+    else:  # the interior sees the interpolated boundary, corners included (:84-88)
+        u[:, ld.Jc] = np.linalg.solve(Acc, fb - A[:, ld.Jc][:, :, ld.Jxreorder] @ u[:, ld.Jxreorder])
     res = np.zeros((nleaf, n, nrhs))
     res[:, ld.Jc] = A[:, ld.Jc] @ u - fb
     return u, res

@@ -104,6 +104,43 @@ def dtn_fixture(p, a, nbox_side, picks, kh, name, seed=0):
          dtn=DtN.numpy(), u_face=uface.numpy(), u_solve=usol.numpy())
 
 
+def smooth_coeffs(x, kh):
+    """Variable coefficients with a mixed-derivative term, of the kind a curved
+    domain's parameter map produces (src_disc/pdo.py:133-310)."""
+    x0, x1 = x[:, 0], x[:, 1]
+    return dict(c11=1.0 + 0.3 * np.sin(3 * x0) * np.cos(2 * x1), c22=1.0 + 0.2 * np.cos(2 * x0 + x1),
+                c12=0.15 * np.sin(2 * x0) * np.cos(3 * x1), c1=0.5 * np.cos(x0 + 2 * x1),
+                c2=-0.4 * np.sin(x0 * x1), c=-(kh ** 2) * (1.0 - 0.3 * np.exp(-((x0 - 0.5) ** 2 + (x1 - 0.5) ** 2) / 0.05)))
+
+
+def dtn_c12_fixture(p, a, nbox_side, picks, kh, name, seed=0):
+    """Reference form_DtNs (build and solve) with every coefficient present,
+    including c12 (the Jxreorder / Interp_mat branch, hps_parallel_leaf_ops.py:59-65, 84-88)."""
+    md = hps_multidomain_disc.HPS_Multidomain(
+        ref_pdo.PDO_2d(ref_pdo.ones, ref_pdo.ones), torch.tensor([[0, 1.0], [0, 1.0]]), a, p)
+    xx = md.grid_xx[picks].clone()
+    vals = smooth_coeffs(xx.reshape(-1, 2).numpy(), kh)
+    npts = len(picks) * p * p
+    fn = {k: (lambda key: (lambda x: torch.tensor(vals[key]) if x.shape[0] == npts else None))(k) for k in vals}
+    op = ref_pdo.PDO_2d(fn['c11'], fn['c22'], c12=fn['c12'], c1=fn['c1'], c2=fn['c2'], c=fn['c'])
+    H = md.H
+    Nx = torch.tensor(H.Nx)
+    Jx = torch.tensor(H.JJ.Jx)
+    Jc = torch.tensor(H.JJ.Jc)
+    Jxr = torch.tensor(H.JJ.Jxreorder)
+    Im = torch.tensor(H.Interp_mat)
+    dev = torch.device('cpu')
+    DtN = leaf_ops.form_DtNs(p, 2, xx, Nx, Jx, Jc, Jxr, H.Ds, Im, op, 0, len(picks), dev,
+                             'build', torch.zeros(len(picks), 4 * (p - 2), 1), None)
+    rng = np.random.default_rng(seed + 1)
+    uface = torch.tensor(rng.standard_normal((len(picks), 4 * (p - 2), 2)))
+    usol = leaf_ops.form_DtNs(p, 2, xx, Nx, Jx, Jc, Jxr, H.Ds, Im, op, 0, len(picks), dev,
+                              'solve', uface, None)
+    save(name, p=p, a=a, kh=kh, picks=np.asarray(picks), xx=xx.numpy(),
+         **{k: v.reshape(len(picks), -1) for k, v in vals.items()},
+         dtn=DtN.numpy(), u_face=uface.numpy(), u_solve=usol.numpy())
+
+
 def assembly_fixture():
     p, a = 8, 0.0125
     geom = torch.tensor([[0, 4 * 2 * a], [0, 3 * 2 * a]])
@@ -187,6 +224,10 @@ def solve_fixtures():
 
 
 if __name__ == '__main__':
+    if len(sys.argv) > 2 and sys.argv[2] == 'c12':  # only the mixed-derivative fixtures
+        dtn_c12_fixture(12, 0.0125, 40, [0, 7, 800, 1599], 60.0, 'dtn_c12_p12.npz', seed=5)
+        dtn_c12_fixture(8, 1 / 64, 32, [0, 5, 500, 1023], 40.0, 'dtn_c12_p8.npz', seed=6)
+        sys.exit(0)
     leaf_fixtures()
     dtn_fixture(22, 0.005, 100, [0, 57, 4950, 9999, 1234, 6789, 3210, 8888], 1258.6, 'dtn_p22.npz')
     dtn_fixture(12, 0.0125, 40, [0, 7, 800, 1599], 253.3, 'dtn_p12.npz', seed=3)

@@ -51,6 +51,25 @@ def test_leaf_dtn_build_and_solve(golden_dir, name):
     assert np.abs(res - ref_res).max() < 1e-6 * np.abs(ref_u).max() * np.abs(g['c']).max()
 
 
+@pytest.mark.parametrize('name', ['dtn_c12_p12.npz', 'dtn_c12_p8.npz'])
+def test_leaf_dtn_with_mixed_derivative(golden_dir, name):
+    """Every coefficient present, c12 included: the reference's Jxreorder / Interp_mat
+    branch of form_DtNs (hps_parallel_leaf_ops.py:59-65, 84-88)."""
+    g = load(golden_dir, name)
+    p = int(g['p'])
+    ld = leaf.leaf_disc(float(g['a']), p)
+    co = {k: g[k] for k in ('c11', 'c22', 'c12', 'c1', 'c2', 'c')}
+    dtn = leaf.dtn_build(ld, co)
+    rel = np.linalg.norm(dtn - g['dtn'], axis=(1, 2)) / np.linalg.norm(g['dtn'], axis=(1, 2))
+    assert rel.max() < 1e-12, rel.max()
+    u, res = leaf.dtn_solve(ld, co, g['u_face'])
+    nrhs = g['u_face'].shape[-1]
+    ref_u = g['u_solve'][..., :nrhs]
+    ref_res = g['u_solve'][..., nrhs:]
+    assert np.linalg.norm(u - ref_u) / np.linalg.norm(ref_u) < 1e-12
+    assert np.abs(res - ref_res).max() < 1e-6 * np.abs(ref_u).max() * np.abs(g['c']).max()
+
+
 def test_sparse_assembly(golden_dir):
     g = load(golden_dir, 'assembly_p8.npz')
     p, a, kh = int(g['p']), float(g['a']), float(g['kh'])
