@@ -7,7 +7,7 @@ Builds once and solves twice (the second solve is the reported one), and
 pickles ``build_info`` then ``solve_info`` with the reference's keys
 (argparse_driver.py:169-188, 248-298).  Added flags: --precision, --tol.
 Out of scope here: --disc fd, curved domains, periodic BC, the superLU/PETSc
-black-box solvers, --disable_cuda (this build has no CPU path).
+black-box solvers, --disable_cuda (slablu_gb300 has no CPU path).
 """
 import argparse
 import pickle
