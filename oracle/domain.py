@@ -91,10 +91,12 @@ class Multidomain:
         return cat(uniq), cat(c1), cat(c2)
 
     def coeffs(self, pdo):
-        """Evaluate the PDO coefficient callables at every leaf node."""
+        """Evaluate the PDO coefficient callables at every leaf node (a 'c12' entry
+        appears only when the PDO has a mixed derivative)."""
         flat = self.xx.reshape(-1, 2)
         out = {}
-        for key in ('c11', 'c22', 'c1', 'c2', 'c'):
+        keys = ('c11', 'c22', 'c1', 'c2', 'c') + (('c12',) if pdo.get('c12') is not None else ())
+        for key in keys:
             f = pdo.get(key)
             out[key] = None if f is None else np.asarray(f(flat), dtype=float).reshape(self.nboxes, -1)
         return out

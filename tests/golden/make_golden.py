@@ -212,6 +212,33 @@ def run_domain(p, n, ppw, pde, solver, bc='free_space'):
     return dom, kh, sol.numpy(), float(res), float(tres), float(rloc)
 
 
+def annulus_fixture(p=22, n=400, ppw=40):
+    """The reference's annulus known-answer test (tests/test_2d.py:51-52): the
+    parameter map of the annulus (src_disc/pdo.py:196-215) turns Helmholtz on the
+    annulus into a variable-coefficient operator with a mixed derivative on the
+    unit square; Dirichlet data is the free-space Green's function at the mapped
+    points (argparse_driver.py:195-203)."""
+    nwaves = int(n / ppw)
+    kh = (nwaves + 0.03) * 2 * np.pi + 1.8
+    op, param_map, _ = ref_pdo.get_param_map_and_pdo('annulus', bif.bfield_constant, kh)
+    a = 1 / (2 * (n / (p - 2)))
+    dom = Domain_Solver(torch.tensor([[0, 1.0], [0, 1.0]]), op, kh, a, p=p, buf_constant=1.0)
+    dom.build('reduced_cpu', 'slabLU', verbose=False)
+    uu = lambda xx: bif.uu_dir_func_greens(param_map(xx), kh)
+    sol, res, tres, rloc, _ = dom.solve(uu, None, known_sol=True)
+    sol, res, tres, rloc, _ = dom.solve(uu, None, known_sol=True)
+    xx = dom.hps.xx_tot
+    pick = np.arange(0, xx.shape[0], 97)
+    xs = xx[pick]
+    coef = {k: (np.zeros(xs.shape[0]) if getattr(op, k) is None else np.asarray(getattr(op, k)(xs)).reshape(-1))
+            for k in ('c11', 'c22', 'c12', 'c1', 'c2', 'c')}
+    stride = 7
+    save(f'annulus_p{p}_n{n}_ppw{ppw}.npz', p=p, n=n, ppw=ppw, kh=kh, stride=stride,
+         sol_sub=sol.numpy()[::stride], sol_norm=np.linalg.norm(sol.numpy()), res=float(res),
+         trueres=float(tres), resloc=float(rloc), coef_pick=pick, coef_xx=xs.numpy(),
+         mapped_xx=param_map(xs).numpy(), **{'coef_' + k: v for k, v in coef.items()})
+
+
 def solve_fixtures():
     dom, kh, sol, res, tres, rloc = run_domain(8, 48, 10, 'bfield_gaussian_bumps', 'superLU')
     save('solve_superlu_p8_n48.npz', p=8, n=48, kh=kh, sol=sol, res=res, trueres=tres, resloc=rloc)
@@ -227,6 +254,7 @@ if __name__ == '__main__':
     if len(sys.argv) > 2 and sys.argv[2] == 'c12':  # only the mixed-derivative fixtures
         dtn_c12_fixture(12, 0.0125, 40, [0, 7, 800, 1599], 60.0, 'dtn_c12_p12.npz', seed=5)
         dtn_c12_fixture(8, 1 / 64, 32, [0, 5, 500, 1023], 40.0, 'dtn_c12_p8.npz', seed=6)
+        annulus_fixture()
         sys.exit(0)
     leaf_fixtures()
     dtn_fixture(22, 0.005, 100, [0, 57, 4950, 9999, 1234, 6789, 3210, 8888], 1258.6, 'dtn_p22.npz')

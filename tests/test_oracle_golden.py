@@ -155,3 +155,33 @@ def test_reference_slablu_solutions(golden_dir, name):
     assert abs(trueres - float(g['trueres'])) < 1e-6 * float(g['trueres']) + 1e-12
     if p == 22:
         assert trueres < 2e-5   # tests/test_2d.py:43 (p=22, n=400, ppw=40)
+
+
+def test_reference_annulus_known_answer(golden_dir):
+    """The reference's annulus test (tests/test_2d.py:51-52): Helmholtz on the annulus
+    through its parameter map (coefficients with a mixed derivative), free-space
+    Green's function data, trueres < 2e-5 (tests/test_2d.py:43), and the reference's
+    solution vector."""
+    g = load(golden_dir, 'annulus_p22_n400_ppw40.npz')
+    p, n, kh = int(g['p']), int(g['n']), float(g['kh'])
+    pdo, pmap = funcs.annulus_pdo(kh, funcs.bfield_constant)
+    # the restated coefficient map against the reference's values at sampled nodes
+    xs = g['coef_xx']
+    assert np.abs(pmap(xs) - g['mapped_xx']).max() < 1e-14
+    for k in ('c11', 'c22', 'c12', 'c2', 'c'):
+        ref = g['coef_' + k]
+        assert np.abs(pdo[k](xs) - ref).max() <= 1e-13 * max(np.abs(ref).max(), 1.0), k
+    assert np.abs(g['coef_c1']).max() == 0.0
+    a = 1 / (2 * (n / (p - 2)))
+    md = domain.Multidomain([[0, 1], [0, 1]], a, p)
+    part = domain.SlabPartition(md, 1.0)
+    co = md.coeffs(pdo)
+    ud = lambda x: funcs.uu_dir_greens(pmap(x), kh)
+    out = domain.solve_full(md, part, co, ud)
+    sol = out['sol_tot']
+    stride = int(g['stride'])
+    assert np.linalg.norm(sol[::stride] - g['sol_sub']) / np.linalg.norm(g['sol_sub']) < 1e-9
+    true = ud(md.xx_tot)
+    trueres = np.linalg.norm(sol - true) / np.linalg.norm(true)
+    assert trueres < 2e-5
+    assert abs(trueres - float(g['trueres'])) < 1e-3 * float(g['trueres'])
