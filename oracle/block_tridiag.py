@@ -9,6 +9,9 @@ Restates, in NumPy/SciPy and FP64,
   src_solver/block_tridiag_solver_structured.py:34-76, 157-187
                                                      interface block LU (build_lowmem_helper,
                                                      __solve_lowmem) on dense blocks
+  src_solver/block_tridiag_solver_structured.py:118-154, 189-206
+                                                     cyclic interface system (periodic
+                                                     boundary): corner block eliminated last
 Pivot vectors are LAPACK's (0-based here, 1-based in torch); the factor
 values are identical to the reference's because both call getrf.
 """
@@ -144,3 +147,41 @@ class InterfaceBlockLU:
             t = _L_solve(self.LU[j], self.piv[j], self.sup[j] @ F[j + 1])
             F[j] = _U_solve(self.LU[j], F[j] - t)
         return F
+
+
+class CyclicInterfaceBlockLU:
+    """Cyclic block-tridiagonal interface system of a periodic domain.
+
+    Block j couples to j-1 and j+1 modulo nb: sub[j] is block (j, j-1 mod nb)
+    and sup[j] is block (j, j+1 mod nb); diag, sub, sup are (nb, n, n).  As in
+    block_tridiag_solver_structured.py:118-154, blocks 1..nb-1 form an acyclic
+    system (factored by InterfaceBlockLU), the two couplings of block 0 are
+    carried through it, V = A'^{-1} [-sub_1; 0; ...; 0; -sup_{nb-1}], and the
+    Schur complement of block 0, X = diag_0 + sup_0 V_0 + sub_0 V_{nb-2}, is
+    LU-factored.  The solve (:189-206): u = A'^{-1} f[1:], x_0 = X^{-1}
+    (f_0 - sup_0 u_0 - sub_0 u_{nb-2}), x[1:] = V x_0 + u.
+    """
+
+    def __init__(self, diag, sub, sup):
+        nb, n = diag.shape[0], diag.shape[1]
+        if nb < 3:
+            raise ValueError('a cyclic interface system needs at least 3 blocks')
+        self.nb, self.n = nb, n
+        self.inner = InterfaceBlockLU(diag[1:], sub[2:], sup[1:nb - 1])
+        W = np.zeros((nb - 1, n, n))
+        W[0] = -sub[1]
+        W[nb - 2] = -sup[nb - 1]
+        self.V = self.inner.solve(W)
+        X = diag[0] + sup[0] @ self.V[0] + sub[0] @ self.V[nb - 2]
+        self.X = _lu(X)
+        self.sub0, self.sup0 = sub[0], sup[0]
+
+    def solve(self, f):
+        """f: (nb, n, nrhs) -> (nb, n, nrhs)."""
+        F = np.asarray(f, dtype=float)
+        u = self.inner.solve(F[1:])
+        rhs = F[0] - self.sup0 @ u[0] - self.sub0 @ u[self.nb - 2]
+        out = np.empty_like(F)
+        out[0] = sla.lu_solve(self.X, rhs, check_finite=False)
+        out[1:] = np.einsum('kij,jr->kir', self.V, out[0]) + u
+        return out

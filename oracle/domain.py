@@ -9,8 +9,11 @@ Restates, in NumPy/SciPy and FP64,
   src_solver/slablu_solver.py:35-46         get_nearest_div
   src_solver/slablu_solver.py:61-123        Domain_Solver.__init__ (I_Ctot, I_Xtot)
   src_solver/slablu_solver.py:127-202       hps_disc / hps_panel_split
-  src_solver/slablu_solver.py:360-385,601-620  superLU black-box path (the FP64 oracle)
+  src_solver/slablu_solver.py:360-385,414-433,601-620  superLU black-box path (the FP64
+                                            oracle), with the periodic fold
   src_solver/slablu_solver.py:297-358,543-599,901-943  two-level slab solve
+  src_solver/slablu_solver.py:89-120,489-541,1232-1303  periodic partition, right-hand
+                                            side and cyclic interface assembly
 """
 import numpy as np
 import scipy.sparse as sp
@@ -121,8 +124,9 @@ class Multidomain:
 class SlabPartition:
     """Slab split of the leaf grid (slablu_solver.py:61-123, 127-202)."""
 
-    def __init__(self, md, buf_constant=1.0):
+    def __init__(self, md, buf_constant=1.0, periodic=False):
         q, n0, n1 = md.q, md.n0, md.n1
+        self.periodic = bool(periodic)
         n_tmp = max(n0, n1) * q - 1
         buf_points = min(400, int(n_tmp ** (2 / 3) * buf_constant))
         buf = max(int(buf_points / q) + 1, 2)
@@ -145,23 +149,63 @@ class SlabPartition:
         self.rem_m, self.rem_bs = n1 - 1, buf * q
         ip = self.inds_pans
         self.I_slabC = ip[:, self.I_C].ravel()
-        self.I_slabX = ip[1:, self.I_L].ravel()
+        if not self.periodic:
+            self.I_slabX = ip[1:, self.I_L].ravel()
+            self.I_Xtot = np.concatenate((ip[0, self.I_L], ip[-1, self.I_R],
+                                          ip[:, self.I_D].ravel(), ip[:, self.I_U].ravel()))
+        else:
+            # the left edge of slab 0 and the right edge of the last slab are the
+            # same curve: both stay in I_Ctot (the right one last), and only the
+            # bottom and top faces carry Dirichlet data (slablu_solver.py:89-120)
+            self.I_slabX = np.concatenate((ip[:, self.I_L].ravel(), ip[-1, self.I_R]))
+            self.I_Xtot = np.concatenate((ip[:, self.I_D].ravel(), ip[:, self.I_U].ravel()))
+            nL, off = self.I_L.size, self.I_C.size * self.Npan
+            self.I_Ctot_unique = np.arange(off + nL * self.Npan)
+            self.I_Ctot_copy1 = np.arange(nL) + off
+            self.I_Ctot_copy2 = np.arange(nL) + off + nL * self.Npan
         self.I_Ctot = np.concatenate((self.I_slabC, self.I_slabX))
-        self.I_Xtot = np.concatenate((ip[0, self.I_L], ip[-1, self.I_R],
-                                      ip[:, self.I_D].ravel(), ip[:, self.I_U].ravel()))
 
 
-def dirichlet_rhs(A, part, u_dir):
-    """ff = -A[I_Ctot, I_Xtot] u_dir (slablu_solver.py:489-507)."""
-    return -(A[part.I_Ctot][:, part.I_Xtot] @ u_dir)
+def dirichlet_rhs(A, part, u_dir, fold=True):
+    """ff = -A[I_Ctot, I_Xtot] u_dir (slablu_solver.py:489-526).  With a periodic
+    partition and ``fold``, the rows of the right edge are added to those of
+    the left edge and dropped (:520-524)."""
+    ff = -(A[part.I_Ctot][:, part.I_Xtot] @ u_dir)
+    if part.periodic and fold:
+        ff[part.I_Ctot_copy1] += ff[part.I_Ctot_copy2]
+        ff = ff[part.I_Ctot_unique]
+    return ff
+
+
+def periodic_fold(part):
+    """Selection matrix P (|I_Ctot| x |unique|): P[k, k] = 1 for the unique
+    unknowns and P[copy2_k, copy1_k] = 1.  P^T A_CC P is the reference's folded
+    matrix (slablu_solver.py:418-433): the right-edge rows and columns added
+    onto the left edge's; at most two nonzero terms meet in an entry, so the
+    sums are exact whatever their order."""
+    n_all, n_u = part.I_Ctot.size, part.I_Ctot_unique.size
+    rows = np.concatenate((part.I_Ctot_unique, part.I_Ctot_copy2))
+    cols = np.concatenate((part.I_Ctot_unique, part.I_Ctot_copy1))
+    return sp.csr_matrix((np.ones(rows.size), (rows, cols)), shape=(n_all, n_u))
+
+
+def reduced_matrix(A, part):
+    """A_CC of the reduced system, folded for a periodic partition."""
+    A_CC = A[part.I_Ctot][:, part.I_Ctot]
+    if part.periodic:
+        P = periodic_fold(part)
+        A_CC = P.T @ A_CC @ P
+    return A_CC.tocsc()
 
 
 def solve_superlu(md, part, A, u_dir):
-    """FP64 sparse direct solve of the reduced system (slablu_solver.py:360-385, 601-620).
+    """FP64 sparse direct solve of the reduced system (slablu_solver.py:360-385,
+    414-433, 601-620).
 
-    Returns the reduced solution on I_Ctot, the RHS and ||A_CC x - f|| / ||f||.
+    Returns the reduced solution (on I_Ctot; on its unique part for a periodic
+    partition), the RHS and ||A_CC x - f|| / ||f||.
     """
-    A_CC = A[part.I_Ctot][:, part.I_Ctot].tocsc()
+    A_CC = reduced_matrix(A, part)
     ff = dirichlet_rhs(A, part, u_dir)
     lu = spla.splu(A_CC)
     x = lu.solve(ff)
@@ -171,9 +215,15 @@ def solve_superlu(md, part, A, u_dir):
 
 
 def assemble_solution(md, part, x, u_dir):
-    """sol_tot on all unique face nodes (slablu_solver.py:630-642)."""
+    """sol_tot on all unique face nodes (slablu_solver.py:630-642); for a periodic
+    partition x is on the unique unknowns and the right edge takes the left
+    edge's values."""
     sol = np.zeros((md.ntot, x.shape[-1]))
-    sol[part.I_Ctot] = x
+    if part.periodic:
+        sol[part.I_Ctot[part.I_Ctot_unique]] = x
+        sol[part.I_Ctot[part.I_Ctot_copy2]] = x[part.I_Ctot_copy1]
+    else:
+        sol[part.I_Ctot] = x
     sol[part.I_Xtot] = u_dir
     return sol
 
@@ -273,10 +323,20 @@ class SlabLU:
             self.T.append(Axx - Axc @ self.slab_solve(s, Acx))
         nL = pt.I_L.size
         Tb = np.stack(self.T)
-        diagI = Tb[:-1, nL:, nL:] + Tb[1:, :nL, :nL]
-        subI = Tb[1:-1, nL:, :nL]
-        supI = Tb[1:-1, :nL, nL:]
-        self.iface = bt.InterfaceBlockLU(diagI, subI, supI)
+        if not pt.periodic:
+            diagI = Tb[:-1, nL:, nL:] + Tb[1:, :nL, :nL]
+            subI = Tb[1:-1, nL:, :nL]
+            supI = Tb[1:-1, :nL, nL:]
+            self.iface = bt.InterfaceBlockLU(diagI, subI, supI)
+        else:
+            # interface j is the left edge of slab j, and the right edge of slab
+            # j-1 (of the last slab for j = 0): diag_j = T_RR(j-1) + T_LL(j),
+            # sub_j = T_RL(j-1), sup_j = T_LR(j) (slablu_solver.py:1260-1303)
+            prev = np.roll(np.arange(pt.Npan), 1)
+            diagI = Tb[prev, nL:, nL:] + Tb[:, :nL, :nL]
+            subI = Tb[prev, nL:, :nL]
+            supI = Tb[:, :nL, nL:]
+            self.iface = bt.CyclicInterfaceBlockLU(diagI, subI, supI)
 
     def _aloc_solve(self, s, rhs, transpose=False):
         pt = self.part
@@ -307,17 +367,29 @@ class SlabLU:
         return np.concatenate((ue, ur))
 
     def solve(self, ff):
-        """Reduced solve on I_Ctot ordering (solve_helper, slablu_solver.py:543-599)."""
+        """Reduced solve on I_Ctot ordering (solve_helper, slablu_solver.py:543-599).
+
+        For a periodic partition ff is the unfolded right-hand side on all of
+        I_Ctot (get_rhs with sum_body_load=False); the interface right-hand
+        side is folded, the cyclic system solved and the left-edge values
+        copied to the right edge; the result is on the unique unknowns."""
         pt = self.part
-        nC = pt.I_C.size
+        nC, nL = pt.I_C.size, pt.I_L.size
         nrhs = ff.shape[-1]
         fC = ff[: pt.Npan * nC]
         yC = np.concatenate([self.slab_solve(s, fC[s * nC:(s + 1) * nC]) for s in range(pt.Npan)])
         fX = ff[pt.Npan * nC:] - self.A[pt.I_slabX][:, pt.I_slabC] @ yC
-        uX = self.iface.solve(fX.reshape(pt.Npan - 1, -1, nrhs)).reshape(-1, nrhs)
+        if pt.periodic:
+            fX[:nL] += fX[pt.Npan * nL:]
+            fX = fX[:pt.Npan * nL]
+            uX = self.iface.solve(fX.reshape(pt.Npan, -1, nrhs)).reshape(-1, nrhs)
+            uX = np.concatenate((uX, uX[:nL]))
+        else:
+            uX = self.iface.solve(fX.reshape(pt.Npan - 1, -1, nrhs)).reshape(-1, nrhs)
         g = fC - self.A[pt.I_slabC][:, pt.I_slabX] @ uX
         uC = np.concatenate([self.slab_solve(s, g[s * nC:(s + 1) * nC]) for s in range(pt.Npan)])
-        return np.concatenate((uC, uX))
+        sol = np.concatenate((uC, uX))
+        return sol[pt.I_Ctot_unique] if pt.periodic else sol
 
 
 def slablu_pipeline(md, part, co, u_dir_func):
@@ -331,7 +403,7 @@ def slablu_pipeline(md, part, co, u_dir_func):
     S = SlabLU(md, part, A)
     t2 = time.perf_counter()
     u_dir = np.asarray(u_dir_func(md.xx_active[part.I_Xtot]), dtype=float).reshape(-1, 1)
-    ff = dirichlet_rhs(A, part, u_dir)
+    ff = dirichlet_rhs(A, part, u_dir, fold=False)
     x = S.solve(ff)
     sol = assemble_solution(md, part, x, u_dir)
     u_tot, _ = leaf_recover(md, co, sol)

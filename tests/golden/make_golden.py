@@ -10,6 +10,7 @@ monkeypatch in its own process; the reference source is not modified.
 Outputs are small .npz files beside this script; they are committed and read
 by the CPU tests (the reference source is not needed afterwards).
 """
+import hashlib
 import os
 import sys
 
@@ -239,6 +240,52 @@ def annulus_fixture(p=22, n=400, ppw=40):
          mapped_xx=param_map(xs).numpy(), **{'coef_' + k: v for k, v in coef.items()})
 
 
+def periodic_fixture(name, geom, box, p, n, ppw, stride=5):
+    """Periodic boundary (Domain_Solver(periodic_bc=True)): the left and right
+    edges of the rectangle are identified, Dirichlet data on the bottom and top.
+    ``geom`` 'curvy_annulus' is the reference's third test (tests/test_2d.py:54-55)
+    at a smaller size; 'square' is Helmholtz with Gaussian bumps on the unit
+    square.  Both the reference's slabLU (cyclic interface solver) and its
+    superLU path (folded sparse matrix) are recorded, with the partition."""
+    nwaves = int(n / ppw)
+    kh = (nwaves + 0.03) * 2 * np.pi + 1.8
+    if geom == 'square':
+        op = ref_pdo.PDO_2d(ref_pdo.ones, ref_pdo.ones,
+                            c=lambda xx: bif.bfield_gaussian_bumps(xx, kh).reshape(-1))
+        pmap = lambda xx: xx.clone()
+    else:
+        op, pmap, _ = ref_pdo.get_param_map_and_pdo(geom, bif.bfield_constant, kh)
+    a = 1 / (2 * (n / (p - 2)))
+    uu = lambda xx: bif.uu_dir_func_greens(pmap(xx), kh)
+    out = dict(p=p, n=n, ppw=ppw, kh=kh, stride=stride, box=np.asarray(box))
+    for solver in ('slabLU', 'superLU'):
+        dom = Domain_Solver(torch.tensor(box), op, kh, a, p=p, buf_constant=1.0, periodic_bc=True)
+        dom.build('reduced_cpu', solver, verbose=False)
+        sol, res, tres, rloc, _ = dom.solve(uu, None, known_sol=True)
+        sol, res, tres, rloc, _ = dom.solve(uu, None, known_sol=True)
+        sol = sol.numpy()
+        out.update({solver + '_sol_sub': sol[::stride], solver + '_sol_norm': np.linalg.norm(sol),
+                    solver + '_res': float(res), solver + '_trueres': float(tres),
+                    solver + '_resloc': float(rloc)})
+    out.update(buf=np.array(dom.buf_pans), Npan=np.array(dom.Npan), nbox=dom.hps.n.numpy())
+    for nm in ('I_Ctot', 'I_Xtot', 'I_slabX', 'I_Ctot_unique', 'I_Ctot_copy1', 'I_Ctot_copy2'):
+        v = np.ascontiguousarray(np.asarray(getattr(dom, nm)), dtype=np.int64)
+        if v.size <= 10000:
+            out[nm] = v
+        else:  # large index sets: length and SHA-256 of the int64 bytes
+            out[nm + '_size'] = np.array(v.size)
+            out[nm + '_sha256'] = np.array(hashlib.sha256(v.tobytes()).hexdigest())
+    if geom != 'square':
+        xx = dom.hps.xx_tot
+        pick = np.arange(0, xx.shape[0], 397)
+        xs = xx[pick]
+        out.update(coef_xx=xs.numpy(), mapped_xx=pmap(xs).numpy())
+        for k in ('c11', 'c22', 'c12', 'c1', 'c2', 'c'):
+            f = getattr(op, k)
+            out['coef_' + k] = np.zeros(xs.shape[0]) if f is None else np.asarray(f(xs)).reshape(-1)
+    save(name, **out)
+
+
 def solve_fixtures():
     dom, kh, sol, res, tres, rloc = run_domain(8, 48, 10, 'bfield_gaussian_bumps', 'superLU')
     save('solve_superlu_p8_n48.npz', p=8, n=48, kh=kh, sol=sol, res=res, trueres=tres, resloc=rloc)
@@ -251,6 +298,11 @@ def solve_fixtures():
 
 
 if __name__ == '__main__':
+    if len(sys.argv) > 2 and sys.argv[2] == 'periodic':  # only the periodic-boundary fixtures
+        periodic_fixture('periodic_curvy_annulus_p12_n230.npz', 'curvy_annulus', [[0, 6.0], [0, 1.0]], 12, 230, 40,
+                         stride=41)
+        periodic_fixture('periodic_square_p12_n210.npz', 'square', [[0, 1.0], [0, 1.0]], 12, 210, 40, stride=7)
+        sys.exit(0)
     if len(sys.argv) > 2 and sys.argv[2] == 'c12':  # only the mixed-derivative fixtures
         dtn_c12_fixture(12, 0.0125, 40, [0, 7, 800, 1599], 60.0, 'dtn_c12_p12.npz', seed=5)
         dtn_c12_fixture(8, 1 / 64, 32, [0, 5, 500, 1023], 40.0, 'dtn_c12_p8.npz', seed=6)
