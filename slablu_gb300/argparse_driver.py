@@ -6,8 +6,10 @@
 Builds once and solves twice (the second solve is the reported one), and
 pickles ``build_info`` then ``solve_info`` with the reference's keys
 (argparse_driver.py:169-188, 248-298).  Added flags: --precision, --tol.
-Out of scope here: --disc fd, curved domains, periodic BC, the superLU/PETSc
-black-box solvers, --disable_cuda (slablu_gb300 has no CPU path).
+--periodic_bc identifies the left and right edges of the box (Dirichlet data on
+the bottom and top only), as in the reference.  Out of scope here: --disc fd,
+curved domains, the superLU/PETSc black-box solvers, --disable_cuda
+(slablu_gb300 has no CPU path).
 """
 import argparse
 import pickle

@@ -19,15 +19,19 @@ Differences from the reference, by design:
   * the reduced sparse operator is not needed by the solver; ``hps.sparse_mat``
     and ``get_rhs`` assemble and apply it on the GPU for callers of the
     reference's sparse interface (slablu_gb300/sparse.py).
-Out of scope (raise NotImplementedError): finite differences (p = 0),
-periodic boundary conditions, mixed second derivatives (c12).
+  * periodic_bc=True couples the shared edge back through its Schur complement
+    on top of the non-periodic factorization (slablu_gb300/periodic.py) instead
+    of the reference's cyclic interface solver; ``rel_err`` is then the
+    relative residual of the folded reduced system, as in the reference.
+Out of scope (raise NotImplementedError): finite differences (p = 0), mixed
+second derivatives (c12), body loads with periodic_bc.
 """
 import time
 
 import numpy as np
 import torch
 
-from . import _lib
+from . import _lib, periodic, sparse
 from .engine import SlabEngine
 from .hps import Geometry
 
@@ -81,14 +85,12 @@ class Domain_Solver:
                  tol=1e-10, max_iter=12, device='cuda'):
         if p == 0:
             raise NotImplementedError('slablu_gb300 provides the HPS discretisation only (p > 0)')
-        if periodic_bc:
-            raise NotImplementedError('periodic boundary conditions are not provided by slablu_gb300')
         if getattr(pdo_op, 'c12', None) is not None:
             raise NotImplementedError('operators with a mixed derivative term c12 are not provided')
         self.kh = kh
         self.pdo = pdo_op
         self.buf_constant = buf_constant
-        self.periodic_bc = False
+        self.periodic_bc = bool(periodic_bc)
         self.precision, self.tol, self.max_iter = precision, tol, max_iter
         self.device = torch.device(device)
         bg = box_geom.detach().cpu().numpy() if isinstance(box_geom, torch.Tensor) else np.asarray(box_geom)
@@ -103,7 +105,14 @@ class Domain_Solver:
         self.I_L, self.I_R, self.I_D, self.I_U, self.I_C = (lt(g.I_L), lt(g.I_R), lt(g.I_D), lt(g.I_U), lt(g.I_C))
         self.I_slabC, self.I_slabX = lt(g.I_slabC), lt(g.I_slabX)
         self.I_Ctot, self.I_Xtot = lt(g.I_Ctot), lt(g.I_Xtot)
+        if self.periodic_bc:
+            self._psets = periodic.periodic_index_sets(g)
+            ps = self._psets
+            self.I_slabX, self.I_Ctot, self.I_Xtot = lt(ps['I_slabX']), lt(ps['I_Ctot']), lt(ps['I_Xtot'])
+            self.I_Ctot_unique = lt(ps['I_Ctot_unique'])
+            self.I_Ctot_copy1, self.I_Ctot_copy2 = lt(ps['I_Ctot_copy1']), lt(ps['I_Ctot_copy2'])
         self.engine = None
+        self._edge = None
         self.solver_type = None
 
     # -- coefficients at every leaf node, evaluated on the device -----------------
@@ -140,9 +149,17 @@ class Domain_Solver:
         self.engine.factor(**co)
         torch.cuda.synchronize()
         toc_factor = time.time() - tic2
+        toc_edge = 0.0
+        if self.periodic_bc:
+            tic3 = time.time()
+            self._build_periodic_edge()
+            torch.cuda.synchronize()
+            toc_edge = time.time() - tic3
         toc_build = time.time() - tic
         info = dict(toc_build=toc_build, toc_assembly=toc_coeff, toc_factor=toc_factor,
                     mem_build=self.engine.factor_bytes / 1e9, precision=self.precision)
+        if self.periodic_bc:
+            info.update(toc_periodic_edge=toc_edge, periodic_edge_size=self._edge.nL)
         if verbose:
             print(f'SLABLU GB300 BUILD ({self.precision}): {toc_build:.3f} s, factors {info["mem_build"]:.2f} GB, '
                   f'buf={self.buf_pans} Npan={self.Npan}')
@@ -165,7 +182,21 @@ class Domain_Solver:
             ud = ud[:, None]
         x = torch.zeros(self.ntot, ud.shape[1], dtype=torch.float64, device=self.device)
         x[self.I_Xtot.to(self.device)] = ud.to(self.device)
-        return -A.matvec(x)[self.I_Ctot.to(self.device)]
+        ff = -A.matvec(x)[self.I_Ctot.to(self.device)]
+        if self.periodic_bc and sum_body_load:
+            ff = periodic.fold(ff, self._psets)
+        return ff
+
+    def _build_periodic_edge(self):
+        """Schur complement of the shared edge (slablu_gb300/periodic.py), with the
+        edge rows of the reduced operator assembled on the GPU."""
+        g = self.geom
+        if getattr(self.hps, '_A', None) is None:
+            self.hps.sparse_mat(self.device)
+        left, right = periodic.edge_faces(g)
+        E = sparse.row_subset(g, self.hps._A, np.concatenate((left, right)))
+        self._edge = periodic.PeriodicEdge(self.engine, E.matvec, left, right, self.ntot, tol=self.tol,
+                                           max_iter=self.max_iter).build(self.device)
 
     def get_rhs_boundary(self, uu_dir_func):
         """Face vector carrying Dirichlet data at I_Xtot (slablu_solver.py:504)."""
@@ -189,15 +220,23 @@ class Domain_Solver:
         bnd = self.get_rhs_boundary(uu_dir_func)
         fb = None
         if ff_body_func is not None:
+            if self.periodic_bc:
+                raise NotImplementedError('body loads with periodic_bc are not provided')
             xx = torch.as_tensor(self.geom.xx_tot, dtype=torch.float64, device=self.device)
             fb = torch.as_tensor(ff_body_func(xx), dtype=torch.float64).to(self.device)
             if fb.dim() == 1:
                 fb = fb[:, None]
-        uleaf, _, iters, st = self.engine.solve(bnd, fb, tol=self.tol, max_iter=self.max_iter, allow_noconv=True)
+        if self.periodic_bc:
+            uleaf, uf, st = self._edge.solve(bnd)
+            iters = st['engine_iters']
+            rel_err = torch.tensor(self._folded_residual(uf, bnd))
+        else:
+            uleaf, _, iters, st = self.engine.solve(bnd, fb, tol=self.tol, max_iter=self.max_iter,
+                                                    allow_noconv=True)
+            rel_err = torch.tensor(st['rel_residual'])
         sol_tot = uleaf.cpu()
         toc_solve = time.time() - tic
         self.last_solve_info = dict(st, iters=iters)
-        rel_err = torch.tensor(st['rel_residual'])
         true_err = torch.tensor([float('nan')])
         if known_sol:
             uu_true = torch.as_tensor(uu_dir_func(self.hps.xx_tot.clone()), dtype=torch.float64)
@@ -205,3 +244,19 @@ class Domain_Solver:
                 uu_true = uu_true[:, None]
             true_err = torch.linalg.norm(sol_tot - uu_true) / torch.linalg.norm(uu_true)
         return sol_tot, rel_err, true_err, st['resloc'], toc_solve
+
+    def _folded_residual(self, uf, bnd):
+        """||A_CC x - ff|| / ||ff|| of the folded periodic reduced system
+        (slablu_solver.py:528-541, 594-596), with A applied on the GPU: at the
+        unknown faces, A u (u with the Dirichlet data) is A_CC x + A_CX d =
+        A_CC x - ff, and -A d is ff."""
+        A = self.hps._A
+        bnd = bnd if bnd.dim() == 2 else bnd[:, None]
+        d = torch.zeros_like(uf)
+        ix = self.I_Xtot.to(uf.device)
+        d[ix] = bnd[ix]
+        ic = self.I_Ctot.to(uf.device)
+        r = periodic.fold(A.matvec(uf)[ic], self._psets)
+        ff = periodic.fold(-A.matvec(d)[ic], self._psets)
+        fn = float(torch.linalg.norm(ff))
+        return float(torch.linalg.norm(r)) / fn if fn > 0 else float(torch.linalg.norm(r))

@@ -76,6 +76,21 @@ class ReducedCSR:
         return Y[:, 0] if squeeze else Y
 
 
+def row_subset(geom, A, rows):
+    """The rows ``rows`` (reduced indices) of the reduced operator ``A`` as a CSR
+    matrix (len(rows) x ntot) sharing A's values (gathered on the device)."""
+    indptr, indices, _ = reduced_pattern(geom)
+    rows = np.asarray(rows, dtype=np.int64)
+    lens = indptr[rows + 1] - indptr[rows]
+    sub_ptr = np.zeros(rows.size + 1, dtype=np.int64)
+    sub_ptr[1:] = np.cumsum(lens)
+    slots = np.repeat(indptr[rows] - sub_ptr[:-1], lens) + np.arange(int(sub_ptr[-1]))
+    dev = A.vals.device
+    sl = torch.as_tensor(slots, device=dev)
+    return ReducedCSR(torch.as_tensor(sub_ptr, device=dev), torch.as_tensor(indices[slots], device=dev),
+                      A.vals[sl].contiguous(), (int(rows.size), A.shape[1]))
+
+
 def assemble(geom, dtn):
     """Reduced operator from leaf DtN maps ``dtn`` (nleaf, nx, nx) FP64 on the GPU."""
     L = _lib.lib()
