@@ -286,6 +286,51 @@ def periodic_fixture(name, geom, box, p, n, ppw, stride=5):
     save(name, **out)
 
 
+def hbs_kernel(x, j):
+    """Test operator for HBS compression: a smooth, slowly decaying interaction plus a
+    diagonal (numerically low-rank off-diagonal blocks, as the slab interface blocks)."""
+    d = (x[:, None] - x[None, :]).abs()
+    return (1.0 + 0.3 * j) / (1.0 + 40.0 * d) + (2.0 + j) * torch.eye(x.shape[0])
+
+
+def hbs_fixture():
+    """The reference's HBS compression from sketches (src_solver/hbs_reconstruction.py)
+    on small test operators: the sketches, the compressed tensors, products with the
+    compressed matrix and its transpose, and the compressed inverse."""
+    from src_solver.hbs_reconstruction import HBS_matrix
+    out = {}
+    for tag, (b, n, k, seed) in (('L3', (2, 64, 4, 11)), ('L1', (2, 32, 8, 12)), ('pad', (1, 48, 4, 13))):
+        torch.manual_seed(seed)
+        x = torch.rand(n).sort().values
+        A = torch.stack([hbs_kernel(x, j) for j in range(b)])
+        hbs = HBS_matrix(b, n, k)
+        ns = hbs.bs + k
+        Om = torch.rand(1, n, ns)
+        Ps = torch.rand(1, n, ns)
+        Y = A @ Om
+        Z = A.transpose(-1, -2) @ Ps
+        state = torch.get_rng_state()
+        hbs.reconstruct(Om.clone(), Ps.clone(), Y.clone(), Z.clone())
+        if hbs.n_pad > 0:  # replay the padding sketches the reference drew inside reconstruct
+            torch.set_rng_state(state)
+            out[tag + '_Om_pad'] = torch.rand(1, hbs.n_pad, ns).numpy()
+            out[tag + '_Ps_pad'] = torch.rand(1, hbs.n_pad, ns).numpy()
+        q = torch.randn(b, n, 3)
+        f = torch.randn(b, n, 2)
+        out.update({tag + '_x': x.numpy(), tag + '_Om': Om.numpy(), tag + '_Ps': Ps.numpy(),
+                    tag + '_Y': Y.numpy(), tag + '_Z': Z.numpy(),
+                    tag + '_shape': np.array([b, n, k, hbs.bs, hbs.m, hbs.n_pad, hbs.L]),
+                    tag + '_q': q.numpy(), tag + '_mv': hbs.matvec(q.clone()).numpy(),
+                    tag + '_mvT': hbs.matvec(q.clone(), transpose=True).numpy()})
+        if n <= 32:  # the compressed tensors (copies: calc_inverse updates D in place) and the dense matrix
+            out.update({tag + '_UV': hbs.UVtensor.clone().numpy(), tag + '_D': hbs.Dtensor.clone().numpy(),
+                        tag + '_dense': hbs.todense().numpy()})
+        hbs.calc_inverse()
+        out.update({tag + '_f': f.numpy(), tag + '_inv': hbs.apply_inverse(f.clone()).numpy(),
+                    tag + '_invT': hbs.apply_inverse(f.clone(), transpose=True).numpy()})
+    save('hbs.npz', **out)
+
+
 def solve_fixtures():
     dom, kh, sol, res, tres, rloc = run_domain(8, 48, 10, 'bfield_gaussian_bumps', 'superLU')
     save('solve_superlu_p8_n48.npz', p=8, n=48, kh=kh, sol=sol, res=res, trueres=tres, resloc=rloc)
@@ -298,6 +343,9 @@ def solve_fixtures():
 
 
 if __name__ == '__main__':
+    if len(sys.argv) > 2 and sys.argv[2] == 'hbs':  # only the HBS compression fixture
+        hbs_fixture()
+        sys.exit(0)
     if len(sys.argv) > 2 and sys.argv[2] == 'periodic':  # only the periodic-boundary fixtures
         periodic_fixture('periodic_curvy_annulus_p12_n230.npz', 'curvy_annulus', [[0, 6.0], [0, 1.0]], 12, 230, 40,
                          stride=41)
