@@ -111,10 +111,11 @@ def run_reference(args):
     tmean = sum(times) / len(times)
     val = N / tmean
     cores = cpu_threads()
-    line = dict(metric=METRIC, value=val, unit='unknowns/s', n_gpus=0, steps=args.steps, warmup=args.warmup,
+    # n_gpus is the launch's N (the arms are compared per launch); this arm computes on the host cores only
+    line = dict(metric=METRIC, value=val, unit='unknowns/s', n_gpus=args.gpus, steps=args.steps, warmup=args.warmup,
                 ms_per_step=1e3 * tmean, higher_is_better=True, scaling='weak', vs_baseline=None, dtype='f64',
                 data='synthetic', impl='reference',
-                config=dict(workload=reference_workload(args), parallelism='host threads',
+                config=dict(workload=reference_workload(args), parallelism='host threads (no GPU used)',
                             sample=f'each step: the oracle port of the reference CPU slabLU, full factor+solve of '
                                    f'the same field at n={CPU_SAMPLE_N} (N={N}); unknowns/s is size-independent '
                                    f'to within ~15 % for the reference'),
