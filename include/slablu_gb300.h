@@ -69,6 +69,25 @@ int slab_leaf_dtn(int nleaf, int p, const double* d_c11, const double* d_c22, co
                   double* d_S, int* d_info, void* stream);
 
 /*
+ * Batched leaf DtN maps with a mixed-derivative term (c12, for the parameter maps of
+ * curved domains).  Replaces the c12 branch of form_DtNs(mode='build')
+ * (src_disc/hps_parallel_leaf_ops.py:59-65):
+ *   Aloc = -c11 D11 - c22 D22 - 2 c12 D12 + c1 D1 + c2 D2 + diag(c)   (D12 = kron(D, D))
+ *   S    = -Aloc[Jc,Jc]^{-1} Aloc[Jc,Jxreorder] Interp_mat
+ *   DtN  = Nx[:,Jc] S + Nx[:,Jx]
+ * d_interp: 4(p-1) x 4(p-2) doubles, row-major (HPS_Disc.Interp_mat);
+ * d_jxreorder: 4(p-1) ints (JJ.Jxreorder).  Other arguments as slab_leaf_dtn,
+ * with a work area of slab_leaf_dtn_mixed_work_bytes() bytes; d_c12 NULL gives
+ * the slab_leaf_dtn result.
+ */
+size_t slab_leaf_dtn_mixed_work_bytes(int nleaf, int p, int precision);
+int slab_leaf_dtn_mixed(int nleaf, int p, const double* d_c11, const double* d_c22, const double* d_c12,
+                        const double* d_c1, const double* d_c2, const double* d_c, const double* d_D,
+                        const double* d_Dsq, const double* d_Nx, const double* d_interp, const int* d_jxreorder,
+                        int precision, void* d_work, size_t work_bytes, double* d_dtn, double* d_S, int* d_info,
+                        void* stream);
+
+/*
  * Allocation-free batched leaf DtN maps.  No counterpart in the reference: it
  * exists for callers that cannot allocate device memory when they need DtN
  * maps (inside CUDA stream capture, where cudaMalloc is not allowed, or under

@@ -48,6 +48,9 @@ _SIGS = {
     'slab_dgemm_emu': (c_int, [c_int, c_int, c_int, c_double, c_void, c_int, c_void, c_int, c_double, c_void, c_int,
                                c_void, c_size, c_void]),
     'slab_csr_assemble': (c_int, [c_ll, c_void, c_void, c_ll, c_void, c_void]),
+    'slab_leaf_dtn_mixed_work_bytes': (c_size, [c_int, c_int, c_int]),
+    'slab_leaf_dtn_mixed': (c_int, [c_int, c_int] + [c_void] * 11 + [c_int, c_void, c_size, c_void, c_void, c_void,
+                                                                      c_void]),
     'slab_csr_spmv': (c_int, [c_int, c_void, c_void, c_void, c_void, c_double, c_double, c_void, c_void]),
 }
 

@@ -4,16 +4,26 @@
 
 namespace slab {
 
+template <typename T, bool kMixed>
+static int leaf_factor_launch(cudaStream_t s, const LeafFactorArgs<T>& a, int nleaf, int ctas_per_sm) {
+  const size_t bytes = leaf_smem_for_occupancy(reinterpret_cast<const void*>(leaf_factor_kernel<T, kMixed>),
+                                               leaf_factor_smem_bytes(a.p, sizeof(T)), ctas_per_sm);
+  SLAB_TRY(ensure_smem(leaf_factor_kernel<T, kMixed>, bytes, "leaf_factor"));
+  leaf_factor_kernel<T, kMixed><<<nleaf, kNT, bytes, s>>>(a);
+  SLAB_CHECK_LAUNCH();
+  return SLAB_OK;
+}
+
 template <typename T>
 int leaf_factor(cudaStream_t s, const LeafFactorArgs<T>& a, int nleaf, int ctas_per_sm) {
   if (nleaf <= 0) return SLAB_OK;
-  if (a.nx > 2 * kCT) return set_error(SLAB_ERR_ARG, "leaf_factor: p = %d too large", a.p);
-  const size_t bytes = leaf_smem_for_occupancy(reinterpret_cast<const void*>(leaf_factor_kernel<T>),
-                                               leaf_factor_smem_bytes(a.p, sizeof(T)), ctas_per_sm);
-  SLAB_TRY(ensure_smem(leaf_factor_kernel<T>, bytes, "leaf_factor"));
-  leaf_factor_kernel<T><<<nleaf, kNT, bytes, s>>>(a);
-  SLAB_CHECK_LAUNCH();
-  return SLAB_OK;
+  if (a.nx > 2 * kCT || a.nxa > 2 * kCT) return set_error(SLAB_ERR_ARG, "leaf_factor: p = %d too large", a.p);
+  if (a.nxa > 0) {  // mixed derivative: Jxreorder columns and the interpolation stage
+    if (!a.co.c12 || !a.interp || !a.jxr)
+      return set_error(SLAB_ERR_ARG, "leaf_factor: c12, interp and jxreorder are needed together");
+    return leaf_factor_launch<T, true>(s, a, nleaf, ctas_per_sm);
+  }
+  return leaf_factor_launch<T, false>(s, a, nleaf, ctas_per_sm);
 }
 
 size_t leaf_smem_for_occupancy(const void* kernel, size_t need, int ctas_per_sm) {
@@ -348,24 +358,38 @@ __global__ void copy_S_kernel(const T* G, long long strideG, int n, int nx, int 
   }
 }
 
+// nxa: extra columns of the leaf system (4(p-2) face nodes; 4(p-1) Jxreorder
+// nodes with a mixed derivative, plus room for the interpolation matrix).
 template <typename T>
-size_t leaf_work_bytes(int nleaf, int p) {
-  const int q = p - 2, n = q * q, nx = 4 * q;
+size_t leaf_work_bytes(int nleaf, int p, bool mixed = false) {
+  const int q = p - 2, n = q * q, nx = 4 * q, nxa = mixed ? 4 * (p - 1) : nx;
   size_t b = 0;
   auto add = [&](size_t bytes) { b += (bytes + 255) / 256 * 256; };
-  add((size_t)nleaf * n * (n + nx) * sizeof(T));  // G
-  add((size_t)nleaf * n * sizeof(int));           // pivots
-  add((size_t)nleaf * nx * nx * sizeof(T));       // DtN (T)
-  add((size_t)nx * n * sizeof(T));                // Nxc
-  add((size_t)nx * nx * sizeof(T));               // Nxx
+  add((size_t)nleaf * n * (n + nxa) * sizeof(T));  // G
+  add((size_t)nleaf * n * sizeof(int));            // pivots
+  add((size_t)nleaf * nx * nx * sizeof(T));        // DtN (T)
+  add((size_t)nx * n * sizeof(T));                 // Nxc
+  add((size_t)nx * nx * sizeof(T));                // Nxx
+  if (mixed) add((size_t)nxa * nx * sizeof(T));    // interpolation matrix
   return b;
 }
 
 template <typename T>
+__global__ void to_type_kernel(const double* in, T* out, int count) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) out[i] = (T)in[i];
+}
+
+template <typename T>
 int leaf_dtn_impl(int nleaf, int p, const LeafCoeffs& co, const double* D, const double* Dsq, const double* Nx,
-                  void* work, size_t work_bytes, double* dtn_out, double* S_out, int* info, cudaStream_t s) {
+                  void* work, size_t work_bytes, double* dtn_out, double* S_out, int* info, cudaStream_t s,
+                  const double* interp = nullptr, const int* jxr = nullptr) {
   const int q = p - 2, n = q * q, nx = 4 * q;
-  if (work_bytes < leaf_work_bytes<T>(nleaf, p)) return set_error(SLAB_ERR_ARG, "slab_leaf_dtn: work too small");
+  const bool mixed = co.c12 != nullptr;
+  const int nxa = mixed ? 4 * (p - 1) : nx;
+  if (mixed && (!interp || !jxr)) return set_error(SLAB_ERR_ARG, "slab_leaf_dtn_mixed: interp and jxreorder needed");
+  if (mixed && ((size_t)nxa * nx + 32 * (size_t)nxa) * sizeof(T) > leaf_factor_smem_bytes(p, sizeof(T)))
+    return set_error(SLAB_ERR_ARG, "slab_leaf_dtn_mixed: p = %d too small for the interpolation stage", p);
+  if (work_bytes < leaf_work_bytes<T>(nleaf, p, mixed)) return set_error(SLAB_ERR_ARG, "slab_leaf_dtn: work too small");
   unsigned char* w = static_cast<unsigned char*>(work);
   size_t off = 0;
   auto take = [&](size_t bytes) {
@@ -373,7 +397,7 @@ int leaf_dtn_impl(int nleaf, int p, const LeafCoeffs& co, const double* D, const
     off += (bytes + 255) / 256 * 256;
     return ptr;
   };
-  T* G = static_cast<T*>(take((size_t)nleaf * n * (n + nx) * sizeof(T)));
+  T* G = static_cast<T*>(take((size_t)nleaf * n * (n + nxa) * sizeof(T)));
   int* piv = static_cast<int*>(take((size_t)nleaf * n * sizeof(int)));
   T* dtn = static_cast<T*>(take((size_t)nleaf * nx * nx * sizeof(T)));
   T* Nxc = static_cast<T*>(take((size_t)nx * n * sizeof(T)));
@@ -383,8 +407,16 @@ int leaf_dtn_impl(int nleaf, int p, const LeafCoeffs& co, const double* D, const
   LeafFactorArgs<T> a{};
   a.p = p; a.q = q; a.n = n; a.nx = nx;
   a.co = co; a.D = D; a.Dsq = Dsq; a.Nxc = Nxc; a.Nxx = Nxx;
-  a.G = G; a.strideG = (long long)n * (n + nx); a.piv = piv; a.dtn = dtn; a.info = info;
+  a.G = G; a.strideG = (long long)n * (n + nxa); a.piv = piv; a.dtn = dtn; a.info = info;
   a.decouple = 0;
+  if (mixed) {
+    T* interpT = static_cast<T*>(take((size_t)nxa * nx * sizeof(T)));
+    to_type_kernel<T><<<ceil_div(nxa * nx, 256), 256, 0, s>>>(interp, interpT, nxa * nx);
+    SLAB_CHECK_LAUNCH();
+    a.nxa = nxa;
+    a.interp = interpT;
+    a.jxr = jxr;
+  }
   SLAB_TRY(leaf_factor<T>(s, a, nleaf));
   transpose_out_kernel<<<1024, 256, 0, s>>>(dtn, dtn_out, nx, nleaf);
   SLAB_CHECK_LAUNCH();
@@ -412,6 +444,33 @@ extern "C" size_t slab_leaf_dtn_work_bytes(int nleaf, int p, int precision) {
   if (nleaf <= 0 || p < 4) return 0;
   return precision == SLAB_PREC_FP64 ? slab::leaf_work_bytes<double>(nleaf, p)
                                      : slab::leaf_work_bytes<float>(nleaf, p);
+}
+
+extern "C" size_t slab_leaf_dtn_mixed_work_bytes(int nleaf, int p, int precision) {
+  if (nleaf <= 0 || p < 4) return 0;
+  return precision == SLAB_PREC_FP64 ? slab::leaf_work_bytes<double>(nleaf, p, true)
+                                     : slab::leaf_work_bytes<float>(nleaf, p, true);
+}
+
+extern "C" int slab_leaf_dtn_mixed(int nleaf, int p, const double* c11, const double* c22, const double* c12,
+                                   const double* c1, const double* c2, const double* c, const double* D,
+                                   const double* Dsq, const double* Nx, const double* interp, const int* jxreorder,
+                                   int precision, void* work, size_t work_bytes, double* dtn, double* S, int* info,
+                                   void* stream) {
+  if (nleaf <= 0 || p < 4 || !D || !Dsq || !Nx || !interp || !jxreorder || !work || !dtn)
+    return slab::set_error(SLAB_ERR_ARG, "slab_leaf_dtn_mixed: invalid argument");
+  if (precision != SLAB_PREC_FP64 && precision != SLAB_PREC_FP32 && precision != SLAB_PREC_MIXED)
+    return slab::set_error(SLAB_ERR_ARG, "slab_leaf_dtn_mixed: unknown precision %d", precision);
+  slab::LeafCoeffs co{c11, c22, c1, c2, c, c12};
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (!c12)  // no mixed derivative: the face-node system of slab_leaf_dtn
+    return precision == SLAB_PREC_FP64
+               ? slab::leaf_dtn_impl<double>(nleaf, p, co, D, Dsq, Nx, work, work_bytes, dtn, S, info, s)
+               : slab::leaf_dtn_impl<float>(nleaf, p, co, D, Dsq, Nx, work, work_bytes, dtn, S, info, s);
+  if (precision == SLAB_PREC_FP64)
+    return slab::leaf_dtn_impl<double>(nleaf, p, co, D, Dsq, Nx, work, work_bytes, dtn, S, info, s, interp,
+                                       jxreorder);
+  return slab::leaf_dtn_impl<float>(nleaf, p, co, D, Dsq, Nx, work, work_bytes, dtn, S, info, s, interp, jxreorder);
 }
 
 extern "C" int slab_leaf_dtn(int nleaf, int p, const double* c11, const double* c22, const double* c1,

@@ -27,6 +27,7 @@ struct LeafCoeffs {
   const double* c1;
   const double* c2;
   const double* c;
+  const double* c12 = nullptr;  // mixed derivative (leaf DtN entry point only)
 };
 
 template <typename T>
@@ -44,17 +45,27 @@ struct LeafFactorArgs {
   int* info;                // per leaf
   int decouple;             // replace Dirichlet-face rows/cols by identity
   int n0, n1, leaf_begin;   // grid geometry (for decouple)
+  // mixed derivative (co.c12): the extra columns are the nxa = 4(p-1) nodes
+  // jxr (Jxreorder, corners included) and S = -A_cc^{-1} A_c,jxr interp with
+  // interp (nxa x nx, row-major); nxa = 0 means the nx face nodes
+  int nxa;
+  const T* interp;
+  const int* jxr;
 };
 
 // Entry (row node k=(i1,i2), column node (j1,j2)) of
-//   Aloc = -c11 D11 - c22 D22 + c1 D1 + c2 D2 + diag(c)
-// accumulated in the reference's term order (src_disc/hps_parallel_leaf_ops.py:17-27).
+//   Aloc = -c11 D11 - c22 D22 - 2 c12 D12 + c1 D1 + c2 D2 + diag(c)
+// accumulated in the reference's term order (src_disc/hps_parallel_leaf_ops.py:17-27);
+// D12 = kron(D, D), so its entry is the single product D[i1,j1] D[i2,j2].  The
+// c12 term exists only in the kMixed instantiation.
+template <bool kMixed = false>
 __device__ __forceinline__ double aloc_entry(const LeafCoeffs& co, int lofs, int p, int i1, int i2, int j1,
                                              int j2, const double* D, const double* Dsq) {
   const int k = lofs + i1 * p + i2;
   double v = 0.0;
   if (i2 == j2 && co.c11) v += (-co.c11[k]) * Dsq[i1 * p + j1];
   if (i1 == j1 && co.c22) v += (-co.c22[k]) * Dsq[i2 * p + j2];
+  if (kMixed && co.c12) v += (-2.0 * co.c12[k]) * (D[i1 * p + j1] * D[i2 * p + j2]);
   if (i2 == j2 && co.c1) v += co.c1[k] * (-D[i1 * p + j1]);
   if (i1 == j1 && co.c2) v += co.c2[k] * (-D[i2 * p + j2]);
   if (i1 == j1 && i2 == j2 && co.c) v += co.c[k];
@@ -62,12 +73,12 @@ __device__ __forceinline__ double aloc_entry(const LeafCoeffs& co, int lofs, int
 }
 
 // Shared-memory bytes of the assembly stage of leaf_factor_kernel: D, Dsq and
-// the leaf's five coefficient fields (FP64, p*p each) and the (i1, i2) node
+// the leaf's six coefficient fields (FP64, p*p each) and the (i1, i2) node
 // indices of every interior row.  They occupy the start of the dynamic region,
 // which the LU reuses once assembly is done.
 inline size_t leaf_assembly_smem_bytes(int p) {
   const int n = (p - 2) * (p - 2);
-  return 7 * (size_t)p * p * sizeof(double) + 2 * (size_t)n;
+  return 8 * (size_t)p * p * sizeof(double) + 2 * (size_t)n;
 }
 
 // Dynamic shared memory of leaf_factor_kernel<T> for order p.
@@ -80,7 +91,10 @@ inline size_t leaf_factor_smem_bytes(int p, size_t elem) {
 
 // One CTA per leaf: assemble [A_cc | A_cx], pivoted LU, S = -A_cc^{-1} A_cx,
 // DtN = Nx[:,Jc] S + Nx[:,Jx] (src_disc/hps_parallel_leaf_ops.py:40-58).
-template <typename T>
+// kMixed: the operator has a mixed derivative c12 (:59-65): the extra columns
+// are the 4(p-1) nodes Jxreorder (corners included), and after the back
+// substitution X = A_cc^{-1} A_c,Jxreorder is replaced by X Interp_mat.
+template <typename T, bool kMixed = false>
 __global__ void __launch_bounds__(kNT) leaf_factor_kernel(LeafFactorArgs<T> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int tid = threadIdx.x;
@@ -95,18 +109,19 @@ __global__ void __launch_bounds__(kNT) leaf_factor_kernel(LeafFactorArgs<T> a) {
   double* csh = Dsqsh + pp;
   const int lofs = leaf * pp;
   LeafCoeffs cs{};
+  constexpr int kNF = kMixed ? 6 : 5;  // coefficient fields staged
   {
-    const double* src[5] = {a.co.c11, a.co.c22, a.co.c1, a.co.c2, a.co.c};
-    const double** dst[5] = {&cs.c11, &cs.c22, &cs.c1, &cs.c2, &cs.c};
+    const double* src[6] = {a.co.c11, a.co.c22, a.co.c1, a.co.c2, a.co.c, a.co.c12};
+    const double** dst[6] = {&cs.c11, &cs.c22, &cs.c1, &cs.c2, &cs.c, &cs.c12};
 #pragma unroll
-    for (int f = 0; f < 5; ++f) {
+    for (int f = 0; f < kNF; ++f) {
       if (!src[f]) continue;
       double* d = csh + f * pp;
       for (int i = tid; i < pp; i += blockDim.x) cp_async_elem(&d[i], &src[f][lofs + i]);
       *dst[f] = d;
     }
   }
-  unsigned char* ri1 = reinterpret_cast<unsigned char*>(csh + 5 * pp);  // x index of interior row r
+  unsigned char* ri1 = reinterpret_cast<unsigned char*>(csh + kNF * pp);  // x index of interior row r
   unsigned char* ri2 = ri1 + n;                                         // y index
   for (int i = tid; i < pp; i += blockDim.x) {
     Dsh[i] = a.D[i];
@@ -121,31 +136,61 @@ __global__ void __launch_bounds__(kNT) leaf_factor_kernel(LeafFactorArgs<T> a) {
   cp_async_wait_all();
   __syncthreads();
   T* G = a.G + a.strideG * leaf;
-  const int nc = n + nx;
-  // one warp per column: Aloc[Jc, col] is nonzero only on the rows that share
-  // the column node's x or y line
+  const int nxa = kMixed ? a.nxa : nx;  // extra columns: face nodes, or Jxreorder with c12
+  const int nc = n + nxa;
+  // one warp per column: without c12, Aloc[Jc, col] is nonzero only on the rows
+  // that share the column node's x or y line
   {
     const int lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
     for (int col = warp; col < nc; col += nwarps) {
       int j1, j2;
-      if (col < n)
+      if (col < n) {
         interior_node(col, q, j1, j2);
-      else
+      } else if (kMixed) {
+        const int t = a.jxr[col - n];
+        j1 = t / p;
+        j2 = t % p;
+      } else {
         face_node(col - n, p, q, j1, j2);
+      }
       T* gc = G + (size_t)col * n;
       for (int r = lane; r < n; r += 32) {
         const int i1 = ri1[r], i2 = ri2[r];
         // zeros are stored as T directly: an FP64 -> FP32 conversion runs at
         // the FP64 rate, which is 1/64 of FP32 on this GPU
         T v = T(0);
-        if (i1 == j1 || i2 == j2) v = (T)aloc_entry(cs, 0, p, i1, i2, j1, j2, Dsh, Dsqsh);
+        if (kMixed || i1 == j1 || i2 == j2) v = (T)aloc_entry<kMixed>(cs, 0, p, i1, i2, j1, j2, Dsh, Dsqsh);
         gc[r] = v;
       }
     }
   }
   __syncthreads();
   cta_getrf_aug<T>(G, n, n, nc, a.piv + (size_t)leaf * n, smem, a.info ? a.info + leaf : nullptr);
-  for (int c0 = 0; c0 < nx; c0 += kCT) cta_backsub<T>(G, n, n, n + c0, min(kCT, nx - c0), smem);
+  for (int c0 = 0; c0 < nxa; c0 += kCT) cta_backsub<T>(G, n, n, n + c0, min(kCT, nxa - c0), smem);
+  if constexpr (kMixed) {
+    // X Interp_mat in place of the first nx extra columns, 32 rows at a time
+    // (each chunk's rows are read completely before they are overwritten;
+    // cta_backsub ends with a block barrier, so the staging area is free)
+    constexpr int kR = 32;
+    T* Is = smem;                    // nxa x nx, row-major
+    T* Xc = Is + (size_t)nxa * nx;   // kR x nxa
+    for (int idx = tid; idx < nxa * nx; idx += blockDim.x) Is[idx] = a.interp[idx];
+    for (int r0 = 0; r0 < n; r0 += kR) {
+      const int rr = min(kR, n - r0);
+      __syncthreads();
+      for (int idx = tid; idx < rr * nxa; idx += blockDim.x) {
+        const int r = idx % rr, t = idx / rr;
+        Xc[r + t * kR] = G[(size_t)(n + t) * n + r0 + r];
+      }
+      __syncthreads();
+      for (int idx = tid; idx < rr * nx; idx += blockDim.x) {
+        const int r = idx % rr, c = idx / rr;
+        T v = T(0);
+        for (int t = 0; t < nxa; ++t) v += Xc[r + t * kR] * Is[(size_t)t * nx + c];
+        G[(size_t)(n + c) * n + r0 + r] = v;
+      }
+    }
+  }
   // DtN = Nxx - Nxc X  (X = A_cc^{-1} A_cx, S = -X)
   T* dtn = a.dtn + (size_t)leaf * nx * nx;
   for (int idx = tid; idx < nx * nx; idx += blockDim.x) dtn[idx] = a.Nxx[idx];

@@ -165,10 +165,12 @@ class SlabEngine:
         return rint, rf.T
 
 
-def leaf_dtn(coeffs, p, D, Dsq, Nx, precision='fp64', return_S=False):
+def leaf_dtn(coeffs, p, D, Dsq, Nx, precision='fp64', return_S=False, interp=None, jxreorder=None):
     """Batched leaf DtN maps (form_DtNs 'build') through slab_leaf_dtn.
 
-    coeffs: dict of device float64 tensors (nleaf, p*p) for 'c11','c22','c1','c2','c'.
+    coeffs: dict of device float64 tensors (nleaf, p*p) for 'c11','c22','c1','c2','c'
+    and optionally 'c12' (mixed derivative: then interp = HPS_Disc.Interp_mat and
+    jxreorder = JJ.Jxreorder are needed, and slab_leaf_dtn_mixed runs).
     Returns DtN (nleaf, 4(p-2), 4(p-2)) float64 on the device (and S if asked).
     """
     L = _lib.lib()
@@ -177,6 +179,8 @@ def leaf_dtn(coeffs, p, D, Dsq, Nx, precision='fp64', return_S=False):
     dev = ref.device
     q = p - 2
     prec = _lib.PREC[precision]
+    if coeffs.get('c12') is not None:
+        return _leaf_dtn_mixed(L, coeffs, nleaf, p, D, Dsq, Nx, prec, return_S, interp, jxreorder, dev)
     wb = int(L.slab_leaf_dtn_work_bytes(nleaf, p, prec))
     work = torch.empty(wb, dtype=torch.uint8, device=dev)
     dtn = torch.empty(nleaf, 4 * q, 4 * q, dtype=torch.float64, device=dev)
@@ -190,4 +194,25 @@ def leaf_dtn(coeffs, p, D, Dsq, Nx, precision='fp64', return_S=False):
                          _lib.ptr(work), wb, _lib.ptr(dtn), _lib.ptr(S), _lib.ptr(info),
                          ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
     _lib.check(st, 'slab_leaf_dtn')
+    return (dtn, S, info) if return_S else (dtn, info)
+
+
+def _leaf_dtn_mixed(L, coeffs, nleaf, p, D, Dsq, Nx, prec, return_S, interp, jxreorder, dev):
+    if interp is None or jxreorder is None:
+        raise ValueError('a mixed derivative (c12) needs interp (Interp_mat) and jxreorder (Jxreorder)')
+    q = p - 2
+    wb = int(L.slab_leaf_dtn_mixed_work_bytes(nleaf, p, prec))
+    work = torch.empty(wb, dtype=torch.uint8, device=dev)
+    dtn = torch.empty(nleaf, 4 * q, 4 * q, dtype=torch.float64, device=dev)
+    S = torch.empty(nleaf, q * q, 4 * q, dtype=torch.float64, device=dev) if return_S else None
+    info = torch.zeros(nleaf, dtype=torch.int32, device=dev)
+    t = lambda a: torch.as_tensor(np.ascontiguousarray(a), dtype=torch.float64, device=dev)
+    Dd, Dsqd, Nxd, Id = t(D), t(Dsq), t(Nx), t(interp)
+    jx = torch.as_tensor(np.ascontiguousarray(jxreorder), dtype=torch.int32, device=dev)
+    cs = [coeffs.get(k) for k in ('c11', 'c22', 'c12', 'c1', 'c2', 'c')]
+    cs = [None if c is None else c.to(torch.float64).contiguous() for c in cs]
+    st = L.slab_leaf_dtn_mixed(nleaf, p, *[_lib.ptr(c) for c in cs], _lib.ptr(Dd), _lib.ptr(Dsqd), _lib.ptr(Nxd),
+                               _lib.ptr(Id), _lib.ptr(jx), prec, _lib.ptr(work), wb, _lib.ptr(dtn), _lib.ptr(S),
+                               _lib.ptr(info), ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    _lib.check(st, 'slab_leaf_dtn_mixed')
     return (dtn, S, info) if return_S else (dtn, info)
