@@ -81,16 +81,19 @@ class SlabEngine:
         st = self.L.slab_engine_factor(self.h, *[_lib.ptr(t) for t in args])
         return _lib.check(st, 'slab_engine_factor')
 
-    def solve(self, bnd, fbody=None, tol=1e-10, max_iter=20, want_faces=False, allow_noconv=False):
+    def solve(self, bnd, fbody=None, tol=1e-10, max_iter=20, want_faces=False, allow_noconv=False, want_leaf=True):
         """bnd: (ntot,) or (ntot, nrhs) face values (only Dirichlet faces are read).
 
-        Returns (u_leaf (npts, nrhs) device tensor, u_faces or None, iters, stats dict).
+        Returns (u_leaf (npts, nrhs) device tensor or None if not want_leaf, u_faces
+        or None, iters, stats dict).
         """
         dev = bnd.device
         nrhs = 1 if bnd.dim() == 1 else bnd.shape[1]
+        if not (want_leaf or want_faces):
+            raise ValueError('solve: ask for the leaf-node solution, the face solution or both')
         bnd_cm = _col_major(bnd.to(torch.float64), self.ntot)
         fb_cm = None if fbody is None else _col_major(fbody.to(torch.float64), self.npts)
-        uleaf = torch.empty(nrhs, self.npts, dtype=torch.float64, device=dev)
+        uleaf = torch.empty(nrhs, self.npts, dtype=torch.float64, device=dev) if want_leaf else None
         ufaces = torch.empty(nrhs, self.ntot, dtype=torch.float64, device=dev) if want_faces else None
         iters = ctypes.c_int(0)
         stats = (ctypes.c_double * 5)()
@@ -99,7 +102,7 @@ class SlabEngine:
         _lib.check(st, 'slab_engine_solve', allow=(_lib.SLAB_ERR_NOCONV,) if allow_noconv else ())
         info = dict(rel_correction=stats[0], residual=stats[1], residual0=stats[2], resloc=stats[3],
                     rel_residual=stats[4], converged=(st == _lib.SLAB_OK))
-        return uleaf.T, (None if ufaces is None else ufaces.T), iters.value, info
+        return (None if uleaf is None else uleaf.T), (None if ufaces is None else ufaces.T), iters.value, info
 
     def adjoint(self, gleaf=None, gfaces=None, tol=1e-10, max_iter=20, want_faces=False, want_bnd=True,
                 allow_noconv=False):

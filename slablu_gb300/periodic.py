@@ -65,9 +65,10 @@ class PeriodicEdge:
     """Schur complement of the shared edge on top of a non-periodic factorization.
 
     ``engine`` has the interface of SlabEngine.solve(bnd, fbody, tol, max_iter,
-    want_faces, allow_noconv) -> (u_leaf, u_faces, iters, stats), with both edge
-    copies among its Dirichlet faces; ``edge_flux(u_faces)`` returns the reduced
-    operator's rows at [left edge; right edge] applied to face vectors (ntot, k).
+    want_faces, allow_noconv, want_leaf) -> (u_leaf, u_faces, iters, stats), with
+    both edge copies among its Dirichlet faces; ``edge_flux(u_faces)`` returns the
+    reduced operator's rows at [left edge; right edge] applied to face vectors
+    (ntot, k).  Only the final solve asks for the leaf-node solution.
     """
 
     def __init__(self, engine, edge_flux, left, right, ntot, tol=1e-10, max_iter=20, chunk=128):
@@ -84,10 +85,9 @@ class PeriodicEdge:
     def _idx(self, dev):
         return (torch.as_tensor(self._left_np, device=dev), torch.as_tensor(self._right_np, device=dev))
 
-    def _solve_faces(self, bnd, fbody=None):
-        uleaf, uf, iters, st = self.engine.solve(bnd, fbody, tol=self.tol, max_iter=self.max_iter,
-                                                 want_faces=True, allow_noconv=True)
-        return uleaf, uf, iters, st
+    def _solve_faces(self, bnd, fbody=None, want_leaf=True):
+        return self.engine.solve(bnd, fbody, tol=self.tol, max_iter=self.max_iter, want_faces=True,
+                                 allow_noconv=True, want_leaf=want_leaf)
 
     def _residual(self, uf):
         f = self.edge_flux(uf)
@@ -106,7 +106,7 @@ class PeriodicEdge:
             cols = torch.arange(k, device=self.dev)
             bnd[L[c0:c0 + k], cols] = 1.0
             bnd[R[c0:c0 + k], cols] = 1.0
-            _, uf, iters, _ = self._solve_faces(bnd)
+            _, uf, iters, _ = self._solve_faces(bnd, want_leaf=False)
             self.build_iters = max(self.build_iters, iters)
             S[:, c0:c0 + k] = self._residual(uf)
         self.S = S
@@ -126,7 +126,7 @@ class PeriodicEdge:
             b = b[:, None]
         b[L] = 0.0
         b[R] = 0.0
-        _, uf, iters, st = self._solve_faces(b, fbody)
+        _, uf, iters, st = self._solve_faces(b, fbody, want_leaf=False)
         r0 = self._residual(uf)
         y = -torch.linalg.lu_solve(self.lu, self.piv, r0)
         steps, total_iters = 0, iters

@@ -29,17 +29,19 @@ class NonPeriodicSolveDouble:
         self.lu = spla.splu(A[part.I_Ctot][:, part.I_Ctot].tocsc())
         self.A_CX = A[part.I_Ctot][:, part.I_Xtot]
         self.calls = []
+        self.leaf_calls = 0
 
-    def solve(self, bnd, fbody=None, tol=1e-10, max_iter=20, want_faces=False, allow_noconv=False):
+    def solve(self, bnd, fbody=None, tol=1e-10, max_iter=20, want_faces=False, allow_noconv=False, want_leaf=True):
         assert fbody is None
         b = bnd.numpy() if bnd.dim() == 2 else bnd.numpy()[:, None]
         self.calls.append(b.shape[1])
         uf = np.zeros_like(b)
         uf[self.part.I_Xtot] = b[self.part.I_Xtot]
         uf[self.part.I_Ctot] = self.lu.solve(-(self.A_CX @ b[self.part.I_Xtot]))
-        u_leaf, _ = domain.leaf_recover(self.md, self.co, uf)
+        u_leaf = torch.as_tensor(domain.leaf_recover(self.md, self.co, uf)[0]) if want_leaf else None
+        self.leaf_calls += int(want_leaf)
         st = dict(rel_correction=0.0, residual=0.0, residual0=0.0, resloc=0.0, rel_residual=0.0, converged=True)
-        return torch.as_tensor(u_leaf), (torch.as_tensor(uf) if want_faces else None), 1, st
+        return u_leaf, (torch.as_tensor(uf) if want_faces else None), 1, st
 
 
 def _setup(golden_dir):
@@ -79,6 +81,8 @@ def test_periodic_edge_schur_solve(golden_dir):
     bnd = torch.zeros(geom.ntot, 1, dtype=torch.float64)
     bnd[sets['I_Xtot']] = torch.as_tensor(ud(geom.xx_active[sets['I_Xtot']]))
     u_leaf, uf, st = edge.solve(bnd)
+    # the Schur columns and the zero-edge solve ask for face values only
+    assert eng.leaf_calls == st['edge_steps']
     stride = int(g['stride'])
     ref = g['superLU_sol_sub']
     assert np.linalg.norm(u_leaf.numpy()[::stride] - ref) / np.linalg.norm(ref) < 1e-10
