@@ -112,7 +112,7 @@ int slab_leaf_dtn_noalloc(int nleaf, int p, const double* d_c11, const double* d
  * assembly, build_slabLU :297-358, build_Tred_solver :668-687) and
  * Domain_Solver.solve (:543-666 with leaf recovery,
  * src_disc/hps_multidomain_disc.py:227-243) for solver_type='slabLU',
- * non-periodic, c12 = None.
+ * non-periodic, c12 = None (c12: slab_engine_create_mixed).
  *
  * Geometry: n0 x n1 leaves (leaf index i*n1 + j, i = x index), polynomial
  * order p, slab width buf leaves (n0 % buf == 0).  Host arrays:
@@ -129,6 +129,18 @@ int slab_engine_create(slab_engine** out, int p, int n0, int n1, int buf, int pr
                        const int* h_jxreorder, void* stream);
 int slab_engine_destroy(slab_engine* e);
 
+/*
+ * Engine for an operator with a mixed derivative (c12, the parameter maps of
+ * curved domains): the c12 branch of form_DtNs (src_disc/hps_parallel_leaf_ops.py
+ * :59-65, 84-92) -- leaves couple to their corners through Interp_mat.  Same
+ * arguments as slab_engine_create; factor it with slab_engine_factor_mixed.
+ * Solves and the residual work as for slab_engine_create; the adjoint and the
+ * coefficient gradients return SLAB_ERR_ARG.
+ */
+int slab_engine_create_mixed(slab_engine** out, int p, int n0, int n1, int buf, int precision, const double* h_D,
+                             const double* h_Dsq, const double* h_Nx, const double* h_interp,
+                             const int* h_jxreorder, void* stream);
+
 /* Number of reduced face unknowns (p-2)(n0(2 n1 + 1) + n1) and of leaves. */
 long long slab_engine_nfaces(const slab_engine* e);
 long long slab_engine_nleaves(const slab_engine* e);
@@ -137,6 +149,11 @@ long long slab_engine_nleaves(const slab_engine* e);
  * doubles each, NULL = absent).  Returns >0 on pivot breakdown. */
 int slab_engine_factor(slab_engine* e, const double* d_c11, const double* d_c22, const double* d_c1,
                        const double* d_c2, const double* d_c);
+/* The same with the mixed-derivative coefficient d_c12 (required), for an
+ * engine from slab_engine_create_mixed:
+ *   -c11 u_xx - c22 u_yy - 2 c12 u_xy + c1 u_x + c2 u_y + c u. */
+int slab_engine_factor_mixed(slab_engine* e, const double* d_c11, const double* d_c22, const double* d_c12,
+                             const double* d_c1, const double* d_c2, const double* d_c);
 
 /*
  * Solve for nrhs right-hand sides with FP64 iterative refinement.

@@ -28,10 +28,13 @@ _SIGS = {
     'slab_leaf_dtn': (c_int, [c_int, c_int] + [c_void] * 8 + [c_int, c_void, c_size, c_void, c_void, c_void, c_void]),
     'slab_engine_create': (c_int, [ctypes.POINTER(c_void), c_int, c_int, c_int, c_int, c_int,
                                    P_double, P_double, P_double, P_double, P_int, c_void]),
+    'slab_engine_create_mixed': (c_int, [ctypes.POINTER(c_void), c_int, c_int, c_int, c_int, c_int,
+                                         P_double, P_double, P_double, P_double, P_int, c_void]),
     'slab_engine_destroy': (c_int, [c_void]),
     'slab_engine_nfaces': (c_ll, [c_void]),
     'slab_engine_nleaves': (c_ll, [c_void]),
     'slab_engine_factor': (c_int, [c_void] * 6),
+    'slab_engine_factor_mixed': (c_int, [c_void] * 7),
     'slab_engine_solve': (c_int, [c_void, c_int, c_void, c_void, c_double, c_int, c_void, c_void, P_int, P_double]),
     'slab_engine_residual': (c_int, [c_void, c_int] + [c_void] * 5),
     'slab_engine_adjoint': (c_int, [c_void, c_int, c_void, c_void, c_double, c_int, c_void, c_void, c_void,

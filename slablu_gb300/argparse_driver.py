@@ -7,9 +7,12 @@ Builds once and solves twice (the second solve is the reported one), and
 pickles ``build_info`` then ``solve_info`` with the reference's keys
 (argparse_driver.py:169-188, 248-298).  Added flags: --precision, --tol.
 --periodic_bc identifies the left and right edges of the box (Dirichlet data on
-the bottom and top only), as in the reference.  Out of scope here: --disc fd,
-curved domains, the superLU/PETSc black-box solvers, --disable_cuda
-(slablu_gb300 has no CPU path).
+the bottom and top only), and --domain curved / annulus / curvy_annulus solve on
+the image of the box under the reference's parameter maps (boundary data at the
+mapped points), as in the reference (its tests run square, annulus, and
+curvy_annulus with --box_xlim 6 --periodic_bc).  Out of scope here: --disc fd,
+the superLU/PETSc black-box solvers, --disable_cuda (slablu_gb300 has no CPU
+path).
 """
 import argparse
 import pickle
@@ -49,8 +52,8 @@ def main(argv=None):
     args = parse(argv)
     if args.disc != 'hps':
         raise ValueError('slablu_gb300 provides the HPS discretisation only')
-    if args.domain != 'square':
-        raise ValueError('slablu_gb300 provides the rectangular domain only')
+    if args.domain not in ('square', 'curved', 'annulus', 'curvy_annulus'):
+        raise ValueError(f'unknown domain {args.domain}')
     if args.disable_cuda:
         raise ValueError('slablu_gb300 runs on the GPU only (no CPU path)')
     if args.p is None:
@@ -70,9 +73,15 @@ def main(argv=None):
         if args.pde not in built_in_funcs.BFIELDS:
             raise ValueError(f'unknown pde {args.pde}')
         bfield = built_in_funcs.BFIELDS[args.pde]
-        op = pdo.PDO_2d(pdo.ones, pdo.ones, c=lambda xx: bfield(xx, kh))
+        if args.domain == 'square':
+            op = pdo.PDO_2d(pdo.ones, pdo.ones, c=lambda xx: bfield(xx, kh))
+        else:  # a curved domain through its parameter map (argparse_driver.py:119-136)
+            op, param_map, _ = pdo.get_param_map_and_pdo(args.domain, bfield, kh)
     else:
         raise ValueError(f'unknown pde {args.pde}')
+    if args.domain != 'square' and not args.pde.startswith('bfield'):
+        raise ValueError('curved domains are set up for the bfield operators')
+    mapped = (lambda xx: param_map(xx)) if args.domain != 'square' else (lambda xx: xx)
     p = args.p
     buf_constant = 1.0 if args.buf_constant is None else args.buf_constant
     a = 1 / (2 * (n / (p - 2)))
@@ -86,9 +95,9 @@ def main(argv=None):
     if args.bc == 'free_space':
         if args.pde != 'bfield_constant':
             raise ValueError('free_space data is the exact solution only for bfield_constant')
-        uu_dir, known = (lambda xx: built_in_funcs.uu_dir_func_greens(xx, kh)), True
+        uu_dir, known = (lambda xx: built_in_funcs.uu_dir_func_greens(mapped(xx), kh)), True
     elif args.bc == 'pulse':
-        uu_dir, known = (lambda xx: built_in_funcs.uu_dir_pulse(xx, kh)), False
+        uu_dir, known = (lambda xx: built_in_funcs.uu_dir_pulse(mapped(xx), kh)), False
     elif args.bc == 'ones':
         uu_dir, known = (lambda xx: torch.ones(xx.shape[0], 1)), False
     elif args.bc == 'log_dist' and args.pde == 'poisson':

@@ -338,10 +338,15 @@ struct EngineImpl : EngineBase {
   bool use_cluster_solve = true;
   int leaf_ctas = 0;  // resident leaves per SM in the leaf kernel (0: as many as fit)
   DevBuf D, Dsq, Nx, NxcT, NxxT, interp, jxr, leafglob, dirmask;
-  DevBuf coef[5];
-  bool has[5] = {false, false, false, false, false};
-  // leaf factors
+  DevBuf coef[6];  // c11, c22, c1, c2, c, c12
+  bool has[6] = {false, false, false, false, false, false};
+  // leaf factors: LU of A_cc and S in G, n x (n + ncolG) per leaf; with a mixed
+  // derivative (c12) the extra columns are the 4(p-1) Jxreorder nodes
   DevBuf G, piv, leafperm, leafinfo;
+  bool mixed = false;
+  int ncolG = 0;
+  long long leaf_stride = 0;
+  DevBuf interpT;  // Interp_mat in the leaf type (mixed derivative)
   // tree
   std::vector<HNode> nodes;
   std::vector<HMerge> merges;
@@ -485,9 +490,10 @@ struct EngineImpl : EngineBase {
     return set_error(SLAB_ERR_ARG, "unknown option %d", key);
   }
 
-  EngineImpl(int p_, int n0_, int n1_, int buf_, cudaStream_t s_)
+  EngineImpl(int p_, int n0_, int n1_, int buf_, cudaStream_t s_, bool mixed_ = false)
       : p(p_), q(p_ - 2), n((p_ - 2) * (p_ - 2)), nx(4 * (p_ - 2)), n0(n0_), n1(n1_), buf(buf_), npan(n0_ / buf_),
         us(s_) {
+    mixed = mixed_;
     const char* ng = getenv("SLAB_NO_GRAPHS");
     use_graphs = !(ng && ng[0] == '1');
     const char* nc = getenv("SLAB_COOP_SOLVE");  // 1: grid-wide cooperative interface solve instead of the cluster one
@@ -731,7 +737,15 @@ struct EngineImpl : EngineBase {
     SLAB_CHECK_LAUNCH();
     SLAB_TRY(build_plan());
     // factor storage
-    SLAB_TRY(G.alloc((size_t)nleaf * n * (n + nx) * sizeof(T)));
+    ncolG = mixed ? 4 * (p - 1) : nx;
+    leaf_stride = (long long)n * (n + ncolG);
+    SLAB_TRY(G.alloc((size_t)nleaf * leaf_stride * sizeof(T)));
+    if (mixed) {
+      const long long ni = (long long)4 * (p - 1) * nx;
+      SLAB_TRY(interpT.alloc((size_t)ni * sizeof(T)));
+      convert_kernel<T, double><<<grid_for(ni), 256, 0, s>>>(interp.as<double>(), interpT.as<T>(), ni);
+      SLAB_CHECK_LAUNCH();
+    }
     SLAB_TRY(piv.alloc((size_t)nleaf * n * sizeof(int)));
     SLAB_TRY(leafperm.alloc((size_t)nleaf * n * sizeof(int)));
     SLAB_TRY(leafinfo.alloc((size_t)nleaf * sizeof(int)));
@@ -790,8 +804,11 @@ struct EngineImpl : EngineBase {
 
   int factor_impl(const LeafCoeffs& co_in) {
     const size_t cbytes = (size_t)nleaf * p * p * sizeof(double);
-    const double* src[5] = {co_in.c11, co_in.c22, co_in.c1, co_in.c2, co_in.c};
-    for (int i = 0; i < 5; ++i) {
+    if ((co_in.c12 != nullptr) != mixed)
+      return set_error(SLAB_ERR_ARG, mixed ? "slab_engine_factor: this engine needs the mixed-derivative coefficient c12"
+                                           : "slab_engine_factor: c12 needs an engine from slab_engine_create_mixed");
+    const double* src[6] = {co_in.c11, co_in.c22, co_in.c1, co_in.c2, co_in.c, co_in.c12};
+    for (int i = 0; i < 6; ++i) {
       has[i] = src[i] != nullptr;
       if (has[i]) {
         SLAB_TRY(coef[i].ensure(cbytes));
@@ -799,14 +816,15 @@ struct EngineImpl : EngineBase {
       }
     }
     const bool layout_changed = !factored || has_prev[0] != has[0] || has_prev[1] != has[1] ||
-                                has_prev[2] != has[2] || has_prev[3] != has[3] || has_prev[4] != has[4];
+                                has_prev[2] != has[2] || has_prev[3] != has[3] || has_prev[4] != has[4] ||
+                                has_prev[5] != has[5];
     if (layout_changed)
       for (auto& g : gfac)
         if (g) {
           cudaGraphExecDestroy(g);
           g = nullptr;
         }
-    for (int i = 0; i < 5; ++i) has_prev[i] = has[i];
+    for (int i = 0; i < 6; ++i) has_prev[i] = has[i];
     SLAB_CUDA_TRY(cudaEventRecord(ev[0], s));
     SLAB_TRY(run_graph(gfac[0], [&]() { return factor_leaf(); }));
     SLAB_CUDA_TRY(cudaEventRecord(ev[1], s));
@@ -817,7 +835,7 @@ struct EngineImpl : EngineBase {
     return factor_check();
   }
 
-  bool has_prev[5] = {false, false, false, false, false};
+  bool has_prev[6] = {false, false, false, false, false, false};
 
   int factor_leaf() {
     LeafCoeffs co = coeffs();
@@ -827,9 +845,14 @@ struct EngineImpl : EngineBase {
     a.p = p; a.q = q; a.n = n; a.nx = nx;
     a.co = co; a.D = D.as<double>(); a.Dsq = Dsq.as<double>();
     a.Nxc = NxcT.as<T>(); a.Nxx = NxxT.as<T>();
-    a.G = G.as<T>(); a.strideG = (long long)n * (n + nx); a.piv = piv.as<int>();
+    a.G = G.as<T>(); a.strideG = leaf_stride; a.piv = piv.as<int>();
     a.dtn = nodepool.as<T>(); a.info = leafinfo.as<int>();
     a.decouple = 1; a.n0 = n0; a.n1 = n1; a.leaf_begin = 0;
+    if (mixed) {
+      a.nxa = ncolG;
+      a.interp = interpT.as<T>();
+      a.jxr = jxr.as<int>();
+    }
     SLAB_TRY(leaf_factor<T>(s, a, (int)nleaf, leaf_ctas));
     return build_perm_batched(s, piv.as<int>(), n, n, (int)nleaf, leafperm.as<int>(), n);
   }
@@ -1003,7 +1026,7 @@ struct EngineImpl : EngineBase {
   LeafCoeffs coeffs() const {
     return LeafCoeffs{has[0] ? coef[0].as<double>() : nullptr, has[1] ? coef[1].as<double>() : nullptr,
                       has[2] ? coef[2].as<double>() : nullptr, has[3] ? coef[3].as<double>() : nullptr,
-                      has[4] ? coef[4].as<double>() : nullptr};
+                      has[4] ? coef[4].as<double>() : nullptr, has[5] ? coef[5].as<double>() : nullptr};
   }
 
   int reserve(int nrhs) {
@@ -1048,7 +1071,7 @@ struct EngineImpl : EngineBase {
     T* g = gvec.as<T>();
     T* u = uvec.as<T>();
     T* w = wc.as<T>();
-    const long long strideG = (long long)n * (n + nx);
+    const long long strideG = leaf_stride;
     SLAB_CUDA_TRY(cudaMemcpyAsync(w, rcT.p, (size_t)nleaf * n * nrhs * sizeof(T), cudaMemcpyDeviceToDevice, s));
     if (nrhs <= 4 && n <= 32 * kWarpSlots)
       SLAB_TRY(getrs_small<T>(s, n, nrhs, G.as<T>(), nullptr, strideG, n, leafperm.as<int>(), nullptr, n, w, nullptr,
@@ -1141,7 +1164,7 @@ struct EngineImpl : EngineBase {
     T* g = gvec.as<T>();
     T* u = uvec.as<T>();
     T* w = wc.as<T>();
-    const long long strideG = (long long)n * (n + nx);
+    const long long strideG = leaf_stride;
     // leaf forward: g_x += S^T g_c
     SLAB_TRY(gemm_tn<T>(s, nx, nrhs, n, T(1), G.as<T>() + (long long)n * n, nullptr, strideG, n, rcT.as<T>(), nullptr,
                         (long long)n * nrhs, n, T(0), flux.as<T>(), nullptr, (long long)nx * nrhs, nx, (int)nleaf));
@@ -1246,6 +1269,7 @@ struct EngineImpl : EngineBase {
 
   int adjoint(int nrhs, const double* gleaf, const double* gfaces, double tol, int max_iter, double* lam_leaf,
               double* lam_faces, double* gbnd, int* iters, double* stats) override {
+    if (mixed) return set_error(SLAB_ERR_ARG, "slab_engine_adjoint: not provided with a mixed derivative (c12)");
     SLAB_TRY(enter());
     int st = SLAB_OK, total_it = 0;
     double worst[5] = {0, 0, 0, 0, 0};
@@ -1377,6 +1401,7 @@ struct EngineImpl : EngineBase {
 
   int coeff_grad(int nrhs, const double* ufaces, const double* uleaf, const double* lam_leaf, double* g11,
                  double* g22, double* g1, double* g2, double* g0) override {
+    if (mixed) return set_error(SLAB_ERR_ARG, "slab_engine_coeff_grad: not provided with a mixed derivative (c12)");
     if (nrhs <= 0 || !ufaces || !uleaf || !lam_leaf)
       return set_error(SLAB_ERR_ARG, "slab_engine_coeff_grad: invalid arguments");
     if (n > 4 * 256) return set_error(SLAB_ERR_ARG, "slab_engine_coeff_grad: leaf order p=%d too large", p);
@@ -1398,7 +1423,14 @@ struct EngineImpl : EngineBase {
     r.co = coeffs(); r.D = D.as<double>(); r.Dsq = Dsq.as<double>();
     r.leafglob = leafglob.as<int>(); r.dirmask = dirmask.as<unsigned char>();
     r.ux = ux; r.uc = uc; r.fbody = fbody; r.rc = rc; r.rx = rx;
-    residual_kernel<<<(unsigned)nleaf, 256, 3 * (size_t)p * p * sizeof(double), s>>>(r);
+    if (mixed) {
+      r.interp = interp.as<double>(); r.jxr = jxr.as<int>(); r.nxa = 4 * (p - 1);
+      const size_t bytes = (4 * (size_t)p * p + nx) * sizeof(double);
+      SLAB_TRY(ensure_smem(residual_mixed_kernel, bytes, "residual_mixed"));
+      residual_mixed_kernel<<<(unsigned)nleaf, 256, bytes, s>>>(r);
+    } else {
+      residual_kernel<<<(unsigned)nleaf, 256, 3 * (size_t)p * p * sizeof(double), s>>>(r);
+    }
     SLAB_CHECK_LAUNCH();
     return SLAB_OK;
   }
@@ -1541,9 +1573,9 @@ extern "C" int slab_version(void) { return 100; }
 
 extern "C" const char* slab_last_error(void) { return slab::last_error(); }
 
-extern "C" int slab_engine_create(slab_engine** out, int p, int n0, int n1, int buf, int precision,
-                                  const double* hD, const double* hDsq, const double* hNx, const double* hinterp,
-                                  const int* hjxr, void* stream) {
+static int engine_create(slab_engine** out, int p, int n0, int n1, int buf, int precision, const double* hD,
+                         const double* hDsq, const double* hNx, const double* hinterp, const int* hjxr, void* stream,
+                         bool mixed) {
   if (!out || p < 4 || n0 < 1 || n1 < 1 || buf < 1 || n0 % buf != 0 || !hD || !hDsq || !hNx || !hinterp || !hjxr)
     return slab::set_error(SLAB_ERR_ARG, "slab_engine_create: invalid geometry or null operator");
   const long long ntot = (long long)(p - 2) * ((long long)n0 * (2 * n1 + 1) + n1);
@@ -1552,15 +1584,15 @@ extern "C" int slab_engine_create(slab_engine** out, int p, int n0, int n1, int 
   auto e = std::make_unique<slab_engine>();
   int st = SLAB_OK;
   if (precision == SLAB_PREC_FP64) {
-    auto im = std::make_unique<slab::EngineImpl<double, double>>(p, n0, n1, buf, s);
+    auto im = std::make_unique<slab::EngineImpl<double, double>>(p, n0, n1, buf, s, mixed);
     st = im->init(hD, hDsq, hNx, hinterp, hjxr);
     e->impl = std::move(im);
   } else if (precision == SLAB_PREC_MIXED) {
-    auto im = std::make_unique<slab::EngineImpl<float, double>>(p, n0, n1, buf, s);
+    auto im = std::make_unique<slab::EngineImpl<float, double>>(p, n0, n1, buf, s, mixed);
     st = im->init(hD, hDsq, hNx, hinterp, hjxr);
     e->impl = std::move(im);
   } else if (precision == SLAB_PREC_FP32) {
-    auto im = std::make_unique<slab::EngineImpl<float, float>>(p, n0, n1, buf, s);
+    auto im = std::make_unique<slab::EngineImpl<float, float>>(p, n0, n1, buf, s, mixed);
     st = im->init(hD, hDsq, hNx, hinterp, hjxr);
     e->impl = std::move(im);
   } else {
@@ -1569,6 +1601,18 @@ extern "C" int slab_engine_create(slab_engine** out, int p, int n0, int n1, int 
   if (st != SLAB_OK) return st;
   *out = e.release();
   return SLAB_OK;
+}
+
+extern "C" int slab_engine_create(slab_engine** out, int p, int n0, int n1, int buf, int precision,
+                                  const double* hD, const double* hDsq, const double* hNx, const double* hinterp,
+                                  const int* hjxr, void* stream) {
+  return engine_create(out, p, n0, n1, buf, precision, hD, hDsq, hNx, hinterp, hjxr, stream, false);
+}
+
+extern "C" int slab_engine_create_mixed(slab_engine** out, int p, int n0, int n1, int buf, int precision,
+                                        const double* hD, const double* hDsq, const double* hNx,
+                                        const double* hinterp, const int* hjxr, void* stream) {
+  return engine_create(out, p, n0, n1, buf, precision, hD, hDsq, hNx, hinterp, hjxr, stream, true);
 }
 
 extern "C" int slab_engine_destroy(slab_engine* e) {
@@ -1603,6 +1647,12 @@ extern "C" int slab_engine_factor(slab_engine* e, const double* c11, const doubl
                                   const double* c2, const double* c) {
   if (!e) return slab::set_error(SLAB_ERR_ARG, "slab_engine_factor: null engine");
   return e->impl->factor(slab::LeafCoeffs{c11, c22, c1, c2, c});
+}
+
+extern "C" int slab_engine_factor_mixed(slab_engine* e, const double* c11, const double* c22, const double* c12,
+                                        const double* c1, const double* c2, const double* c) {
+  if (!e) return slab::set_error(SLAB_ERR_ARG, "slab_engine_factor_mixed: null engine");
+  return e->impl->factor(slab::LeafCoeffs{c11, c22, c1, c2, c, c12});
 }
 
 extern "C" int slab_engine_solve(slab_engine* e, int nrhs, const double* bnd, const double* fbody, double tol,

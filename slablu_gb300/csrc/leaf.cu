@@ -21,6 +21,9 @@ int leaf_factor(cudaStream_t s, const LeafFactorArgs<T>& a, int nleaf, int ctas_
   if (a.nxa > 0) {  // mixed derivative: Jxreorder columns and the interpolation stage
     if (!a.co.c12 || !a.interp || !a.jxr)
       return set_error(SLAB_ERR_ARG, "leaf_factor: c12, interp and jxreorder are needed together");
+    // the interpolation stage holds Interp_mat and 32 rows of X in the dynamic shared memory
+    if (((size_t)a.nxa * a.nx + 32 * (size_t)a.nxa) * sizeof(T) > leaf_factor_smem_bytes(a.p, sizeof(T)))
+      return set_error(SLAB_ERR_ARG, "leaf_factor: p = %d too small for the interpolation stage", a.p);
     return leaf_factor_launch<T, true>(s, a, nleaf, ctas_per_sm);
   }
   return leaf_factor_launch<T, false>(s, a, nleaf, ctas_per_sm);
@@ -105,6 +108,95 @@ __global__ void __launch_bounds__(256) residual_kernel(ResidualArgs a) {
       const int f = s / q, t = s % q + 1;
       double flux = 0.0;
       // Nx rows: [-D1[Jl]; D1[Jr]; -D2[Jd]; D2[Ju]] with D1 = -kron(D,I), D2 = -kron(I,D)
+      if (f == 0)
+        for (int j = 0; j < p; ++j) flux += Dsh[j] * u[j * p + t];
+      else if (f == 1)
+        for (int j = 0; j < p; ++j) flux -= Dsh[(p - 1) * p + j] * u[j * p + t];
+      else if (f == 2)
+        for (int j = 0; j < p; ++j) flux += Dsh[j] * u[t * p + j];
+      else
+        for (int j = 0; j < p; ++j) flux -= Dsh[(p - 1) * p + j] * u[t * p + j];
+      atomicAdd(&a.rx[g + (size_t)c * a.ntot], -flux);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256) residual_mixed_kernel(ResidualArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int p = a.p, q = a.q, n = a.n, nx = a.nx, nxa = a.nxa, pp = p * p;
+  double* Dsh = reinterpret_cast<double*>(smem_raw);
+  double* Dsqsh = Dsh + pp;
+  double* u = Dsqsh + pp;  // leaf node values
+  double* W = u + pp;      // U D^T
+  double* uf = W + pp;     // the leaf's nx face values
+  const int leaf = blockIdx.x;
+  const int tid = threadIdx.x;
+  for (int i = tid; i < pp; i += blockDim.x) {
+    Dsh[i] = a.D[i];
+    Dsqsh[i] = a.Dsq[i];
+  }
+  const int lofs = leaf * pp;
+  const LeafCoeffs& co = a.co;
+  for (int c = 0; c < a.nrhs; ++c) {
+    __syncthreads();
+    for (int i = tid; i < pp; i += blockDim.x) u[i] = 0.0;
+    for (int s = tid; s < nx; s += blockDim.x) uf[s] = a.ux[a.leafglob[(size_t)leaf * nx + s] + (size_t)c * a.ntot];
+    __syncthreads();
+    for (int r = tid; r < n; r += blockDim.x) {
+      int i1, i2;
+      interior_node(r, q, i1, i2);
+      u[i1 * p + i2] = a.uc[((size_t)leaf * a.nrhs + c) * n + r];
+    }
+    // the interpolated boundary (faces and corners), Interp_mat u_faces
+    for (int t = tid; t < nxa; t += blockDim.x) {
+      double v = 0.0;
+      for (int s = 0; s < nx; ++s) v += a.interp[(size_t)t * nx + s] * uf[s];
+      u[a.jxr[t]] = v;
+    }
+    __syncthreads();
+    for (int idx = tid; idx < pp; idx += blockDim.x) {
+      const int j1 = idx / p, i2 = idx % p;
+      double w = 0.0;
+      for (int j2 = 0; j2 < p; ++j2) w += u[j1 * p + j2] * Dsh[i2 * p + j2];
+      W[idx] = w;
+    }
+    __syncthreads();
+    for (int r = tid; r < n; r += blockDim.x) {
+      int i1, i2;
+      interior_node(r, q, i1, i2);
+      const int k = lofs + i1 * p + i2;
+      double t11 = 0, t22 = 0, t1 = 0, t2 = 0, t12 = 0;
+      for (int j = 0; j < p; ++j) {
+        const double ux1 = u[j * p + i2], ux2 = u[i1 * p + j];
+        t11 += Dsqsh[i1 * p + j] * ux1;
+        t22 += Dsqsh[i2 * p + j] * ux2;
+        t1 += Dsh[i1 * p + j] * ux1;
+        t2 += Dsh[i2 * p + j] * ux2;
+        t12 += Dsh[i1 * p + j] * W[j * p + i2];
+      }
+      double Au = 0.0;
+      if (co.c11) Au -= co.c11[k] * t11;
+      if (co.c22) Au -= co.c22[k] * t22;
+      if (co.c12) Au += (-2.0 * co.c12[k]) * t12;
+      if (co.c1) Au -= co.c1[k] * t1;
+      if (co.c2) Au -= co.c2[k] * t2;
+      if (co.c) Au += co.c[k] * u[i1 * p + i2];
+      const double f = a.fbody ? a.fbody[(size_t)k + (size_t)c * a.nleaf * p * p] : 0.0;
+      a.rc[((size_t)leaf * a.nrhs + c) * n + r] = f - Au;
+    }
+    __syncthreads();
+    // the flux rows see the face values themselves (Nx has no corner columns)
+    for (int s = tid; s < nx; s += blockDim.x) {
+      int j1, j2;
+      face_node(s, p, q, j1, j2);
+      u[j1 * p + j2] = uf[s];
+    }
+    __syncthreads();
+    for (int s = tid; s < nx; s += blockDim.x) {
+      const int g = a.leafglob[(size_t)leaf * nx + s];
+      if (a.dirmask[g]) continue;
+      const int f = s / q, t = s % q + 1;
+      double flux = 0.0;
       if (f == 0)
         for (int j = 0; j < p; ++j) flux += Dsh[j] * u[j * p + t];
       else if (f == 1)

@@ -269,9 +269,21 @@ struct ResidualArgs {
   double* rc;                   // leaf-major like uc
   double* rx;                   // ntot x nrhs, accumulated with atomicAdd (caller zeroes)
   int all_faces;                // residual_t_kernel: also accumulate into Dirichlet face columns
+  // residual_mixed_kernel only: Interp_mat (nxa x nx, row-major) and the Jxreorder nodes
+  const double* interp;
+  const int* jxr;
+  int nxa;
 };
 
 __global__ void residual_kernel(ResidualArgs a);
+
+// The residual with a mixed derivative c12 (shared memory (4 p^2 + nx) doubles):
+// the PDE rows see the interpolated boundary u[Jxreorder] = Interp_mat u_faces
+// (corners included) and carry -2 c12 (D U D^T); the flux rows see the face
+// values themselves -- the split of the reference's c12 branch, whose leaf
+// solve interpolates the boundary and whose DtN map is Nx[:,Jc] S + Nx[:,Jx]
+// (src_disc/hps_parallel_leaf_ops.py:59-65, 84-92).
+__global__ void residual_mixed_kernel(ResidualArgs a);
 
 // FP64 residual of the transposed system, one CTA per leaf:
 //   rc = g_int - (A^T lam) at interior columns (leaf-major, like uc),

@@ -23,7 +23,9 @@ def _col_major(x, rows):
 class SlabEngine:
     """Factorization of the HPS operator on a ``Geometry`` (see include/slablu_gb300.h)."""
 
-    def __init__(self, geom: Geometry, precision='mixed', stream=None):
+    def __init__(self, geom: Geometry, precision='mixed', stream=None, mixed=False):
+        """mixed: the operator has a mixed derivative c12 (slab_engine_create_mixed);
+        factor() then takes c12."""
         if precision not in _lib.PREC:
             raise ValueError(f'precision must be one of {sorted(_lib.PREC)}')
         if not torch.cuda.is_available():
@@ -36,7 +38,9 @@ class SlabEngine:
         self._host = dict(D=h(ops.D), Dsq=h(ops.Dsq), Nx=h(ops.Nx), interp=h(ops.Interp_mat),
                           jxr=np.ascontiguousarray(ops.Jxreorder, dtype=np.int32))
         handle = ctypes.c_void_p()
-        st = self.L.slab_engine_create(ctypes.byref(handle), geom.p, geom.n0, geom.n1, geom.buf,
+        self.mixed = bool(mixed)
+        create = self.L.slab_engine_create_mixed if self.mixed else self.L.slab_engine_create
+        st = create(ctypes.byref(handle), geom.p, geom.n0, geom.n1, geom.buf,
                                        _lib.PREC[precision],
                                        _lib.np_ptr(self._host['D'], ctypes.c_double),
                                        _lib.np_ptr(self._host['Dsq'], ctypes.c_double),
@@ -68,17 +72,24 @@ class SlabEngine:
     def factor_bytes(self):
         return int(self.L.slab_engine_factor_bytes(self.h))
 
-    def factor(self, c11=None, c22=None, c1=None, c2=None, c=None):
-        """Coefficients: device float64 tensors with nleaf*p*p entries (or None)."""
+    def factor(self, c11=None, c22=None, c1=None, c2=None, c=None, c12=None):
+        """Coefficients: device float64 tensors with nleaf*p*p entries (or None);
+        c12 (the mixed derivative) only, and always, for an engine made with mixed=True."""
+        if (c12 is not None) != self.mixed:
+            raise ValueError('c12 goes with SlabEngine(mixed=True), and such an engine needs it')
         args = []
-        for t in (c11, c22, c1, c2, c):
+        for t in (c11, c22, c1, c2, c, c12):
             if t is not None:
                 t = t.reshape(-1)
                 assert t.dtype == torch.float64 and t.is_cuda and t.numel() == self.npts and t.is_contiguous()
             args.append(t)
         self._coef = args  # keep alive until the factorization has read them
         self.generation = getattr(self, 'generation', 0) + 1
-        st = self.L.slab_engine_factor(self.h, *[_lib.ptr(t) for t in args])
+        if self.mixed:
+            a11, a22, a1, a2, a0, a12 = [_lib.ptr(t) for t in args]
+            st = self.L.slab_engine_factor_mixed(self.h, a11, a22, a12, a1, a2, a0)
+            return _lib.check(st, 'slab_engine_factor_mixed')
+        st = self.L.slab_engine_factor(self.h, *[_lib.ptr(t) for t in args[:5]])
         return _lib.check(st, 'slab_engine_factor')
 
     def solve(self, bnd, fbody=None, tol=1e-10, max_iter=20, want_faces=False, allow_noconv=False, want_leaf=True):

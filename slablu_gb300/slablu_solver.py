@@ -23,8 +23,11 @@ Differences from the reference, by design:
     on top of the non-periodic factorization (slablu_gb300/periodic.py) instead
     of the reference's cyclic interface solver; ``rel_err`` is then the
     relative residual of the folded reduced system, as in the reference.
-Out of scope (raise NotImplementedError): finite differences (p = 0), mixed
-second derivatives (c12), body loads with periodic_bc.
+  * a mixed derivative (c12, curved domains through a parameter map) runs
+    the reference's c12 leaf branch (slab_engine_create_mixed); its adjoint
+    is not provided.
+Out of scope (raise NotImplementedError): finite differences (p = 0), body
+loads with periodic_bc.
 """
 import time
 
@@ -65,7 +68,10 @@ class _HPSView:
         torch.cuda.synchronize()
         tic = time.time()
         co = {k: (None if v is None else v.reshape(g.nboxes, g.p * g.p)) for k, v in self._coeff_fn().items()}
-        dtn, info = leaf_dtn(co, g.p, g.ops.D, g.ops.Dsq, g.ops.Nx, precision='fp64')
+        kw = {}
+        if co.get('c12') is not None:  # mixed derivative: the Jxreorder / Interp_mat branch
+            kw = dict(interp=g.ops.Interp_mat, jxreorder=g.ops.Jxreorder)
+        dtn, info = leaf_dtn(co, g.p, g.ops.D, g.ops.Dsq, g.ops.Nx, precision='fp64', **kw)
         if int(info.abs().sum()) != 0:
             raise RuntimeError('leaf DtN: zero pivot in a leaf interior block')
         torch.cuda.synchronize()
@@ -85,12 +91,12 @@ class Domain_Solver:
                  tol=1e-10, max_iter=12, device='cuda'):
         if p == 0:
             raise NotImplementedError('slablu_gb300 provides the HPS discretisation only (p > 0)')
-        if getattr(pdo_op, 'c12', None) is not None:
-            raise NotImplementedError('operators with a mixed derivative term c12 are not provided')
         self.kh = kh
         self.pdo = pdo_op
         self.buf_constant = buf_constant
         self.periodic_bc = bool(periodic_bc)
+        # a mixed derivative (curved domains): the c12 branch of the leaf operators
+        self.mixed = getattr(pdo_op, 'c12', None) is not None
         self.precision, self.tol, self.max_iter = precision, tol, max_iter
         self.device = torch.device(device)
         bg = box_geom.detach().cpu().numpy() if isinstance(box_geom, torch.Tensor) else np.asarray(box_geom)
@@ -119,7 +125,7 @@ class Domain_Solver:
     def _coeffs(self):
         xx = torch.as_tensor(self.geom.xx_tot, dtype=torch.float64, device=self.device)
         out = {}
-        for key in ('c11', 'c22', 'c1', 'c2', 'c'):
+        for key in ('c11', 'c22', 'c1', 'c2', 'c') + (('c12',) if self.mixed else ()):
             f = getattr(self.pdo, key, None)
             if f is None:
                 out[key] = None
@@ -141,7 +147,7 @@ class Domain_Solver:
         torch.cuda.synchronize()
         tic = time.time()
         if self.engine is None:
-            self.engine = SlabEngine(self.geom, self.precision)
+            self.engine = SlabEngine(self.geom, self.precision, mixed=self.mixed)
         co = self._coeffs()
         torch.cuda.synchronize()
         toc_coeff = time.time() - tic

@@ -12,14 +12,20 @@ GOLDEN = os.path.join(ROOT, 'tests', 'golden')
 
 def pytest_configure(config):
     config.addinivalue_line('markers', 'gpu: test needs a CUDA GPU (GB300) and the built extension')
-    config.addinivalue_line('markers', 'unverified: GPU test written after the last GPU run of the code it '
-                                       'covers; runs after all other tests')
+    config.addinivalue_line('markers', 'unverified(order=0): GPU test written after the last GPU run of the code '
+                                       'it covers; runs after all other tests, in increasing order')
+
+
+def _run_order(item):
+    m = item.get_closest_marker('unverified')
+    return (0, 0) if m is None else (1, int(m.kwargs.get('order', 0)))
 
 
 def pytest_collection_modifyitems(config, items):
-    # tests that have not yet run on a GPU go last (stable sort), so that under -x a
-    # failure among them cannot keep the verified tests from running
-    items.sort(key=lambda item: item.get_closest_marker('unverified') is not None)
+    # tests that have not yet run on a GPU go last (stable sort), those exercising
+    # the least new device code first, so that under -x a failure among them
+    # cannot keep the verified tests from running
+    items.sort(key=_run_order)
 
 
 @pytest.fixture(scope='session')

@@ -16,7 +16,7 @@ from oracle import adjoint as oadjoint
 from oracle import domain as odomain
 from oracle import funcs as ofuncs
 
-pytestmark = [pytest.mark.gpu, pytest.mark.unverified]
+pytestmark = [pytest.mark.gpu, pytest.mark.unverified(order=1)]
 
 
 @pytest.fixture(scope='module', autouse=True)
