@@ -4,12 +4,15 @@ The GPU engine is replaced by a test double with the same solve() interface
 that solves the non-periodic reduced system (both copies of the shared edge are
 Dirichlet faces) with SciPy; the edge Schur complement, its correction steps,
 the folded residual and the periodic index sets are the product's own code.
-Checked against the reference's periodic solution (tests/golden fixture made by
-the reference's superLU path on a periodic square with Gaussian bumps).
+Checked against the reference's periodic solutions (tests/golden fixtures made by
+the reference's superLU path): a periodic square with Gaussian bumps, and the
+periodic curvy annulus of the reference's third test (mixed derivative; leaves
+couple to their corners through Interp_mat) at a smaller size.
 """
 import os
 
 import numpy as np
+import pytest
 import scipy.sparse.linalg as spla
 import torch
 
@@ -44,16 +47,20 @@ class NonPeriodicSolveDouble:
         return u_leaf, (torch.as_tensor(uf) if want_faces else None), 1, st
 
 
-def _setup(golden_dir):
-    g = np.load(os.path.join(golden_dir, NAME))
+def _setup(golden_dir, name=NAME):
+    g = np.load(os.path.join(golden_dir, name))
     p, n, kh = int(g['p']), int(g['n']), float(g['kh'])
     a = 1 / (2 * (n / (p - 2)))
     geom = Geometry(g['box'], a, p, 1.0)
     md = domain.Multidomain(g['box'], a, p)
     part = domain.SlabPartition(md, 1.0)                 # non-periodic: the engine's partition
-    co = md.coeffs(funcs.helmholtz_pdo(lambda x: funcs.bfield_gaussian_bumps(x, kh)))
+    if 'curvy' in name:   # mixed derivative: the Jxreorder / Interp_mat leaf branch
+        pdo, pmap = funcs.curvy_annulus_pdo(kh, funcs.bfield_constant)
+    else:
+        pdo, pmap = funcs.helmholtz_pdo(lambda x: funcs.bfield_gaussian_bumps(x, kh)), (lambda x: x)
+    co = md.coeffs(pdo)
     A = md.sparse_mat(oleaf.dtn_build(md.ld, co)).tocsr()
-    ud = lambda x: funcs.uu_dir_greens(x, kh)
+    ud = lambda x: funcs.uu_dir_greens(pmap(x), kh)
     return g, geom, md, part, co, A, ud
 
 
@@ -67,8 +74,9 @@ def test_periodic_index_sets_match_reference(golden_dir):
     assert np.array_equal(sets['I_Ctot'][sets['I_Ctot_copy2']], right)
 
 
-def test_periodic_edge_schur_solve(golden_dir):
-    g, geom, md, part, co, A, ud = _setup(golden_dir)
+@pytest.mark.parametrize('name', [NAME, 'periodic_curvy_annulus_p12_n230.npz'])
+def test_periodic_edge_schur_solve(golden_dir, name):
+    g, geom, md, part, co, A, ud = _setup(golden_dir, name)
     left, right = periodic.edge_faces(geom)
     rows = np.concatenate((left, right))
     Aedge = A[rows]
@@ -76,7 +84,7 @@ def test_periodic_edge_schur_solve(golden_dir):
     eng = NonPeriodicSolveDouble(md, part, A, co)
     edge = periodic.PeriodicEdge(eng, flux, left, right, geom.ntot, chunk=64).build('cpu')
     nL = left.size
-    assert eng.calls[:4] == [64, 64, 64, nL - 3 * 64]
+    assert eng.calls[:(nL + 63) // 64] == [64] * (nL // 64) + ([nL % 64] if nL % 64 else [])
     sets = periodic.periodic_index_sets(geom)
     bnd = torch.zeros(geom.ntot, 1, dtype=torch.float64)
     bnd[sets['I_Xtot']] = torch.as_tensor(ud(geom.xx_active[sets['I_Xtot']]))
