@@ -129,8 +129,9 @@ def _sinusoidal(kh, bfield):
 def get_param_map_and_pdo(geom, bfield, kh):
     """(op, param_map, inv_param_map) as src_disc/pdo.py:321-333.  'square' is the
     identity map; 'annulus', 'curvy_annulus' and 'sinusoidal' / 'curved' give
-    operators with a mixed derivative (c12), which Domain_Solver does not take
-    (the curved-domain leaf path is not provided on the GPU)."""
+    operators with a mixed derivative (c12), for which Domain_Solver runs the
+    reference's c12 leaf branch (the annulus's map is orthogonal, so its c12 is
+    zero to rounding)."""
     if geom == 'square':
         ident = lambda xx: xx.clone()
         return PDO_2d(const(1), const(1), c=lambda xx: bfield(xx, kh)), ident, ident
