@@ -74,6 +74,20 @@ def test_library_exports_every_declared_symbol():
     assert b'invalid' in lib.slab_last_error()
     assert lib.slab_leaf_dtn_work_bytes(0, 22, 0) == 0
     assert lib.slab_leaf_dtn_work_bytes(10, 22, 0) > 10 * 400 * 480 * 8
+    # the mixed-derivative entry points: 4(p-1) extra columns and the interpolation matrix
+    assert lib.slab_leaf_dtn_mixed_work_bytes(0, 22, 0) == 0
+    assert lib.slab_leaf_dtn_mixed_work_bytes(10, 22, 0) >= lib.slab_leaf_dtn_work_bytes(10, 22, 0) + \
+        10 * 400 * 4 * 8 + 84 * 80 * 8
+    st = lib.slab_engine_create_mixed(ctypes.byref(h), 1, 1, 1, 1, 1, _lib.np_ptr(z, ctypes.c_double),
+                                      _lib.np_ptr(z, ctypes.c_double), _lib.np_ptr(z, ctypes.c_double),
+                                      _lib.np_ptr(z, ctypes.c_double), _lib.np_ptr(np.zeros(4, np.int32), ctypes.c_int),
+                                      None)
+    assert st == -1
+    assert lib.slab_engine_factor_mixed(None, None, None, None, None, None, None) == -1
+    assert b'null engine' in lib.slab_last_error()
+    assert lib.slab_leaf_dtn_mixed(4, 22, *([None] * 11), 0, None, 0, None, None, None, None) == -1
+    assert lib.slab_csr_assemble(-1, None, None, 0, None, None) == -1
+    assert lib.slab_csr_spmv(-1, None, None, None, None, 1.0, 0.0, None, None) == -1
 
 
 @pytest.mark.parametrize('geom,p,n', [([[0, 1], [0, 1]], 8, 48), ([[0, 1], [0, 0.5]], 6, 28)])
