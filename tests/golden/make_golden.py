@@ -331,6 +331,43 @@ def hbs_fixture():
     save('hbs.npz', **out)
 
 
+def fd_fixture(name, n, ppw, pde, box=((0, 1.0), (0, 1.0)), buf_constant=0.6, stride=7):
+    """The reference's finite-difference discretisation (src_disc/fd_disc.py,
+    --disc fd in argparse_driver.py:144-150): the grid, its index sets, the
+    five-point operator, the slab partition, and the superLU and slabLU
+    solutions with free-space Dirichlet data."""
+    nwaves = int(n / ppw)
+    kh = (nwaves + 0.03) * 2 * np.pi + 1.8
+    if pde == 'bfield_constant':
+        cf = lambda xx: bif.bfield_constant(xx, kh)
+    else:
+        cf = lambda xx: bif.bfield_gaussian_bumps(xx, kh).reshape(-1)
+    op = ref_pdo.PDO_2d(ref_pdo.ones, ref_pdo.ones, c=cf)
+    h = 1 / n
+    uu = lambda xx: bif.uu_dir_func_greens(xx, kh)
+    out = dict(n=n, ppw=ppw, kh=kh, h=h, box=np.asarray(box), buf_constant=buf_constant, stride=stride)
+    for solver in ('superLU', 'slabLU'):
+        dom = Domain_Solver(torch.tensor(box), op, kh, h, buf_constant=buf_constant)
+        dom.build('reduced_cpu', solver, verbose=False)
+        sol, res, tres, rloc, _ = dom.solve(uu, None, known_sol=True)
+        sol, res, tres, rloc, _ = dom.solve(uu, None, known_sol=True)
+        sol = sol.numpy()
+        out.update({solver + '_sol_sub': sol[::stride], solver + '_sol_norm': np.linalg.norm(sol),
+                    solver + '_res': float(res), solver + '_trueres': float(tres)})
+    fd = dom.fd
+    A = dom.A.tocsr()
+    A.sort_indices()
+    out.update(ns=fd.ns.numpy(), XX=fd.XX.numpy()[::stride], buf=np.array(dom.buf), buf_prime=np.array(dom.buf_prime),
+               Npan=np.array(dom.Npan), Npan_loc=np.array(dom.Npan_loc), A_data_sub=A.data[::stride],
+               A_nnz=np.array(A.nnz), A_indptr_sha=np.array(hashlib.sha256(A.indptr.astype(np.int64).tobytes()).hexdigest()),
+               A_indices_sha=np.array(hashlib.sha256(A.indices.astype(np.int64).tobytes()).hexdigest()))
+    for nm in ('I_L', 'I_R', 'I_D', 'I_U', 'I_C', 'I_Ctot', 'I_Xtot'):
+        out[nm] = np.asarray(getattr(dom, nm))
+    out['I_X'] = np.asarray(fd.I_X)
+    out['inds_pans'] = np.asarray(dom.inds_pans)
+    save(name, **out)
+
+
 def solve_fixtures():
     dom, kh, sol, res, tres, rloc = run_domain(8, 48, 10, 'bfield_gaussian_bumps', 'superLU')
     save('solve_superlu_p8_n48.npz', p=8, n=48, kh=kh, sol=sol, res=res, trueres=tres, resloc=rloc)
@@ -343,6 +380,9 @@ def solve_fixtures():
 
 
 if __name__ == '__main__':
+    if len(sys.argv) > 2 and sys.argv[2] == 'fd':  # only the finite-difference fixture
+        fd_fixture('fd_n120_ppw20.npz', 120, 20, 'bfield_constant')
+        sys.exit(0)
     if len(sys.argv) > 2 and sys.argv[2] == 'hbs':  # only the HBS compression fixture
         hbs_fixture()
         sys.exit(0)
