@@ -27,7 +27,7 @@ struct LeafCoeffs {
   const double* c1;
   const double* c2;
   const double* c;
-  const double* c12 = nullptr;  // mixed derivative (leaf DtN entry point only)
+  const double* c12 = nullptr;  // mixed derivative (read by the kMixed kernels only)
 };
 
 template <typename T>
