@@ -386,6 +386,10 @@ if __name__ == '__main__':
     if len(sys.argv) > 2 and sys.argv[2] == 'hbs':  # only the HBS compression fixture
         hbs_fixture()
         sys.exit(0)
+    if len(sys.argv) > 2 and sys.argv[2] == 'periodic_full':  # the reference's third test at its own size
+        periodic_fixture('periodic_curvy_annulus_p22_n400.npz', 'curvy_annulus', [[0, 6.0], [0, 1.0]], 22, 400, 40,
+                         stride=97)
+        sys.exit(0)
     if len(sys.argv) > 2 and sys.argv[2] == 'periodic':  # only the periodic-boundary fixtures
         periodic_fixture('periodic_curvy_annulus_p12_n230.npz', 'curvy_annulus', [[0, 6.0], [0, 1.0]], 12, 230, 40,
                          stride=41)

@@ -7,10 +7,9 @@ and leaves then couple to their corners through Interp_mat
   * the engine (slab_engine_create_mixed) against the oracle's sparse direct
     solve of the same discretisation, given the same Interp_mat (1e-9);
   * Domain_Solver on the reference's own tests (tests/test_2d.py:51-55):
-    the annulus at the test's size against the reference's solution, the
-    periodic curvy annulus at a smaller size against the reference's
-    solution, and both at the tests' sizes through the argparse driver with
-    the tests' criterion trueres < 2e-5.
+    the annulus and the periodic curvy annulus at the tests' sizes (and the
+    latter smaller) against the reference's solutions, and both through the
+    argparse driver with the tests' criterion trueres < 2e-5.
 Tolerance against the reference's solutions: 1e-8, since the reference's
 Interp_mat is an ill-conditioned least-squares fit whose last digits depend on
 the LAPACK build (its face rows differ from the identity by ~1e-10).
@@ -95,10 +94,12 @@ def test_domain_solver_annulus_matches_reference(golden_dir):
     assert float(res) < 1e-10
 
 
-def test_domain_solver_periodic_curvy_annulus_matches_reference(golden_dir):
-    """The periodic curvy annulus (the reference's third test at p = 12, n = 230)."""
+@pytest.mark.parametrize('name', ['periodic_curvy_annulus_p12_n230.npz', 'periodic_curvy_annulus_p22_n400.npz'])
+def test_domain_solver_periodic_curvy_annulus_matches_reference(golden_dir, name):
+    """The periodic curvy annulus: the reference's third test (p = 22, n = 400 on
+    [0, 6] x [0, 1]) and a smaller case (p = 12, n = 230)."""
     import slablu_gb300 as sg
-    g = np.load(os.path.join(golden_dir, 'periodic_curvy_annulus_p12_n230.npz'))
+    g = np.load(os.path.join(golden_dir, name))
     dom, uu, kh = _annulus_solver(sg, 'curvy_annulus', g['box'].tolist(), int(g['p']), int(g['n']),
                                   int(g['ppw']), True)
     sol, res, tres, rloc, _ = dom.solve(uu, None, known_sol=True)
@@ -108,6 +109,8 @@ def test_domain_solver_periodic_curvy_annulus_matches_reference(golden_dir):
     assert err < 1e-8, err
     assert abs(float(tres) - float(g['superLU_trueres'])) < 1e-4 * float(g['superLU_trueres'])
     assert float(res) < 1e-8
+    if int(g['p']) == 22:
+        assert float(tres) < 2e-5   # the reference test's criterion (tests/test_2d.py:43)
 
 
 @pytest.mark.parametrize('domain,extra', [('annulus', []), ('curvy_annulus', ['--box_xlim', '6.0', '--periodic_bc'])])

@@ -64,6 +64,24 @@ def _setup(golden_dir, name=NAME):
     return g, geom, md, part, co, A, ud
 
 
+def test_periodic_index_sets_of_the_reference_test(golden_dir):
+    """The reference's third test at its own size (p = 22, n = 400, [0, 6] x [0, 1]):
+    partition and periodic index sets (large sets by length and SHA-256)."""
+    import hashlib
+    g = np.load(os.path.join(golden_dir, 'periodic_curvy_annulus_p22_n400.npz'))
+    p, n = int(g['p']), int(g['n'])
+    geom = Geometry(g['box'], 1 / (2 * (n / (p - 2))), p, 1.0)
+    assert (geom.buf, geom.Npan, geom.n0, geom.n1) == (int(g['buf']), int(g['Npan']), *map(int, g['nbox']))
+    sets = periodic.periodic_index_sets(geom)
+    for nm in ('I_Ctot', 'I_Xtot', 'I_slabX', 'I_Ctot_unique', 'I_Ctot_copy1', 'I_Ctot_copy2'):
+        v = np.ascontiguousarray(sets[nm], dtype=np.int64)
+        if nm in g.files:
+            assert np.array_equal(v, g[nm]), nm
+        else:
+            assert v.size == int(g[nm + '_size']), nm
+            assert hashlib.sha256(v.tobytes()).hexdigest() == str(g[nm + '_sha256']), nm
+
+
 def test_periodic_index_sets_match_reference(golden_dir):
     g, geom, *_ = _setup(golden_dir)
     sets = periodic.periodic_index_sets(geom)
