@@ -146,3 +146,71 @@ def test_fold_and_row_subset(golden_dir):
     E = sparse.row_subset(geom, R, rows)
     dense = E.to_torch().to_dense().numpy()
     assert np.array_equal(dense, As[rows].toarray())
+
+
+@pytest.mark.parametrize('name', [NAME, 'periodic_curvy_annulus_p12_n230.npz'])
+def test_domain_solver_periodic_flow_on_cpu(golden_dir, monkeypatch, name):
+    """Domain_Solver(periodic_bc=True) end to end with the GPU pieces replaced by CPU
+    doubles (the engine's non-periodic solve by a sparse direct solve, the reduced
+    operator by the oracle's assembly and torch's CSR product): build, the periodic
+    solve, the folded right-hand side and the folded residual are the product's code."""
+    import slablu_gb300 as sg
+    import slablu_gb300.slablu_solver as ss
+    g, geom, md, part, co, A, ud = _setup(golden_dir, name)
+    kh = float(g['kh'])
+    curvy = 'curvy' in name
+    As = A.copy()
+    As.sort_indices()
+
+    class EngineDouble(NonPeriodicSolveDouble):
+        def __init__(self, geom_, precision, mixed=False):
+            assert mixed == curvy
+            super().__init__(md, part, A, co)
+            self.factor_bytes = 0
+
+        def factor(self, **coeffs):
+            self.factored = sorted(k for k, v in coeffs.items() if v is not None)
+
+    def sparse_mat(view, device='cuda', verbose=False):
+        R = sparse.ReducedCSR(torch.as_tensor(As.indptr, dtype=torch.int64),
+                              torch.as_tensor(As.indices, dtype=torch.int32),
+                              torch.as_tensor(As.data), (geom.ntot, geom.ntot))
+        view._A = R
+        return R.to_torch(), {}
+
+    def matvec(self, x, alpha=1.0, beta=0.0, y=None):
+        X = x[:, None] if x.dim() == 1 else x
+        M = torch.sparse_csr_tensor(self.indptr, self.indices.to(torch.int64), self.vals, size=self.shape)
+        out = alpha * (M @ X.contiguous())
+        return out[:, 0] if x.dim() == 1 else out
+
+    monkeypatch.setattr(ss, 'SlabEngine', EngineDouble)
+    monkeypatch.setattr(ss._HPSView, 'sparse_mat', sparse_mat)
+    monkeypatch.setattr(sparse.ReducedCSR, 'matvec', matvec)
+    monkeypatch.setattr(ss.torch.cuda, 'synchronize', lambda *a, **k: None)
+    p, n = int(g['p']), int(g['n'])
+    if curvy:
+        op, pmap, _ = sg.pdo.get_param_map_and_pdo('curvy_annulus', sg.built_in_funcs.bfield_constant, kh)
+    else:
+        op = sg.pdo.PDO_2d(sg.pdo.ones, sg.pdo.ones, c=lambda xx: sg.built_in_funcs.bfield_gaussian_bumps(xx, kh))
+        pmap = lambda xx: xx
+    dom = sg.Domain_Solver(torch.tensor(g['box']), op, kh, 1 / (2 * (n / (p - 2))), p=p, buf_constant=1.0,
+                           periodic_bc=True, device='cpu')
+    info = dom.build('reduced_gpu', 'slabLU', verbose=False)
+    assert info['periodic_edge_size'] == g['I_Ctot_copy1'].size
+    assert dom.engine.factored == (['c', 'c1', 'c11', 'c12', 'c2', 'c22'] if curvy else ['c', 'c11', 'c22'])
+    uu = lambda xx: sg.built_in_funcs.uu_dir_func_greens(pmap(xx), kh)
+    sol, res, tres, rloc, _ = dom.solve(uu, None, known_sol=True)
+    stride = int(g['stride'])
+    ref = g['superLU_sol_sub']
+    assert np.linalg.norm(sol.numpy()[::stride] - ref) / np.linalg.norm(ref) < 1e-10
+    assert float(res) < 1e-12
+    assert abs(float(tres) - float(g['superLU_trueres'])) < 1e-8 * float(g['superLU_trueres'])
+    ff = dom.get_rhs(uu)
+    n_unique = g['I_Ctot_unique'].size if 'I_Ctot_unique' in g.files else int(g['I_Ctot_unique_size'])
+    assert ff.shape[0] == n_unique
+    ffr = domain.dirichlet_rhs(A, domain.SlabPartition(md, 1.0, periodic=True),
+                               ud(md.xx_active[dom.I_Xtot.numpy()]).reshape(-1, 1))
+    assert np.linalg.norm(ff.numpy() - ffr) <= 1e-12 * np.linalg.norm(ffr)
+    with pytest.raises(NotImplementedError):
+        dom.solve(uu, lambda xx: torch.ones(xx.shape[0], 1, dtype=torch.float64))
