@@ -82,3 +82,37 @@ def test_driver_sets_up_the_reference_curved_tests(monkeypatch):
     with pytest.raises(ValueError):
         argparse_driver.main(['--n', '400', '--pde', 'bfield_constant', '--bc', 'free_space', '--disc', 'hps',
                               '--p', '22', '--domain', 'corner', '--ppw', '40'])
+
+
+def test_driver_pickles_the_reference_keys(monkeypatch, tmp_path):
+    """The driver writes two pickles, build_info then solve_info, with the keys the
+    reference's driver writes (argparse_driver.py:169-188, 248-298)."""
+    import pickle
+    from slablu_gb300 import argparse_driver
+
+    class SolverDouble:
+        def __init__(self, box_geom, op, kh, a, p=0, buf_constant=0.5, periodic_bc=False, precision='mixed',
+                     tol=1e-10):
+            self.hps = type('H', (), {'n': torch.tensor([4, 4]), 'xx_tot': torch.zeros(16 * p * p, 2)})()
+            self.buf_pans = 2
+            self.last_solve_info = dict(iters=3)
+
+        def build(self, sparse_assembly, solver_type, verbose=True):
+            return dict(toc_build=0.5, toc_assembly=0.1, toc_factor=0.4, mem_build=1.0, precision='mixed')
+
+        def solve(self, uu_dir, ff_body, known_sol=False):
+            return torch.zeros(1, 1), torch.tensor(1e-12), torch.tensor(1e-9), 1e-10, 0.25
+
+    monkeypatch.setattr(argparse_driver, 'Domain_Solver', SolverDouble)
+    out = tmp_path / 'res.pkl'
+    argparse_driver.main(['--n', '80', '--pde', 'bfield_constant', '--bc', 'free_space', '--disc', 'hps', '--p', '12',
+                          '--domain', 'square', '--ppw', '10', '--pickle', str(out)])
+    with open(out, 'rb') as f:
+        build_info = pickle.load(f)
+        solve_info = pickle.load(f)
+    for k in ('toc_build', 'mem_build', 'toc_assembly', 'N', 'n', 'disc', 'buf', 'pde', 'bc', 'domain', 'solver',
+              'sparse_assembly', 'box_geom', 'kh', 'periodic_bc', 'a', 'p'):
+        assert k in build_info, k
+    for k in ('res_solve', 'trueres_solve', 'resloc_hps_solve', 'toc_solve'):
+        assert k in solve_info, k
+    assert build_info['N'] == 10 * (12 * 16 + 4 + 4) and build_info['buf'] == 2 * 10
