@@ -60,10 +60,10 @@ class FDDisc:
     def assemble_sparse(self):
         h, op, n0, n1 = self.h, self.pdo, self.n0, self.n1
         N = n0 * n1
-        d0sq = (1 / (h * h)) * sp.diags([1, -2, 1], [-1, 0, 1], shape=(n0, n0), format='csc')
-        d1sq = (1 / (h * h)) * sp.diags([1, -2, 1], [-1, 0, 1], shape=(n1, n1), format='csc')
-        d0 = (1 / (2 * h)) * sp.diags([-1, 0, +1], [-1, 0, 1], shape=(n0, n0), format='csc')
-        d1 = (1 / (2 * h)) * sp.diags([-1, 0, +1], [-1, 0, 1], shape=(n1, n1), format='csc')
+        d0sq = (1 / (h * h)) * sp.diags([1, -2, 1], [-1, 0, 1], shape=(n0, n0), format='csc', dtype=np.float64)
+        d1sq = (1 / (h * h)) * sp.diags([1, -2, 1], [-1, 0, 1], shape=(n1, n1), format='csc', dtype=np.float64)
+        d0 = (1 / (2 * h)) * sp.diags([-1, 0, +1], [-1, 0, 1], shape=(n0, n0), format='csc', dtype=np.float64)
+        d1 = (1 / (2 * h)) * sp.diags([-1, 0, +1], [-1, 0, 1], shape=(n1, n1), format='csc', dtype=np.float64)
         D00 = sp.kron(d0sq, sp.eye(n1))
         D11 = sp.kron(sp.eye(n0), d1sq)
         diag = lambda key: sp.diags(np.asarray(op[key](self.XX), dtype=float).reshape(N), 0, shape=(N, N))

@@ -9,6 +9,7 @@ the reference's superLU path): a periodic square with Gaussian bumps, and the
 periodic curvy annulus of the reference's third test (mixed derivative; leaves
 couple to their corners through Interp_mat) at a smaller size.
 """
+import functools
 import os
 
 import numpy as np
@@ -47,6 +48,7 @@ class NonPeriodicSolveDouble:
         return u_leaf, (torch.as_tensor(uf) if want_faces else None), 1, st
 
 
+@functools.lru_cache(maxsize=None)
 def _setup(golden_dir, name=NAME):
     g = np.load(os.path.join(golden_dir, name))
     p, n, kh = int(g['p']), int(g['n']), float(g['kh'])
