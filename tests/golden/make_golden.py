@@ -368,6 +368,24 @@ def fd_fixture(name, n, ppw, pde, box=((0, 1.0), (0, 1.0)), buf_constant=0.6, st
     save(name, **out)
 
 
+def param_map_fixture(name='param_maps.npz', kh=25.0, seed=9):
+    """The reference's parameter maps (src_disc/pdo.py:164-319) at seeded points of the
+    unit square (and of [0, 6] x [0, 1] for the curvy annulus): mapped points and every
+    coefficient of the pulled-back operator."""
+    rng = np.random.default_rng(seed)
+    out = {}
+    for geom, xmax in (('curved', 1.0), ('annulus', 1.0), ('curvy_annulus', 6.0)):
+        xs = torch.tensor(rng.random((200, 2)) * np.array([xmax, 1.0]))
+        op, pmap, inv = ref_pdo.get_param_map_and_pdo(geom, bif.bfield_constant, kh)
+        out[geom + '_xx'] = xs.numpy()
+        out[geom + '_mapped'] = pmap(xs.clone()).numpy()
+        for k in ('c11', 'c22', 'c12', 'c1', 'c2', 'c'):
+            f = getattr(op, k)
+            out[geom + '_' + k] = np.zeros(xs.shape[0]) if f is None else np.asarray(f(xs.clone())).reshape(-1)
+    out['kh'] = np.array(kh)
+    save(name, **out)
+
+
 def solve_fixtures():
     dom, kh, sol, res, tres, rloc = run_domain(8, 48, 10, 'bfield_gaussian_bumps', 'superLU')
     save('solve_superlu_p8_n48.npz', p=8, n=48, kh=kh, sol=sol, res=res, trueres=tres, resloc=rloc)
@@ -380,6 +398,9 @@ def solve_fixtures():
 
 
 if __name__ == '__main__':
+    if len(sys.argv) > 2 and sys.argv[2] == 'maps':  # only the parameter-map fixture
+        param_map_fixture()
+        sys.exit(0)
     if len(sys.argv) > 2 and sys.argv[2] == 'fd':  # only the finite-difference fixture
         fd_fixture('fd_n120_ppw20.npz', 120, 20, 'bfield_constant')
         sys.exit(0)

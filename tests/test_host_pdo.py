@@ -47,3 +47,27 @@ def test_square_and_unknown_geometry():
     assert torch.allclose(inv(pmap(xs)), xs, atol=1e-14)
     with pytest.raises(ValueError):
         pdo.get_param_map_and_pdo('corner', _bfield_constant, 3.0)
+
+
+@pytest.mark.parametrize('geom', ['curved', 'annulus', 'curvy_annulus'])
+def test_every_parameter_map_matches_reference(golden_dir, geom):
+    """All three curved domains of the reference (the sinusoidal strip included), product
+    (torch) and oracle (NumPy), at seeded points (tests/golden/param_maps.npz)."""
+    from oracle import funcs
+    g = np.load(os.path.join(golden_dir, 'param_maps.npz'))
+    kh = float(g['kh'])
+    xs = g[geom + '_xx']
+    op, pmap, _ = pdo.get_param_map_and_pdo(geom, _bfield_constant, kh)
+    opo, pmapo = funcs.param_pdo(geom, kh, funcs.bfield_constant)
+    assert np.abs(pmap(torch.as_tensor(xs)).numpy() - g[geom + '_mapped']).max() < 1e-14
+    assert np.abs(pmapo(xs) - g[geom + '_mapped']).max() < 1e-14
+    for k in ('c11', 'c22', 'c12', 'c1', 'c2', 'c'):
+        ref = g[geom + '_' + k]
+        tol = 1e-13 * max(np.abs(ref).max(), 1.0)
+        f = getattr(op, k)
+        fo = opo.get(k)
+        if f is None:
+            assert np.abs(ref).max() == 0.0 and fo is None, k
+            continue
+        assert np.abs(f(torch.as_tensor(xs)).numpy() - ref).max() <= tol, k
+        assert np.abs(fo(xs) - ref).max() <= tol, k
