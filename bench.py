@@ -35,6 +35,8 @@ P, NSIDE = 22, 2000
 CPU_SAMPLE_N = 400
 # DRAM bytes per leaf of leaf_factor_kernel<float>, measured with ncu on 1024 leaves
 LEAF_DRAM_BYTES_PER_LEAF = 9.82e9 / 1024
+# FP32 FMA peak of the CUDA cores: 152 SMs x 128 lanes x 2 flops x 2.07 GHz
+FP32_SIMT_PEAK = 152 * 128 * 2 * 2.07e9 / 1e12
 
 
 def parse():
@@ -51,6 +53,8 @@ def parse():
     ap.add_argument('--no-cpu-baseline', action='store_true')
     ap.add_argument('--no-autotune', action='store_true', help='keep the default launch choices')
     ap.add_argument('--nrhs', type=int, default=256, help='right-hand sides of the multi-RHS solve (0 = skip)')
+    ap.add_argument('--no-config2', action='store_true', help='skip the 16,384-leaf DtN microbenchmark')
+    ap.add_argument('--no-config5', action='store_true', help='skip the inverse-scattering gradient check')
     return ap.parse_args()
 
 
@@ -208,6 +212,159 @@ def combine_ranks(t_local, units_local, world, device):
     return t_max, units_local * world / t_max
 
 
+def oracle_fixtures(n):
+    """FP64 oracle solutions of the benchmark workload made by running the reference
+    itself (tests/golden/make_golden.py): its superLU sparse direct solve and its
+    slabLU, each a strided sample of the leaf-node solution with its norm."""
+    out = {}
+    if n != NSIDE:
+        return out
+    for solver in ('superLU', 'slabLU'):
+        path = os.path.join(ROOT, 'tests', 'golden', f'config3_{solver}_p22_n2000.npz')
+        if os.path.exists(path):
+            out[solver] = np.load(path)
+    return out
+
+
+def rel_to_oracle(u, fx):
+    """Relative error of the leaf-node solution u (host array) against each oracle sample."""
+    res = {}
+    for solver, g in fx.items():
+        stride = int(g['stride'])
+        ref = g['sol_sub']
+        if u.size != int(g['sol_len']):
+            continue
+        res[solver] = float(np.linalg.norm(u[::stride] - ref) / np.linalg.norm(ref))
+    return res
+
+
+def bench_config2(dev, reps=3):
+    """Config 2: batched leaf DtN maps of 16,384 leaves (128 x 128 tiling, p = 22,
+    32-bump field) through slab_leaf_dtn in FP64 and FP32: device time per batch
+    (CUDA events on the launching stream, best of `reps`), per-leaf relative
+    error of the FP32 maps against the FP64 maps, and both against the
+    reference's form_DtNs on sampled leaves (tests/golden/config2_dtn_p22.npz)."""
+    import ctypes
+    import torch
+    from slablu_gb300 import _lib, hps, problems
+    L = _lib.lib()
+    cfg = problems.config2()
+    p = cfg['p']
+    geo = hps.Geometry([[0, 1], [0, 1]], cfg['a'], p, 1.0)
+    nl, q = geo.nboxes, p - 2
+    xx = torch.as_tensor(geo.xx_tot, device=dev)
+    c = cfg['c'](xx).reshape(nl, p * p).contiguous()
+    one = torch.ones_like(c)
+    t = lambda a: torch.as_tensor(np.ascontiguousarray(a), dtype=torch.float64, device=dev)
+    D, Dsq, Nx = t(geo.ops.D), t(geo.ops.Dsq), t(geo.ops.Nx)
+    stream = torch.cuda.current_stream(dev)
+    out = dict(leaves=nl, p=p, kh=cfg['kh'], flops_per_leaf=leaf_flops(p))
+    maps = {}
+    for name, prec in (('fp64', 0), ('fp32', 2)):
+        wb = int(L.slab_leaf_dtn_work_bytes(nl, p, prec))
+        work = torch.empty(wb, dtype=torch.uint8, device=dev)
+        dtn = torch.empty(nl, 4 * q, 4 * q, dtype=torch.float64, device=dev)
+        info = torch.zeros(nl, dtype=torch.int32, device=dev)
+        best = None
+        for _ in range(reps + 1):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            st = L.slab_leaf_dtn(nl, p, _lib.ptr(one), _lib.ptr(one), None, None, _lib.ptr(c), _lib.ptr(D),
+                                 _lib.ptr(Dsq), _lib.ptr(Nx), prec, _lib.ptr(work), ctypes.c_size_t(wb), _lib.ptr(dtn),
+                                 None, _lib.ptr(info), ctypes.c_void_p(stream.cuda_stream))
+            e1.record(stream)
+            _lib.check(st, 'slab_leaf_dtn')
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1)
+            best = ms if best is None else min(best, ms)
+        assert int(info.abs().sum()) == 0
+        maps[name] = dtn
+        out[f'ms_{name}'] = best
+        out[f'leaves_per_s_{name}'] = nl / (best / 1e3)
+        out[f'tflops_{name}'] = leaf_flops(p) * nl / (best / 1e3) / 1e12
+        del work
+        torch.cuda.empty_cache()
+    rel = torch.linalg.norm((maps['fp32'] - maps['fp64']).flatten(1), dim=1) / \
+        torch.linalg.norm(maps['fp64'].flatten(1), dim=1)
+    out['rel_err_fp32_vs_fp64_max'] = float(rel.max())
+    out['rel_err_fp32_vs_fp64_median'] = float(rel.median())
+    path = os.path.join(ROOT, 'tests', 'golden', 'config2_dtn_p22.npz')
+    if os.path.exists(path):
+        gld = np.load(path)
+        ref = gld['dtn']
+        for name in ('fp64', 'fp32'):
+            got = maps[name][torch.as_tensor(gld['picks'], device=dev)].cpu().numpy()
+            out[f'rel_err_vs_reference_{name}'] = float(
+                (np.linalg.norm(got - ref, axis=(1, 2)) / np.linalg.norm(ref, axis=(1, 2))).max())
+    out['note'] = ('per-leaf maps without refinement; the FP32 factors are refined against the FP64 residual '
+                   'of the whole system in the factor+solve path')
+    return out
+
+
+def bench_config5(dev, nfd=16, h=1e-4):
+    """Config 5: differentiable inverse scattering at p = 16, n = 1008 (FP64).
+    Loss ||P u(b) - d||^2 (P: 4,096 seeded interior leaf nodes); the gradient
+    with respect to b at every leaf node by the hand-written adjoint
+    (slab_solve's backward), checked against central differences along nfd
+    seeded smooth directions, Richardson-extrapolated from the steps h and h/2
+    (the O(h^2) term cancels; the loss is strongly nonlinear in b at kh = 630).
+    Times are host wall times with the device synchronised, after a warm-up
+    pass that captures the forward and transposed graphs (forward = factor +
+    refined solve; gradient = refined transposed solve + coefficient-gradient
+    reduction)."""
+    import torch
+    from slablu_gb300 import hps, problems
+    from slablu_gb300.adjoint import slab_solve
+    from slablu_gb300.engine import SlabEngine
+    cfg = problems.config5()
+    geo = hps.Geometry([[0, 1], [0, 1]], cfg['a'], cfg['p'], 1.0)
+    xx = torch.as_tensor(geo.xx_tot, device=dev)
+    b = cfg['b'](xx)
+    ones = torch.ones_like(b)
+    bnd = torch.ones(geo.ntot, dtype=torch.float64, device=dev)
+    probes = torch.as_tensor(problems.probe_nodes(geo.xx_tot, cfg['nprobe']), device=dev)
+    eng = SlabEngine(geo, 'fp64')
+    tol = 1e-12
+    solve = lambda bb: slab_solve(eng, bnd, tol=tol, max_iter=60, c11=ones, c22=ones, c=cfg['c_of_b'](bb))
+    with torch.no_grad():
+        d = solve(cfg['b_perturbed'](xx))[probes].clone()
+    loss_fn = lambda bb: ((solve(bb)[probes] - d) ** 2).sum()
+    bb = b.clone().requires_grad_(True)
+    loss_fn(bb).backward()   # warm-up: graphs captured
+    bb = b.clone().requires_grad_(True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    loss = loss_fn(bb)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    loss.backward()
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    grad = bb.grad.detach()
+    with torch.no_grad():
+        u = solve(b)
+        gl = torch.zeros_like(u)
+        gl[probes] = 2 * (u[probes] - d)
+        _, _, _, adj_iters, adj_info = eng.adjoint(gleaf=gl, tol=tol, max_iter=60, allow_noconv=True)
+    errs = []
+    with torch.no_grad():
+        for i in range(nfd):
+            v = problems.grf(xx, seed=500 + i)
+            fd = {}
+            for hh in (h, h / 2):
+                lp = float(loss_fn(b + hh * v))
+                lm = float(loss_fn(b - hh * v))
+                fd[hh] = (lp - lm) / (2 * hh)
+            fdr = (4 * fd[h / 2] - fd[h]) / 3
+            ad = float((grad * v).sum())
+            errs.append(abs(fdr - ad) / max(abs(fdr), 1e-300))
+    return dict(p=cfg['p'], n=cfg['n'], leaves=geo.nboxes, N=geo.N_reported, kh=cfg['kh'], probes=cfg['nprobe'],
+                loss=float(loss), forward_ms=1e3 * (t1 - t0), gradient_ms=1e3 * (t2 - t1),
+                adjoint_iters=int(adj_iters), adjoint_rel_residual=adj_info['rel_residual'],
+                fd_directions=nfd, fd_steps=[h, h / 2], fd='central differences, Richardson-extrapolated',
+                fd_rel_err_max=max(errs), fd_rel_errs=errs, fd_ok=max(errs) <= 1e-5, precision='fp64', tol=tol)
+
+
 def workload_name(p, n, g, cfg, tol):
     return (f'HPS SlabLU p={p} n={n} ({g.n0}x{g.n1} leaves, N={g.N_reported}), Gaussian-lattice Helmholtz '
             f'kh={cfg["kh"]:.1f}, u=1 Dirichlet; mixed precision + FP64 refinement to tol {tol:g}')
@@ -256,7 +413,7 @@ def run_ours(args):
     picks = None
     if not args.no_autotune:
         from slablu_gb300 import autotune
-        picks = autotune.tune(eng, dict(c11=one, c22=one, c=c), bnd, use_cache=False)
+        picks = autotune.tune(eng, dict(c11=one, c22=one, c=c), bnd, use_cache=False, tol=args.tol)
 
     def step():
         eng.factor(c11=one, c22=one, c=c)
@@ -265,6 +422,9 @@ def run_ours(args):
     for _ in range(args.warmup):
         u, _, iters, st = step()
     rel_err = float(torch.linalg.norm(u[:, 0] - u64) / torch.linalg.norm(u64))
+    fx = oracle_fixtures(n)
+    rel_oracle = rel_to_oracle(u[:, 0].cpu().numpy(), fx)
+    rel_oracle_fp64 = rel_to_oracle(u64.cpu().numpy(), fx)
 
     # ---- timed region: K steps, device time with CUDA events ------------------
     leaf_ms, iface_ms, tree_ms, apply_ms, napply = [], [], [], [], []
@@ -287,23 +447,33 @@ def run_ours(args):
     t_total, value = combine_ranks(ev0.elapsed_time(ev1) / 1e3, N * args.steps, world, dev)
     clocks = clk.summary()
 
-    # ---- end-to-end through the C ABI with host buffers -----------------------
-    hc = c.cpu().pin_memory()
-    h1 = one.cpu().pin_memory()
-    hb = bnd.cpu().pin_memory()
-    hout = torch.empty(eng.npts, dtype=torch.float64).pin_memory()
+    # ---- end to end through the drop-in API (Domain_Solver.build + solve) -----
+    # the reference driver's calls (argparse_driver.py:161-170, 250-251): the leaf
+    # nodes go to the device and the coefficient field is evaluated there, the
+    # Dirichlet data is evaluated on the host and copied over, and the leaf-node
+    # solution comes back to the host as sol_tot
+    import slablu_gb300 as sg
+    op = sg.pdo.PDO_2d(sg.pdo.ones, sg.pdo.ones, c=cfg['c'])
+    dom = sg.Domain_Solver(torch.tensor([[0, 1.0], [0, 1.0]]), op, cfg['kh'], problems.leaf_half_width(n, p), p=p,
+                           buf_constant=1.0, precision='mixed', tol=args.tol, max_iter=30, device=str(dev))
+    dom.build('reduced_gpu', 'slabLU', verbose=False)
+    if picks:
+        from slablu_gb300 import autotune
+        autotune.set_options(dom.engine, {k: v for k, v in picks.items() if k in autotune.TUNABLES})
+    dom.solve(cfg['uu_dir'])
     e2e_times = []
     for i in range(2):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        dc, d1, db = hc.to(dev, non_blocking=True), h1.to(dev, non_blocking=True), hb.to(dev, non_blocking=True)
-        eng.factor(c11=d1, c22=d1, c=dc)
-        ue, _, _, _ = eng.solve(db, tol=args.tol, max_iter=30)
-        hout.copy_(ue[:, 0])
+        dom.build('reduced_gpu', 'slabLU', verbose=False)
+        sol_e2e, _, _, _, _ = dom.solve(cfg['uu_dir'])
         torch.cuda.synchronize()
         e2e_times.append(time.perf_counter() - t0)
-    h2d = 3 * hc.numel() * 8 + hb.numel() * 8
-    d2h = hout.numel() * 8
+    rel_oracle_e2e = rel_to_oracle(sol_e2e.numpy()[:, 0], fx)
+    h2d = g.xx_tot.size * 8 + len(g.I_Xtot) * 8     # leaf nodes (coefficients) + Dirichlet data
+    d2h = sol_e2e.numel() * 8                          # sol_tot
+    del dom
+    torch.cuda.empty_cache()
 
     # ---- 256 right-hand sides on the same factorization (one graph per application)
     multi = None
@@ -336,6 +506,10 @@ def run_ours(args):
     achieved = lf / leaf_avg / 1e12
     iface_avg = sum(iface_ms) / len(iface_ms) / 1e3
     if_fl = iface_flops(g.Npan - 1, g.n1 * g.q)
+    hbm_peak = peaks.get('hbm_gbs') or 6800.0
+    solve_bytes = eng.solve_bytes
+    app_s = (sum(apply_ms) / max(sum(napply), 1)) / 1e3
+    solve_gbs = solve_bytes / app_s / 1e9 if app_s > 0 else None
 
     line = dict(
         metric=METRIC, value=value, unit='unknowns/s', n_gpus=world, steps=args.steps, warmup=args.warmup,
@@ -344,7 +518,11 @@ def run_ours(args):
         config=dict(workload=workload_name(p, n, g, cfg, args.tol), buf=g.buf, Npan=g.Npan,
                     parallelism='replicas' if world > 1 else 'single GPU',
                     l2='inputs and factors (~17 GB) larger than L2; no flush'),
-        rel_err_vs_fp64=rel_err, refine_iters=int(iters), fp64_iters=int(it64),
+        rel_err_vs_fp64=rel_err, rel_err_vs_oracle=rel_oracle, rel_err_vs_oracle_e2e=rel_oracle_e2e,
+        fp64_rel_err_vs_oracle=rel_oracle_fp64,
+        oracle='FP64 solutions of this workload by the reference itself (its superLU sparse direct solve and its '
+               'slabLU; tests/golden/config3_*.npz, strided samples)',
+        refine_iters=int(iters), fp64_iters=int(it64),
         fp64_value=(N / (sum(fp64_times) / len(fp64_times))) if fp64_times else None,
         speedup_vs_fp64=((sum(fp64_times) / len(fp64_times)) / (t_total / args.steps)) if fp64_times else None,
         phases_ms=dict(leaf=leaf_avg * 1e3, tree=sum(tree_ms) / len(tree_ms), interface=iface_avg * 1e3,
@@ -356,12 +534,18 @@ def run_ours(args):
         roofline=dict(kernel='leaf_factor_kernel<float> (one launch per step)', bound='tensor', achieved=achieved,
                       peak=peak, unit='TFLOP/s', frac=achieved / peak,
                       traffic=LEAF_DRAM_BYTES_PER_LEAF * g.nboxes,
-                      traffic_source='dram read+write per leaf from the 1024-leaf ncu capture '
-                                     '(profiles/leaf_factor_kernel_fp32_1024leaves.md) x leaves per launch',
+                      traffic_source='dram read+write per leaf of the 1024-leaf ncu capture x leaves per launch',
                       peak_source='MEASURED_PEAKS.json bf16_tflops (measured)' if bf16 else 'fallback 1.9 PF bf16',
                       algorithmic_flops_per_launch=lf,
-                      note='the leaf kernel computes on the FP32 CUDA cores (nominal 80 TFLOP/s at 2.07 GHz); '
-                           'its fraction of the BF16 tensor peak is small by construction'),
+                      pipe='FP32 CUDA cores (this kernel issues no MMA; the compute class is the tensor roofline '
+                           'the contract names, its peak is not the pipe it runs on)',
+                      fp32_simt_peak_tflops=FP32_SIMT_PEAK,
+                      frac_of_fp32_simt=achieved / FP32_SIMT_PEAK),
+        roofline_solve=dict(kernel='one refinement application (leaf, merge-tree and interface sweeps)',
+                            bound='hbm', unit='GB/s', bytes_per_application=solve_bytes,
+                            achieved=solve_gbs, peak=hbm_peak, frac=solve_gbs / hbm_peak if solve_gbs else None,
+                            peak_source='MEASURED_PEAKS.json hbm_gbs (measured)' if peaks.get('hbm_gbs')
+                            else 'fallback 6800 GB/s'),
         clocks=clocks,
         e2e=dict(value=N / (sum(e2e_times) / len(e2e_times)), unit='unknowns/s', h2d_bytes_per_step=h2d,
                  d2h_bytes_per_step=d2h),
@@ -369,13 +553,34 @@ def run_ours(args):
         autotune=picks,
         multi_rhs=multi,
     )
+    del eng
+    torch.cuda.empty_cache()
+    # the other configurations' sections report a failure in the line instead of
+    # losing the headline measurement above
+    if rank == 0 and not args.no_config2:
+        try:
+            line['config2'] = bench_config2(dev)
+        except Exception as e:  # noqa: BLE001
+            line['config2'] = dict(error=f'{type(e).__name__}: {e}')
+        torch.cuda.empty_cache()
+    if rank == 0 and not args.no_config5:
+        try:
+            line['config5'] = bench_config5(dev)
+        except Exception as e:  # noqa: BLE001
+            line['config5'] = dict(error=f'{type(e).__name__}: {e}')
+        torch.cuda.empty_cache()
     if rank == 0 and not args.no_cpu_baseline:
         Nc, tc = cpu_sample()
         line['cpu_baseline'] = dict(value=Nc / tc['total'], unit='unknowns/s', cores=cpu_threads(), kind='port',
                                     sample=f'oracle port of the reference CPU slabLU, full factor+solve of the same '
                                            f'field at n={CPU_SAMPLE_N} (N={Nc}), {tc["total"]:.1f} s')
+    # the sparse direct solve is the oracle of record; the reference's slabLU (randomised
+    # HBS compression of the interface blocks) stands in where that fixture is absent
+    primary = rel_oracle.get('superLU', rel_oracle.get('slabLU'))
     if rel_err > 1e-6:
         line['invalid'] = f'mixed vs FP64 relative error {rel_err:.2e} > 1e-6'
+    elif primary is not None and primary > 1e-6:
+        line['invalid'] = f'relative error against the FP64 oracle {primary:.2e} > 1e-6'
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -90,8 +90,9 @@ int slab_leaf_dtn_mixed(int nleaf, int p, const double* d_c11, const double* d_c
 /*
  * Allocation-free batched leaf DtN maps.  No counterpart in the reference: it
  * exists for callers that cannot allocate device memory when they need DtN
- * maps (inside CUDA stream capture, where cudaMalloc is not allowed, or under
- * a host application that owns all device memory).  Same arguments and
+ * maps (a host application whose own pool allocator owns all device memory and
+ * forbids library allocations, or a program with a device-memory budget fixed
+ * at start-up).  Same arguments and
  * results as slab_leaf_dtn without the work buffer and without S; the leaf
  * factors live in a fixed scratch array compiled into the library
  * (slab_leaf_dtn_noalloc_max_bytes() bytes, held on every device that loads
@@ -226,6 +227,24 @@ size_t slab_dgemm_emu_work_bytes(int m, int n, int k);
 int slab_dgemm_emu(int m, int n, int k, double alpha, const double* d_A, int lda, const double* d_B, int ldb,
                    double beta, double* d_C, int ldc, void* d_work, size_t work_bytes, void* stream);
 
+/* Batched FP32 matrix product on the TF32 tensor cores (tcgen05) by exact
+ * three-way TF32 splitting: C[b] = alpha A[b] B[b] + beta C[b] for b < batch,
+ * A (m x k), B (k x n), C (m x n) column-major device arrays with batch strides
+ * in elements.  Each operand is split into three TF32 values summing to it
+ * exactly and the six slice products of weight down to 2^-22 are accumulated
+ * in FP32 in tensor memory: the error stays within the FP32 dot-product bound
+ * k 2^-24 max|A(i,:)| max|B(:,j)|.  C may alias B.  d_work: at least
+ * 256 + slab_sgemm_tc_work_bytes(m, n, k, batch) bytes, 256-byte aligned.
+ * Synchronizes the stream to report failures.  Replaces the batched products
+ * of the slab Schur arithmetic (the Schur update T_i - L U of
+ * src_solver/block_tridiag_solver_dense.py:169 and the slab interface products
+ * of src_solver/slablu_solver.py:1066-1136), which the engine calls
+ * asynchronously inside its factorization. */
+size_t slab_sgemm_tc_work_bytes(int m, int n, int k, int batch);
+int slab_sgemm_tc(int m, int n, int k, float alpha, const float* d_A, int lda, long long strideA, const float* d_B,
+                  int ldb, long long strideB, float beta, float* d_C, int ldc, long long strideC, int batch,
+                  void* d_work, size_t work_bytes, void* stream);
+
 /*
  * Reduced sparse operator on the device (CSR, FP64).
  * Replaces the COO -> CSR assembly of HPS_Multidomain.sparse_mat
@@ -255,15 +274,38 @@ int slab_csr_spmv(int nrows, const long long* d_indptr, const int* d_indices, co
  *                        each outer block's update of the columns beyond the next
  *                        block with that block's panels (second stream), 0 serial;
  *                        both give the same factors
+ *   SLAB_OPT_TREE_TC     FP32 merge tree (mixed and fp32 engines): 1 forms the
+ *                        merges' Schur updates F -= col W as TF32-split
+ *                        tensor-core products (slab_sgemm_tc), 0 on the CUDA
+ *                        cores; fp64 engines accept 0 only
+ *   SLAB_OPT_LEAF_ASSEMBLY leaf operators without c12: 1 assembled by a kernel
+ *                        of their own at full occupancy before the factor
+ *                        kernel, 0 inside the factor kernel; same factors
+ *   SLAB_OPT_IFACE_OUTER_INV interface block LU (mixed precision): 1 applies
+ *                        S_j^{-1} to the Schur right-hand sides through inverted
+ *                        256-row diagonal blocks of L and U, every product on the
+ *                        tensor cores; 0 solves inside each 256-row block with
+ *                        FP64-core triangular solves of 64-row blocks
  * set returns a status; get returns the value (or a negative status). */
 #define SLAB_OPT_LEAF_CTAS 1
 #define SLAB_OPT_IFACE_SOLVE 2
 #define SLAB_OPT_IFACE_LOOKAHEAD 3
+#define SLAB_OPT_TREE_TC 4
+#define SLAB_OPT_LEAF_ASSEMBLY 5
+#define SLAB_OPT_IFACE_OUTER_INV 6
 int slab_engine_set_option(slab_engine* e, int key, int value);
 int slab_engine_get_option(const slab_engine* e, int key);
 
 /* Bytes of device memory held by the engine's factorization. */
 size_t slab_engine_factor_bytes(const slab_engine* e);
+
+/* Bytes of stored factors one solve application reads (leaf LU and S, merge
+ * factors, the interface factors applied in the solve phase, pivots): the
+ * algorithmic traffic of the memory-bound solve sweep.  The reference reads
+ * its factors in lusolve_sweep and __solve_lowmem
+ * (src_solver/block_tridiag_solver_dense.py:179-202,
+ * src_solver/block_tridiag_solver_structured.py:157-187). */
+size_t slab_engine_solve_bytes(const slab_engine* e);
 
 /* Device times (CUDA events on the engine stream, milliseconds) of the last
  * factor and solve: [0] leaf kernel, [1] slab merge tree, [2] interface block

@@ -41,6 +41,7 @@ _SIGS = {
                                     P_int, P_double]),
     'slab_engine_coeff_grad': (c_int, [c_void, c_int] + [c_void] * 8),
     'slab_engine_factor_bytes': (c_size, [c_void]),
+    'slab_engine_solve_bytes': (c_size, [c_void]),
     'slab_engine_timings': (c_int, [c_void, P_double, c_int]),
     'slab_leaf_dtn_noalloc_max_bytes': (c_size, []),
     'slab_leaf_dtn_noalloc': (c_int, [c_int, c_int] + [c_void] * 8 + [c_int, c_void, c_void, c_void]),
@@ -55,12 +56,18 @@ _SIGS = {
     'slab_leaf_dtn_mixed': (c_int, [c_int, c_int] + [c_void] * 11 + [c_int, c_void, c_size, c_void, c_void, c_void,
                                                                       c_void]),
     'slab_csr_spmv': (c_int, [c_int, c_void, c_void, c_void, c_void, c_double, c_double, c_void, c_void]),
+    'slab_sgemm_tc_work_bytes': (c_size, [c_int, c_int, c_int, c_int]),
+    'slab_sgemm_tc': (c_int, [c_int, c_int, c_int, ctypes.c_float, c_void, c_int, c_ll, c_void, c_int, c_ll,
+                              ctypes.c_float, c_void, c_int, c_ll, c_int, c_void, c_size, c_void]),
 }
 
 
 SLAB_OPT_LEAF_CTAS = 1
 SLAB_OPT_IFACE_SOLVE = 2
 SLAB_OPT_IFACE_LOOKAHEAD = 3
+SLAB_OPT_TREE_TC = 4
+SLAB_OPT_LEAF_ASSEMBLY = 5
+SLAB_OPT_IFACE_OUTER_INV = 6
 
 
 class SlabError(RuntimeError):

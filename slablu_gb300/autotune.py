@@ -21,6 +21,9 @@ TUNABLES = {
     'leaf_ctas': (_lib.SLAB_OPT_LEAF_CTAS, (0, 2, 1)),
     'iface_solve': (_lib.SLAB_OPT_IFACE_SOLVE, (0, 1)),
     'iface_lookahead': (_lib.SLAB_OPT_IFACE_LOOKAHEAD, (1, 0)),
+    'tree_tc': (_lib.SLAB_OPT_TREE_TC, (0, 1)),
+    'leaf_assembly': (_lib.SLAB_OPT_LEAF_ASSEMBLY, (1, 0)),
+    'iface_outer_inv': (_lib.SLAB_OPT_IFACE_OUTER_INV, (1, 0)),
 }
 
 
@@ -98,7 +101,19 @@ def _time_apply(engine, bnd, reps):
     return best
 
 
-def tune(engine, coeffs, bnd, reps=2, use_cache=True, path=None):
+def _time_tree_and_solve(engine, coeffs, bnd, reps, tol):
+    """Merge-tree time plus the refined solve's time: a choice that changes the
+    factors' accuracy changes the number of refinement applications too."""
+    best = float('inf')
+    for _ in range(reps):
+        engine.factor(**coeffs)
+        t_tree = engine.timings()['tree_ms']
+        engine.solve(bnd, tol=tol, max_iter=30, allow_noconv=True)
+        best = min(best, t_tree + engine.timings()['solve_ms'])
+    return best
+
+
+def tune(engine, coeffs, bnd, reps=2, use_cache=True, path=None, tol=1e-6):
     """Time the candidates of every tunable on this engine and keep the fastest.
 
     coeffs: the engine.factor keyword arguments; bnd: a face vector for solve.
@@ -118,6 +133,24 @@ def tune(engine, coeffs, bnd, reps=2, use_cache=True, path=None):
     picks['leaf_ctas'] = min(cands, key=lambda v: (t_leaf[v], cands.index(v)))
     timings['leaf_ms'] = {str(v): t for v, t in t_leaf.items()}
     _lib.check(engine.L.slab_engine_set_option(engine.h, key, picks['leaf_ctas']), 'slab_engine_set_option')
+    if not getattr(engine, 'mixed', False):
+        key, cands = TUNABLES['leaf_assembly']
+        t_asm = {}
+        for v in cands:
+            _lib.check(engine.L.slab_engine_set_option(engine.h, key, v), 'slab_engine_set_option')
+            t_asm[v] = _time_leaf(engine, coeffs, reps)
+        picks['leaf_assembly'] = min(cands, key=lambda v: (t_asm[v], cands.index(v)))
+        timings['leaf_assembly_ms'] = {str(v): t for v, t in t_asm.items()}
+        _lib.check(engine.L.slab_engine_set_option(engine.h, key, picks['leaf_assembly']), 'slab_engine_set_option')
+    if engine.geom.Npan > 2 and engine.precision == 'mixed':
+        key, cands = TUNABLES['iface_outer_inv']
+        t_oi = {}
+        for v in cands:
+            _lib.check(engine.L.slab_engine_set_option(engine.h, key, v), 'slab_engine_set_option')
+            t_oi[v] = _time_interface(engine, coeffs, reps)
+        picks['iface_outer_inv'] = min(cands, key=lambda v: (t_oi[v], cands.index(v)))
+        timings['iface_outer_inv_ms'] = {str(v): t for v, t in t_oi.items()}
+        _lib.check(engine.L.slab_engine_set_option(engine.h, key, picks['iface_outer_inv']), 'slab_engine_set_option')
     if engine.geom.Npan > 1 and engine.precision == 'mixed':
         key, cands = TUNABLES['iface_lookahead']
         t_if = {}
@@ -127,6 +160,15 @@ def tune(engine, coeffs, bnd, reps=2, use_cache=True, path=None):
         picks['iface_lookahead'] = min(cands, key=lambda v: (t_if[v], cands.index(v)))
         timings['interface_ms'] = {str(v): t for v, t in t_if.items()}
         _lib.check(engine.L.slab_engine_set_option(engine.h, key, picks['iface_lookahead']), 'slab_engine_set_option')
+    if engine.precision != 'fp64':
+        key, cands = TUNABLES['tree_tc']
+        t_tc = {}
+        for v in cands:
+            _lib.check(engine.L.slab_engine_set_option(engine.h, key, v), 'slab_engine_set_option')
+            t_tc[v] = _time_tree_and_solve(engine, coeffs, bnd, reps, tol)
+        picks['tree_tc'] = min(cands, key=lambda v: (t_tc[v], cands.index(v)))
+        timings['tree_plus_solve_ms'] = {str(v): t for v, t in t_tc.items()}
+        _lib.check(engine.L.slab_engine_set_option(engine.h, key, picks['tree_tc']), 'slab_engine_set_option')
     engine.factor(**coeffs)
     key, cands = TUNABLES['iface_solve']
     if engine.geom.Npan > 1:

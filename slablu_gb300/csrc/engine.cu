@@ -34,6 +34,7 @@
 
 #include "leaf.cuh"
 #include "ozaki.cuh"
+#include "tcgemm.cuh"
 
 namespace slab {
 
@@ -314,6 +315,7 @@ struct EngineBase {
   virtual int coeff_grad(int nrhs, const double* ufaces, const double* uleaf, const double* lam_leaf, double* g11,
                          double* g22, double* g1, double* g2, double* g0) = 0;
   virtual size_t factor_bytes() const = 0;
+  virtual size_t solve_bytes() const = 0;
   virtual double timing(int i) const = 0;
   virtual int set_option(int key, int value) = 0;
   virtual int get_option(int key) const = 0;
@@ -337,6 +339,7 @@ struct EngineImpl : EngineBase {
   bool use_graphs = true;
   bool use_cluster_solve = true;
   int leaf_ctas = 0;  // resident leaves per SM in the leaf kernel (0: as many as fit)
+  bool leaf_split_asm = false;  // leaf operators assembled by a kernel of their own (no c12)
   DevBuf D, Dsq, Nx, NxcT, NxxT, interp, jxr, leafglob, dirmask;
   DevBuf coef[6];  // c11, c22, c1, c2, c, c12
   bool has[6] = {false, false, false, false, false, false};
@@ -360,12 +363,22 @@ struct EngineImpl : EngineBase {
   int nI = 0, nbI = 0;
   DevBuf ifLU, ifPiv, ifPerm, ifX, ifSub, ifSup, ifInfo, ifGlob, ifLinv, ifUinv, ifWork;
   DevBuf emuWork, emuErr, emuLinv;  // tensor-core FP64 products of the interface (mixed precision)
+  // inverses of the 256-row diagonal blocks of each interface LU, so that the
+  // Schur right-hand sides X_j = S_j^{-1} sup_j are all tensor-core products
+  DevBuf ifLoInv, ifUoInv, emuY, emuT;
+  bool use_outer_inv = false;
+  int nOB = 0;
   // Solve-phase copies of the interface factors in the leaf/tree type T (mixed
   // precision: FP32 copies of the FP64 factors; every correction is applied
   // through FP32 leaf and tree factors anyway, and the residual stays FP64).
   DevBuf sLU, sLinv, sUinv, sX, sSub;
   static constexpr bool kSplitSolve = !std::is_same<T, TI>::value;
   bool use_emu = false;
+  // FP32 merge tree on the tensor cores: the Schur update F_parent -= col W by
+  // gemm_tf32s (W = M^{-1} R stays a pivoted triangular solve)
+  bool use_tc_tree = false;
+  static constexpr int kTcMinE = 32;  // merges with fewer eliminated unknowns stay on the CUDA cores
+  DevBuf tcWork, tcErr;
   static constexpr int kInvBs = 64;  // diagonal-block size of the interface triangular inverses
   int nInvBlk = 0;
   // solve buffers
@@ -373,6 +386,7 @@ struct EngineImpl : EngineBase {
   DevBuf wc, flux, gvec, uvec, Ybuf, Zbuf, ifF, ifZ, ux_d, uc_d, rc_d, rx_d, rcT, acc;
   DevBuf gi_d, gf_d;  // adjoint right-hand side (interior leaf-major, faces)
   size_t factor_bytes_ = 0;
+  size_t solve_bytes_ = 0;
   bool factored = false;
   // phase timing (CUDA events on the engine stream), milliseconds
   cudaEvent_t ev[8] = {};
@@ -481,9 +495,44 @@ struct EngineImpl : EngineBase {
       use_cluster_solve = cl;
       return SLAB_OK;
     }
+    if (key == SLAB_OPT_IFACE_OUTER_INV) {
+      if (value != 0 && value != 1) return set_error(SLAB_ERR_ARG, "iface_outer_inv %d not 0 or 1", value);
+      if ((value == 1) != use_outer_inv && gfac[2]) {
+        cudaGraphExecDestroy(gfac[2]);
+        gfac[2] = nullptr;
+      }
+      use_outer_inv = value == 1;
+      return SLAB_OK;
+    }
+    if (key == SLAB_OPT_LEAF_ASSEMBLY) {
+      if (value != 0 && value != 1) return set_error(SLAB_ERR_ARG, "leaf_assembly %d not 0 or 1", value);
+      if ((value == 1) != leaf_split_asm && gfac[0]) {
+        cudaGraphExecDestroy(gfac[0]);
+        gfac[0] = nullptr;
+      }
+      leaf_split_asm = value == 1;
+      return SLAB_OK;
+    }
+    if (key == SLAB_OPT_TREE_TC) {
+      if (value != 0 && value != 1) return set_error(SLAB_ERR_ARG, "tree_tc %d not 0 or 1", value);
+      if (value == 1 && !std::is_same<T, float>::value)
+        return set_error(SLAB_ERR_ARG, "tree_tc: tensor-core merges need FP32 tree factors");
+      if ((value == 1) != use_tc_tree) {
+        if (value == 1) SLAB_TRY(alloc_tc_tree());
+        if (gfac[1]) {
+          cudaGraphExecDestroy(gfac[1]);
+          gfac[1] = nullptr;
+        }
+      }
+      use_tc_tree = value == 1;
+      return SLAB_OK;
+    }
     return set_error(SLAB_ERR_ARG, "unknown option %d", key);
   }
   int get_option(int key) const override {
+    if (key == SLAB_OPT_TREE_TC) return use_tc_tree ? 1 : 0;
+    if (key == SLAB_OPT_LEAF_ASSEMBLY) return leaf_split_asm ? 1 : 0;
+    if (key == SLAB_OPT_IFACE_OUTER_INV) return use_outer_inv ? 1 : 0;
     if (key == SLAB_OPT_LEAF_CTAS) return leaf_ctas;
     if (key == SLAB_OPT_IFACE_SOLVE) return use_cluster_solve ? 0 : 1;
     if (key == SLAB_OPT_IFACE_LOOKAHEAD) return use_lookahead ? 1 : 0;
@@ -500,10 +549,19 @@ struct EngineImpl : EngineBase {
     use_cluster_solve = !(nc && nc[0] == '1');
     const char* lc = getenv("SLAB_LEAF_CTAS");
     if (lc) leaf_ctas = atoi(lc);
+    const char* la = getenv("SLAB_LEAF_ASSEMBLY");  // 1: assembly by a kernel of its own
+    if (la) leaf_split_asm = la[0] == '1';
+    const char* oi = getenv("SLAB_IFACE_OUTER_INV");  // 1: inverted 256-row blocks, tensor-core products
+    if (oi) use_outer_inv = oi[0] == '1';
     // FP64 interface products on the tensor cores in the mixed mode (FP32 leaves and
     // tree, FP64 interface); SLAB_NATIVE_FP64=1 keeps them on the FP64 cores
     const char* nf = getenv("SLAB_NATIVE_FP64");
     use_emu = std::is_same<T, float>::value && std::is_same<TI, double>::value && !(nf && nf[0] == '1');
+    // 1: the FP32 merge tree's Schur updates on the tensor cores.  Off by default:
+    // at N = 4.4M it shortens the tree by 3 ms but its looser FP32 accumulation
+    // costs one more refinement application (6 ms); the autotuner decides.
+    const char* tt = getenv("SLAB_TREE_TC");
+    use_tc_tree = std::is_same<T, float>::value && tt && tt[0] == '1';
     ntot = (long long)q * ((long long)n0 * (2 * n1 + 1) + n1);
     nleaf = (long long)n0 * n1;
   }
@@ -780,20 +838,35 @@ struct EngineImpl : EngineBase {
         SLAB_TRY(emuWork.alloc(dgemm_emu_work_bytes(nI, nI, nI)));
         SLAB_TRY(emuErr.alloc(sizeof(int)));
         SLAB_TRY(emuLinv.alloc((size_t)kEmuOuter * 64 * sizeof(double)));
+        nOB = ceil_div(nI, kEmuOuter);
+        if (nbI > 1) {
+          SLAB_TRY(ifLoInv.alloc((size_t)(nbI - 1) * nOB * kEmuOuter * kEmuOuter * sizeof(double)));
+          SLAB_TRY(ifUoInv.alloc((size_t)(nbI - 1) * nOB * kEmuOuter * kEmuOuter * sizeof(double)));
+          SLAB_TRY(emuY.alloc((size_t)kEmuOuter * nI * sizeof(double)));
+          SLAB_TRY(emuT.alloc(outer_tri_tmp_elems(nI) * sizeof(double)));
+        }
         SLAB_TRY(laPerm.alloc((size_t)(1 + 2 * kRowpermMax) * sizeof(int)));
         SLAB_CUDA_TRY(cudaMemsetAsync(emuErr.p, 0, sizeof(int), s));
       }
     }
+    if (use_tc_tree) SLAB_TRY(alloc_tc_tree());
     SLAB_TRY(acc.alloc(4 * sizeof(double)));
     for (auto& e : ev) SLAB_CUDA_TRY(cudaEventCreate(&e));
     SLAB_CUDA_TRY(cudaStreamSynchronize(s));
     factor_bytes_ = G.bytes + piv.bytes + leafperm.bytes + nodepool.bytes + fpool.bytes + pivpool.bytes +
                     permpool.bytes + ifLU.bytes + ifPiv.bytes + ifPerm.bytes + ifSub.bytes + ifSup.bytes + ifX.bytes +
                     ifLinv.bytes + ifUinv.bytes + sLU.bytes + sX.bytes + sSub.bytes + sLinv.bytes + sUinv.bytes;
+    // factors one solve application streams: the leaf LU and S, the merge factors
+    // ([M | W] and col), the interface factors it applies (LU, X, sub; the FP32
+    // copies in the mixed mode) and the pivot vectors
+    solve_bytes_ = G.bytes + leafperm.bytes + fpool.bytes + pivpool.bytes +
+                   (kSplitSolve ? sLU.bytes + sX.bytes + sSub.bytes : ifLU.bytes + ifX.bytes + ifSub.bytes) +
+                   ifPerm.bytes;
     return SLAB_OK;
   }
 
   size_t factor_bytes() const override { return factor_bytes_; }
+  size_t solve_bytes() const override { return solve_bytes_; }
 
   int factor(const LeafCoeffs& co_in) override {
     SLAB_TRY(enter());
@@ -848,6 +921,7 @@ struct EngineImpl : EngineBase {
     a.G = G.as<T>(); a.strideG = leaf_stride; a.piv = piv.as<int>();
     a.dtn = nodepool.as<T>(); a.info = leafinfo.as<int>();
     a.decouple = 1; a.n0 = n0; a.n1 = n1; a.leaf_begin = 0;
+    a.preassembled = (!mixed && leaf_split_asm) ? 1 : 0;
     if (mixed) {
       a.nxa = ncolG;
       a.interp = interpT.as<T>();
@@ -857,9 +931,25 @@ struct EngineImpl : EngineBase {
     return build_perm_batched(s, piv.as<int>(), n, n, (int)nleaf, leafperm.as<int>(), n);
   }
 
+  // Work of the tensor-core merges: the operand slices of the largest Schur
+  // product of any batch.
+  int alloc_tc_tree() {
+    size_t wb = 256;
+    for (auto& bp : batches) {
+      const Batch& b = *bp;
+      if (b.nE < kTcMinE || b.nO <= 0) continue;
+      wb = std::max(wb, gemm_tf32s_work_bytes(b.nO, b.nO, b.nE, b.count));
+    }
+    SLAB_TRY(tcWork.ensure(wb));
+    SLAB_TRY(tcErr.ensure(sizeof(int)));
+    SLAB_CUDA_TRY(cudaMemsetAsync(tcErr.p, 0, sizeof(int), s));
+    return SLAB_OK;
+  }
+
   int factor_tree() {
     // merge tree, level by level
     int info_ofs = 0;
+    if (use_tc_tree) SLAB_CUDA_TRY(cudaMemsetAsync(tcErr.p, 0, sizeof(int), s));
     for (auto& bp : batches) {
       Batch& b = *bp;
       MergeGatherArgs g{b.nA, b.nB, b.nE, b.nO, b.count, b.eA.as<int>(), b.eB.as<int>(), b.oChild.as<int>(),
@@ -876,16 +966,30 @@ struct EngineImpl : EngineBase {
       SLAB_TRY(getrf_batched<T>(s, b.nE, b.nE, Maug, nullptr, strideM, b.nE, pv, nullptr, b.nE,
                                 mergeinfo.as<int>() + info_ofs, b.count));
       SLAB_TRY(build_perm_batched(s, pv, b.nE, b.nE, b.count, permpool.as<int>() + b.offPiv0, b.nE));
-      SLAB_TRY(getrs_batched<T>(s, b.nE, b.nO, Maug, nullptr, strideM, b.nE, pv, nullptr, b.nE,
-                                Maug + (long long)b.nE * b.nE, nullptr, strideM, b.nE, b.count));
-      SLAB_TRY(gemm<T>(s, b.nO, b.nO, b.nE, T(-1), fpool.as<T>() + b.offC0, nullptr, (long long)b.nO * b.nE, b.nO,
-                       Maug + (long long)b.nE * b.nE, nullptr, strideM, b.nE, T(1), nodepool.as<T>() + b.offP0,
-                       nullptr, (long long)b.nO * b.nO, b.nO, b.count));
+      T* R = Maug + (long long)b.nE * b.nE;
+      SLAB_TRY(getrs_batched<T>(s, b.nE, b.nO, Maug, nullptr, strideM, b.nE, pv, nullptr, b.nE, R, nullptr, strideM,
+                                b.nE, b.count));
+      bool done = false;
+      if constexpr (std::is_same<T, float>::value) {
+        if (use_tc_tree && b.nE >= kTcMinE && b.nO > 0) {
+          // F_parent -= col W on the tensor cores (TF32-split products, FP32 error bound)
+          SLAB_TRY(gemm_tf32s(s, b.nO, b.nO, b.nE, -1.f, fpool.as<T>() + b.offC0, b.nO, (long long)b.nO * b.nE, R,
+                              b.nE, strideM, 1.f, nodepool.as<T>() + b.offP0, b.nO, (long long)b.nO * b.nO, b.count,
+                              tcWork.p, tcWork.bytes, tcErr.as<int>()));
+          done = true;
+        }
+      }
+      if (!done)
+        SLAB_TRY(gemm<T>(s, b.nO, b.nO, b.nE, T(-1), fpool.as<T>() + b.offC0, nullptr, (long long)b.nO * b.nE, b.nO,
+                         R, nullptr, strideM, b.nE, T(1), nodepool.as<T>() + b.offP0, nullptr,
+                         (long long)b.nO * b.nO, b.nO, b.count));
       info_ofs += b.count;
     }
     return SLAB_OK;
   }
 
+  double* loinv(int j) { return ifLoInv.as<double>() + (size_t)j * nOB * kEmuOuter * kEmuOuter; }
+  double* uoinv(int j) { return ifUoInv.as<double>() + (size_t)j * nOB * kEmuOuter * kEmuOuter; }
   TI* linv(int j) { return ifLinv.as<TI>() + (size_t)j * nInvBlk * kInvBs * kInvBs; }
   TI* uinv(int j) { return ifUinv.as<TI>() + (size_t)j * nInvBlk * kInvBs * kInvBs; }
   // solve-phase views (type T)
@@ -933,8 +1037,12 @@ struct EngineImpl : EngineBase {
     if constexpr (std::is_same<TI, double>::value) {
       if (use_emu) {
         EmuWork w{emuWork.p, emuWork.bytes, emuErr.as<int>()};
-        SLAB_TRY(bigtrs_inv_emu(s, LUp, nI, nI, pp, linv(j - 1), uinv(j - 1), kInvBs, ifSup.as<TI>() + blk * (j - 1),
-                                nI, Xprev, nI, nI, w));
+        if (use_outer_inv)
+          SLAB_TRY(bigtrs_outer_emu(s, LUp, nI, nI, pp, loinv(j - 1), uoinv(j - 1), ifSup.as<TI>() + blk * (j - 1), nI,
+                                    Xprev, nI, nI, emuY.as<double>(), w));
+        else
+          SLAB_TRY(bigtrs_inv_emu(s, LUp, nI, nI, pp, linv(j - 1), uinv(j - 1), kInvBs, ifSup.as<TI>() + blk * (j - 1),
+                                  nI, Xprev, nI, nI, w));
         return dgemm_emu(s, nI, nI, nI, -1.0, ifSub.as<TI>() + blk * j, nI, Xprev, nI, 1.0, Sj, nI, w.buf, w.bytes,
                          w.err);
       }
@@ -970,6 +1078,10 @@ struct EngineImpl : EngineBase {
           SLAB_TRY(biglu<TI>(s, Sj, nI, nI, ifPiv.as<int>() + (long long)nI * j, ifInfo.as<int>(), ifWork.as<TI>()));
         SLAB_TRY(build_perm(s, ifPiv.as<int>() + (long long)nI * j, nI, ifPerm.as<int>() + (long long)nI * j));
         SLAB_TRY(tri_inv_blocks<TI>(s, Sj, nI, nI, kInvBs, linv(j), uinv(j)));
+        if constexpr (std::is_same<TI, double>::value) {
+          if (use_emu && use_outer_inv && j + 1 < nbI)
+            SLAB_TRY(outer_tri_inverses(s, Sj, nI, nI, linv(j), uinv(j), loinv(j), uoinv(j), emuT.as<double>()));
+        }
       }
       SLAB_TRY(split_solve_copies());
     }
@@ -1000,6 +1112,8 @@ struct EngineImpl : EngineBase {
     int iinfo = 0, eerr = 0;
     if (nbI > 0) SLAB_CUDA_TRY(cudaMemcpyAsync(&iinfo, ifInfo.p, sizeof(int), cudaMemcpyDeviceToHost, s));
     if (nbI > 0 && use_emu) SLAB_CUDA_TRY(cudaMemcpyAsync(&eerr, emuErr.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    int terr = 0;
+    if (use_tc_tree) SLAB_CUDA_TRY(cudaMemcpyAsync(&terr, tcErr.p, sizeof(int), cudaMemcpyDeviceToHost, s));
     SLAB_CUDA_TRY(cudaStreamSynchronize(s));
     tms[0] = elapsed(0, 1);
     tms[1] = elapsed(1, 2);
@@ -1020,6 +1134,7 @@ struct EngineImpl : EngineBase {
       return iinfo;
     }
     if (eerr != 0) return set_error(SLAB_ERR_CUDA, "interface: tensor-core pipeline wait expired (code %d)", eerr);
+    if (terr != 0) return set_error(SLAB_ERR_CUDA, "merge tree: tensor-core pipeline wait expired (code %d)", terr);
     return SLAB_OK;
   }
 
@@ -1642,6 +1757,7 @@ extern "C" int slab_engine_get_option(const slab_engine* e, int key) {
 extern "C" long long slab_engine_nfaces(const slab_engine* e) { return e ? e->impl->ntot : -1; }
 extern "C" long long slab_engine_nleaves(const slab_engine* e) { return e ? e->impl->nleaf : -1; }
 extern "C" size_t slab_engine_factor_bytes(const slab_engine* e) { return e ? e->impl->factor_bytes() : 0; }
+extern "C" size_t slab_engine_solve_bytes(const slab_engine* e) { return e ? e->impl->solve_bytes() : 0; }
 
 extern "C" int slab_engine_factor(slab_engine* e, const double* c11, const double* c22, const double* c1,
                                   const double* c2, const double* c) {

@@ -17,6 +17,12 @@ static int leaf_factor_launch(cudaStream_t s, const LeafFactorArgs<T>& a, int nl
 template <typename T>
 int leaf_factor(cudaStream_t s, const LeafFactorArgs<T>& a, int nleaf, int ctas_per_sm) {
   if (nleaf <= 0) return SLAB_OK;
+  if (a.preassembled && a.nxa == 0) {
+    const size_t bytes = 7 * (size_t)a.p * a.p * sizeof(double) + 2 * (size_t)a.n;
+    SLAB_TRY(ensure_smem(leaf_assemble_kernel<T>, bytes, "leaf_assemble"));
+    leaf_assemble_kernel<T><<<nleaf, kNT, bytes, s>>>(a);
+    SLAB_CHECK_LAUNCH();
+  }
   if (a.nx > 2 * kCT || a.nxa > 2 * kCT) return set_error(SLAB_ERR_ARG, "leaf_factor: p = %d too large", a.p);
   if (a.nxa > 0) {  // mixed derivative: Jxreorder columns and the interpolation stage
     if (!a.co.c12 || !a.interp || !a.jxr)
@@ -501,6 +507,7 @@ int leaf_dtn_impl(int nleaf, int p, const LeafCoeffs& co, const double* D, const
   a.co = co; a.D = D; a.Dsq = Dsq; a.Nxc = Nxc; a.Nxx = Nxx;
   a.G = G; a.strideG = (long long)n * (n + nxa); a.piv = piv; a.dtn = dtn; a.info = info;
   a.decouple = 0;
+  a.preassembled = 0;
   if (mixed) {
     T* interpT = static_cast<T*>(take((size_t)nxa * nx * sizeof(T)));
     to_type_kernel<T><<<ceil_div(nxa * nx, 256), 256, 0, s>>>(interp, interpT, nxa * nx);

@@ -51,6 +51,9 @@ struct LeafFactorArgs {
   int nxa;
   const T* interp;
   const int* jxr;
+  // [A_cc | A_cx] already written into G by leaf_assemble_kernel (no mixed
+  // derivative): the factor kernel starts at the LU
+  int preassembled = 0;
 };
 
 // Entry (row node k=(i1,i2), column node (j1,j2)) of
@@ -94,6 +97,64 @@ inline size_t leaf_factor_smem_bytes(int p, size_t elem) {
 // kMixed: the operator has a mixed derivative c12 (:59-65): the extra columns
 // are the 4(p-1) nodes Jxreorder (corners included), and after the back
 // substitution X = A_cc^{-1} A_c,Jxreorder is replaced by X Interp_mat.
+// Assembly of [A_cc | A_cx] (no mixed derivative) for every leaf into G, in the
+// layout and term order of leaf_factor_kernel's own assembly: one CTA per leaf
+// with the leaf's coefficients and D, Dsq staged in shared memory, one warp per
+// column.  Separate from the factorization, the FP64 evaluation of the entries
+// runs at full occupancy instead of inside the latency-bound factor kernel.
+template <typename T>
+__global__ void __launch_bounds__(kNT) leaf_assemble_kernel(LeafFactorArgs<T> a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int tid = threadIdx.x, leaf = blockIdx.x;
+  const int p = a.p, q = a.q, n = a.n, nx = a.nx, pp = p * p;
+  double* Dsh = reinterpret_cast<double*>(smem_raw);
+  double* Dsqsh = Dsh + pp;
+  double* csh = Dsqsh + pp;
+  const int lofs = leaf * pp;
+  LeafCoeffs cs{};
+  {
+    const double* src[5] = {a.co.c11, a.co.c22, a.co.c1, a.co.c2, a.co.c};
+    const double** dst[5] = {&cs.c11, &cs.c22, &cs.c1, &cs.c2, &cs.c};
+#pragma unroll
+    for (int f = 0; f < 5; ++f) {
+      if (!src[f]) continue;
+      double* d = csh + f * pp;
+      for (int i = tid; i < pp; i += blockDim.x) d[i] = src[f][lofs + i];
+      *dst[f] = d;
+    }
+  }
+  unsigned char* ri1 = reinterpret_cast<unsigned char*>(csh + 5 * pp);
+  unsigned char* ri2 = ri1 + n;
+  for (int i = tid; i < pp; i += blockDim.x) {
+    Dsh[i] = a.D[i];
+    Dsqsh[i] = a.Dsq[i];
+  }
+  for (int r = tid; r < n; r += blockDim.x) {
+    int i1, i2;
+    interior_node(r, q, i1, i2);
+    ri1[r] = (unsigned char)i1;
+    ri2[r] = (unsigned char)i2;
+  }
+  __syncthreads();
+  T* G = a.G + a.strideG * leaf;
+  const int nc = n + nx;
+  const int lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
+  for (int col = warp; col < nc; col += nwarps) {
+    int j1, j2;
+    if (col < n)
+      interior_node(col, q, j1, j2);
+    else
+      face_node(col - n, p, q, j1, j2);
+    T* gc = G + (size_t)col * n;
+    for (int r = lane; r < n; r += 32) {
+      const int i1 = ri1[r], i2 = ri2[r];
+      T v = T(0);
+      if (i1 == j1 || i2 == j2) v = (T)aloc_entry<false>(cs, 0, p, i1, i2, j1, j2, Dsh, Dsqsh);
+      gc[r] = v;
+    }
+  }
+}
+
 template <typename T, bool kMixed = false>
 __global__ void __launch_bounds__(kNT) leaf_factor_kernel(LeafFactorArgs<T> a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -102,6 +163,10 @@ __global__ void __launch_bounds__(kNT) leaf_factor_kernel(LeafFactorArgs<T> a) {
   const int p = a.p, q = a.q, n = a.n, nx = a.nx;
   T* smem = reinterpret_cast<T*>(smem_raw);
   const int pp = p * p;
+  T* G = a.G + a.strideG * leaf;
+  const int nxa = kMixed ? a.nxa : nx;  // extra columns: face nodes, or Jxreorder with c12
+  const int nc = n + nxa;
+  if (kMixed || !a.preassembled) {
   double* Dsh = reinterpret_cast<double*>(smem_raw);
   double* Dsqsh = Dsh + pp;
   // the leaf's coefficients in shared memory: the assembly reads each of them
@@ -135,9 +200,6 @@ __global__ void __launch_bounds__(kNT) leaf_factor_kernel(LeafFactorArgs<T> a) {
   }
   cp_async_wait_all();
   __syncthreads();
-  T* G = a.G + a.strideG * leaf;
-  const int nxa = kMixed ? a.nxa : nx;  // extra columns: face nodes, or Jxreorder with c12
-  const int nc = n + nxa;
   // one warp per column: without c12, Aloc[Jc, col] is nonzero only on the rows
   // that share the column node's x or y line
   {
@@ -164,6 +226,7 @@ __global__ void __launch_bounds__(kNT) leaf_factor_kernel(LeafFactorArgs<T> a) {
       }
     }
   }
+  }  // assembly
   __syncthreads();
   cta_getrf_aug<T>(G, n, n, nc, a.piv + (size_t)leaf * n, smem, a.info ? a.info + leaf : nullptr);
   for (int c0 = 0; c0 < nxa; c0 += kCT) cta_backsub<T>(G, n, n, n + c0, min(kCT, nxa - c0), smem);

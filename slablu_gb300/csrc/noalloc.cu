@@ -1,9 +1,10 @@
 // Allocation-free variant of the batched leaf DtN entry point.
 //
 // Some callers cannot allocate device memory at the point where they need
-// leaf DtN maps: code that runs while a CUDA stream is being captured into a
-// graph (cudaMalloc is not allowed there), or host applications whose device
-// memory is owned by their own pool and that forbid allocations by libraries.
+// leaf DtN maps: host applications whose device memory is owned by their own
+// pool allocator and that forbid allocations by libraries, or programs that fix
+// their device-memory budget at start-up, where an allocation inside a library
+// call would fail or break that budget.
 // slab_leaf_dtn needs a work area for the leaf LU factors; this variant uses
 // a fixed scratch array compiled into the library instead, so the caller only
 // provides inputs and outputs.
@@ -75,7 +76,10 @@ extern "C" int slab_leaf_dtn_noalloc(int nleaf, int p, const double* c11, const 
   void* scratch = nullptr;
   const int st = slab::scratch_address(&scratch);
   if (st != SLAB_OK) return st;
+  // the c12-free leaf path only: its work size is slab_leaf_dtn_work_bytes (the
+  // mixed-derivative variant needs slab_leaf_dtn_mixed_work_bytes and is not
+  // offered here)
   slab::LeafCoeffs co{c11, c22, c1, c2, c};
-  return slab::leaf_dtn_with_work(nleaf, p, co, D, Dsq, Nx, precision, scratch, SLAB_NOALLOC_SCRATCH_BYTES, dtn,
-                                  nullptr, info, static_cast<cudaStream_t>(stream));
+  return slab::leaf_dtn_with_work(nleaf, p, co, D, Dsq, Nx, precision, scratch, need, dtn, nullptr, info,
+                                  static_cast<cudaStream_t>(stream));
 }

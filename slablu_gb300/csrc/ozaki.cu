@@ -27,6 +27,7 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <climits>
 #include <cstdint>
 #include <mutex>
@@ -494,6 +495,124 @@ int bigtrs_inv_emu(cudaStream_t s, const double* LU, int lda, int n, const int* 
     if (ob0 > 0)
       SLAB_TRY(dgemm_emu(s, ob0, nrhs, obe - ob0, -1.0, LU + (size_t)ob0 * lda, lda, X + ob0, ldx, 1.0, X, ldx, w.buf,
                          w.bytes, w.err));
+  }
+  return SLAB_OK;
+}
+
+namespace {
+// Block (r, c) of size kB of an outer block's inverse, ld kEmuOuter.
+constexpr int kOB = kEmuOuter;
+
+// Copies the 64 x 64 diagonal inverses into their places in the outer blocks
+// (grid: one CTA per 64-row block; blocks past n are left zero).
+__global__ void place_diag_inv_kernel(const double* __restrict__ Inv64, int nblk64, double* __restrict__ Out) {
+  const int k = blockIdx.x;
+  if (k >= nblk64) return;
+  const int ob = k / (kOB / 64), i0 = (k % (kOB / 64)) * 64;
+  double* O = Out + (size_t)ob * kOB * kOB;
+  const double* I = Inv64 + (size_t)k * 64 * 64;
+  for (int idx = threadIdx.x; idx < 64 * 64; idx += blockDim.x) {
+    const int r = idx % 64, c = idx / 64;
+    O[(size_t)(i0 + c) * kOB + i0 + r] = I[idx];
+  }
+}
+}  // namespace
+
+size_t outer_tri_tmp_elems(int n) {
+  const int nob = (n + kOB - 1) / kOB;
+  return (size_t)nob * 128 * 128;
+}
+
+// One doubling step for every outer block, halves [base, base + sa) and
+// [base + sa, base + sa + sc) of each (sa = sc = h for the full blocks).
+// lower: O = -C^{-1} (B A^{-1}) with B = L[below, left]; upper: O = -A^{-1} (B C^{-1})
+// with B = U[above, right].  The full outer blocks go as one batched product,
+// the last (partial) outer block on its own with its true sizes.
+static int doubling_step(cudaStream_t s, const double* LU, int lda, int n, double* Inv, double* tmp, int h, int base,
+                         bool upper) {
+  const int nob = (n + kOB - 1) / kOB;
+  const int nfull = n / kOB;
+  const long long sLU = (long long)kOB * lda + kOB, sInv = (long long)kOB * kOB, sT = 128LL * 128;
+  auto step = [&](int count, int ob0, int sa, int sc) -> int {
+    if (count <= 0 || sa <= 0 || sc <= 0) return SLAB_OK;
+    const long long r0 = (long long)ob0 * kOB + base;
+    double* I0 = Inv + (size_t)ob0 * sInv;
+    const double* Ai = I0 + (size_t)base * kOB + base;              // sa x sa
+    const double* Ci = I0 + (size_t)(base + sa) * kOB + base + sa;   // sc x sc
+    if (!upper) {
+      const double* B = LU + (size_t)r0 * lda + r0 + sa;              // L[r0+sa.., r0..]: sc x sa
+      double* O = I0 + (size_t)base * kOB + base + sa;                // rows base+sa.., cols base..
+      SLAB_TRY(gemm<double>(s, sc, sa, sa, 1.0, B, nullptr, sLU, lda, Ai, nullptr, sInv, kOB, 0.0, tmp, nullptr, sT,
+                            sc, count));
+      SLAB_TRY(gemm<double>(s, sc, sa, sc, -1.0, Ci, nullptr, sInv, kOB, tmp, nullptr, sT, sc, 0.0, O, nullptr, sInv,
+                            kOB, count));
+    } else {
+      const double* B = LU + (size_t)(r0 + sa) * lda + r0;            // U[r0.., r0+sa..]: sa x sc
+      double* O = I0 + (size_t)(base + sa) * kOB + base;              // rows base.., cols base+sa..
+      SLAB_TRY(gemm<double>(s, sa, sc, sc, 1.0, B, nullptr, sLU, lda, Ci, nullptr, sInv, kOB, 0.0, tmp, nullptr, sT,
+                            sa, count));
+      SLAB_TRY(gemm<double>(s, sa, sc, sa, -1.0, Ai, nullptr, sInv, kOB, tmp, nullptr, sT, sa, 0.0, O, nullptr, sInv,
+                            kOB, count));
+    }
+    return SLAB_OK;
+  };
+  SLAB_TRY(step(nfull, 0, h, h));
+  if (nob > nfull) {  // last outer block, rows [nfull*kOB, n)
+    const int nb = n - nfull * kOB;
+    const int sa = std::min(h, nb - base), sc = std::min(h, nb - base - h);
+    SLAB_TRY(step(1, nfull, sa, sc));
+  }
+  return SLAB_OK;
+}
+
+int outer_tri_inverses(cudaStream_t s, const double* LU, int lda, int n, const double* Linv64, const double* Uinv64,
+                       double* LoInv, double* UoInv, double* tmp) {
+  static_assert(kEmuOuter == 256, "two doubling steps from 64-row blocks");
+  if (n <= 0) return SLAB_OK;
+  const int nob = (n + kOB - 1) / kOB, nblk64 = (n + 63) / 64;
+  for (double* Inv : {LoInv, UoInv}) SLAB_CUDA_TRY(cudaMemsetAsync(Inv, 0, (size_t)nob * kOB * kOB * 8, s));
+  place_diag_inv_kernel<<<nblk64, 256, 0, s>>>(Linv64, nblk64, LoInv);
+  SLAB_CHECK_LAUNCH();
+  place_diag_inv_kernel<<<nblk64, 256, 0, s>>>(Uinv64, nblk64, UoInv);
+  SLAB_CHECK_LAUNCH();
+  for (int up = 0; up < 2; ++up) {
+    double* Inv = up ? UoInv : LoInv;
+    SLAB_TRY(doubling_step(s, LU, lda, n, Inv, tmp, 64, 0, up));
+    SLAB_TRY(doubling_step(s, LU, lda, n, Inv, tmp, 64, 128, up));
+    SLAB_TRY(doubling_step(s, LU, lda, n, Inv, tmp, 128, 0, up));
+  }
+  return SLAB_OK;
+}
+
+int bigtrs_outer_emu(cudaStream_t s, const double* LU, int lda, int n, const int* perm, const double* LoInv,
+                     const double* UoInv, const double* B, int ldb, double* X, int ldx, int nrhs, double* Y,
+                     const EmuWork& w) {
+  if (n <= 0 || nrhs <= 0) return SLAB_OK;
+  const long long tot = (long long)n * nrhs;
+  permute_rows_kernel<double><<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(B, ldb, X, ldx, n, nrhs, perm);
+  SLAB_CHECK_LAUNCH();
+  const int nob = (n + kOB - 1) / kOB;
+  auto diag = [&](const double* Inv, int ob) -> int {
+    const int ob0 = ob * kOB, nb = std::min(kOB, n - ob0);
+    SLAB_TRY(dgemm_emu(s, nb, nrhs, nb, 1.0, Inv + (size_t)ob * kOB * kOB, kOB, X + ob0, ldx, 0.0, Y, kOB, w.buf,
+                       w.bytes, w.err));
+    SLAB_CUDA_TRY(cudaMemcpy2DAsync(X + ob0, (size_t)ldx * 8, Y, (size_t)kOB * 8, (size_t)nb * 8, nrhs,
+                                    cudaMemcpyDeviceToDevice, s));
+    return SLAB_OK;
+  };
+  for (int ob = 0; ob < nob; ++ob) {
+    const int ob0 = ob * kOB, obe = std::min(n, ob0 + kOB);
+    SLAB_TRY(diag(LoInv, ob));
+    if (obe < n)
+      SLAB_TRY(dgemm_emu(s, n - obe, nrhs, obe - ob0, -1.0, LU + (size_t)ob0 * lda + obe, lda, X + ob0, ldx, 1.0,
+                         X + obe, ldx, w.buf, w.bytes, w.err));
+  }
+  for (int ob = nob - 1; ob >= 0; --ob) {
+    const int ob0 = ob * kOB, obe = std::min(n, ob0 + kOB);
+    SLAB_TRY(diag(UoInv, ob));
+    if (ob0 > 0)
+      SLAB_TRY(dgemm_emu(s, ob0, nrhs, obe - ob0, -1.0, LU + (size_t)ob0 * lda, lda, X + ob0, ldx, 1.0, X, ldx,
+                         w.buf, w.bytes, w.err));
   }
   return SLAB_OK;
 }

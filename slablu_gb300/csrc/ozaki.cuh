@@ -34,6 +34,26 @@ int bigtrs_inv_emu(cudaStream_t s, const double* LU, int lda, int n, const int* 
                    const double* Uinv, int bs, const double* B, int ldb, double* X, int ldx, int nrhs,
                    const EmuWork& w);
 
+// Inverses of the kEmuOuter-row diagonal blocks of the unit-lower L and the
+// upper U of an n x n LU (column-major, lda), built from the inverses of their
+// 64-row diagonal blocks (tri_inv_blocks layout: block k at Linv64 + k*64*64,
+// ld 64, zero outside its triangle) by two doubling steps on the FP64 cores:
+//   [[A, 0], [B, C]]^{-1} = [[A^{-1}, 0], [-C^{-1} B A^{-1}, C^{-1}]]
+//   [[A, B], [0, C]]^{-1} = [[A^{-1}, -A^{-1} B C^{-1}], [0, C^{-1}]].
+// LoInv / UoInv: ceil(n / kEmuOuter) blocks of kEmuOuter x kEmuOuter (ld
+// kEmuOuter, zero outside the triangle); tmp: outer_tri_tmp_elems(n) doubles.
+size_t outer_tri_tmp_elems(int n);
+int outer_tri_inverses(cudaStream_t s, const double* LU, int lda, int n, const double* Linv64, const double* Uinv64,
+                       double* LoInv, double* UoInv, double* tmp);
+
+// X = U^{-1} L^{-1} P B with the outer-block inverses of outer_tri_inverses:
+// per outer block one tensor-core product with the inverted diagonal block
+// (through Y, kEmuOuter x nrhs doubles) and one with the off-diagonal rows, all
+// by dgemm_emu (no FP64-core triangular solves).
+int bigtrs_outer_emu(cudaStream_t s, const double* LU, int lda, int n, const int* perm, const double* LoInv,
+                     const double* UoInv, const double* B, int ldb, double* X, int ldx, int nrhs, double* Y,
+                     const EmuWork& w);
+
 // Second stream for the lookahead of biglu_emu.  side == null: serial.
 struct Lookahead {
   cudaStream_t side = nullptr;

@@ -72,6 +72,11 @@ class SlabEngine:
     def factor_bytes(self):
         return int(self.L.slab_engine_factor_bytes(self.h))
 
+    @property
+    def solve_bytes(self):
+        """Bytes of stored factors one solve application reads (slab_engine_solve_bytes)."""
+        return int(self.L.slab_engine_solve_bytes(self.h))
+
     def factor(self, c11=None, c22=None, c1=None, c2=None, c=None, c12=None):
         """Coefficients: device float64 tensors with nleaf*p*p entries (or None);
         c12 (the mixed derivative) only, and always, for an engine made with mixed=True."""

@@ -15,6 +15,15 @@ nwaves = n / ppw (argparse_driver.py:86-90).
   config4  256 right-hand sides on the config3 factors: i.i.d. N(0,1) at the
            Dirichlet nodes, smoothed by a width-8 moving average along the
            boundary ordering.
+  config5  p=16, n=1008 (72 x 72 leaves, N = 1,163,232; n = 1000 would give a
+           prime 71 x 71 leaf grid, which the reference's slab partition turns
+           into one-leaf slabs): c = -kh^2 b, b = 1 + 0.3 g with g a seeded
+           Gaussian random field of correlation length 0.05, kh for 20
+           wavelengths across the domain (kh = (20 + 0.03) 2 pi + 1.8, the
+           driver's formula with nwaves = 20), Dirichlet u = 1; loss
+           ||P u(b) - d||^2 with P the
+           values at 4,096 seeded interior leaf nodes and d = P u(b') for a
+           perturbed field b' = b + 0.05 g'.
 """
 import math
 
@@ -97,3 +106,40 @@ def config4_rhs(nbnd, nrhs=256, seed=0, width=8):
     z = torch.randn(nrhs, 1, nbnd + width - 1, generator=g, dtype=torch.float64)
     k = torch.ones(1, 1, width, dtype=torch.float64) / width
     return torch.nn.functional.conv1d(z, k)[:, 0, :].T.contiguous()
+
+
+def grf(xx, seed=0, ell=0.05, nfeat=1024):
+    """Seeded Gaussian random field of unit variance with the squared-exponential
+    covariance exp(-|x - y|^2 / (2 ell^2)), sampled by random Fourier features
+    (Rahimi and Recht): g(x) = sqrt(2/M) sum_m cos(w_m . x + phi_m) with
+    w_m ~ N(0, I / ell^2) and phi_m ~ U[0, 2 pi).  Defined at any point, so the
+    leaf nodes of any grid see the same field."""
+    g = torch.Generator().manual_seed(seed)
+    w = torch.randn(nfeat, 2, generator=g, dtype=torch.float64) / ell
+    ph = torch.rand(nfeat, generator=g, dtype=torch.float64) * 2 * math.pi
+    xx = torch.as_tensor(xx, dtype=torch.float64)
+    w, ph = w.to(xx.device), ph.to(xx.device)
+    out = torch.zeros(xx.shape[0], dtype=torch.float64, device=xx.device)
+    for i0 in range(0, xx.shape[0], 1 << 18):  # chunks keep the (points x features) product small
+        x = xx[i0:i0 + (1 << 18)]
+        out[i0:i0 + x.shape[0]] = torch.cos(x @ w.T + ph).sum(1)
+    return out * math.sqrt(2.0 / nfeat)
+
+
+def config5(seed=0, n=1008, nwaves=20):
+    p = 16
+    kh = (nwaves + 0.03) * 2 * math.pi + 1.8
+    return dict(p=p, n=n, kh=kh, a=leaf_half_width(n, p), nprobe=4096,
+                b=lambda xx: 1.0 + 0.3 * grf(xx, seed),
+                b_perturbed=lambda xx: 1.0 + 0.3 * grf(xx, seed) + 0.05 * grf(xx, seed + 100),
+                c_of_b=lambda b: -(kh ** 2) * b,
+                uu_dir=lambda xx: torch.ones(xx.shape[0], 1, dtype=torch.float64))
+
+
+def probe_nodes(xx, nprobe=4096, seed=0, margin=1e-12):
+    """Indices of `nprobe` distinct seeded leaf nodes strictly inside the unit square."""
+    xx = np.asarray(xx)
+    inside = np.where((xx[:, 0] > margin) & (xx[:, 0] < 1 - margin) & (xx[:, 1] > margin) &
+                      (xx[:, 1] < 1 - margin))[0]
+    rng = np.random.default_rng(seed)
+    return np.sort(rng.choice(inside, size=nprobe, replace=False))

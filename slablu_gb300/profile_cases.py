@@ -3,12 +3,15 @@
     python -m slablu_gb300.profile_cases factor --n 640 --precision mixed
     python -m slablu_gb300.profile_cases solve  --n 2000 --precision mixed --iters 1
     python -m slablu_gb300.profile_cases dgemm  --n 2000 --reps 2
+    python -m slablu_gb300.profile_cases sgemm  --n 4000 --k 200 --batch 10 --reps 2
 
 `factor` and `solve` use the Gaussian-lattice Helmholtz field of the benchmark
 (p = 22) on an n x n-point grid ((n/20)^2 leaves): one factorization, and for
 `solve` one refined solve with at most --iters steps.  `dgemm` runs --reps
 tensor-core FP64 products C = A B of n x n random matrices (the shape of the
-interface Schur update at n = 2000).
+interface Schur update at n = 2000); `sgemm` runs --reps batched TF32-split FP32
+products C -= A B with A n x k and B k x n (--batch of them: the shape of the
+top merge level's Schur updates at N = 4.4M).
 """
 import argparse
 
@@ -20,12 +23,25 @@ from .engine import SlabEngine
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument('case', choices=['factor', 'solve', 'dgemm'])
+    ap.add_argument('case', choices=['factor', 'solve', 'dgemm', 'sgemm'])
     ap.add_argument('--n', type=int, default=640)
     ap.add_argument('--precision', default='mixed', choices=['fp64', 'mixed', 'fp32'])
     ap.add_argument('--iters', type=int, default=1)
     ap.add_argument('--reps', type=int, default=2)
+    ap.add_argument('--k', type=int, default=200)
+    ap.add_argument('--batch', type=int, default=10)
     a = ap.parse_args(argv)
+    if a.case == 'sgemm':
+        from .dgemm import sgemm_tc
+        gen = torch.Generator(device='cuda').manual_seed(1)
+        A = torch.randn(a.batch, a.n, a.k, dtype=torch.float32, device='cuda', generator=gen)
+        B = torch.randn(a.batch, a.k, a.n, dtype=torch.float32, device='cuda', generator=gen)
+        C = torch.zeros(a.batch, a.n, a.n, dtype=torch.float32, device='cuda')
+        for _ in range(a.reps):
+            C = sgemm_tc(A, B, C, alpha=-1.0, beta=1.0)
+        torch.cuda.synchronize()
+        print('ok sgemm', a.batch, a.n, a.k, float(C.abs().max()))
+        return
     if a.case == 'dgemm':
         from .dgemm import dgemm_emu
         gen = torch.Generator(device='cuda').manual_seed(1)

@@ -1,7 +1,22 @@
 import os
 import sys
 
-import pytest
+# Host-side linear algebra in these tests runs on one thread: on some hosts the
+# multi-threaded BLAS/LAPACK paths (batched LU and solves in NumPy's OpenBLAS and
+# in torch's MKL) stop making progress, and the test matrices are small.  The
+# variables must be set before NumPy and torch load their BLAS.
+for _v in ('OMP_NUM_THREADS', 'OPENBLAS_NUM_THREADS', 'MKL_NUM_THREADS'):
+    os.environ.setdefault(_v, '1')
+
+import pytest  # noqa: E402
+import torch  # noqa: E402
+
+torch.set_num_threads(1)
+try:
+    from threadpoolctl import threadpool_limits
+    threadpool_limits(1)
+except ImportError:
+    pass
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 if ROOT not in sys.path:
@@ -12,20 +27,6 @@ GOLDEN = os.path.join(ROOT, 'tests', 'golden')
 
 def pytest_configure(config):
     config.addinivalue_line('markers', 'gpu: test needs a CUDA GPU (GB300) and the built extension')
-    config.addinivalue_line('markers', 'unverified(order=0): GPU test written after the last GPU run of the code '
-                                       'it covers; runs after all other tests, in increasing order')
-
-
-def _run_order(item):
-    m = item.get_closest_marker('unverified')
-    return (0, 0) if m is None else (1, int(m.kwargs.get('order', 0)))
-
-
-def pytest_collection_modifyitems(config, items):
-    # tests that have not yet run on a GPU go last (stable sort), those exercising
-    # the least new device code first, so that under -x a failure among them
-    # cannot keep the verified tests from running
-    items.sort(key=_run_order)
 
 
 @pytest.fixture(scope='session')

@@ -1,8 +1,8 @@
 """Generate golden vectors by running the reference (annayesy/slabLU) itself.
 
-Run in a container where the reference source is mounted:
+Run in a container where the reference source is mounted, giving its path:
 
-    python tests/golden/make_golden.py [/root/reference]
+    python tests/golden/make_golden.py REFERENCE_DIR [mode]
 
 The reference needs SciPy sparse indexing to accept torch index tensors
 (SciPy >= 1.11 rejects them).  This script installs that conversion as a
@@ -13,11 +13,14 @@ by the CPU tests (the reference source is not needed afterwards).
 import hashlib
 import os
 import sys
+import time
 
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = sys.argv[1] if len(sys.argv) > 1 else '/root/reference'
+if len(sys.argv) < 2:
+    sys.exit('usage: make_golden.py REFERENCE_DIR [mode]')
+REF = sys.argv[1]
 os.environ['CUDA_VISIBLE_DEVICES'] = ''
 
 import torch  # noqa: E402
@@ -397,7 +400,130 @@ def solve_fixtures():
              resloc=rloc)
 
 
+
+def _ref_threads():
+    """Host threads for the reference runs: SLAB_REF_THREADS, default 1.  With more
+    than one thread, batched torch.linalg.lu_factor / solve on the CPU (the torch
+    2.11 + MKL 2024.2 build of this image) stops making progress on some hosts; one
+    thread always completes."""
+    return int(os.environ.get('SLAB_REF_THREADS', '1'))
+
+
+def _product_problems():
+    """The seeded synthetic fields of the benchmark configurations (the product's
+    own generators, so that the fixture and the GPU runs see the same input)."""
+    sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+    from slablu_gb300 import problems
+    return problems
+
+
+def _solve_config(cfg, solver, uu, extra_rhs=(), stride=331):
+    """Reference Domain_Solver on the unit square for a problem dict of
+    slablu_gb300.problems: build, then the driver's two solves (the second is the
+    timed one, argparse_driver.py:169-170, 250-258), then the extra right-hand
+    sides on the same factorization."""
+    p, kh, a = cfg['p'], cfg['kh'], cfg['a']
+    op = ref_pdo.PDO_2d(ref_pdo.ones, ref_pdo.ones, c=lambda xx: cfg['c'](xx).reshape(-1))
+    t0 = time.time()
+    dom = Domain_Solver(torch.tensor([[0, 1.0], [0, 1.0]]), op, kh, a, p=p, buf_constant=1.0)
+    t_disc = time.time() - t0
+    t0 = time.time()
+    info = dom.build('reduced_cpu', solver, verbose=False)
+    t_build = time.time() - t0
+    dom.solve(uu, None, known_sol=False)
+    t0 = time.time()
+    sol, res, _, rloc, toc_solve = dom.solve(uu, None, known_sol=False)
+    t_solve = time.time() - t0
+    sol = sol.numpy()[:, 0]
+    out = dict(stride=stride, sol_sub=sol[::stride], sol_norm=np.linalg.norm(sol), sol_len=sol.size,
+               res=float(res), resloc=float(rloc), t_disc=t_disc, t_build=t_build, t_solve=t_solve,
+               toc_build=float(info.get('toc_build', info.get('toc_build_blackbox', np.nan))),
+               toc_assembly=float(info['toc_assembly']), toc_solve=float(toc_solve),
+               threads=torch.get_num_threads())
+    for k, col in enumerate(extra_rhs):
+        f = lambda xx, col=col: torch.as_tensor(col).reshape(-1, 1) if xx.shape[0] == col.shape[0] else uu(xx)
+        s2, r2, _, _, _ = dom.solve(f, None, known_sol=False)
+        s2 = s2.numpy()[:, 0]
+        out.update({f'rhs{k}_sol_sub': s2[::stride], f'rhs{k}_sol_norm': np.linalg.norm(s2), f'rhs{k}_res': float(r2)})
+    return dom, out
+
+
+def config3_fixture(solver='slabLU'):
+    """Config 3 (p = 22, n = 2000, N = 4,404,000): the Gaussian-lattice Helmholtz
+    field with Dirichlet data u = 1, solved by the reference itself (its slabLU,
+    or its superLU black-box path); with slabLU also two of config 4's smoothed
+    random boundary-data columns (0 and 255) on the same factorization."""
+    problems = _product_problems()
+    cfg = problems.config3()
+    torch.set_num_threads(_ref_threads())
+    uu = lambda xx: torch.ones(xx.shape[0], 1)
+    # config 4's boundary data is defined on the Dirichlet nodes I_Xtot, in their order
+    cfg_dom = Domain_Solver(torch.tensor([[0, 1.0], [0, 1.0]]), ref_pdo.PDO_2d(ref_pdo.ones, ref_pdo.ones), 0.0,
+                            cfg['a'], p=cfg['p'], buf_constant=1.0)
+    nbnd = len(cfg_dom.I_Xtot)
+    del cfg_dom
+    B = problems.config4_rhs(nbnd, 256).numpy()
+    extra = (B[:, 0].copy(), B[:, 255].copy()) if solver == 'slabLU' else ()
+    dom, out = _solve_config(cfg, solver, uu, extra)
+    out.update(p=cfg['p'], n=cfg['n'], kh=cfg['kh'], nbnd=nbnd, rhs_cols=np.array([0, 255]), solver=solver,
+               N=int((cfg['p'] - 2) * (cfg['p'] * dom.hps.n[0] * dom.hps.n[1] + dom.hps.n[0] + dom.hps.n[1])))
+    print({k: v for k, v in out.items() if np.ndim(v) == 0})
+    save(f'config3_{solver}_p22_n2000.npz', **out)
+
+
+def config1_fixture():
+    """Config 1 (p = 12, n = 400): constant-coefficient Helmholtz at 10 points per
+    wavelength with Dirichlet data a sum of 8 seeded plane waves, solved by the
+    reference's slabLU."""
+    problems = _product_problems()
+    cfg = problems.config1()
+    torch.set_num_threads(_ref_threads())
+    dom, out = _solve_config(cfg, 'slabLU', cfg['uu_dir'], stride=7)
+    out.update(p=cfg['p'], n=cfg['n'], kh=cfg['kh'])
+    print({k: v for k, v in out.items() if np.ndim(v) == 0})
+    save('config1_slabLU_p12_n400.npz', **out)
+
+
+def config2_fixture(picks=(0, 1, 127, 128, 5000, 8191, 8256, 12345, 16256, 16383)):
+    """Config 2 (16,384 leaves of a 128 x 128 tiling, p = 22): the reference's
+    form_DtNs in FP64 (hps_parallel_leaf_ops.py:40-72) on a sample of the leaves
+    of the 32-bump field, c = -kh^2 b.  The leaf points follow the reference's
+    get_grid (hps_multidomain_disc.py:111-124: leaf i*n1 + j is centred at
+    (a + 2a i, a + 2a j)); the whole multidomain object is not built, its index
+    bookkeeping for 16,384 leaves takes very long."""
+    problems = _product_problems()
+    cfg = problems.config2()
+    p, a, kh, ns = cfg['p'], cfg['a'], cfg['kh'], cfg['nside']
+    H = HPS_Disc(a, p, 2)
+    Ds = torch.stack((torch.tensor(H.Ds.D11), torch.tensor(H.Ds.D22), torch.tensor(H.Ds.D12),
+                      torch.tensor(H.Ds.D1), torch.tensor(H.Ds.D2)))
+    zz = torch.tensor(H.zz.T)
+    picks = list(picks)
+    xx = torch.zeros(len(picks), p * p, 2)
+    for t, box in enumerate(picks):
+        i, j = divmod(box, ns)
+        xx[t, :, 0] = zz[:, 0] + a + 2 * a * i
+        xx[t, :, 1] = zz[:, 1] + a + 2 * a * j
+    cvals = cfg['c'](xx.reshape(-1, 2)).reshape(-1)
+    op = ref_pdo.PDO_2d(ref_pdo.ones, ref_pdo.ones, c=lambda x: cvals if x.shape[0] == cvals.shape[0] else None)
+    DtN = leaf_ops.form_DtNs(p, 2, xx, torch.tensor(H.Nx), torch.tensor(H.JJ.Jx), torch.tensor(H.JJ.Jc),
+                             torch.tensor(H.JJ.Jxreorder), Ds, torch.tensor(H.Interp_mat), op, 0, len(picks),
+                             torch.device('cpu'), 'build', torch.zeros(len(picks), 4 * (p - 2), 1), None)
+    save('config2_dtn_p22.npz', p=p, a=a, kh=kh, nside=ns, picks=np.asarray(picks), xx=xx.numpy(),
+         c=cvals.reshape(len(picks), -1).numpy(), dtn=DtN.numpy())
+
+
 if __name__ == '__main__':
+    if len(sys.argv) > 2 and sys.argv[2] == 'config3':  # config 3 by the reference's slabLU (minutes)
+        config3_fixture('slabLU')
+        sys.exit(0)
+    if len(sys.argv) > 2 and sys.argv[2] == 'config3_superlu':  # config 3 by its superLU (~11 min, 22 GB)
+        config3_fixture('superLU')
+        sys.exit(0)
+    if len(sys.argv) > 2 and sys.argv[2] == 'configs':  # configs 1 and 2
+        config1_fixture()
+        config2_fixture()
+        sys.exit(0)
     if len(sys.argv) > 2 and sys.argv[2] == 'maps':  # only the parameter-map fixture
         param_map_fixture()
         sys.exit(0)

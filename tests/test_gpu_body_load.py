@@ -16,7 +16,7 @@ from oracle import adjoint as oadjoint
 from oracle import domain as odomain
 from oracle import funcs as ofuncs
 
-pytestmark = [pytest.mark.gpu, pytest.mark.unverified(order=1)]
+pytestmark = pytest.mark.gpu
 
 
 @pytest.fixture(scope='module', autouse=True)

@@ -24,7 +24,7 @@ import torch
 from oracle import domain as odomain
 from oracle import funcs as ofuncs
 
-pytestmark = [pytest.mark.gpu, pytest.mark.unverified(order=2)]
+pytestmark = pytest.mark.gpu
 
 
 @pytest.fixture(scope='module', autouse=True)

@@ -55,3 +55,39 @@ def test_lookahead_matches_serial_order_and_oracle():
     assert diff < 1e-11, diff
     rel = np.linalg.norm(sols[1] - ref) / np.linalg.norm(ref)
     assert rel < 1e-9, rel
+
+
+@pytest.mark.parametrize('nblocks', [3, 4])
+def test_outer_inverse_schur_solves_match_fp64_core_solves_and_oracle(nblocks):
+    """The Schur right-hand sides X_j = S_j^{-1} sup_j through inverted 256-row
+    diagonal blocks of L and U (every product on the tensor cores,
+    SLAB_OPT_IFACE_OUTER_INV = 1) against the FP64-core triangular solves of 64-row
+    blocks (0): same solution after refinement, and the oracle's.  Interface blocks
+    of 520 unknowns: two full 256-row outer blocks and a partial one of 8 rows."""
+    from slablu_gb300 import _lib, hps
+    from slablu_gb300.engine import SlabEngine
+    p, kh, n1 = 6, 20.0, 130
+    a = 1 / (2 * n1)
+    geom = [[0, 2 * nblocks * 2 * a], [0, 1]]  # 2 leaf columns per slab
+    md = odomain.Multidomain(geom, a, p)
+    part = odomain.SlabPartition(md, 0.05)
+    co = md.coeffs(ofuncs.helmholtz_pdo(lambda x: ofuncs.bfield_gaussian_bumps(x, kh)))
+    ud = lambda x: ofuncs.uu_dir_greens(x, kh)
+    ref = odomain.solve_full(md, part, co, ud)['sol_tot'][:, 0]
+    g = hps.Geometry(geom, a, p, 0.05)
+    assert g.Npan >= 3 and g.n1 * g.q > 2 * 256
+    coeffs = {k: torch.as_tensor(v.ravel(), device='cuda') for k, v in co.items() if v is not None}
+    bnd = torch.as_tensor(ud(md.xx_active), device='cuda')
+    sols = {}
+    for oi in (0, 1):
+        eng = SlabEngine(g, 'mixed')
+        assert eng.L.slab_engine_set_option(eng.h, _lib.SLAB_OPT_IFACE_OUTER_INV, oi) == 0
+        assert eng.L.slab_engine_get_option(eng.h, _lib.SLAB_OPT_IFACE_OUTER_INV) == oi
+        eng.factor(**coeffs)
+        u, _, iters, st = eng.solve(bnd, tol=1e-12, max_iter=40)
+        assert st['converged'], (oi, iters, st)
+        sols[oi] = u[:, 0].cpu().numpy()
+    diff = np.linalg.norm(sols[1] - sols[0]) / np.linalg.norm(sols[0])
+    assert diff < 1e-11, diff
+    rel = np.linalg.norm(sols[1] - ref) / np.linalg.norm(ref)
+    assert rel < 1e-9, rel

@@ -95,7 +95,6 @@ def test_leaf_dtn_matches_reference_golden():
 C12_REF_TOL = {8: 2e-9, 12: 1e-10}
 
 
-@pytest.mark.unverified
 @pytest.mark.parametrize('p', [8, 12])
 def test_leaf_dtn_mixed_derivative_matches_reference(p):
     """Every coefficient present, c12 included (curved-domain parameter maps): the

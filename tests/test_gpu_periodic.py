@@ -18,7 +18,7 @@ import numpy as np
 import pytest
 import torch
 
-pytestmark = [pytest.mark.gpu, pytest.mark.unverified(order=1)]
+pytestmark = pytest.mark.gpu
 
 NAME = 'periodic_square_p12_n210.npz'
 

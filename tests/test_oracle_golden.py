@@ -185,3 +185,46 @@ def test_reference_annulus_known_answer(golden_dir):
     trueres = np.linalg.norm(sol - true) / np.linalg.norm(true)
     assert trueres < 2e-5
     assert abs(trueres - float(g['trueres'])) < 1e-3 * float(g['trueres'])
+
+
+def test_reference_config1_plane_waves(golden_dir):
+    """Config 1 (p = 12, n = 400, 10 points per wavelength): Dirichlet data a sum of
+    8 seeded plane waves; the oracle's sparse direct solve against the reference's
+    slabLU solution vector."""
+    import torch
+    from slablu_gb300 import problems
+    g = load(golden_dir, 'config1_slabLU_p12_n400.npz')
+    cfg = problems.config1()
+    p, n, kh = int(g['p']), int(g['n']), float(g['kh'])
+    assert (p, n) == (cfg['p'], cfg['n']) and kh == cfg['kh']
+    md = domain.Multidomain([[0, 1], [0, 1]], cfg['a'], p)
+    part = domain.SlabPartition(md, 1.0)
+    co = md.coeffs(funcs.helmholtz_pdo(lambda x: funcs.bfield_constant(x, kh)))
+    out = domain.solve_full(md, part, co, lambda x: cfg['uu_dir'](torch.as_tensor(x)).numpy())
+    sol = out['sol_tot'][:, 0]
+    stride = int(g['stride'])
+    assert sol.size == int(g['sol_len'])
+    assert np.linalg.norm(sol[::stride] - g['sol_sub']) / np.linalg.norm(g['sol_sub']) < 1e-9
+    assert abs(np.linalg.norm(sol) - float(g['sol_norm'])) < 1e-9 * float(g['sol_norm'])
+
+
+def test_reference_config2_leaf_dtn(golden_dir):
+    """Config 2 (128 x 128 leaves, p = 22, 32-bump field): the oracle's leaf DtN maps
+    against the reference's form_DtNs on the sampled leaves, and the sampled
+    leaves' points and coefficients against the product's generators."""
+    import torch
+    from slablu_gb300 import hps, problems
+    g = load(golden_dir, 'config2_dtn_p22.npz')
+    cfg = problems.config2()
+    p, a = int(g['p']), float(g['a'])
+    assert p == cfg['p'] and a == cfg['a'] and int(g['nside']) == cfg['nside']
+    geo = hps.Geometry([[0, 1], [0, 1]], a, p, 1.0)
+    xx = np.asarray(geo.xx).reshape(-1, p * p, 2)[g['picks']]
+    assert np.abs(xx - g['xx']).max() < 1e-15
+    c = cfg['c'](torch.as_tensor(xx.reshape(-1, 2))).numpy().reshape(len(g['picks']), -1)
+    assert np.array_equal(c, g['c'])
+    ld = leaf.leaf_disc(a, p)
+    n = c.shape[0]
+    dtn = leaf.dtn_build(ld, {'c11': np.ones((n, p * p)), 'c22': np.ones((n, p * p)), 'c': g['c']})
+    rel = np.linalg.norm(dtn - g['dtn'], axis=(1, 2)) / np.linalg.norm(g['dtn'], axis=(1, 2))
+    assert rel.max() < 1e-12, rel.max()

@@ -1,12 +1,14 @@
 """GPU test of slab_leaf_dtn_noalloc, the leaf DtN entry point that allocates nothing.
 
-Callers that cannot allocate device memory at the point of use (code running
-inside CUDA stream capture, or an application that owns every device byte)
-get DtN maps from a scratch array built into the library instead of a work
-buffer they pass in.  This file checks, through the C ABI, that two calls in a
-row give the same maps as slab_leaf_dtn with its own work buffer, and that a
-batch too large for the built-in scratch is refused with a clear error.  It is
-named to be collected last.
+Callers that cannot allocate device memory at the point of use (an
+application whose own pool allocator owns every device byte, or a program with
+a device-memory budget fixed at start-up) get DtN maps from a scratch array
+built into the library instead of a work buffer they pass in.  This file
+checks, through the C ABI, that two calls in a row give the same maps as
+slab_leaf_dtn with its own work buffer, that a call after the first one on the
+device takes no device memory (free bytes and torch's allocation unchanged),
+and that a batch too large for the built-in scratch is refused with a clear
+error.  It is named to be collected last.
 """
 import ctypes
 
@@ -74,6 +76,28 @@ def test_no_alloc_matches_work_buffer_entry_point(lib, precision, tol):
         assert int(ginfo.abs().sum()) == 0 and int(rinfo.abs().sum()) == 0
         rel = (torch.linalg.norm(got - ref) / torch.linalg.norm(ref)).item()
         assert rel <= tol, (call, rel)
+
+
+def test_no_alloc_call_takes_no_device_memory(lib):
+    """After the first call on the device (which loads the library's kernels and
+    looks up the scratch address), a call leaves the device's free memory and
+    torch's allocations exactly as they were."""
+    L = lib.lib()
+    p, nleaf = 22, 16
+    co, D, Dsq, Nx = _operands(p, nleaf, 21)
+    _with_work(L, p, nleaf, co, D, Dsq, Nx, 2)
+    _no_alloc(L, p, nleaf, co, D, Dsq, Nx, 2)     # first call on this device
+    q = p - 2
+    dtn = torch.empty(nleaf, 4 * q, 4 * q, dtype=torch.float64, device='cuda')
+    info = torch.zeros(nleaf, dtype=torch.int32, device='cuda')
+    P = lambda t: None if t is None else ctypes.c_void_p(t.data_ptr())
+    torch.cuda.synchronize()
+    free0, alloc0 = torch.cuda.mem_get_info()[0], torch.cuda.memory_allocated()
+    st = L.slab_leaf_dtn_noalloc(nleaf, p, *[P(c) for c in co], P(D), P(Dsq), P(Nx), 2, P(dtn), P(info), None)
+    torch.cuda.synchronize()
+    assert st == 0, L.slab_last_error()
+    assert torch.cuda.mem_get_info()[0] == free0
+    assert torch.cuda.memory_allocated() == alloc0
 
 
 def test_no_alloc_rejects_batches_beyond_its_scratch(lib):
