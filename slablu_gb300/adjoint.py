@@ -69,3 +69,23 @@ def slab_solve(engine: SlabEngine, bnd, fbody=None, tol=1e-12, max_iter=30, **co
     coefs = [coeffs[k].to(torch.float64) for k in keys]
     return _SlabSolve.apply(engine, keys, tol, max_iter, bnd.to(torch.float64),
                             None if fbody is None else fbody.to(torch.float64), *coefs)
+
+
+def fd_check(loss_fn, b, v, ad, steps=(1e-5, 1e-6, 1e-7)):
+    """Central differences of loss_fn along v with the step chosen a posteriori:
+    for each h the estimates at h and h/2 are combined by Richardson extrapolation
+    (the O(h^2) term cancels) and their discrepancy |fd(h) - fd(h/2)| estimates the
+    error; the step with the smallest estimate is kept.  The adjoint value ad is
+    used only for the reported error, not for the choice.  Returns
+    (relative error against ad, chosen step, error estimate)."""
+    best = None
+    for h in steps:
+        fd = []
+        for hh in (h, h / 2):
+            fd.append((float(loss_fn(b + hh * v)) - float(loss_fn(b - hh * v))) / (2 * hh))
+        rich = (4 * fd[1] - fd[0]) / 3
+        est = abs(fd[1] - fd[0]) / max(abs(rich), 1e-300)
+        if best is None or est < best[2]:
+            best = (rich, h, est)
+    rich, h, est = best
+    return abs(rich - ad) / max(abs(rich), 1e-300), h, est

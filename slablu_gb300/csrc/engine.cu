@@ -366,7 +366,7 @@ struct EngineImpl : EngineBase {
   // inverses of the 256-row diagonal blocks of each interface LU, so that the
   // Schur right-hand sides X_j = S_j^{-1} sup_j are all tensor-core products
   DevBuf ifLoInv, ifUoInv, emuY, emuT;
-  bool use_outer_inv = false;
+  bool use_outer_inv = true;
   int nOB = 0;
   // Solve-phase copies of the interface factors in the leaf/tree type T (mixed
   // precision: FP32 copies of the FP64 factors; every correction is applied
@@ -551,7 +551,7 @@ struct EngineImpl : EngineBase {
     if (lc) leaf_ctas = atoi(lc);
     const char* la = getenv("SLAB_LEAF_ASSEMBLY");  // 1: assembly by a kernel of its own
     if (la) leaf_split_asm = la[0] == '1';
-    const char* oi = getenv("SLAB_IFACE_OUTER_INV");  // 1: inverted 256-row blocks, tensor-core products
+    const char* oi = getenv("SLAB_IFACE_OUTER_INV");  // 0: FP64-core triangular solves of 64-row blocks
     if (oi) use_outer_inv = oi[0] == '1';
     // FP64 interface products on the tensor cores in the mixed mode (FP32 leaves and
     // tree, FP64 interface); SLAB_NATIVE_FP64=1 keeps them on the FP64 cores

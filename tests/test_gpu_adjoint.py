@@ -179,3 +179,51 @@ def test_autograd_refuses_stale_factorization():
     eng.factor(c11=ones, c22=ones, c=c.detach() * 1.01)
     with pytest.raises(RuntimeError):
         u.sum().backward()
+
+
+def test_config5_loss_gradient_against_dense_oracle_and_differences():
+    """Config 5's inverse-scattering loss ||P u(b) - d||^2 on a reduced grid (p = 16,
+    8 x 8 leaves, 4 wavelengths, the same Gaussian-random-field b, 64 seeded probes):
+    dL/db from slab_solve's backward against the dense FP64 reference gradient of the
+    oracle's collocation system (1e-9) and against central differences along 4 smooth
+    directions (1e-5, the bench's check at full size)."""
+    from slablu_gb300 import hps, problems
+    from slablu_gb300.adjoint import fd_check, slab_solve
+    from slablu_gb300.engine import SlabEngine
+    cfg = problems.config5(n=112, nwaves=4)
+    p, kh = cfg['p'], cfg['kh']
+    a = cfg['a']
+    geom = [[0, 1], [0, 1]]
+    md = odomain.Multidomain(geom, a, p)
+    part = odomain.SlabPartition(md, 1.0)
+    g = hps.Geometry(geom, a, p, 1.0)
+    xx = torch.as_tensor(g.xx_tot, device='cuda')
+    b = cfg['b'](xx)
+    ones = torch.ones_like(b)
+    bnd = torch.ones(g.ntot, dtype=torch.float64, device='cuda')
+    probes = torch.as_tensor(problems.probe_nodes(g.xx_tot, 64), device='cuda')
+    eng = SlabEngine(g, 'fp64')
+    solve = lambda bb: slab_solve(eng, bnd, tol=1e-13, max_iter=40, c11=ones, c22=ones, c=cfg['c_of_b'](bb))
+    with torch.no_grad():
+        d = solve(cfg['b_perturbed'](xx))[probes].clone()
+    loss_fn = lambda bb: ((solve(bb)[probes] - d) ** 2).sum()
+    bb = b.clone().requires_grad_(True)
+    loss_fn(bb).backward()
+    grad = bb.grad.detach()
+    # dense FP64 reference: the oracle's collocation system with the same coefficients
+    npts = g.nboxes * p * p
+    co = {'c11': np.ones((g.nboxes, p * p)), 'c22': np.ones((g.nboxes, p * p)),
+          'c': cfg['c_of_b'](b).cpu().numpy().reshape(g.nboxes, p * p)}
+    col = oadj.Collocation(md, part, co)
+    uU, uf, sol = col.solve(np.ones((part.I_Xtot.size, 1)))
+    pr = probes.cpu().numpy()
+    w = np.zeros((npts, 1))
+    w[pr, 0] = 2 * (sol[pr, 0] - d.cpu().numpy())
+    ref = col.gradient(uU, uf, w)
+    ref_b = -(kh ** 2) * ref['c']
+    assert _rel(grad.cpu().numpy(), ref_b) < 1e-9
+    with torch.no_grad():
+        for i in range(4):
+            v = problems.grf(xx, seed=500 + i)
+            err, h, est = fd_check(loss_fn, b, v, float((grad * v).sum()))
+            assert err < 1e-5, (i, err, h, est)
