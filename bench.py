@@ -93,6 +93,25 @@ def cpu_threads():
         return os.cpu_count() or 1
 
 
+def reference_measured():
+    """The unmodified reference's own run of this exact workload (n = 2000), recorded
+    when its oracle fixtures were made (tests/golden/make_golden.py, one x86 host
+    thread): build and second-solve seconds and unknowns/s of its slabLU and superLU
+    paths.  The reference is Python and is not shipped, so it cannot be re-run on
+    the GPU machine; this is the measurement of record at the benchmark's size."""
+    out = {}
+    for solver in ('slabLU', 'superLU'):
+        path = os.path.join(ROOT, 'tests', 'golden', f'config3_{solver}_p22_n2000.npz')
+        if not os.path.exists(path):
+            continue
+        g = np.load(path)
+        t = float(g['t_build']) + float(g['t_solve'])
+        out[solver] = dict(build_s=float(g['t_build']), solve_s=float(g['t_solve']), N=int(g['N']),
+                           unknowns_per_s=int(g['N']) / t, threads=int(g['threads']),
+                           host='x86 build container (one thread: multi-threaded batched LU stalls there)')
+    return out
+
+
 def reference_workload(args):
     """The workload string of our arm, so both arms name the same configuration."""
     from slablu_gb300 import hps, problems
@@ -115,6 +134,7 @@ def run_reference(args):
     tmean = sum(times) / len(times)
     val = N / tmean
     cores = cpu_threads()
+    ref_measured = reference_measured()
     # n_gpus is the launch's N (the arms are compared per launch); this arm computes on the host cores only
     line = dict(metric=METRIC, value=val, unit='unknowns/s', n_gpus=args.gpus, steps=args.steps, warmup=args.warmup,
                 ms_per_step=1e3 * tmean, higher_is_better=True, scaling='weak', vs_baseline=None, dtype='f64',
@@ -123,9 +143,10 @@ def run_reference(args):
                             sample=f'each step: the oracle port of the reference CPU slabLU, full factor+solve of '
                                    f'the same field at n={CPU_SAMPLE_N} (N={N}); unknowns/s is size-independent '
                                    f'to within ~15 % for the reference'),
-                cpu_baseline=dict(value=val, unit='unknowns/s', cores=cores, kind='port',
+                cpu_baseline=dict(value=val, unit='unknowns/s', cores=cores, host_cores=os.cpu_count(), kind='port',
                                   sample=f'full factor+solve at n={CPU_SAMPLE_N} (N={N}) per step'),
-                e2e=dict(value=val, unit='unknowns/s', h2d_bytes_per_step=0, d2h_bytes_per_step=0))
+                e2e=dict(value=val, unit='unknowns/s', h2d_bytes_per_step=0, d2h_bytes_per_step=0),
+                reference_measured=ref_measured)
     print(json.dumps(line), flush=True)
 
 
@@ -548,6 +569,7 @@ def run_ours(args):
         e2e=dict(value=N / (sum(e2e_times) / len(e2e_times)), unit='unknowns/s', h2d_bytes_per_step=h2d,
                  d2h_bytes_per_step=d2h),
         gpu_launches=int(launches),
+        reference_measured=reference_measured(),
         autotune=picks,
         multi_rhs=multi,
     )

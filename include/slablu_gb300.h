@@ -240,6 +240,21 @@ int slab_dgemm_emu(int m, int n, int k, double alpha, const double* d_A, int lda
  * src_solver/block_tridiag_solver_dense.py:169 and the slab interface products
  * of src_solver/slablu_solver.py:1066-1136), which the engine calls
  * asynchronously inside its factorization. */
+/* Dense FP64 LU with partial pivoting of one n x n column-major device matrix
+ * (in place, L unit-lower and U) with the library's FP64 panel and update
+ * kernels, and solves with it.  d_work (slab_dense_lu_work_bytes(n) bytes,
+ * 256-byte aligned) keeps the pivots and the inverted 64-row diagonal blocks
+ * between the two calls.  slab_dense_lu returns the LAPACK info of the first
+ * zero pivot (> 0) and also writes it to *h_info (may be NULL); it synchronizes
+ * the stream.  slab_dense_lu_solve: X = A^{-1} B (n x nrhs, X != B),
+ * asynchronous.  Replaces the lu_factor / lu_solve of the periodic interface
+ * Schur complement (src_solver/block_tridiag_solver_structured.py:118-154,
+ * 193-206), used by the periodic edge (slablu_gb300/periodic.py). */
+size_t slab_dense_lu_work_bytes(int n);
+int slab_dense_lu(int n, double* d_A, int lda, void* d_work, size_t work_bytes, int* h_info, void* stream);
+int slab_dense_lu_solve(int n, int nrhs, const double* d_LU, int lda, const void* d_work, const double* d_B, int ldb,
+                        double* d_X, int ldx, void* stream);
+
 size_t slab_sgemm_tc_work_bytes(int m, int n, int k, int batch);
 int slab_sgemm_tc(int m, int n, int k, float alpha, const float* d_A, int lda, long long strideA, const float* d_B,
                   int ldb, long long strideB, float beta, float* d_C, int ldc, long long strideC, int batch,

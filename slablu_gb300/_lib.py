@@ -56,6 +56,9 @@ _SIGS = {
     'slab_leaf_dtn_mixed': (c_int, [c_int, c_int] + [c_void] * 11 + [c_int, c_void, c_size, c_void, c_void, c_void,
                                                                       c_void]),
     'slab_csr_spmv': (c_int, [c_int, c_void, c_void, c_void, c_void, c_double, c_double, c_void, c_void]),
+    'slab_dense_lu_work_bytes': (c_size, [c_int]),
+    'slab_dense_lu': (c_int, [c_int, c_void, c_int, c_void, c_size, P_int, c_void]),
+    'slab_dense_lu_solve': (c_int, [c_int, c_int, c_void, c_int, c_void, c_void, c_int, c_void, c_int, c_void]),
     'slab_sgemm_tc_work_bytes': (c_size, [c_int, c_int, c_int, c_int]),
     'slab_sgemm_tc': (c_int, [c_int, c_int, c_int, ctypes.c_float, c_void, c_int, c_ll, c_void, c_int, c_ll,
                               ctypes.c_float, c_void, c_int, c_ll, c_int, c_void, c_size, c_void]),

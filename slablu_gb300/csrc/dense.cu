@@ -695,4 +695,69 @@ template int gemm_tn<double>(cudaStream_t, int, int, int, double, const double*,
                              const double*, const long long*, long long, int, double, double*, const long long*,
                              long long, int, int);
 
+// ---------------------------------------------------------------------------
+// Dense FP64 LU of one n x n matrix through the C ABI (the periodic edge's Schur
+// complement).  Work layout (256-byte aligned pieces): ipiv (n ints), perm (n
+// ints), info (1 int), panel inverse (kNB x kNB), Linv and Uinv (ceil(n/64)
+// blocks of 64 x 64 each).
+namespace {
+constexpr int kDenseInvBs = 64;
+size_t al256d(size_t b) { return (b + 255) / 256 * 256; }
+struct DenseWork {
+  int *ipiv, *perm, *info;
+  double *panel, *linv, *uinv;
+};
+DenseWork dense_work(void* w, int n) {
+  unsigned char* p = static_cast<unsigned char*>(w);
+  DenseWork d{};
+  const size_t nblk = (size_t)(n + kDenseInvBs - 1) / kDenseInvBs;
+  d.ipiv = reinterpret_cast<int*>(p);
+  p += al256d((size_t)n * 4);
+  d.perm = reinterpret_cast<int*>(p);
+  p += al256d((size_t)n * 4);
+  d.info = reinterpret_cast<int*>(p);
+  p += 256;
+  d.panel = reinterpret_cast<double*>(p);
+  p += al256d((size_t)kNB * kNB * 8);
+  d.linv = reinterpret_cast<double*>(p);
+  p += al256d(nblk * kDenseInvBs * kDenseInvBs * 8);
+  d.uinv = reinterpret_cast<double*>(p);
+  return d;
+}
+}  // namespace
+
 }  // namespace slab
+
+extern "C" size_t slab_dense_lu_work_bytes(int n) {
+  if (n <= 0) return 256;
+  const size_t nblk = (size_t)(n + slab::kDenseInvBs - 1) / slab::kDenseInvBs;
+  return 2 * slab::al256d((size_t)n * 4) + 256 + slab::al256d((size_t)slab::kNB * slab::kNB * 8) +
+         2 * slab::al256d(nblk * slab::kDenseInvBs * slab::kDenseInvBs * 8);
+}
+
+extern "C" int slab_dense_lu(int n, double* A, int lda, void* work, size_t work_bytes, int* h_info, void* stream) {
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (n <= 0 || !A || lda < n || !work || work_bytes < slab_dense_lu_work_bytes(n) ||
+      reinterpret_cast<uintptr_t>(work) % 256 != 0)
+    return slab::set_error(SLAB_ERR_ARG, "slab_dense_lu: invalid arguments");
+  slab::DenseWork d = slab::dense_work(work, n);
+  SLAB_CUDA_TRY(cudaMemsetAsync(d.info, 0, sizeof(int), s));
+  SLAB_TRY(slab::biglu<double>(s, A, lda, n, d.ipiv, d.info, d.panel));
+  SLAB_TRY(slab::build_perm(s, d.ipiv, n, d.perm));
+  SLAB_TRY(slab::tri_inv_blocks<double>(s, A, lda, n, slab::kDenseInvBs, d.linv, d.uinv));
+  int info = 0;
+  SLAB_CUDA_TRY(cudaMemcpyAsync(&info, d.info, sizeof(int), cudaMemcpyDeviceToHost, s));
+  SLAB_CUDA_TRY(cudaStreamSynchronize(s));
+  if (h_info) *h_info = info;
+  if (info > 0) return slab::set_error(info, "slab_dense_lu: zero pivot at column %d", info);
+  return SLAB_OK;
+}
+
+extern "C" int slab_dense_lu_solve(int n, int nrhs, const double* LU, int lda, const void* work, const double* B,
+                                   int ldb, double* X, int ldx, void* stream) {
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (n <= 0 || nrhs <= 0 || !LU || !work || !B || !X || lda < n || ldb < n || ldx < n || B == X)
+    return slab::set_error(SLAB_ERR_ARG, "slab_dense_lu_solve: invalid arguments");
+  slab::DenseWork d = slab::dense_work(const_cast<void*>(work), n);
+  return slab::bigtrs_inv<double>(s, LU, lda, n, d.perm, d.linv, d.uinv, slab::kDenseInvBs, B, ldb, X, ldx, nrhs);
+}

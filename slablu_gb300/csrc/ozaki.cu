@@ -54,10 +54,13 @@ constexpr int kAbytes = kBM * kBK * 2;
 constexpr int kBbytes = kBN * kBK * 2;
 constexpr int kBStageBytes = kSl * kBbytes;
 constexpr int kNonFinite = INT_MIN;
-constexpr int kTmemCols = 256;
+// Two sets of the eight level accumulators: the MMAs of K chunk c + 1 run into
+// one while the epilogue drains chunk c from the other.
+constexpr int kAccCols = kGroups * kBN;
+constexpr int kTmemCols = 2 * kAccCols;
 constexpr size_t kGemmSmem = (size_t)kAStages * kAbytes + (size_t)kBStages * kBStageBytes + 1024 + 256;
 
-static_assert(kGroups * kBN <= kTmemCols, "accumulators must fit tensor memory");
+static_assert(kTmemCols <= 512, "both accumulator sets must fit tensor memory");
 static_assert(kSl * kBN <= 256, "one MMA covers all B slices of an A slice (N <= 256)");
 
 __device__ __forceinline__ int biased_exp(double x) {
@@ -192,9 +195,9 @@ __global__ void __launch_bounds__(192, 1) ozaki_gemm_kernel(const __grid_constan
   uint64_t* emptyA = fullA + kAStages;
   uint64_t* fullB = emptyA + kAStages;
   uint64_t* emptyB = fullB + kBStages;
-  uint64_t* accf = emptyB + kBStages;
-  uint64_t* acce = accf + 1;
-  uint64_t* fin = acce + 1;
+  uint64_t* accf = emptyB + kBStages;  // [2]: chunk products complete in accumulator set b
+  uint64_t* acce = accf + 2;           // [2]: accumulator set b drained
+  uint64_t* fin = acce + 2;
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(fin + 1);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int i0 = blockIdx.x * kBM, j0 = blockIdx.y * kBN;
@@ -208,8 +211,10 @@ __global__ void __launch_bounds__(192, 1) ozaki_gemm_kernel(const __grid_constan
       tc::mbar_init(&fullB[s], 1);
       tc::mbar_init(&emptyB[s], 1);
     }
-    tc::mbar_init(accf, 1);
-    tc::mbar_init(acce, 128);
+    for (int b = 0; b < 2; ++b) {
+      tc::mbar_init(&accf[b], 1);
+      tc::mbar_init(&acce[b], 128);
+    }
     tc::mbar_init(fin, 1);
     tc::fence_mbar_init();
   }
@@ -274,8 +279,10 @@ __global__ void __launch_bounds__(192, 1) ozaki_gemm_kernel(const __grid_constan
       int itA = 0, itB = 0;
       bool ok = true;
       for (int c = 0; c < nchunk && ok; ++c) {
-        if (c > 0) {
-          if (!tc::mbar_wait(acce, (uint32_t)((c - 1) & 1), a.err, 3)) break;
+        // accumulator set c & 1 was last used by chunk c - 2 (its ((c >> 1) - 1)-th drain)
+        const int buf = c & 1;
+        if (c >= 2) {
+          if (!tc::mbar_wait(&acce[buf], (uint32_t)(((c >> 1) - 1) & 1), a.err, 3)) break;
           tc::tc_fence_after();
         }
         const int nkb = min(kChunk, a.kp - c * kChunk + kBK - 1) / kBK;
@@ -299,7 +306,7 @@ __global__ void __launch_bounds__(192, 1) ozaki_gemm_kernel(const __grid_constan
             // A_s0 against B slices 0 .. 7-s0 (rows 0 .. 32 (8-s0) - 1 of the B block):
             // block t0 of the result is level s0 + t0 + 2, at column 32 (s0 + t0)
             const uint32_t idesc = tc::idesc_bf16_f32(kBM, kBN * (kSl - s0));
-            const uint32_t dcol = tbase + (uint32_t)(kBN * s0);
+            const uint32_t dcol = tbase + (uint32_t)(buf * kAccCols + kBN * s0);
             // the chunk's first MMA (s0 = 0 spans every level) starts the accumulators
             tc::mma_bf16(dcol, adesc, bdesc0, idesc, (kb == 0 && s0 == 0) ? 0u : 1u);
 #pragma unroll
@@ -311,7 +318,7 @@ __global__ void __launch_bounds__(192, 1) ozaki_gemm_kernel(const __grid_constan
           if (ok) tc::mma_commit(&emptyB[stB]);  // and the B block after the last slice of this step
           ++itB;
         }
-        if (ok) tc::mma_commit(accf);
+        if (ok) tc::mma_commit(&accf[buf]);
       }
       tc::mma_commit(fin);  // every product issued has completed before tensor memory is released
       final_wait(fin, 0, a.err);
@@ -324,7 +331,8 @@ __global__ void __launch_bounds__(192, 1) ozaki_gemm_kernel(const __grid_constan
     for (int j = 0; j < kBN; ++j) hi[j] = lo[j] = 0;
     bool ok = true;
     for (int c = 0; c < nchunk; ++c) {
-      if (!tc::mbar_wait(accf, (uint32_t)(c & 1), a.err, 5)) {
+      const int buf = c & 1;
+      if (!tc::mbar_wait(&accf[buf], (uint32_t)((c >> 1) & 1), a.err, 5)) {
         ok = false;
         break;
       }
@@ -332,7 +340,7 @@ __global__ void __launch_bounds__(192, 1) ozaki_gemm_kernel(const __grid_constan
 #pragma unroll 1
       for (int g = 0; g < kGroups; ++g) {
         uint32_t r[32];
-        tc::tmem_ld_32x32b_x32(tbase + ((uint32_t)(q * 32) << 16) + (uint32_t)(g * kBN), r);
+        tc::tmem_ld_32x32b_x32(tbase + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * kAccCols + g * kBN), r);
         tc::tmem_ld_wait();
         const int L = g + 2;
         if (g < 4) {
@@ -346,7 +354,7 @@ __global__ void __launch_bounds__(192, 1) ozaki_gemm_kernel(const __grid_constan
         }
       }
       tc::tc_fence_before();
-      tc::mbar_arrive(acce);
+      tc::mbar_arrive(&acce[buf]);
     }
     if (ok && *reinterpret_cast<volatile int*>(a.err) == 0) {
       const int i = i0 + row;

@@ -22,8 +22,12 @@ to solution is linear); a few correction steps S dy = -r(u) take it to the
 engine's FP64 accuracy.  Building S costs one engine solve column per edge node
 (n1 (p-2) columns, done in chunks) and one dense LU of n1 (p-2) unknowns.
 """
+import ctypes
+
 import numpy as np
 import torch
+
+from . import _lib
 
 
 def periodic_index_sets(geom):
@@ -61,6 +65,40 @@ def fold(v, sets):
     return out[u]
 
 
+class DenseLU:
+    """FP64 LU with partial pivoting of a square CUDA matrix and solves with it,
+    by the library's FP64 kernels (slab_dense_lu / slab_dense_lu_solve)."""
+
+    def __init__(self, S):
+        if not S.is_cuda:
+            raise ValueError('DenseLU factors CUDA matrices (slablu_gb300 has no CPU path)')
+        L = _lib.lib()
+        self.n = S.shape[0]
+        self.LU = S.T.contiguous().to(torch.float64)       # column-major storage
+        self.wb = int(L.slab_dense_lu_work_bytes(self.n))
+        self.work = torch.empty(self.wb, dtype=torch.uint8, device=S.device)
+        info = ctypes.c_int(0)
+        st = L.slab_dense_lu(self.n, _lib.ptr(self.LU), self.n, _lib.ptr(self.work), ctypes.c_size_t(self.wb),
+                             ctypes.byref(info), _stream(S.device))
+        _lib.check(st, 'slab_dense_lu')
+
+    def solve(self, B):
+        """A^{-1} B for B (n,) or (n, k)."""
+        L = _lib.lib()
+        B2 = B if B.dim() == 2 else B[:, None]
+        Bc = B2.T.contiguous().to(torch.float64)
+        X = torch.empty_like(Bc)
+        st = L.slab_dense_lu_solve(self.n, Bc.shape[0], _lib.ptr(self.LU), self.n, _lib.ptr(self.work),
+                                   _lib.ptr(Bc), self.n, _lib.ptr(X), self.n, _stream(B.device))
+        _lib.check(st, 'slab_dense_lu_solve')
+        X = X.T
+        return X if B.dim() == 2 else X[:, 0]
+
+
+def _stream(dev):
+    return ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+
+
 class PeriodicEdge:
     """Schur complement of the shared edge on top of a non-periodic factorization.
 
@@ -71,8 +109,9 @@ class PeriodicEdge:
     (ntot, k).  Only the final solve asks for the leaf-node solution.
     """
 
-    def __init__(self, engine, edge_flux, left, right, ntot, tol=1e-10, max_iter=20, chunk=128):
+    def __init__(self, engine, edge_flux, left, right, ntot, tol=1e-10, max_iter=20, chunk=128, dense_lu=DenseLU):
         self.engine, self.edge_flux = engine, edge_flux
+        self.dense_lu = dense_lu   # factorization of the edge Schur complement: DenseLU(S).solve(B)
         self.ntot, self.tol, self.max_iter = int(ntot), tol, max_iter
         self.nL = len(left)
         if len(right) != self.nL:
@@ -110,7 +149,7 @@ class PeriodicEdge:
             self.build_iters = max(self.build_iters, iters)
             S[:, c0:c0 + k] = self._residual(uf)
         self.S = S
-        self.lu, self.piv = torch.linalg.lu_factor(S)
+        self.lu = self.dense_lu(S)
         return self
 
     def solve(self, bnd, fbody=None, max_refine=4):
@@ -128,7 +167,7 @@ class PeriodicEdge:
         b[R] = 0.0
         _, uf, iters, st = self._solve_faces(b, fbody, want_leaf=False)
         r0 = self._residual(uf)
-        y = -torch.linalg.lu_solve(self.lu, self.piv, r0)
+        y = -self.lu.solve(r0)
         steps, total_iters = 0, iters
         r0n = float(torch.linalg.norm(r0))
         while True:
@@ -139,7 +178,7 @@ class PeriodicEdge:
             steps += 1
             r = self._residual(uf)
             rn = float(torch.linalg.norm(r))
-            dy = -torch.linalg.lu_solve(self.lu, self.piv, r)
+            dy = -self.lu.solve(r)
             yn = float(torch.linalg.norm(y))
             if steps >= max_refine or yn == 0.0 or float(torch.linalg.norm(dy)) <= self.tol * yn:
                 break

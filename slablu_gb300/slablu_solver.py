@@ -20,9 +20,10 @@ Differences from the reference, by design:
     and ``get_rhs`` assemble and apply it on the GPU for callers of the
     reference's sparse interface (slablu_gb300/sparse.py).
   * periodic_bc=True couples the shared edge back through its Schur complement
-    on top of the non-periodic factorization (slablu_gb300/periodic.py) instead
-    of the reference's cyclic interface solver; ``rel_err`` is then the
-    relative residual of the folded reduced system, as in the reference.
+    on top of the non-periodic factorization (slablu_gb300/periodic.py; the
+    complement is LU-factored by the library's FP64 kernels) instead of the
+    reference's cyclic interface solver; ``rel_err`` is then the relative
+    residual of the folded reduced system, as in the reference.
   * a mixed derivative (c12, curved domains through a parameter map) runs
     the reference's c12 leaf branch (slab_engine_create_mixed); its adjoint
     is not provided.
@@ -202,7 +203,7 @@ class Domain_Solver:
         left, right = periodic.edge_faces(g)
         E = sparse.row_subset(g, self.hps._A, np.concatenate((left, right)))
         self._edge = periodic.PeriodicEdge(self.engine, E.matvec, left, right, self.ntot, tol=self.tol,
-                                           max_iter=self.max_iter).build(self.device)
+                                           max_iter=self.max_iter, dense_lu=periodic.DenseLU).build(self.device)
 
     def get_rhs_boundary(self, uu_dir_func):
         """Face vector carrying Dirichlet data at I_Xtot (slablu_solver.py:504)."""

@@ -49,6 +49,17 @@ class NonPeriodicSolveDouble:
 
 
 @functools.lru_cache(maxsize=None)
+class _CpuLU:
+    """Test double of periodic.DenseLU for CPU tensors (the product factors the edge
+    Schur complement on the GPU with the library's LU)."""
+
+    def __init__(self, S):
+        self.lu, self.piv = torch.linalg.lu_factor(S)
+
+    def solve(self, B):
+        return torch.linalg.lu_solve(self.lu, self.piv, B)
+
+
 def _setup(golden_dir, name=NAME):
     g = np.load(os.path.join(golden_dir, name))
     p, n, kh = int(g['p']), int(g['n']), float(g['kh'])
@@ -102,7 +113,7 @@ def test_periodic_edge_schur_solve(golden_dir, name):
     Aedge = A[rows]
     flux = lambda U: torch.as_tensor(Aedge @ U.numpy())
     eng = NonPeriodicSolveDouble(md, part, A, co)
-    edge = periodic.PeriodicEdge(eng, flux, left, right, geom.ntot, chunk=64).build('cpu')
+    edge = periodic.PeriodicEdge(eng, flux, left, right, geom.ntot, chunk=64, dense_lu=_CpuLU).build('cpu')
     nL = left.size
     assert eng.calls[:(nL + 63) // 64] == [64] * (nL // 64) + ([nL % 64] if nL % 64 else [])
     sets = periodic.periodic_index_sets(geom)
@@ -187,6 +198,7 @@ def test_domain_solver_periodic_flow_on_cpu(golden_dir, monkeypatch, name):
         return out[:, 0] if x.dim() == 1 else out
 
     monkeypatch.setattr(ss, 'SlabEngine', EngineDouble)
+    monkeypatch.setattr(ss.periodic, 'DenseLU', _CpuLU)
     monkeypatch.setattr(ss._HPSView, 'sparse_mat', sparse_mat)
     monkeypatch.setattr(sparse.ReducedCSR, 'matvec', matvec)
     monkeypatch.setattr(ss.torch.cuda, 'synchronize', lambda *a, **k: None)
