@@ -37,20 +37,32 @@ def main(argv=None):
         A = torch.randn(a.batch, a.n, a.k, dtype=torch.float32, device='cuda', generator=gen)
         B = torch.randn(a.batch, a.k, a.n, dtype=torch.float32, device='cuda', generator=gen)
         C = torch.zeros(a.batch, a.n, a.n, dtype=torch.float32, device='cuda')
+        times = []
         for _ in range(a.reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
             C = sgemm_tc(A, B, C, alpha=-1.0, beta=1.0)
-        torch.cuda.synchronize()
-        print('ok sgemm', a.batch, a.n, a.k, float(C.abs().max()))
+            e1.record()
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1))
+        print('ok sgemm', a.batch, a.n, a.k, float(C.abs().max()), 'ms per batch (incl. layout copies and slicing):',
+              [round(t, 3) for t in times])
         return
     if a.case == 'dgemm':
         from .dgemm import dgemm_emu
         gen = torch.Generator(device='cuda').manual_seed(1)
         A = torch.randn(a.n, a.n, dtype=torch.float64, device='cuda', generator=gen)
         B = torch.randn(a.n, a.n, dtype=torch.float64, device='cuda', generator=gen)
+        times = []
         for _ in range(a.reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
             C = dgemm_emu(A, B)
-        torch.cuda.synchronize()
-        print('ok dgemm', a.n, float(C.abs().max()))
+            e1.record()
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1))
+        print('ok dgemm', a.n, float(C.abs().max()), 'ms per product (incl. slicing):', [round(t, 3) for t in times],
+              'FP64-equivalent TFLOP/s of the best:', round(2 * a.n ** 3 / (min(times) / 1e3) / 1e12, 2))
         return
     cfg = problems.config3()
     p = cfg['p']

@@ -124,7 +124,12 @@ class Domain_Solver:
 
     # -- coefficients at every leaf node, evaluated on the device -----------------
     def _coeffs(self):
-        xx = torch.as_tensor(self.geom.xx_tot, dtype=torch.float64, device=self.device)
+        # the leaf nodes go to the device on every build (from a pinned host copy)
+        if getattr(self, '_xx_host', None) is None:
+            self._xx_host = torch.as_tensor(self.geom.xx_tot, dtype=torch.float64)
+            if self.device.type == 'cuda':
+                self._xx_host = self._xx_host.pin_memory()
+        xx = self._xx_host.to(self.device, non_blocking=True)
         out = {}
         for key in ('c11', 'c22', 'c1', 'c2', 'c') + (('c12',) if self.mixed else ()):
             f = getattr(self.pdo, key, None)
@@ -241,7 +246,13 @@ class Domain_Solver:
             uleaf, _, iters, st = self.engine.solve(bnd, fb, tol=self.tol, max_iter=self.max_iter,
                                                     allow_noconv=True)
             rel_err = torch.tensor(st['rel_residual'])
-        sol_tot = uleaf.cpu()
+        # the leaf-node solution comes back into pinned host memory (torch's
+        # caching host allocator reuses the blocks of freed results)
+        if uleaf.is_cuda:
+            sol_tot = torch.empty(uleaf.shape, dtype=uleaf.dtype, pin_memory=True)
+            sol_tot.copy_(uleaf)
+        else:
+            sol_tot = uleaf.cpu()
         toc_solve = time.time() - tic
         self.last_solve_info = dict(st, iters=iters)
         true_err = torch.tensor([float('nan')])
