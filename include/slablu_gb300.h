@@ -175,6 +175,41 @@ int slab_engine_factor_mixed(slab_engine* e, const double* d_c11, const double* 
 int slab_engine_solve(slab_engine* e, int nrhs, const double* d_bnd, const double* d_fbody, double tol,
                       int max_iter, double* d_ufaces, double* d_uleaf, int* h_iters, double* h_stats);
 
+/*
+ * The refined solves of several factored engines (any geometries, one engine
+ * at most once) as one CUDA graph: per engine the set-up, a conditional WHILE
+ * node whose body is one refinement step (FP64 residual, one application of
+ * the factors, update; a one-thread kernel decides on the device whether
+ * another step runs) and the final residual and assembly into d_uleaf[i].  A
+ * launch needs no host round trip between steps and runs the engines'
+ * solves side by side.  Same results as slab_engine_solve (the graph takes
+ * one extra step when the first residual is exactly zero).
+ *   count       : number of engines
+ *   nrhs[i]     : right-hand sides of engine i
+ *   d_bnd[i], d_fbody[i] (d_fbody may be NULL, as may its entries),
+ *   d_uleaf[i]  : device buffers of the caller, laid out as for
+ *                 slab_engine_solve, read and written at every launch
+ * The graph reads each engine's current factors, so a re-factorization of the
+ * same coefficient set is picked up by the next launch.  A launch fails with
+ * SLAB_ERR_STATE once an engine has reallocated the buffers the graph uses
+ * (a later solve with more right-hand sides, another set of coefficients).
+ * Destroy graphs before their engines.  Replaces, per engine, the host-driven
+ * loop of Domain_Solver.solve (src_solver/slablu_solver.py:543-600 sweeps
+ * solve_slab and Tred_solver.solve once per call); the reference has no
+ * multi-problem launch.
+ */
+typedef struct slab_solve_graph slab_solve_graph;
+int slab_solve_graph_create(slab_solve_graph** out, slab_engine* const* engines, int count, const int* nrhs,
+                            const double* const* d_bnd, const double* const* d_fbody, double* const* d_uleaf,
+                            double tol, int max_iter);
+/* Launch on `stream` (cudaStream_t; NULL = legacy stream): ordered after all
+ * earlier work of the engines and before their later work; asynchronous. */
+int slab_solve_graph_launch(slab_solve_graph* g, void* stream);
+/* Waits for the last launch; h_iters / h_stats (5 doubles, as for
+ * slab_engine_solve) of engine i.  SLAB_ERR_NOCONV if it did not reach tol. */
+int slab_solve_graph_status(slab_solve_graph* g, int i, int* h_iters, double* h_stats);
+int slab_solve_graph_destroy(slab_solve_graph* g);
+
 /* FP64 residual of the full HPS collocation system at (u_faces, u_int):
  * r_int = f - Aloc[Jc,:] u per leaf, r_faces = -sum of leaf fluxes Nx u at
  * interior faces (nfaces x nrhs column-major; zero on Dirichlet faces).

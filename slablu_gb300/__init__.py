@@ -15,8 +15,8 @@ import torch
 torch.set_default_dtype(torch.double)  # the reference's modules set this on import
 
 from . import pdo, built_in_funcs, hps  # noqa: E402,F401
-from .engine import SlabEngine, leaf_dtn  # noqa: E402,F401
+from .engine import SlabEngine, SolveGraph, leaf_dtn  # noqa: E402,F401
 from .slablu_solver import Domain_Solver  # noqa: E402,F401
 from .adjoint import slab_solve  # noqa: E402,F401
 
-__all__ = ['Domain_Solver', 'SlabEngine', 'leaf_dtn', 'slab_solve', 'pdo', 'built_in_funcs', 'hps']
+__all__ = ['Domain_Solver', 'SlabEngine', 'SolveGraph', 'leaf_dtn', 'slab_solve', 'pdo', 'built_in_funcs', 'hps']

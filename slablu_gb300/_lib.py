@@ -37,6 +37,11 @@ _SIGS = {
     'slab_engine_factor_mixed': (c_int, [c_void] * 7),
     'slab_engine_solve': (c_int, [c_void, c_int, c_void, c_void, c_double, c_int, c_void, c_void, P_int, P_double]),
     'slab_engine_residual': (c_int, [c_void, c_int] + [c_void] * 5),
+    'slab_solve_graph_create': (c_int, [ctypes.POINTER(c_void), c_void, c_int, c_void, c_void, c_void, c_void,
+                                        c_double, c_int]),
+    'slab_solve_graph_launch': (c_int, [c_void, c_void]),
+    'slab_solve_graph_status': (c_int, [c_void, c_int, P_int, P_double]),
+    'slab_solve_graph_destroy': (c_int, [c_void]),
     'slab_engine_adjoint': (c_int, [c_void, c_int, c_void, c_void, c_double, c_int, c_void, c_void, c_void,
                                     P_int, P_double]),
     'slab_engine_coeff_grad': (c_int, [c_void, c_int] + [c_void] * 8),

@@ -284,6 +284,27 @@ __global__ void iface_gather_kernel(const T* __restrict__ pool, const long long*
 }
 
 // ---------------------------------------------------------------------------
+// Status words of a refined solve run as one graph (capture_solve):
+//   [0] completed refinement steps, [1] ||r||^2 of the current step, [2] ||r0||^2,
+//   [3] ||du||^2, [4] ||u||^2, [5] relative correction of the last step,
+//   [6] 1 once the correction reached tol, [7] final ||r||^2, [8] final ||r_int||^2.
+constexpr int kGstatWords = 16;
+
+// End of one refinement step inside the WHILE node: record the step, decide
+// whether another one runs, and clear the accumulators of the next step.
+__global__ void refine_step_kernel(cudaGraphConditionalHandle h, double* st, double tol, int max_iter) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const int it = (int)st[0] + 1;
+  st[0] = (double)it;
+  if (it == 1) st[2] = st[1];
+  const double rel = st[4] > 0.0 ? sqrt(st[3] / st[4]) : 0.0;
+  st[5] = rel;
+  const bool done = st[1] == 0.0 || rel <= tol;
+  if (done) st[6] = 1.0;
+  st[1] = st[3] = st[4] = 0.0;
+  cudaGraphSetConditional(h, (!done && it < max_iter) ? 1u : 0u);
+}
+
 // Host-side plan.
 struct HNode {
   long long off = -1;
@@ -316,6 +337,13 @@ struct EngineBase {
                          double* g22, double* g1, double* g2, double* g0) = 0;
   virtual size_t factor_bytes() const = 0;
   virtual size_t solve_bytes() const = 0;
+  virtual int capture_solve(cudaGraph_t G, int nrhs, const double* bnd, const double* fbody, double* uleaf,
+                            double tol, int max_iter) = 0;
+  // iters/stats of the last launch; count: add its kernels to the launch count
+  virtual int graph_status(int* iters, double* stats, bool count) = 0;
+  virtual cudaStream_t stream() const = 0;
+  // changes whenever a buffer that a captured solve reads is reallocated
+  virtual long long epoch() const = 0;
   virtual double timing(int i) const = 0;
   virtual int set_option(int key, int value) = 0;
   virtual int get_option(int key) const = 0;
@@ -383,6 +411,7 @@ struct EngineImpl : EngineBase {
   int nInvBlk = 0;
   // solve buffers
   int cap_nrhs = 0;
+  long long epoch_ = 0;
   DevBuf wc, flux, gvec, uvec, Ybuf, Zbuf, ifF, ifZ, ux_d, uc_d, rc_d, rx_d, rcT, acc;
   DevBuf gi_d, gf_d;  // adjoint right-hand side (interior leaf-major, faces)
   size_t factor_bytes_ = 0;
@@ -882,8 +911,10 @@ struct EngineImpl : EngineBase {
                                            : "slab_engine_factor: c12 needs an engine from slab_engine_create_mixed");
     const double* src[6] = {co_in.c11, co_in.c22, co_in.c1, co_in.c2, co_in.c, co_in.c12};
     for (int i = 0; i < 6; ++i) {
+      if (has[i] != (src[i] != nullptr)) ++epoch_;
       has[i] = src[i] != nullptr;
       if (has[i]) {
+        if (coef[i].bytes < cbytes) ++epoch_;
         SLAB_TRY(coef[i].ensure(cbytes));
         SLAB_CUDA_TRY(cudaMemcpyAsync(coef[i].p, src[i], cbytes, cudaMemcpyDeviceToDevice, s));
       }
@@ -1176,6 +1207,7 @@ struct EngineImpl : EngineBase {
     SLAB_TRY(rx_d.alloc((size_t)ntot * nrhs * sizeof(double)));
     SLAB_TRY(rcT.alloc((size_t)nleaf * n * nrhs * sizeof(T)));
     cap_nrhs = nrhs;
+    ++epoch_;
     return SLAB_OK;
   }
 
@@ -1667,6 +1699,145 @@ struct EngineImpl : EngineBase {
     return SLAB_OK;
   }
 
+  // ---- the refined solve as one CUDA graph --------------------------------------
+  // Adds to G: the set-up of a solve, a conditional WHILE node whose body is one
+  // refinement step (FP64 residual, application of the factors, update, and a
+  // one-thread kernel that decides on the device whether another step runs), and
+  // the final residual and assembly into uleaf.  bnd, fbody and uleaf are device
+  // buffers of the caller, read and written at every launch of the graph.
+  DevBuf gstat;
+  long long gr_pre = 0, gr_body = 0, gr_post = 0;
+  cudaStream_t stream() const override { return s; }
+  long long epoch() const override { return epoch_; }
+
+  int sumsq_into(const void* x, bool xd, long long nel, double* slot) {
+    if (nel <= 0) return SLAB_OK;
+    if (xd)
+      sumsq_kernel<double><<<grid_for(nel), 256, 0, s>>>((const double*)x, nel, slot);
+    else
+      sumsq_kernel<T><<<grid_for(nel), 256, 0, s>>>((const T*)x, nel, slot);
+    SLAB_CHECK_LAUNCH();
+    return SLAB_OK;
+  }
+
+  int capture_solve(cudaGraph_t G, int nrhs, const double* bnd, const double* fbody, double* uleaf, double tol,
+                    int max_iter) override {
+    if (!factored) return set_error(SLAB_ERR_STATE, "solve graph: engine not factored");
+    if (nrhs <= 0 || !bnd || !uleaf || max_iter <= 0) return set_error(SLAB_ERR_ARG, "solve graph: invalid arguments");
+    SLAB_TRY(reserve(nrhs));
+    SLAB_TRY(gstat.ensure(kGstatWords * sizeof(double)));
+    SLAB_CUDA_TRY(cudaStreamSynchronize(s));
+    const long long nc_el = nleaf * n * nrhs, nf_el = ntot * nrhs;
+    double* st = gstat.as<double>();
+    // set-up: faces with the Dirichlet data, zero interiors and status
+    long long c0 = launch_count();
+    SLAB_CUDA_TRY(cudaStreamBeginCaptureToGraph(s, G, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+    int stc = SLAB_OK;
+    {
+      init_faces_kernel<<<grid_for(nf_el), 256, 0, s>>>(bnd, dirmask.as<unsigned char>(), ux_d.as<double>(), ntot,
+                                                       nrhs);
+      count_launch();
+      if (cudaMemsetAsync(uc_d.p, 0, (size_t)nc_el * sizeof(double), s) != cudaSuccess ||
+          cudaMemsetAsync(st, 0, kGstatWords * sizeof(double), s) != cudaSuccess)
+        stc = set_error(SLAB_ERR_CUDA, "solve graph: set-up capture failed");
+    }
+    cudaStreamCaptureStatus cs;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t ndeps = 0;
+    cudaGraph_t cg = nullptr;
+    std::vector<cudaGraphNode_t> pre_sinks;
+    if (cudaStreamGetCaptureInfo(s, &cs, nullptr, &cg, &deps, nullptr, &ndeps) == cudaSuccess)
+      pre_sinks.assign(deps, deps + ndeps);
+    cudaGraph_t gout = nullptr;
+    const cudaError_t ee = cudaStreamEndCapture(s, &gout);
+    if (stc != SLAB_OK) return stc;
+    if (ee != cudaSuccess) return set_error(SLAB_ERR_CUDA, "solve graph: set-up capture: %s", cudaGetErrorString(ee));
+    gr_pre = launch_count() - c0;
+    add_launches(-gr_pre);
+    // the WHILE node
+    cudaGraphConditionalHandle h;
+    SLAB_CUDA_TRY(cudaGraphConditionalHandleCreate(&h, G, 1u, cudaGraphCondAssignDefault));
+    cudaGraphNodeParams np = {};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = h;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    cudaGraphNode_t cnode;
+    SLAB_CUDA_TRY(cudaGraphAddNode(&cnode, G, pre_sinks.data(), nullptr, pre_sinks.size(), &np));
+    cudaGraph_t body = np.conditional.phGraph_out[0];
+    // one refinement step
+    c0 = launch_count();
+    SLAB_CUDA_TRY(cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+    stc = [&]() -> int {
+      SLAB_TRY(residual_impl(nrhs, ux_d.as<double>(), uc_d.as<double>(), fbody, rc_d.as<double>(), rx_d.as<double>()));
+      SLAB_TRY(sumsq_into(rc_d.p, true, nc_el, st + 1));
+      SLAB_TRY(sumsq_into(rx_d.p, true, nf_el, st + 1));
+      convert_kernel<T, double><<<grid_for(nc_el), 256, 0, s>>>(rc_d.as<double>(), rcT.as<T>(), nc_el);
+      SLAB_CHECK_LAUNCH();
+      convert_kernel<T, double><<<grid_for(nf_el), 256, 0, s>>>(rx_d.as<double>(), gvec.as<T>(), nf_el);
+      SLAB_CHECK_LAUNCH();
+      SLAB_TRY(apply(nrhs));
+      axpy_kernel<T><<<grid_for(nc_el), 256, 0, s>>>(uc_d.as<double>(), wc.as<T>(), nc_el);
+      SLAB_CHECK_LAUNCH();
+      axpy_kernel<T><<<grid_for(nf_el), 256, 0, s>>>(ux_d.as<double>(), uvec.as<T>(), nf_el);
+      SLAB_CHECK_LAUNCH();
+      SLAB_TRY(sumsq_into(wc.p, false, nc_el, st + 3));
+      SLAB_TRY(sumsq_into(uvec.p, false, nf_el, st + 3));
+      SLAB_TRY(sumsq_into(uc_d.p, true, nc_el, st + 4));
+      SLAB_TRY(sumsq_into(ux_d.p, true, nf_el, st + 4));
+      refine_step_kernel<<<1, 32, 0, s>>>(h, st, tol, max_iter);
+      SLAB_CHECK_LAUNCH();
+      return SLAB_OK;
+    }();
+    const cudaError_t eb = cudaStreamEndCapture(s, &body);
+    if (stc != SLAB_OK) return stc;
+    if (eb != cudaSuccess) return set_error(SLAB_ERR_CUDA, "solve graph: step capture: %s", cudaGetErrorString(eb));
+    gr_body = launch_count() - c0;
+    add_launches(-gr_body);
+    // final residual and the leaf-node solution
+    c0 = launch_count();
+    SLAB_CUDA_TRY(cudaStreamBeginCaptureToGraph(s, G, &cnode, nullptr, 1, cudaStreamCaptureModeRelaxed));
+    stc = [&]() -> int {
+      SLAB_TRY(residual_impl(nrhs, ux_d.as<double>(), uc_d.as<double>(), fbody, rc_d.as<double>(), rx_d.as<double>()));
+      SLAB_TRY(sumsq_into(rc_d.p, true, nc_el, st + 8));
+      SLAB_TRY(sumsq_into(rc_d.p, true, nc_el, st + 7));
+      SLAB_TRY(sumsq_into(rx_d.p, true, nf_el, st + 7));
+      AssembleArgs aa{};
+      aa.p = p; aa.q = q; aa.n = n; aa.nx = nx; aa.nleaf = (int)nleaf; aa.nrhs = nrhs; aa.ntot = ntot;
+      aa.leafglob = leafglob.as<int>(); aa.interp = interp.as<double>(); aa.jxreorder = jxr.as<int>();
+      aa.ux = ux_d.as<double>(); aa.uc = uc_d.as<double>(); aa.out = uleaf;
+      assemble_solution_kernel<<<(unsigned)nleaf, 256, (size_t)nx * sizeof(double), s>>>(aa);
+      SLAB_CHECK_LAUNCH();
+      return SLAB_OK;
+    }();
+    const cudaError_t ep = cudaStreamEndCapture(s, &gout);
+    if (stc != SLAB_OK) return stc;
+    if (ep != cudaSuccess) return set_error(SLAB_ERR_CUDA, "solve graph: final capture: %s", cudaGetErrorString(ep));
+    gr_post = launch_count() - c0;
+    add_launches(-gr_post);
+    return SLAB_OK;
+  }
+
+  int graph_status(int* iters, double* stats, bool count) override {
+    double h[kGstatWords];
+    if (!gstat.p) return set_error(SLAB_ERR_STATE, "solve graph: no graph captured on this engine");
+    SLAB_CUDA_TRY(cudaMemcpy(h, gstat.p, sizeof(h), cudaMemcpyDeviceToHost));
+    const int it = (int)h[0];
+    if (count) add_launches(gr_pre + gr_post + gr_body * it);
+    if (iters) *iters = it;
+    if (stats) {
+      const double r0 = std::sqrt(h[2]), rn = std::sqrt(h[7]);
+      stats[0] = h[5];
+      stats[1] = rn;
+      stats[2] = r0;
+      stats[3] = std::sqrt(h[8]);
+      stats[4] = r0 > 0 ? rn / r0 : 0.0;
+    }
+    if (h[6] == 0.0)
+      return set_error(SLAB_ERR_NOCONV, "refinement (graph): relative correction %.3e after %d steps", h[5], it);
+    return SLAB_OK;
+  }
+
   int residual(int nrhs, const double* ufaces, const double* uint, const double* fbody, double* rint,
                double* rfaces) override {
     if (!factored && !has[0] && !has[1] && !has[4])
@@ -1775,6 +1946,99 @@ extern "C" int slab_engine_solve(slab_engine* e, int nrhs, const double* bnd, co
                                  int max_iter, double* ufaces, double* uleaf, int* iters, double* stats) {
   if (!e) return slab::set_error(SLAB_ERR_ARG, "slab_engine_solve: null engine");
   return e->impl->solve(nrhs, bnd, fbody, tol, max_iter, ufaces, uleaf, iters, stats);
+}
+
+// ---------------------------------------------------------------------------
+// Several refined solves (independent engines, any sizes) as one CUDA graph.
+struct slab_solve_graph {
+  std::vector<slab_engine*> engines;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaEvent_t ev = nullptr;
+  std::vector<cudaEvent_t> eng_ev;
+  std::vector<long long> epoch;  // engine buffer epochs at capture
+  std::vector<char> counted;      // kernels of the last launch added to the count
+};
+
+extern "C" int slab_solve_graph_destroy(slab_solve_graph* g) {
+  if (!g) return SLAB_OK;
+  if (g->exec) cudaGraphExecDestroy(g->exec);
+  if (g->graph) cudaGraphDestroy(g->graph);
+  if (g->ev) cudaEventDestroy(g->ev);
+  for (cudaEvent_t e : g->eng_ev)
+    if (e) cudaEventDestroy(e);
+  delete g;
+  return SLAB_OK;
+}
+
+extern "C" int slab_solve_graph_create(slab_solve_graph** out, slab_engine* const* engines, int count, const int* nrhs,
+                                       const double* const* bnd, const double* const* fbody, double* const* uleaf,
+                                       double tol, int max_iter) {
+  if (!out || !engines || count <= 0 || !nrhs || !bnd || !uleaf)
+    return slab::set_error(SLAB_ERR_ARG, "slab_solve_graph_create: invalid arguments");
+  *out = nullptr;
+  for (int i = 0; i < count; ++i) {
+    if (!engines[i]) return slab::set_error(SLAB_ERR_ARG, "slab_solve_graph_create: null engine %d", i);
+    for (int j = 0; j < i; ++j)
+      if (engines[j] == engines[i])
+        return slab::set_error(SLAB_ERR_ARG, "slab_solve_graph_create: engine %d appears twice", i);
+  }
+  auto* g = new slab_solve_graph();
+  g->engines.assign(engines, engines + count);
+  int st = SLAB_OK;
+  if (cudaGraphCreate(&g->graph, 0) != cudaSuccess || cudaEventCreateWithFlags(&g->ev, cudaEventDisableTiming) != cudaSuccess)
+    st = slab::set_error(SLAB_ERR_CUDA, "slab_solve_graph_create: graph creation failed");
+  for (int i = 0; i < count && st == SLAB_OK; ++i)
+    st = engines[i]->impl->capture_solve(g->graph, nrhs[i], bnd[i], fbody ? fbody[i] : nullptr, uleaf[i], tol,
+                                         max_iter);
+  if (st == SLAB_OK) {
+    const cudaError_t e = cudaGraphInstantiate(&g->exec, g->graph, 0);
+    if (e != cudaSuccess) {
+      g->exec = nullptr;
+      st = slab::set_error(SLAB_ERR_CUDA, "slab_solve_graph_create: instantiate: %s", cudaGetErrorString(e));
+    }
+  }
+  g->eng_ev.assign(count, nullptr);
+  g->counted.assign(count, 1);
+  for (int i = 0; i < count; ++i) g->epoch.push_back(engines[i]->impl->epoch());
+  for (int i = 0; i < count && st == SLAB_OK; ++i)
+    if (cudaEventCreateWithFlags(&g->eng_ev[i], cudaEventDisableTiming) != cudaSuccess)
+      st = slab::set_error(SLAB_ERR_CUDA, "slab_solve_graph_create: event creation failed");
+  if (st != SLAB_OK) {
+    slab_solve_graph_destroy(g);
+    return st;
+  }
+  *out = g;
+  return SLAB_OK;
+}
+
+extern "C" int slab_solve_graph_launch(slab_solve_graph* g, void* stream) {
+  if (!g || !g->exec) return slab::set_error(SLAB_ERR_ARG, "slab_solve_graph_launch: no graph");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  for (size_t i = 0; i < g->engines.size(); ++i)
+    if (g->engines[i]->impl->epoch() != g->epoch[i])
+      return slab::set_error(SLAB_ERR_STATE,
+                             "slab_solve_graph_launch: engine %zu reallocated its buffers after the graph was made "
+                             "(a solve with more right-hand sides or another set of coefficients); create a new graph",
+                             i);
+  // after the engines' earlier work (their factorizations); before their later work
+  for (size_t i = 0; i < g->engines.size(); ++i) {
+    SLAB_CUDA_TRY(cudaEventRecord(g->eng_ev[i], g->engines[i]->impl->stream()));
+    SLAB_CUDA_TRY(cudaStreamWaitEvent(s, g->eng_ev[i], 0));
+  }
+  SLAB_CUDA_TRY(cudaGraphLaunch(g->exec, s));
+  SLAB_CUDA_TRY(cudaEventRecord(g->ev, s));
+  g->counted.assign(g->engines.size(), 0);
+  for (slab_engine* e : g->engines) SLAB_CUDA_TRY(cudaStreamWaitEvent(e->impl->stream(), g->ev, 0));
+  return SLAB_OK;
+}
+
+extern "C" int slab_solve_graph_status(slab_solve_graph* g, int i, int* iters, double* stats) {
+  if (!g || i < 0 || i >= (int)g->engines.size()) return slab::set_error(SLAB_ERR_ARG, "slab_solve_graph_status: index");
+  SLAB_CUDA_TRY(cudaEventSynchronize(g->ev));
+  const bool count = !g->counted[i];
+  g->counted[i] = 1;
+  return g->engines[i]->impl->graph_status(iters, stats, count);
 }
 
 extern "C" int slab_engine_adjoint(slab_engine* e, int nrhs, const double* gleaf, const double* gfaces, double tol,

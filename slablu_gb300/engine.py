@@ -184,6 +184,75 @@ class SlabEngine:
         return rint, rf.T
 
 
+
+class SolveGraph:
+    """The refined solves of several factored engines as one CUDA graph
+    (slab_solve_graph_create / _launch / _status): per engine a conditional
+    WHILE node runs the refinement steps, decided on the device, so a launch
+    makes no host round trip between steps and the engines' solves run side by
+    side.  Inputs and outputs are persistent device buffers owned here:
+
+        g = SolveGraph([e1, e2], nrhs=[1, 4])
+        g.set_inputs(0, bnd1); g.set_inputs(1, bnd2)
+        g.launch()
+        u1, it1, info1 = g.result(0)      # (npts, nrhs) on engine 0's leaf nodes
+
+    The graph reads the engines' current factors (re-factoring with the same
+    coefficient set needs no new graph); it must be rebuilt once an engine has
+    reallocated its solve buffers (a solve with more right-hand sides)."""
+
+    def __init__(self, engines, nrhs=1, with_fbody=False, tol=1e-10, max_iter=20):
+        self.engines = list(engines)
+        k = len(self.engines)
+        self.nrhs = [int(nrhs)] * k if np.isscalar(nrhs) else [int(r) for r in nrhs]
+        if len(self.nrhs) != k:
+            raise ValueError('SolveGraph: one nrhs per engine')
+        dev = torch.device('cuda', torch.cuda.current_device())
+        z = lambda r, m: torch.zeros(r, m, dtype=torch.float64, device=dev)
+        self.bnd = [z(r, e.ntot) for e, r in zip(self.engines, self.nrhs)]
+        self.fbody = [z(r, e.npts) for e, r in zip(self.engines, self.nrhs)] if with_fbody else None
+        self.uleaf = [z(r, e.npts) for e, r in zip(self.engines, self.nrhs)]
+        self.L = _lib.lib()
+        arr = lambda ts: (ctypes.c_void_p * k)(*[_lib.ptr(t) for t in ts])
+        handle = ctypes.c_void_p()
+        st = self.L.slab_solve_graph_create(ctypes.byref(handle), (ctypes.c_void_p * k)(*[e.h for e in self.engines]),
+                                            k, (ctypes.c_int * k)(*self.nrhs), arr(self.bnd),
+                                            None if self.fbody is None else arr(self.fbody), arr(self.uleaf),
+                                            float(tol), int(max_iter))
+        _lib.check(st, 'slab_solve_graph_create')
+        self.h = handle
+
+    def __del__(self):
+        h = getattr(self, 'h', None)
+        if h is not None and h.value:
+            self.L.slab_solve_graph_destroy(h)
+            self.h = None
+
+    def set_inputs(self, i, bnd, fbody=None):
+        """bnd: (ntot,) or (ntot, nrhs) face values of engine i; fbody: (npts,) or (npts, nrhs)."""
+        self.bnd[i].copy_(_col_major(bnd.to(torch.float64), self.engines[i].ntot))
+        if fbody is not None:
+            if self.fbody is None:
+                raise ValueError('SolveGraph made without body loads (with_fbody=False)')
+            self.fbody[i].copy_(_col_major(fbody.to(torch.float64), self.engines[i].npts))
+
+    def launch(self, stream=None):
+        """Asynchronous on stream (default: torch's current stream)."""
+        stream = stream if stream is not None else torch.cuda.current_stream()
+        _lib.check(self.L.slab_solve_graph_launch(self.h, ctypes.c_void_p(stream.cuda_stream)),
+                   'slab_solve_graph_launch')
+
+    def result(self, i, allow_noconv=False):
+        """(u_leaf (npts, nrhs), iters, stats dict) of engine i from the last launch."""
+        iters = ctypes.c_int(0)
+        stats = (ctypes.c_double * 5)()
+        st = self.L.slab_solve_graph_status(self.h, int(i), ctypes.byref(iters), stats)
+        _lib.check(st, 'slab_solve_graph_status', allow=(_lib.SLAB_ERR_NOCONV,) if allow_noconv else ())
+        info = dict(rel_correction=stats[0], residual=stats[1], residual0=stats[2], resloc=stats[3],
+                    rel_residual=stats[4], converged=(st == _lib.SLAB_OK))
+        return self.uleaf[i].T, iters.value, info
+
+
 def leaf_dtn(coeffs, p, D, Dsq, Nx, precision='fp64', return_S=False, interp=None, jxreorder=None):
     """Batched leaf DtN maps (form_DtNs 'build') through slab_leaf_dtn.
 
