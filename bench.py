@@ -4,10 +4,13 @@ Workload (our arm): the N = 4,404,000 problem (p = 22, n = 2000: 100 x 100
 leaves, 10 slabs of 10 leaf columns), variable-coefficient Helmholtz with a
 Gaussian-lattice scatterer (spacing 0.04, width 0.005, amplitude 1, seeded
 offset), kh for 10 points per wavelength, Dirichlet u = 1.  One step = build
-(leaf DtN, slab elimination, FP64 interface block LU) + solve with FP64
-iterative refinement, mixed precision (FP32 leaf/slab factors, FP64
-interface).  Validity: the mixed-precision solution must agree with the
-all-FP64 GPU solution to <= 1e-6 relative error (checked every run).
+(leaf DtN, slab elimination, interface block LU) + solve with FP64 iterative
+refinement against the FP64 residual of the whole collocation system; the
+factors in reduced precision (--precision fp32: every factor FP32, the
+default; mixed: FP32 leaf/slab factors and an FP64 interface factorization,
+reported beside it).  Validity: the solution must agree with the all-FP64 GPU
+solution and with the reference's own FP64 solutions of this workload to
+<= 1e-6 relative error (checked every run).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -50,6 +53,10 @@ def parse():
                     help='refinement tolerance on the relative correction (the metric asks for 1e-6 relative '
                          'error against FP64; the error left is ~0.1x this and is checked every run)')
     ap.add_argument('--fp64-steps', type=int, default=1, help='timed steps of the all-FP64 path')
+    ap.add_argument('--precision', default='fp32', choices=['fp32', 'mixed'],
+                    help='factor precision of the timed path (refinement is FP64 in both)')
+    ap.add_argument('--alt-steps', type=int, default=2,
+                    help='timed steps of the other reduced-precision mode, reported beside the headline (0 = skip)')
     ap.add_argument('--no-cpu-baseline', action='store_true')
     ap.add_argument('--no-autotune', action='store_true', help='keep the default launch choices')
     ap.add_argument('--nrhs', type=int, default=256, help='right-hand sides of the multi-RHS solve (0 = skip)')
@@ -118,7 +125,7 @@ def reference_workload(args):
     cfg = problems.config3()
     p = cfg['p']
     g = hps.Geometry([[0, 1], [0, 1]], problems.leaf_half_width(args.n, p), p, 1.0)
-    return workload_name(p, args.n, g, cfg, args.tol)
+    return workload_name(p, args.n, g, cfg, args.tol, args.precision)
 
 
 def run_reference(args):
@@ -384,9 +391,12 @@ def bench_config5(dev, nfd=16):
                 fd_ok=max(errs) <= 1e-5, precision='fp64', tol=tol)
 
 
-def workload_name(p, n, g, cfg, tol):
+PREC_DESC = {'fp32': 'FP32 factors', 'mixed': 'FP32 leaf/slab factors + FP64 interface'}
+
+
+def workload_name(p, n, g, cfg, tol, precision):
     return (f'HPS SlabLU p={p} n={n} ({g.n0}x{g.n1} leaves, N={g.N_reported}), Gaussian-lattice Helmholtz '
-            f'kh={cfg["kh"]:.1f}, u=1 Dirichlet; mixed precision + FP64 refinement to tol {tol:g}')
+            f'kh={cfg["kh"]:.1f}, u=1 Dirichlet; {PREC_DESC[precision]} + FP64 refinement to tol {tol:g}')
 
 
 def run_ours(args):
@@ -426,7 +436,31 @@ def run_ours(args):
     del e64
     torch.cuda.empty_cache()
 
-    eng = SlabEngine(g, 'mixed')
+    # ---- the other reduced-precision mode, for comparison (outside the timed region)
+    alt = None
+    if args.alt_steps > 0:
+        alt_prec = 'mixed' if args.precision == 'fp32' else 'fp32'
+        ea = SlabEngine(g, alt_prec)
+        ea.factor(c11=one, c22=one, c=c)
+        ua, _, ita, _ = ea.solve(bnd, tol=args.tol, max_iter=30)
+        alt_t = []
+        for _ in range(args.alt_steps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            ea.factor(c11=one, c22=one, c=c)
+            ea.solve(bnd, tol=args.tol, max_iter=30)
+            torch.cuda.synchronize()
+            alt_t.append(time.perf_counter() - t0)
+        tma = ea.timings()
+        alt = dict(precision=alt_prec, value=N / min(alt_t), ms_per_step=1e3 * min(alt_t), refine_iters=int(ita),
+                   rel_err_vs_fp64=float(torch.linalg.norm(ua[:, 0] - u64) / torch.linalg.norm(u64)),
+                   phases_ms=dict(leaf=tma['leaf_ms'], tree=tma['tree_ms'], interface=tma['interface_ms'],
+                                  solve_applications=tma['apply_ms'], applications=tma['n_apply']),
+                   note='default launch choices, host-clock time of one factor+solve (best of the steps)')
+        del ea, ua
+        torch.cuda.empty_cache()
+
+    eng = SlabEngine(g, args.precision)
     stream = eng.stream
     # launch choices timed on this factorization (outside the timed region)
     picks = None
@@ -474,7 +508,7 @@ def run_ours(args):
     import slablu_gb300 as sg
     op = sg.pdo.PDO_2d(sg.pdo.ones, sg.pdo.ones, c=cfg['c'])
     dom = sg.Domain_Solver(torch.tensor([[0, 1.0], [0, 1.0]]), op, cfg['kh'], problems.leaf_half_width(n, p), p=p,
-                           buf_constant=1.0, precision='mixed', tol=args.tol, max_iter=30, device=str(dev))
+                           buf_constant=1.0, precision=args.precision, tol=args.tol, max_iter=30, device=str(dev))
     dom.build('reduced_gpu', 'slabLU', verbose=False)
     if picks:
         from slablu_gb300 import autotune
@@ -534,7 +568,7 @@ def run_ours(args):
         metric=METRIC, value=value, unit='unknowns/s', n_gpus=world, steps=args.steps, warmup=args.warmup,
         ms_per_step=1e3 * t_total / args.steps, higher_is_better=True, scaling='weak', vs_baseline=None,
         dtype='f32+f64', data='synthetic',
-        config=dict(workload=workload_name(p, n, g, cfg, args.tol), buf=g.buf, Npan=g.Npan,
+        config=dict(workload=workload_name(p, n, g, cfg, args.tol, args.precision), buf=g.buf, Npan=g.Npan,
                     parallelism='replicas' if world > 1 else 'single GPU',
                     l2='inputs and factors (~17 GB) larger than L2; no flush'),
         rel_err_vs_fp64=rel_err, rel_err_vs_oracle=rel_oracle, rel_err_vs_oracle_e2e=rel_oracle_e2e,
@@ -547,7 +581,8 @@ def run_ours(args):
         phases_ms=dict(leaf=leaf_avg * 1e3, tree=sum(tree_ms) / len(tree_ms), interface=iface_avg * 1e3,
                        solve_applications=sum(apply_ms) / len(apply_ms), applications=sum(napply) / len(napply),
                        fp64_leaf=tim64['leaf_ms'], fp64_tree=tim64['tree_ms'], fp64_interface=tim64['interface_ms']),
-        # FP64 flops of the interface factorization / its time; in the mixed mode the big
+        # FP64-equivalent flops of the interface factorization / its time (FP32 flops in
+        # the fp32 mode); in the mixed mode the big
         # products run as exactly sliced BF16 products on the tcgen05 tensor cores
         interface_fp64_equiv_tflops=if_fl / iface_avg / 1e12,
         roofline=dict(kernel='leaf_factor_kernel<float> (one launch per step)', bound='tensor', achieved=achieved,
@@ -572,6 +607,8 @@ def run_ours(args):
         reference_measured=reference_measured(),
         autotune=picks,
         multi_rhs=multi,
+        precision=args.precision,
+        other_precision=alt,
     )
     del eng
     torch.cuda.empty_cache()
@@ -598,7 +635,7 @@ def run_ours(args):
     # HBS compression of the interface blocks) stands in where that fixture is absent
     primary = rel_oracle.get('superLU', rel_oracle.get('slabLU'))
     if rel_err > 1e-6:
-        line['invalid'] = f'mixed vs FP64 relative error {rel_err:.2e} > 1e-6'
+        line['invalid'] = f'{args.precision} vs FP64 relative error {rel_err:.2e} > 1e-6'
     elif primary is not None and primary > 1e-6:
         line['invalid'] = f'relative error against the FP64 oracle {primary:.2e} > 1e-6'
     if rank == 0:

@@ -336,6 +336,11 @@ int slab_csr_spmv(int nrows, const long long* d_indptr, const int* d_indices, co
  *                        256-row diagonal blocks of L and U, every product on the
  *                        tensor cores; 0 solves inside each 256-row block with
  *                        FP64-core triangular solves of 64-row blocks
+ *   SLAB_OPT_IFACE_PANEL interface block LU (fp32 engines): 0 factors each
+ *                        32-column pivoted panel of up to 1536 rows in one CTA
+ *                        (one block barrier per column; taller panels in a
+ *                        cluster), 1 every panel in a thread-block cluster (one
+ *                        cluster barrier per column); same pivots and factors
  * set returns a status; get returns the value (or a negative status). */
 #define SLAB_OPT_LEAF_CTAS 1
 #define SLAB_OPT_IFACE_SOLVE 2
@@ -343,6 +348,7 @@ int slab_csr_spmv(int nrows, const long long* d_indptr, const int* d_indices, co
 #define SLAB_OPT_TREE_TC 4
 #define SLAB_OPT_LEAF_ASSEMBLY 5
 #define SLAB_OPT_IFACE_OUTER_INV 6
+#define SLAB_OPT_IFACE_PANEL 7
 int slab_engine_set_option(slab_engine* e, int key, int value);
 int slab_engine_get_option(const slab_engine* e, int key);
 

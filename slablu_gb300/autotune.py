@@ -24,6 +24,7 @@ TUNABLES = {
     'tree_tc': (_lib.SLAB_OPT_TREE_TC, (0, 1)),
     'leaf_assembly': (_lib.SLAB_OPT_LEAF_ASSEMBLY, (1, 0)),
     'iface_outer_inv': (_lib.SLAB_OPT_IFACE_OUTER_INV, (1, 0)),
+    'iface_panel': (_lib.SLAB_OPT_IFACE_PANEL, (0, 1)),
 }
 
 
@@ -160,6 +161,15 @@ def tune(engine, coeffs, bnd, reps=2, use_cache=True, path=None, tol=1e-6):
         picks['iface_lookahead'] = min(cands, key=lambda v: (t_if[v], cands.index(v)))
         timings['interface_ms'] = {str(v): t for v, t in t_if.items()}
         _lib.check(engine.L.slab_engine_set_option(engine.h, key, picks['iface_lookahead']), 'slab_engine_set_option')
+    if engine.geom.Npan > 1 and engine.precision == 'fp32':
+        key, cands = TUNABLES['iface_panel']
+        t_pn = {}
+        for v in cands:
+            _lib.check(engine.L.slab_engine_set_option(engine.h, key, v), 'slab_engine_set_option')
+            t_pn[v] = _time_interface(engine, coeffs, reps)
+        picks['iface_panel'] = min(cands, key=lambda v: (t_pn[v], cands.index(v)))
+        timings['iface_panel_ms'] = {str(v): t for v, t in t_pn.items()}
+        _lib.check(engine.L.slab_engine_set_option(engine.h, key, picks['iface_panel']), 'slab_engine_set_option')
     if engine.precision != 'fp64':
         key, cands = TUNABLES['tree_tc']
         t_tc = {}

@@ -430,15 +430,274 @@ int getrs_batched(cudaStream_t s, int n, int nrhs, const T* LU, const long long*
   return SLAB_OK;
 }
 
+// Pivoted FP32 panel (rows k0..n, columns k0..k0+nb, nb <= 32) in ONE CTA of NT
+// threads, for m = n - k0 <= 4 NT: thread t owns the physical rows t and t + NT
+// in registers and t + 2NT, t + 3NT in shared memory (column-major, ld 2NT).
+// The register rows are kept rotated -- entry k holds column j + k at step j, so
+// the current column is entry 0 and every register index is static -- and turn
+// once per step; the j loop is unrolled by four so that the compiler renames
+// three of the four turns away.  One __syncthreads per column: the owner of
+// each warp's best candidate (magnitude key, then the smaller logical index)
+// publishes the candidate row, rotated and zero-padded, in a double-buffered
+// slot; after the barrier every warp reduces the slots itself, relabels the
+// interchange, forms its multipliers and updates its rows (register rows with
+// all 31 FMAs against the zero padding, shared-memory rows with exactly the
+// 31 - j columns left).  A slot buffer is rewritten two columns later, after a
+// barrier that every reader of it has passed.  The pivot sequence is LAPACK's,
+// and each entry sees the same operations in the same order as in
+// biglu_panel_cluster_kernel, so both give the same factors.  At the end each
+// thread writes its rows to their logical positions, and L11^{-1} goes to linv.
+// above this height the cluster kernel is faster
+constexpr int kPanelCtaMaxRows = 1536;
+template <int NT>
+__host__ __device__ inline size_t panel_cta_smem_bytes() {
+  constexpr int NW = NT / 32;
+  return ((size_t)2 * NT * kNB + 2 * NW * kNB + 2 * (size_t)kNB * (kNB + 1)) * sizeof(float) +
+         2 * NW * (sizeof(unsigned) + sizeof(int));
+}
+
+// x[c * LDS] -= l * p[c - j] for c = j+1 .. 31, exactly the columns left (x:
+// column 0 of a shared-memory row; p: the rotated pivot row)
+template <int LDS>
+__device__ __forceinline__ void smem_row_update(float* x, int j, float l, const float* p) {
+  float* y = x + j * LDS;
+  switch (31 - j) {
+#define SLAB_PANEL_UPD(K) \
+  case K:                 \
+    y[K * LDS] -= l * p[K];
+    SLAB_PANEL_UPD(31) SLAB_PANEL_UPD(30) SLAB_PANEL_UPD(29) SLAB_PANEL_UPD(28) SLAB_PANEL_UPD(27)
+    SLAB_PANEL_UPD(26) SLAB_PANEL_UPD(25) SLAB_PANEL_UPD(24) SLAB_PANEL_UPD(23) SLAB_PANEL_UPD(22)
+    SLAB_PANEL_UPD(21) SLAB_PANEL_UPD(20) SLAB_PANEL_UPD(19) SLAB_PANEL_UPD(18) SLAB_PANEL_UPD(17)
+    SLAB_PANEL_UPD(16) SLAB_PANEL_UPD(15) SLAB_PANEL_UPD(14) SLAB_PANEL_UPD(13) SLAB_PANEL_UPD(12)
+    SLAB_PANEL_UPD(11) SLAB_PANEL_UPD(10) SLAB_PANEL_UPD(9) SLAB_PANEL_UPD(8) SLAB_PANEL_UPD(7)
+    SLAB_PANEL_UPD(6) SLAB_PANEL_UPD(5) SLAB_PANEL_UPD(4) SLAB_PANEL_UPD(3) SLAB_PANEL_UPD(2)
+    SLAB_PANEL_UPD(1)
+#undef SLAB_PANEL_UPD
+    default:
+      break;
+  }
+}
+
+template <int NT>
+__global__ void __launch_bounds__(NT, 1)
+    biglu_panel_cta_kernel(float* A, int lda, int n, int k0, int nb, int* ipiv, int* info, float* linv) {
+  constexpr int NW = NT / 32, LDS = 2 * NT, W = kNB;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float* S = reinterpret_cast<float*>(smem_raw);  // LDS x W: physical rows 2NT .. 4NT-1
+  float* srow = S + (size_t)LDS * W;             // [2][NW][W]: pivot candidates, rotated (entry k = column j + k)
+  float* Ls = srow + 2 * NW * W;
+  float* Xs = Ls + W * (W + 1);
+  unsigned* skey = reinterpret_cast<unsigned*>(Xs + W * (W + 1));
+  int* sli = reinterpret_cast<int*>(skey + 2 * NW);
+  const int m = n - k0;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  float r0[W], r1[W];
+  int li0 = tid < m ? tid : INT_MAX, li1 = tid + NT < m ? tid + NT : INT_MAX;
+  int li2 = tid + 2 * NT < m ? tid + 2 * NT : INT_MAX, li3 = tid + 3 * NT < m ? tid + 3 * NT : INT_MAX;
+  float* s2 = S + tid;
+  float* s3 = S + tid + NT;
+#pragma unroll
+  for (int c = 0; c < W; ++c) {
+    const float* col = A + (size_t)(k0 + c) * lda + k0;
+    const bool cv = c < nb;
+    r0[c] = cv && li0 != INT_MAX ? col[tid] : 0.f;
+    r1[c] = cv && li1 != INT_MAX ? col[tid + NT] : 0.f;
+    s2[c * LDS] = cv && li2 != INT_MAX ? col[tid + 2 * NT] : 0.f;
+    s3[c * LDS] = cv && li3 != INT_MAX ? col[tid + 3 * NT] : 0.f;
+  }
+  __syncthreads();
+  const int steps = min(nb, m);
+  const int steps4 = (steps + 3) & ~3;  // register rows rotate once per step, padded steps included
+#pragma unroll 1
+  for (int j0 = 0; j0 < steps4; j0 += 4) {
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int j = j0 + u;
+      if (j < steps) {
+        const int buf = j & 1;
+        unsigned kb = 0;
+        int ib = INT_MAX;
+        auto cand = [&](unsigned k, int i) {
+          if (i >= j && (k > kb || (k == kb && i < ib))) {
+            kb = k;
+            ib = i;
+          }
+        };
+        cand(mag_key(r0[0]), li0);
+        cand(mag_key(r1[0]), li1);
+        cand(mag_key(s2[j * LDS]), li2);
+        cand(mag_key(s3[j * LDS]), li3);
+        const unsigned kw = __reduce_max_sync(0xffffffffu, kb);
+        const int iw = __reduce_min_sync(0xffffffffu, kb == kw ? ib : INT_MAX);
+        if (iw != INT_MAX && ib == iw) {
+          float4* dst = reinterpret_cast<float4*>(srow + (buf * NW + warp) * W);
+          float v[W];
+          if (li0 == iw || li1 == iw) {
+            const bool z = li0 == iw;
+#pragma unroll
+            for (int k = 0; k < W; ++k) v[k] = k < W - j ? (z ? r0[k] : r1[k]) : 0.f;
+          } else {
+            const float* src = (li2 == iw ? s2 : s3) + j * LDS;
+#pragma unroll
+            for (int k = 0; k < W; ++k) v[k] = k < W - j ? src[k * LDS] : 0.f;
+          }
+#pragma unroll
+          for (int k = 0; k < W / 4; ++k) dst[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
+        }
+        if (lane == 0) {
+          skey[buf * NW + warp] = kw;
+          sli[buf * NW + warp] = iw;
+        }
+        __syncthreads();
+        const unsigned sk = lane < NW ? skey[buf * NW + lane] : 0u;
+        const int si = lane < NW ? sli[buf * NW + lane] : INT_MAX;
+        const unsigned kc = __reduce_max_sync(0xffffffffu, sk);
+        const int ic = __reduce_min_sync(0xffffffffu, sk == kc ? si : INT_MAX);
+        const unsigned wm = __ballot_sync(0xffffffffu, lane < NW && si == ic && ic != INT_MAX);
+        const int wwin = wm ? __ffs(wm) - 1 : 0;
+        const int piv = ic == INT_MAX ? j : ic;
+        const float4* p4 = reinterpret_cast<const float4*>(srow + (buf * NW + wwin) * W);
+        float pv[W];
+#pragma unroll
+        for (int k = 0; k < W / 4; ++k) {
+          const float4 t = p4[k];
+          pv[4 * k] = t.x;
+          pv[4 * k + 1] = t.y;
+          pv[4 * k + 2] = t.z;
+          pv[4 * k + 3] = t.w;
+        }
+        if (tid == 0) ipiv[k0 + j] = k0 + piv;
+        const bool ok = ic != INT_MAX && mag_key(pv[0]) != 0;
+        if (!ok && tid == 0 && info && *info == 0) *info = k0 + j + 1;
+        auto relabel = [&](int& x) {
+          if (x == INT_MAX) return;
+          if (x == piv)
+            x = j;
+          else if (x == j)
+            x = piv;
+        };
+        relabel(li0);
+        relabel(li1);
+        relabel(li2);
+        relabel(li3);
+        if (ok) {
+          const float rd = recip_newton(pv[0]);
+          if (li0 > j && li0 != INT_MAX) {
+            const float l = r0[0] * rd;
+            r0[0] = l;
+#pragma unroll
+            for (int k = 1; k < W; ++k) r0[k] -= l * pv[k];
+          }
+          if (li1 > j && li1 != INT_MAX) {
+            const float l = r1[0] * rd;
+            r1[0] = l;
+#pragma unroll
+            for (int k = 1; k < W; ++k) r1[k] -= l * pv[k];
+          }
+          if (li2 > j && li2 != INT_MAX) {
+            const float l = s2[j * LDS] * rd;
+            s2[j * LDS] = l;
+            smem_row_update<LDS>(s2, j, l, pv);
+          }
+          if (li3 > j && li3 != INT_MAX) {
+            const float l = s3[j * LDS] * rd;
+            s3[j * LDS] = l;
+            smem_row_update<LDS>(s3, j, l, pv);
+          }
+        }
+      }
+      // rotate the register rows by one (padded steps rotate too)
+      const float t0 = r0[0], t1 = r1[0];
+#pragma unroll
+      for (int k = 0; k < W - 1; ++k) {
+        r0[k] = r0[k + 1];
+        r1[k] = r1[k + 1];
+      }
+      r0[W - 1] = t0;
+      r1[W - 1] = t1;
+    }
+  }
+  __syncthreads();
+  // r[k] holds column (k + steps4) mod W
+#pragma unroll
+  for (int k = 0; k < W; ++k) {
+    const int c = (k + steps4) & (W - 1);
+    if (c >= nb) continue;
+    float* col = A + (size_t)(k0 + c) * lda + k0;
+    if (li0 != INT_MAX) col[li0] = r0[k];
+    if (li1 != INT_MAX) col[li1] = r1[k];
+  }
+  for (int c = 0; c < nb; ++c) {
+    float* col = A + (size_t)(k0 + c) * lda + k0;
+    if (li2 != INT_MAX) col[li2] = s2[c * LDS];
+    if (li3 != INT_MAX) col[li3] = s3[c * LDS];
+  }
+  if (linv && nb <= m) {
+    constexpr int ldx = W + 1;
+#pragma unroll
+    for (int k = 0; k < W; ++k) {
+      const int c = (k + steps4) & (W - 1);
+      if (c >= nb) continue;
+      if (li0 < nb) Ls[li0 + c * ldx] = r0[k];
+      if (li1 < nb) Ls[li1 + c * ldx] = r1[k];
+    }
+    for (int c = 0; c < nb; ++c) {
+      if (li2 < nb) Ls[li2 + c * ldx] = s2[c * LDS];
+      if (li3 < nb) Ls[li3 + c * ldx] = s3[c * LDS];
+    }
+    __syncthreads();
+    constexpr int kCols = 4;
+    for (int c0 = warp * kCols; c0 < nb; c0 += NW * kCols) {
+      float x[kCols];
+#pragma unroll
+      for (int q = 0; q < kCols; ++q) x[q] = lane == c0 + q ? 1.f : 0.f;
+      for (int k = c0; k < nb - 1; ++k) {
+        const float lik = lane > k && lane < nb ? Ls[lane + k * ldx] : 0.f;
+#pragma unroll
+        for (int q = 0; q < kCols; ++q) {
+          const float xk = __shfl_sync(0xffffffffu, x[q], k);
+          x[q] -= lik * xk;
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < kCols; ++q)
+        if (c0 + q < nb && lane < nb) Xs[lane + (c0 + q) * ldx] = x[q];
+    }
+    __syncthreads();
+    for (int idx = tid; idx < nb * nb; idx += NT) linv[idx] = Xs[(idx % nb) + (idx / nb) * ldx];
+  }
+}
+
 namespace {
-// Panel factorization: distributed shared memory of one 16-CTA (or 8-CTA)
-// cluster (one panel row per thread) when the panel fits, the global-memory
-// kernel otherwise.
+// Panel factorization: an FP32 panel of up to kPanelCtaMaxRows rows in one CTA
+// (kind 0), else distributed shared memory of one 16-CTA (or 8-CTA) cluster
+// (one panel row per thread) when the panel fits, the global-memory kernel
+// otherwise.
 template <typename T>
 int panel_factor(cudaStream_t s, T* A, int lda, int n, int k0, int nb, int* ipiv, int* info, T* linv,
-                 bool* linv_done) {
+                 bool* linv_done, int kind) {
   *linv_done = false;
   const int m = n - k0;
+  if constexpr (std::is_same<T, float>::value) {
+    // measured per panel on GB300 (32 columns): the cluster kernel ~69 us at any
+    // height; one CTA 75 us at 2000 rows, 65 at 1500, 59 at 1000, 43 at 500 (256
+    // threads), 36 at 100 (128 threads)
+    if (kind == 0 && m <= kPanelCtaMaxRows && m >= nb && nb <= kNB) {
+      if (m > 512) {
+        SLAB_TRY(ensure_smem(biglu_panel_cta_kernel<512>, panel_cta_smem_bytes<512>(), "biglu_panel_cta"));
+        biglu_panel_cta_kernel<512><<<1, 512, panel_cta_smem_bytes<512>(), s>>>(A, lda, n, k0, nb, ipiv, info, linv);
+      } else if (m > 256) {
+        SLAB_TRY(ensure_smem(biglu_panel_cta_kernel<256>, panel_cta_smem_bytes<256>(), "biglu_panel_cta"));
+        biglu_panel_cta_kernel<256><<<1, 256, panel_cta_smem_bytes<256>(), s>>>(A, lda, n, k0, nb, ipiv, info, linv);
+      } else {
+        SLAB_TRY(ensure_smem(biglu_panel_cta_kernel<128>, panel_cta_smem_bytes<128>(), "biglu_panel_cta"));
+        biglu_panel_cta_kernel<128><<<1, 128, panel_cta_smem_bytes<128>(), s>>>(A, lda, n, k0, nb, ipiv, info, linv);
+      }
+      SLAB_CHECK_LAUNCH();
+      *linv_done = linv != nullptr;
+      return SLAB_OK;
+    }
+  }
   const void* kern = reinterpret_cast<const void*>(biglu_panel_cluster_kernel<T>);
   const size_t lim = allow_dynamic_smem(kern);
   int CL = cluster_size_for(kern, panel_cluster_smem_bytes(m, nb, ceil_div(m, 16), sizeof(T)), 256);
@@ -486,7 +745,7 @@ int trsm_inv(cudaStream_t s, const T* Inv, int bs, int k0, int nb, T* X, int ldx
 template <typename T>
 int biglu_panel_swap(cudaStream_t s, T* A, int lda, int n, int k0, int nb, int* ipiv, int* info, T* linv,
                      bool* linv_done) {
-  SLAB_TRY(panel_factor<T>(s, A, lda, n, k0, nb, ipiv, info, linv, linv_done));
+  SLAB_TRY(panel_factor<T>(s, A, lda, n, k0, nb, ipiv, info, linv, linv_done, 0));
   if (n - nb > 0) {
     biglu_swap_kernel<T><<<ceil_div(n - nb, 256), 256, 0, s>>>(A, lda, n, k0, nb, ipiv);
     SLAB_CHECK_LAUNCH();
@@ -496,7 +755,7 @@ int biglu_panel_swap(cudaStream_t s, T* A, int lda, int n, int k0, int nb, int* 
 template <typename T>
 int biglu_panel_swap_range(cudaStream_t s, T* A, int lda, int n, int k0, int nb, int c_lo, int c_hi, int* ipiv,
                            int* info, T* linv, bool* linv_done) {
-  SLAB_TRY(panel_factor<T>(s, A, lda, n, k0, nb, ipiv, info, linv, linv_done));
+  SLAB_TRY(panel_factor<T>(s, A, lda, n, k0, nb, ipiv, info, linv, linv_done, 0));
   const int ncols = (c_hi - c_lo) - nb;  // the panel lies inside [c_lo, c_hi)
   if (ncols > 0) {
     swap_cols_kernel<T><<<ceil_div(ncols, 128), 128, 0, s>>>(A, lda, c_lo, c_hi, k0, nb, ipiv);
@@ -559,11 +818,11 @@ template int biglu_panel_swap<float>(cudaStream_t, float*, int, int, int, int, i
 template int biglu_panel_swap<double>(cudaStream_t, double*, int, int, int, int, int*, int*, double*, bool*);
 
 template <typename T>
-int biglu(cudaStream_t s, T* A, int lda, int n, int* ipiv, int* info, T* work) {
+int biglu(cudaStream_t s, T* A, int lda, int n, int* ipiv, int* info, T* work, int panel_kind) {
   for (int k0 = 0; k0 < n; k0 += kNB) {
     const int nb = n - k0 < kNB ? n - k0 : kNB;
     bool linv_done = false;
-    SLAB_TRY(panel_factor<T>(s, A, lda, n, k0, nb, ipiv, info, work, &linv_done));
+    SLAB_TRY(panel_factor<T>(s, A, lda, n, k0, nb, ipiv, info, work, &linv_done, panel_kind));
     if (n - nb > 0) {
       biglu_swap_kernel<T><<<ceil_div(n - nb, 256), 256, 0, s>>>(A, lda, n, k0, nb, ipiv);
       SLAB_CHECK_LAUNCH();
@@ -659,7 +918,7 @@ int bigtrs(cudaStream_t s, const T* LU, int lda, int n, const int* perm, const T
   template int getrs_batched<T>(cudaStream_t, int, int, const T*, const long long*, long long, int,           \
                                 const int*, const long long*, long long, T*, const long long*, long long,     \
                                 int, int, bool, bool);                                                        \
-  template int biglu<T>(cudaStream_t, T*, int, int, int*, int*, T*);                                          \
+  template int biglu<T>(cudaStream_t, T*, int, int, int*, int*, T*, int);                                          \
   template int tri_inv_blocks<T>(cudaStream_t, const T*, int, int, int, T*, T*);                              \
   template int bigtrs_inv<T>(cudaStream_t, const T*, int, int, const int*, const T*, const T*, int, const T*,  \
                              int, T*, int, int);                                                              \

@@ -1967,8 +1967,10 @@ int getrs_batched(cudaStream_t s, int n, int nrhs, const T* LU, const long long*
 
 // Large single-matrix LU in place (n x n, lda); ipiv/info device pointers.
 // work: kNB*kNB elements (inverse of the current panel's unit-lower triangle).
+// panel_kind 0: FP32 panels of up to 1536 rows in one CTA; 1: always
+// the cluster panel kernel (same pivots and factors).
 template <typename T>
-int biglu(cudaStream_t s, T* A, int lda, int n, int* ipiv, int* info, T* work = nullptr);
+int biglu(cudaStream_t s, T* A, int lda, int n, int* ipiv, int* info, T* work = nullptr, int panel_kind = 0);
 
 // Inverses of the bs x bs diagonal triangles of a factored matrix:
 // Linv/Uinv hold ceil(n/bs) blocks of bs x bs each.

@@ -366,6 +366,7 @@ struct EngineImpl : EngineBase {
   int gapp_nrhs = 0, gapp_t_nrhs = 0;
   bool use_graphs = true;
   bool use_cluster_solve = true;
+  int panel_kind = 0;  // SLAB_OPT_IFACE_PANEL
   int leaf_ctas = 0;  // resident leaves per SM in the leaf kernel (0: as many as fit)
   bool leaf_split_asm = false;  // leaf operators assembled by a kernel of their own (no c12)
   DevBuf D, Dsq, Nx, NxcT, NxxT, interp, jxr, leafglob, dirmask;
@@ -556,9 +557,19 @@ struct EngineImpl : EngineBase {
       use_tc_tree = value == 1;
       return SLAB_OK;
     }
+    if (key == SLAB_OPT_IFACE_PANEL) {
+      if (value != 0 && value != 1) return set_error(SLAB_ERR_ARG, "iface_panel %d not 0 or 1", value);
+      if (value != panel_kind && gfac[2]) {
+        cudaGraphExecDestroy(gfac[2]);
+        gfac[2] = nullptr;
+      }
+      panel_kind = value;
+      return SLAB_OK;
+    }
     return set_error(SLAB_ERR_ARG, "unknown option %d", key);
   }
   int get_option(int key) const override {
+    if (key == SLAB_OPT_IFACE_PANEL) return panel_kind;
     if (key == SLAB_OPT_TREE_TC) return use_tc_tree ? 1 : 0;
     if (key == SLAB_OPT_LEAF_ASSEMBLY) return leaf_split_asm ? 1 : 0;
     if (key == SLAB_OPT_IFACE_OUTER_INV) return use_outer_inv ? 1 : 0;
@@ -578,6 +589,8 @@ struct EngineImpl : EngineBase {
     use_cluster_solve = !(nc && nc[0] == '1');
     const char* lc = getenv("SLAB_LEAF_CTAS");
     if (lc) leaf_ctas = atoi(lc);
+    const char* ip = getenv("SLAB_IFACE_PANEL");  // 1: cluster panels for the FP32 interface
+    if (ip) panel_kind = ip[0] == '1' ? 1 : 0;
     const char* la = getenv("SLAB_LEAF_ASSEMBLY");  // 1: assembly by a kernel of its own
     if (la) leaf_split_asm = la[0] == '1';
     const char* oi = getenv("SLAB_IFACE_OUTER_INV");  // 0: FP64-core triangular solves of 64-row blocks
@@ -1106,7 +1119,8 @@ struct EngineImpl : EngineBase {
           }
         }
         if (!done)
-          SLAB_TRY(biglu<TI>(s, Sj, nI, nI, ifPiv.as<int>() + (long long)nI * j, ifInfo.as<int>(), ifWork.as<TI>()));
+          SLAB_TRY(biglu<TI>(s, Sj, nI, nI, ifPiv.as<int>() + (long long)nI * j, ifInfo.as<int>(), ifWork.as<TI>(),
+                             panel_kind));
         SLAB_TRY(build_perm(s, ifPiv.as<int>() + (long long)nI * j, nI, ifPerm.as<int>() + (long long)nI * j));
         SLAB_TRY(tri_inv_blocks<TI>(s, Sj, nI, nI, kInvBs, linv(j), uinv(j)));
         if constexpr (std::is_same<TI, double>::value) {

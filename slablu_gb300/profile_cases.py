@@ -4,6 +4,7 @@
     python -m slablu_gb300.profile_cases solve  --n 2000 --precision mixed --iters 1
     python -m slablu_gb300.profile_cases dgemm  --n 2000 --reps 2
     python -m slablu_gb300.profile_cases sgemm  --n 4000 --k 200 --batch 10 --reps 2
+    python -m slablu_gb300.profile_cases graph  --n 400 --count 8 --reps 3
 
 `factor` and `solve` use the Gaussian-lattice Helmholtz field of the benchmark
 (p = 22) on an n x n-point grid ((n/20)^2 leaves): one factorization, and for
@@ -11,7 +12,10 @@
 tensor-core FP64 products C = A B of n x n random matrices (the shape of the
 interface Schur update at n = 2000); `sgemm` runs --reps batched TF32-split FP32
 products C -= A B with A n x k and B k x n (--batch of them: the shape of the
-top merge level's Schur updates at N = 4.4M).
+top merge level's Schur updates at N = 4.4M); `graph` factors --count engines of
+alternating sizes (n and n/2 points a side) and times their refined solves
+(u = 1 on the boundary, tol 1e-10) one after another through slab_engine_solve
+against one launch of a SolveGraph over all of them.
 """
 import argparse
 
@@ -23,14 +27,17 @@ from .engine import SlabEngine
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument('case', choices=['factor', 'solve', 'dgemm', 'sgemm'])
+    ap.add_argument('case', choices=['factor', 'solve', 'dgemm', 'sgemm', 'graph'])
     ap.add_argument('--n', type=int, default=640)
     ap.add_argument('--precision', default='mixed', choices=['fp64', 'mixed', 'fp32'])
     ap.add_argument('--iters', type=int, default=1)
     ap.add_argument('--reps', type=int, default=2)
     ap.add_argument('--k', type=int, default=200)
     ap.add_argument('--batch', type=int, default=10)
+    ap.add_argument('--count', type=int, default=8)
     a = ap.parse_args(argv)
+    if a.case == 'graph':
+        return _graph_case(a)
     if a.case == 'sgemm':
         from .dgemm import sgemm_tc
         gen = torch.Generator(device='cuda').manual_seed(1)
@@ -73,10 +80,49 @@ def main(argv=None):
     eng = SlabEngine(g, a.precision)
     eng.factor(c11=one, c22=one, c=c)
     if a.case == 'solve':
-        eng.solve(torch.ones(g.ntot, dtype=torch.float64, device='cuda'), tol=1e-10, max_iter=a.iters,
-                  allow_noconv=True)
+        _, _, it, info = eng.solve(torch.ones(g.ntot, dtype=torch.float64, device='cuda'), tol=1e-10,
+                                   max_iter=a.iters, allow_noconv=True)
+        print('refinement steps', it, info)
     torch.cuda.synchronize()
     print('ok', a.case, g.nboxes, 'leaves', eng.timings())
+
+
+def _graph_case(a):
+    from .engine import SolveGraph
+    cfg = problems.config3()
+    p = cfg['p']
+    engines, bnds = [], []
+    for i in range(a.count):
+        n = a.n if i % 2 == 0 else max(20, (a.n // 40) * 20)
+        g = hps.Geometry([[0, 1], [0, 1]], problems.leaf_half_width(n, p), p, 1.0)
+        c = cfg['c'](torch.as_tensor(g.xx_tot, device='cuda')).contiguous()
+        eng = SlabEngine(g, a.precision)
+        eng.factor(c11=torch.ones_like(c), c22=torch.ones_like(c), c=c)
+        engines.append(eng)
+        bnds.append(torch.ones(g.ntot, dtype=torch.float64, device='cuda'))
+    graph = SolveGraph(engines, nrhs=1, tol=1e-10, max_iter=40)
+    for i, b in enumerate(bnds):
+        graph.set_inputs(i, b)
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1)
+    seq, one = [], []
+    for _ in range(a.reps + 1):
+        seq.append(timed(lambda: [e.solve(b, tol=1e-10, max_iter=40) for e, b in zip(engines, bnds)]))
+        one.append(timed(lambda: (graph.launch(), [graph.result(i) for i in range(len(engines))])))
+    its = [graph.result(i)[1] for i in range(len(engines))]
+    err = max(float(torch.linalg.norm(graph.result(i)[0][:, 0] - e.solve(b, tol=1e-10, max_iter=40)[0][:, 0]) /
+                    torch.linalg.norm(graph.result(i)[0]))
+              for i, (e, b) in enumerate(zip(engines, bnds)))
+    print('ok graph', a.count, 'engines', [e.nleaf for e in engines], 'leaves; steps', its,
+          '; ms one after another', [round(t, 3) for t in seq[1:]], '; ms one graph', [round(t, 3) for t in one[1:]],
+          '; max rel difference', err)
 
 
 if __name__ == '__main__':

@@ -46,7 +46,7 @@ def _rel(sol, g, key='sol'):
     return float(np.linalg.norm(sol[::stride] - ref) / np.linalg.norm(ref))
 
 
-@pytest.mark.parametrize('precision', ['fp64', 'mixed'])
+@pytest.mark.parametrize('precision', ['fp64', 'mixed', 'fp32'])
 def test_config1_plane_waves(precision):
     from slablu_gb300 import problems
     g = np.load(os.path.join(GOLD, 'config1_slabLU_p12_n400.npz'))
@@ -110,13 +110,22 @@ def config3_mixed():
     return cfg, _solver(cfg, 'mixed', tol=1e-6)
 
 
+@pytest.fixture(scope='module')
+def config3_fp32():
+    from slablu_gb300 import problems
+    cfg = problems.config3()
+    return cfg, _solver(cfg, 'fp32', tol=1e-6)
+
+
+@pytest.mark.parametrize('precision', ['fp32', 'mixed'])
 @pytest.mark.parametrize('solver', ['superLU', 'slabLU'])
-def test_config3_mixed_against_reference(config3_mixed, solver):
+def test_config3_reduced_precision_against_reference(request, precision, solver):
     """The benchmark's workload and refinement tolerance (1e-6 on the relative
-    correction): the leaf-node solution within the metric's 1e-6 of the
-    reference's FP64 solutions at N = 4,404,000 (its superLU sparse direct solve
-    and its slabLU, which differ from each other by 4e-8)."""
-    cfg, dom = config3_mixed
+    correction), with every factor in FP32 (the benchmark's mode) and with the
+    FP64 interface factorization: the leaf-node solution within the metric's 1e-6
+    of the reference's FP64 solutions at N = 4,404,000 (its superLU sparse direct
+    solve and its slabLU, which differ from each other by 4e-8)."""
+    cfg, dom = request.getfixturevalue(f'config3_{precision}')
     g = np.load(os.path.join(GOLD, f'config3_{solver}_p22_n2000.npz'))
     sol, rel, _, _, _ = dom.solve(cfg['uu_dir'], None)
     sol = sol.numpy()[:, 0]
@@ -139,11 +148,12 @@ def test_config3_fp64_against_superlu():
     torch.cuda.empty_cache()
 
 
-def test_config4_columns_against_reference(config3_mixed):
+def test_config4_columns_against_reference(config3_fp32):
     """Config 4's smoothed random boundary data (columns 0 and 255 of the 256) on the
-    config-3 factorization, solved together, against the reference's solutions."""
+    config-3 factorization (FP32 factors, as in the benchmark), solved together,
+    against the reference's solutions."""
     from slablu_gb300 import problems
-    cfg, dom = config3_mixed
+    cfg, dom = config3_fp32
     g = np.load(os.path.join(GOLD, 'config3_slabLU_p22_n2000.npz'))
     B = problems.config4_rhs(int(g['nbnd']), 256)
     cols = [int(c) for c in g['rhs_cols']]

@@ -91,3 +91,43 @@ def test_outer_inverse_schur_solves_match_fp64_core_solves_and_oracle(nblocks):
     assert diff < 1e-11, diff
     rel = np.linalg.norm(sols[1] - ref) / np.linalg.norm(ref)
     assert rel < 1e-9, rel
+
+
+def test_fp32_panel_in_one_cta_matches_cluster_panel():
+    """FP32 interface panels factored in one CTA (SLAB_OPT_IFACE_PANEL 0) against
+    the thread-block-cluster kernel (1): the same pivot sequence and operations,
+    so the same factors.  Interface blocks of 2,080 unknowns (520 leaves of p = 6
+    per slab interface, two interfaces): the first panels are taller than the
+    one-CTA kernel takes (1,536 rows) and go to the cluster kernel, the rest use
+    512 threads with shared-memory rows (above 1,024 rows), 512, 256 and 128
+    threads with register rows only."""
+    from slablu_gb300 import _lib, hps
+    from slablu_gb300.engine import SlabEngine
+    p, kh, n1 = 6, 20.0, 520
+    a = 1 / (2 * n1)
+    geom = [[0, 6 * 2 * a], [0, 1]]  # 6 x 520 leaves, three slabs of two leaf columns
+    g = hps.Geometry(geom, a, p, 0.02)
+    assert g.Npan == 3 and g.n1 * g.q == 2080
+    xx = torch.as_tensor(g.xx_tot, device='cuda')
+    c = (-kh ** 2 * (1 - 0.5 * torch.exp(-((xx[:, 0] - 0.01) ** 2 + (xx[:, 1] - 0.5) ** 2) / 0.02))).contiguous()
+    one = torch.ones_like(c)
+    gen = torch.Generator(device='cuda').manual_seed(3)
+    bnd = torch.randn(g.ntot, 2, generator=gen, device='cuda', dtype=torch.float64)
+    sols = {}
+    for kind in (1, 0):
+        eng = SlabEngine(g, 'fp32')
+        assert eng.L.slab_engine_set_option(eng.h, _lib.SLAB_OPT_IFACE_PANEL, kind) == 0
+        assert eng.L.slab_engine_get_option(eng.h, _lib.SLAB_OPT_IFACE_PANEL) == kind
+        eng.factor(c11=one, c22=one, c=c)
+        u, _, iters, st = eng.solve(bnd, tol=1e-12, max_iter=60)
+        assert st['converged'], (kind, iters, st)
+        sols[kind] = (u.cpu().numpy(), iters)
+    e64 = SlabEngine(g, 'fp64')
+    e64.factor(c11=one, c22=one, c=c)
+    u64 = e64.solve(bnd, tol=1e-13, max_iter=10)[0].cpu().numpy()
+    assert sols[0][1] == sols[1][1]
+    diff = np.linalg.norm(sols[0][0] - sols[1][0]) / np.linalg.norm(sols[1][0])
+    assert diff < 1e-11, diff
+    for kind in (0, 1):
+        rel = np.linalg.norm(sols[kind][0] - u64) / np.linalg.norm(u64)
+        assert rel < 1e-9, (kind, rel)
