@@ -320,10 +320,10 @@ int slab_csr_spmv(int nrows, const long long* d_indptr, const int* d_indices, co
  *                        as fit (fewer keep more of each leaf matrix in L2)
  *   SLAB_OPT_IFACE_SOLVE interface triangular solves: 0 one thread-block cluster,
  *                        1 grid-wide cooperative kernel
- *   SLAB_OPT_IFACE_LOOKAHEAD interface block LU (mixed precision): 1 overlaps
- *                        each outer block's update of the columns beyond the next
- *                        block with that block's panels (second stream), 0 serial;
- *                        both give the same factors
+ *   SLAB_OPT_IFACE_LOOKAHEAD interface block LU (mixed and fp32 engines): 1
+ *                        overlaps each 256-column outer block's update of the
+ *                        columns beyond the next block with that block's panels
+ *                        (second stream), 0 serial; both give the same factors
  *   SLAB_OPT_TREE_TC     FP32 merge tree (mixed and fp32 engines): 1 forms the
  *                        merges' Schur updates F -= col W as TF32-split
  *                        tensor-core products (slab_sgemm_tc), 0 on the CUDA

@@ -152,7 +152,7 @@ def tune(engine, coeffs, bnd, reps=2, use_cache=True, path=None, tol=1e-6):
         picks['iface_outer_inv'] = min(cands, key=lambda v: (t_oi[v], cands.index(v)))
         timings['iface_outer_inv_ms'] = {str(v): t for v, t in t_oi.items()}
         _lib.check(engine.L.slab_engine_set_option(engine.h, key, picks['iface_outer_inv']), 'slab_engine_set_option')
-    if engine.geom.Npan > 1 and engine.precision == 'mixed':
+    if engine.geom.Npan > 1 and engine.precision in ('mixed', 'fp32'):
         key, cands = TUNABLES['iface_lookahead']
         t_if = {}
         for v in cands:

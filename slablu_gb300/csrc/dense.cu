@@ -813,6 +813,7 @@ int laswp_gather(cudaStream_t s, T* A, int lda, int n, int k0, int npiv, const i
   return SLAB_OK;
 }
 template int laswp_gather<double>(cudaStream_t, double*, int, int, int, int, const int*, int, int, int, int, int*);
+template int laswp_gather<float>(cudaStream_t, float*, int, int, int, int, const int*, int, int, int, int, int*);
 
 template int biglu_panel_swap<float>(cudaStream_t, float*, int, int, int, int, int*, int*, float*, bool*);
 template int biglu_panel_swap<double>(cudaStream_t, double*, int, int, int, int, int*, int*, double*, bool*);
@@ -845,6 +846,87 @@ int biglu(cudaStream_t s, T* A, int lda, int n, int* ipiv, int* info, T* work, i
   }
   return SLAB_OK;
 }
+
+// A22 -= A21 L11^{-1} A12 for the nc columns c0.. of an outer block [ob0, obe):
+// U12 = L11^{-1} A12 block by block (inverted 64 x 64 diagonal triangles of the
+// unit-lower L11 in blk_linv, products below them inside the block), then one
+// (n - obe) x nc x (obe - ob0) product for the rows below the block.
+template <typename T>
+int outer_block_update(cudaStream_t s, T* A, int lda, int n, int ob0, int obe, int c0, int nc, const T* blk_linv) {
+  constexpr int kB = 64;
+  if (nc <= 0) return SLAB_OK;
+  T* A12 = A + (size_t)c0 * lda;
+  for (int b0 = ob0; b0 < obe; b0 += kB) {
+    const int bn = obe - b0 < kB ? obe - b0 : kB;
+    SLAB_TRY(trsm_inv<T>(s, blk_linv + (size_t)((b0 - ob0) / kB) * kB * kB, kB, b0, bn, A12, lda, nc));
+    const int below = obe - b0 - bn;
+    if (below > 0)
+      SLAB_TRY(gemm<T>(s, below, nc, bn, T(-1), A + (size_t)b0 * lda + b0 + bn, nullptr, 0, lda, A12 + b0, nullptr, 0,
+                       lda, T(1), A12 + b0 + bn, nullptr, 0, lda, 1));
+  }
+  if (n - obe <= 0) return SLAB_OK;
+  return gemm<T>(s, n - obe, nc, obe - ob0, T(-1), A + (size_t)ob0 * lda + obe, nullptr, 0, lda, A12 + ob0, nullptr,
+                 0, lda, T(1), A12 + obe, nullptr, 0, lda, 1);
+}
+
+template <typename T>
+int biglu_blocked(cudaStream_t s, T* A, int lda, int n, int* ipiv, int* info, T* panel_linv, T* blk_linv,
+                  int panel_kind, cudaStream_t side, cudaEvent_t fork, cudaEvent_t join, int* perm) {
+  constexpr int kOuter = 256, kB = 64;
+  const bool look = side && fork && join && perm;
+  bool side_busy = false;
+  for (int ob0 = 0; ob0 < n; ob0 += kOuter) {
+    const int obe = n - ob0 < kOuter ? n : ob0 + kOuter;
+    for (int k0 = ob0; k0 < obe; k0 += kNB) {
+      const int nb = obe - k0 < kNB ? obe - k0 : kNB;
+      bool linv_done = false;
+      SLAB_TRY(panel_factor<T>(s, A, lda, n, k0, nb, ipiv, info, panel_linv, &linv_done, panel_kind));
+      if (look) {
+        const int ncols = (obe - ob0) - nb;  // interchanges inside the outer block now, the rest after it
+        if (ncols > 0) {
+          swap_cols_kernel<T><<<ceil_div(ncols, 128), 128, 0, s>>>(A, lda, ob0, obe, k0, nb, ipiv);
+          SLAB_CHECK_LAUNCH();
+        }
+      } else if (n - nb > 0) {
+        biglu_swap_kernel<T><<<ceil_div(n - nb, 256), 256, 0, s>>>(A, lda, n, k0, nb, ipiv);
+        SLAB_CHECK_LAUNCH();
+      }
+      const int inner = obe - k0 - nb;
+      if (inner > 0) {
+        if (!linv_done) SLAB_TRY(tri_inv_blocks<T>(s, A + (size_t)k0 * lda + k0, lda, nb, kNB, panel_linv, nullptr));
+        SLAB_TRY(trsm_inv<T>(s, panel_linv, linv_done ? nb : kNB, k0, nb, A + (size_t)(k0 + nb) * lda, lda, inner));
+        SLAB_TRY(gemm<T>(s, n - k0 - nb, inner, nb, T(-1), A + (size_t)k0 * lda + k0 + nb, nullptr, 0, lda,
+                         A + (size_t)(k0 + nb) * lda + k0, nullptr, 0, lda, T(1),
+                         A + (size_t)(k0 + nb) * lda + k0 + nb, nullptr, 0, lda, 1));
+      }
+    }
+    const int rest = n - obe;
+    if (look) {
+      // the side stream's update of the previous outer block reads the columns
+      // left of ob0 and writes those right of obe: it finishes before this
+      // block's interchanges reach them
+      if (side_busy) SLAB_CUDA_TRY(cudaStreamWaitEvent(s, join, 0));
+      side_busy = false;
+      SLAB_TRY(laswp_gather<T>(s, A, lda, n, ob0, obe - ob0, ipiv, 0, ob0, obe, n, perm));
+    }
+    if (rest > 0) {
+      SLAB_TRY(tri_inv_blocks<T>(s, A + (size_t)ob0 * lda + ob0, lda, obe - ob0, kB, blk_linv, nullptr));
+      const int now = look ? (rest < kOuter ? rest : kOuter) : rest;  // the columns the next outer block needs
+      SLAB_TRY(outer_block_update<T>(s, A, lda, n, ob0, obe, obe, now, blk_linv));
+      if (now < rest) {
+        SLAB_CUDA_TRY(cudaEventRecord(fork, s));
+        SLAB_CUDA_TRY(cudaStreamWaitEvent(side, fork, 0));
+        SLAB_TRY(outer_block_update<T>(side, A, lda, n, ob0, obe, obe + now, rest - now, blk_linv));
+        SLAB_CUDA_TRY(cudaEventRecord(join, side));
+        side_busy = true;
+      }
+    }
+  }
+  if (side_busy) SLAB_CUDA_TRY(cudaStreamWaitEvent(s, join, 0));
+  return SLAB_OK;
+}
+template int biglu_blocked<float>(cudaStream_t, float*, int, int, int*, int*, float*, float*, int, cudaStream_t,
+                                  cudaEvent_t, cudaEvent_t, int*);
 
 template <typename T>
 int bigtrs_inv(cudaStream_t s, const T* LU, int lda, int n, const int* perm, const T* Linv, const T* Uinv, int bs,

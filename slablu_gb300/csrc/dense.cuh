@@ -1972,6 +1972,20 @@ int getrs_batched(cudaStream_t s, int n, int nrhs, const T* LU, const long long*
 template <typename T>
 int biglu(cudaStream_t s, T* A, int lda, int n, int* ipiv, int* info, T* work = nullptr, int panel_kind = 0);
 
+// biglu in outer blocks of 256 columns: 32-column pivoted panels (panel_kind as
+// for biglu) with their updates inside the outer block, then the update of the
+// columns beyond it through inverted 64 x 64 triangles of its L11 and one
+// product.  With side/fork/join/perm (perm: 1 + 2 * kRowpermMax ints), the
+// update of the columns beyond the next outer block runs on the side stream
+// while that block's panels are factored; the panels' interchanges reach the
+// other columns as one gather after the block.  The elimination of biglu with
+// the products grouped differently: the factors agree to rounding (and so do
+// the pivots, but for near ties).  panel_linv: kNB x kNB elements; blk_linv:
+// 256 x 64 elements.
+template <typename T>
+int biglu_blocked(cudaStream_t s, T* A, int lda, int n, int* ipiv, int* info, T* panel_linv, T* blk_linv,
+                  int panel_kind, cudaStream_t side, cudaEvent_t fork, cudaEvent_t join, int* perm);
+
 // Inverses of the bs x bs diagonal triangles of a factored matrix:
 // Linv/Uinv hold ceil(n/bs) blocks of bs x bs each.
 template <typename T>

@@ -360,13 +360,16 @@ struct EngineImpl : EngineBase {
   // low-priority stream (forked from and joined back into s)
   cudaStream_t side = nullptr;
   cudaEvent_t la_fork = nullptr, la_join = nullptr;
-  DevBuf laPerm;
+  DevBuf laPerm, ifBlkLinv;  // row-interchange gather scratch; inverted 64-row triangles of an FP32 outer block
   bool use_lookahead = true;
   cudaGraphExec_t gfac[3] = {nullptr, nullptr, nullptr}, gapp = nullptr, gapp_t = nullptr;
   int gapp_nrhs = 0, gapp_t_nrhs = 0;
   bool use_graphs = true;
   bool use_cluster_solve = true;
   int panel_kind = 0;  // SLAB_OPT_IFACE_PANEL
+  // FP32 interface blocks: 1 factors them with the unblocked biglu (SLAB_IFACE_UNBLOCKED=1,
+  // for comparison) instead of biglu_blocked
+  bool unblocked_iface = false;
   int leaf_ctas = 0;  // resident leaves per SM in the leaf kernel (0: as many as fit)
   bool leaf_split_asm = false;  // leaf operators assembled by a kernel of their own (no c12)
   DevBuf D, Dsq, Nx, NxcT, NxxT, interp, jxr, leafglob, dirmask;
@@ -589,6 +592,8 @@ struct EngineImpl : EngineBase {
     use_cluster_solve = !(nc && nc[0] == '1');
     const char* lc = getenv("SLAB_LEAF_CTAS");
     if (lc) leaf_ctas = atoi(lc);
+    const char* ub = getenv("SLAB_IFACE_UNBLOCKED");
+    unblocked_iface = ub && ub[0] == '1';
     const char* ip = getenv("SLAB_IFACE_PANEL");  // 1: cluster panels for the FP32 interface
     if (ip) panel_kind = ip[0] == '1' ? 1 : 0;
     const char* la = getenv("SLAB_LEAF_ASSEMBLY");  // 1: assembly by a kernel of its own
@@ -887,9 +892,10 @@ struct EngineImpl : EngineBase {
           SLAB_TRY(emuY.alloc((size_t)kEmuOuter * nI * sizeof(double)));
           SLAB_TRY(emuT.alloc(outer_tri_tmp_elems(nI) * sizeof(double)));
         }
-        SLAB_TRY(laPerm.alloc((size_t)(1 + 2 * kRowpermMax) * sizeof(int)));
         SLAB_CUDA_TRY(cudaMemsetAsync(emuErr.p, 0, sizeof(int), s));
       }
+      SLAB_TRY(laPerm.alloc((size_t)(1 + 2 * kRowpermMax) * sizeof(int)));
+      if (std::is_same<TI, float>::value) SLAB_TRY(ifBlkLinv.alloc((size_t)kEmuOuter * 64 * sizeof(TI)));
     }
     if (use_tc_tree) SLAB_TRY(alloc_tc_tree());
     SLAB_TRY(acc.alloc(4 * sizeof(double)));
@@ -1115,6 +1121,16 @@ struct EngineImpl : EngineBase {
             Lookahead la{use_lookahead ? side : nullptr, la_fork, la_join, laPerm.as<int>()};
             SLAB_TRY(biglu_emu(s, Sj, nI, nI, ifPiv.as<int>() + (long long)nI * j, ifInfo.as<int>(), ifWork.as<TI>(),
                                emuLinv.as<double>(), w, &la));
+            done = true;
+          }
+        }
+        if constexpr (std::is_same<TI, float>::value) {
+          if (!unblocked_iface) {
+            const bool la = use_lookahead;
+            SLAB_TRY(biglu_blocked<TI>(s, Sj, nI, nI, ifPiv.as<int>() + (long long)nI * j, ifInfo.as<int>(),
+                                       ifWork.as<TI>(), ifBlkLinv.as<TI>(), panel_kind, la ? side : nullptr,
+                                       la ? la_fork : nullptr, la ? la_join : nullptr,
+                                       la ? laPerm.as<int>() : nullptr));
             done = true;
           }
         }
