@@ -1,6 +1,7 @@
 // Host launchers for the dense building blocks (float and double).
 #include <atomic>
 #include <cstdarg>
+#include <cstdlib>
 #include <map>
 #include <mutex>
 #include <string>
@@ -307,6 +308,113 @@ static int sm_count() {
   return sms;
 }
 
+// SLAB_GEMM64=1: every FP32 product on the 64 x 64 kernel (for comparisons; read at
+// each launch, so at each graph capture)
+static bool gemm64_only() {
+  const char* e = getenv("SLAB_GEMM64");
+  return e && e[0] == '1';
+}
+
+// FP32 product C = beta*C + alpha * A B (column-major, batched like gemm_kernel)
+// with 128 x 128 output tiles: 256 threads, 8 x 8 outputs per thread (two 4-row
+// by two 4-column groups, so each k step reads four float4 from shared memory
+// for 64 FMAs), k staged 8 at a time in double-buffered shared memory; the next
+// k slice is loaded into registers while the current one is multiplied, so one
+// __syncthreads per slice.  For products whose 128-wide tiles fill the GPU.
+constexpr int kG8K = 8;
+constexpr int kG8LD = 132;  // 128 + 4: the float4 reads stay 16-byte aligned
+__global__ void __launch_bounds__(256) gemm128_kernel(int m, int n, int k, float alpha, const float* __restrict__ A,
+                                                     const long long* offA, long long strideA, int lda,
+                                                     const float* __restrict__ B, const long long* offB,
+                                                     long long strideB, int ldb, float beta, float* C,
+                                                     const long long* offC, long long strideC, int ldc) {
+  __shared__ __align__(16) float As[2][kG8K * kG8LD];
+  __shared__ __align__(16) float Bs[2][kG8K * kG8LD];
+  const int bz = blockIdx.z;
+  A += batch_off(offA, strideA, bz);
+  B += batch_off(offB, strideB, bz);
+  C += batch_off(offC, strideC, bz);
+  const int r0 = blockIdx.x * 128, c0 = blockIdx.y * 128;
+  const int tid = threadIdx.x;
+  const int tx = tid & 15, ty = tid >> 4;
+  // loads: A slice 128 x 8 (thread: rows ar + 32 q, column ak), B slice 8 x 128 (thread: row bk, columns bc + 32 q)
+  const int ar = tid & 31, ak = tid >> 5;
+  const int bk = tid & 7, bc = tid >> 3;
+  float ra[4], rb[4];
+  auto load = [&](int k0) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int gr = r0 + ar + 32 * q, gk = k0 + ak;
+      ra[q] = (gr < m && gk < k) ? A[gr + (size_t)gk * lda] : 0.f;
+      const int gc = c0 + bc + 32 * q, gk2 = k0 + bk;
+      rb[q] = (gc < n && gk2 < k) ? B[gk2 + (size_t)gc * ldb] : 0.f;
+    }
+  };
+  auto store = [&](int buf) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      As[buf][(ar + 32 * q) + ak * kG8LD] = ra[q];
+      Bs[buf][(bc + 32 * q) + bk * kG8LD] = rb[q];
+    }
+  };
+  float acc[8][8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
+  const int nk = (k + kG8K - 1) / kG8K;
+  if (nk > 0) {
+    load(0);
+    store(0);
+  }
+  __syncthreads();
+  for (int t = 0; t < nk; ++t) {
+    const int buf = t & 1;
+    if (t + 1 < nk) load((t + 1) * kG8K);
+    const float* as = As[buf];
+    const float* bs = Bs[buf];
+#pragma unroll
+    for (int kk = 0; kk < kG8K; ++kk) {
+      const float4 a0 = *reinterpret_cast<const float4*>(as + 4 * tx + kk * kG8LD);
+      const float4 a1 = *reinterpret_cast<const float4*>(as + 64 + 4 * tx + kk * kG8LD);
+      const float4 b0 = *reinterpret_cast<const float4*>(bs + 4 * ty + kk * kG8LD);
+      const float4 b1 = *reinterpret_cast<const float4*>(bs + 64 + 4 * ty + kk * kG8LD);
+      const float a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+      const float b[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+      for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) acc[i][j] += a[i] * b[j];
+    }
+    if (t + 1 < nk) store(buf ^ 1);
+    __syncthreads();
+  }
+  // rows 4 tx + {0..3} and 64 + 4 tx + {0..3}; columns 4 ty + {0..3} and 64 + 4 ty + {0..3}
+#pragma unroll
+  for (int jb = 0; jb < 2; ++jb) {
+    float cv[4][8];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int c = c0 + 64 * jb + 4 * ty + j;
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        const int r = r0 + (i < 4 ? 4 * tx + i : 64 + 4 * tx + i - 4);
+        cv[j][i] = (beta != 0.f && c < n && r < m) ? C[r + (size_t)c * ldc] : 0.f;
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int c = c0 + 64 * jb + 4 * ty + j;
+      if (c >= n) continue;
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        const int r = r0 + (i < 4 ? 4 * tx + i : 64 + 4 * tx + i - 4);
+        if (r < m) C[r + (size_t)c * ldc] = (beta == 0.f ? 0.f : beta * cv[j][i]) + alpha * acc[i][4 * jb + j];
+      }
+    }
+  }
+}
+
 template <typename T>
 int gemm(cudaStream_t s, int m, int n, int k, T alpha, const T* A, const long long* offA, long long strideA,
          int lda, const T* B, const long long* offB, long long strideB, int ldb, T beta, T* C,
@@ -391,6 +499,18 @@ int gemm(cudaStream_t s, int m, int n, int k, T alpha, const T* A, const long lo
                                          beta, C, offC, strideC, ldc);
     SLAB_CHECK_LAUNCH();
     return SLAB_OK;
+  }
+  if constexpr (std::is_same<T, float>::value) {
+    // 128-wide tiles only where they still give every SM a CTA (narrow products,
+    // e.g. one 256-column outer block, keep the 64 x 64 grid and its parallelism)
+    if (m >= 128 && n >= 128 && !gemm64_only() &&
+        (long long)ceil_div(m, 128) * ceil_div(n, 128) * batch >= sm_count()) {
+      dim3 g128(ceil_div(m, 128), ceil_div(n, 128), batch);
+      gemm128_kernel<<<g128, 256, 0, s>>>(m, n, k < 0 ? 0 : k, alpha, A, offA, strideA, lda, B, offB, strideB, ldb,
+                                          beta, C, offC, strideC, ldc);
+      SLAB_CHECK_LAUNCH();
+      return SLAB_OK;
+    }
   }
   dim3 grid(ceil_div(m, 64), ceil_div(n, 64), batch);
   gemm_kernel<T, false><<<grid, 256, 0, s>>>(m, n, k < 0 ? 0 : k, alpha, A, offA, strideA, lda, B, offB, strideB, ldb,

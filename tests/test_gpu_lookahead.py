@@ -167,3 +167,37 @@ def test_fp32_blocked_interface_lu_matches_unblocked(monkeypatch):
         assert diff < 1e-11, (name, diff)
     assert np.array_equal(sols['serial'][0], sols['lookahead'][0]) or \
         np.linalg.norm(sols['serial'][0] - sols['lookahead'][0]) < 1e-11 * np.linalg.norm(ref)
+
+
+def test_fp32_products_on_128_tiles_match_64_tiles(monkeypatch):
+    """The FP32 products with both sides at least 128 run on 128 x 128 tiles
+    (gemm128_kernel); SLAB_GEMM64=1 keeps them on the 64 x 64 kernel.  The two
+    sum each entry's k terms in different groupings, so the factors agree to
+    rounding and the refined solutions to the refinement level, against each
+    other and against the FP64 engine (interface blocks of 2,080, merge fronts
+    up to 1,040)."""
+    from slablu_gb300 import hps
+    from slablu_gb300.engine import SlabEngine
+    p, kh, n1 = 6, 20.0, 520
+    a = 1 / (2 * n1)
+    g = hps.Geometry([[0, 6 * 2 * a], [0, 1]], a, p, 0.02)
+    xx = torch.as_tensor(g.xx_tot, device='cuda')
+    c = (-kh ** 2 * (1 - 0.5 * torch.exp(-((xx[:, 0] - 0.01) ** 2 + (xx[:, 1] - 0.5) ** 2) / 0.02))).contiguous()
+    one = torch.ones_like(c)
+    gen = torch.Generator(device='cuda').manual_seed(5)
+    bnd = torch.randn(g.ntot, 2, generator=gen, device='cuda', dtype=torch.float64)
+    sols = {}
+    for flag in ('1', '0'):
+        monkeypatch.setenv('SLAB_GEMM64', flag)
+        for prec in ('fp32', 'mixed'):
+            eng = SlabEngine(g, prec)
+            eng.factor(c11=one, c22=one, c=c)
+            u, _, iters, st = eng.solve(bnd, tol=1e-12, max_iter=60)
+            assert st['converged'], (flag, prec, iters, st)
+            sols[flag, prec] = u.cpu().numpy()
+    e64 = SlabEngine(g, 'fp64')
+    e64.factor(c11=one, c22=one, c=c)
+    u64 = e64.solve(bnd, tol=1e-13, max_iter=10)[0].cpu().numpy()
+    for key, u in sols.items():
+        rel = np.linalg.norm(u - u64) / np.linalg.norm(u64)
+        assert rel < 1e-9, (key, rel)
