@@ -1251,15 +1251,23 @@ constexpr int kClBs = 64;
 // The column loop is a runtime loop and the FMA chain has no per-column
 // predicate: GB300 retires about two FP64 FMAs per clock per SM, so issued but
 // predicated-off FP64 instructions cost as much as useful ones.
+// A tile (rb x kb, rows r, k columns from A with leading dimension lda) as held
+// by one thread of cl_gemv_n: row tid % 64, the k-quarter tid / 64.
 template <typename T>
-__device__ __forceinline__ void cl_gemv_n(const T* __restrict__ A, int lda, int rb, int kb, const T* x, int nrhs,
-                                          T* red) {
+__device__ __forceinline__ void cl_load_n(const T* __restrict__ A, int lda, int rb, int kb, T (&a)[kClBs / 4]) {
   const int tid = threadIdx.x;
   const int r = tid & (kClBs - 1), kq = tid >> 6;  // 256 threads: 64 rows x 4 k-quarters
   const int kbeg = kq * (kClBs / 4);
-  T a[kClBs / 4];
 #pragma unroll
   for (int t = 0; t < kClBs / 4; ++t) a[t] = (r < rb && kbeg + t < kb) ? A[r + (size_t)(kbeg + t) * lda] : T(0);
+}
+
+// Partial products of a loaded tile with x (nrhs columns of ld kClBs) into red.
+template <typename T>
+__device__ __forceinline__ void cl_mul_n(const T (&a)[kClBs / 4], const T* x, int nrhs, T* red) {
+  const int tid = threadIdx.x;
+  const int r = tid & (kClBs - 1), kq = tid >> 6;
+  const int kbeg = kq * (kClBs / 4);
   for (int c = 0; c < nrhs; ++c) {
     const T* xc = x + kbeg + c * kClBs;
     T part0 = T(0), part1 = T(0);
@@ -1270,6 +1278,16 @@ __device__ __forceinline__ void cl_gemv_n(const T* __restrict__ A, int lda, int 
     }
     red[(kq * kClBs + r) + (size_t)c * 4 * kClBs] = part0 + part1;
   }
+}
+
+// y = A x for an rb x kb tile: partial sums of 64 rows x 4 k-quarters into red
+// (cl_reduce finishes them).
+template <typename T>
+__device__ __forceinline__ void cl_gemv_n(const T* __restrict__ A, int lda, int rb, int kb, const T* x, int nrhs,
+                                          T* red) {
+  T a[kClBs / 4];
+  cl_load_n(A, lda, rb, kb, a);
+  cl_mul_n(a, x, nrhs, red);
 }
 
 template <typename T>
@@ -1321,6 +1339,22 @@ __global__ void __launch_bounds__(256) trsv_cluster_kernel(const T* __restrict__
       acc[(size_t)o * vb + idx] = (r0 + r < n) ? Bin[(trans ? r0 + r : perm[r0 + r]) + (size_t)c * ldb] : T(0);
     }
   }
+  // Non-transposed solves load their tiles one step ahead: at the start of a
+  // step, the tiles of this step's updates (which do not depend on x_b) and the
+  // next step's owner its inverted diagonal block, so the loads overlap the
+  // owner's product and the cluster barrier.  Blocks past the second owned one
+  // load at use.
+  constexpr int kPre = 2;
+  T pre[kPre][kClBs / 4];
+  T ipre[kClBs / 4];
+  int ipre_step = -1;  // step_all whose inverse tile ipre holds
+  auto step_block = [&](int sa) { return sa < nblk ? sa : 2 * nblk - 1 - sa; };  // b of a step_all
+  auto step_inv = [&](int sa) { return (sa < nblk) != (trans != 0) ? Linv : Uinv; };
+  if (!trans && rank == step_block(0) % CL) {
+    const int b = step_block(0), kb = min(bs, n - b * bs);
+    cl_load_n(step_inv(0) + (size_t)b * bs * bs, bs, kb, kb, ipre);
+    ipre_step = 0;
+  }
   int step_all = 0;
   for (int pass = 0; pass < 2; ++pass) {
     const bool fwd = pass == 0;
@@ -1330,13 +1364,37 @@ __global__ void __launch_bounds__(256) trsv_cluster_kernel(const T* __restrict__
       const int k0 = b * bs, kb = min(bs, n - k0);
       const int owner = b % CL;
       T* xb = xbuf + (size_t)(step_all & 1) * vb;
+      T ib_now[kClBs / 4];
+      bool ib_ready = false;
+      if (!trans) {
+        if (ipre_step == step_all) {
+#pragma unroll
+          for (int t = 0; t < kClBs / 4; ++t) ib_now[t] = ipre[t];
+          ib_ready = true;
+        }
+#pragma unroll
+        for (int o = 0; o < kPre; ++o) {
+          const int ob = rank + o * CL;
+          if (o < nown && (fwd ? ob > b : ob < b))
+            cl_load_n(LU + (size_t)k0 * lda + ob * bs, lda, min(bs, n - ob * bs), kb, pre[o]);
+        }
+        const int sn = step_all + 1;
+        if (sn < 2 * nblk && rank == step_block(sn) % CL) {
+          const int bn = step_block(sn), kbn = min(bs, n - bn * bs);
+          cl_load_n(step_inv(sn) + (size_t)bn * bs * bs, bs, kbn, kbn, ipre);
+          ipre_step = sn;
+        }
+      }
       if (rank == owner) {
         const int o = b / CL;
         T* a = acc + (size_t)o * vb;
         const T* Ib = Inv + (size_t)b * bs * bs;
         __syncthreads();
         if (!trans) {
-          cl_gemv_n(Ib, bs, kb, kb, a, nrhs, red);
+          if (ib_ready)
+            cl_mul_n(ib_now, a, nrhs, red);
+          else
+            cl_gemv_n(Ib, bs, kb, kb, a, nrhs, red);
           __syncthreads();
           for (int idx = tid; idx < kb * nrhs; idx += blockDim.x) {
             const int r = idx % kb, c = idx / kb;
@@ -1367,7 +1425,15 @@ __global__ void __launch_bounds__(256) trsv_cluster_kernel(const T* __restrict__
       __syncthreads();
       // blocks still to come in this pass: b+1.. (forward) or ..b-1 (backward)
       int nupd = 0;
-      for (int o = 0; o < nown; ++o) {
+      // the prefetched tiles (static indices keep them in registers), then the rest
+#pragma unroll
+      for (int o = 0; o < kPre; ++o) {
+        const int ob = rank + o * CL;
+        if (trans || o >= nown || (fwd ? ob <= b : ob >= b)) continue;
+        cl_mul_n(pre[o], xloc, nrhs, red + (size_t)o * 4 * vb);
+        ++nupd;
+      }
+      for (int o = trans ? 0 : kPre; o < nown; ++o) {
         const int ob = rank + o * CL;
         if (fwd ? ob <= b : ob >= b) continue;
         const int r0 = ob * bs, rb = min(bs, n - r0);
