@@ -213,6 +213,9 @@ struct MergeGatherArgs {
   long long offP0, offM0, offC0;
 };
 
+// One warp per column of the parent front P (nO x nO), of Maug (nE x (nE + nO))
+// or of col (nO x nE), the lanes down the rows: the column's source (child and
+// position) is read once per warp, and no index is divided.
 template <typename T>
 __global__ void merge_gather_kernel(MergeGatherArgs a, const T* __restrict__ pool, T* __restrict__ ppool,
                                     T* __restrict__ fpool) {
@@ -223,38 +226,35 @@ __global__ void merge_gather_kernel(MergeGatherArgs a, const T* __restrict__ poo
   T* M = fpool + a.offM0 + (long long)e * a.nE * (a.nE + a.nO);
   T* C = fpool + a.offC0 + (long long)e * a.nO * a.nE;
   const int nE = a.nE, nO = a.nO;
-  // per merge the element count is below 2^31 (checked by the launcher): 32-bit
-  // index arithmetic, whose divisions cost a fraction of 64-bit ones
-  const int totP = nO * nO;
-  const int totM = nE * (nE + nO);
-  const int totC = nO * nE;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < totP + totM + totC; i += gridDim.x * blockDim.x) {
-    if (i < totP) {
-      const int r = i % nO, c = i / nO;
-      const int cr = a.oChild[r], cc = a.oChild[c];
-      T v = T(0);
-      if (cr == cc) {
-        if (cr == 0)
-          v = A[a.oPos[r] + (long long)a.oPos[c] * a.nA];
-        else
-          v = B[a.oPos[r] + (long long)a.oPos[c] * a.nB];
-      }
-      P[i] = v;
-    } else if (i < totP + totM) {
-      const int j = i - totP;
-      const int r = j % nE, c = j / nE;
-      T v;
+  const int ncol = 2 * nO + 2 * nE;  // P's columns, then Maug's, then col's
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int wpb = blockDim.x >> 5;
+  for (int vc = blockIdx.x * wpb + warp; vc < ncol; vc += gridDim.x * wpb) {
+    if (vc < nO) {
+      const int c = vc, cc = a.oChild[c];
+      const T* src = cc == 0 ? A + (long long)a.oPos[c] * a.nA : B + (long long)a.oPos[c] * a.nB;
+      T* dst = P + (long long)c * nO;
+      for (int r = lane; r < nO; r += 32) dst[r] = a.oChild[r] == cc ? src[a.oPos[r]] : T(0);
+    } else if (vc < 2 * nO + nE) {
+      const int c = vc - nO;
+      T* dst = M + (long long)c * nE;
       if (c < nE) {
-        v = A[a.eA[r] + (long long)a.eA[c] * a.nA] + B[a.eB[r] + (long long)a.eB[c] * a.nB];
+        const T* sa = A + (long long)a.eA[c] * a.nA;
+        const T* sb = B + (long long)a.eB[c] * a.nB;
+        for (int r = lane; r < nE; r += 32) dst[r] = sa[a.eA[r]] + sb[a.eB[r]];
       } else {
         const int o = c - nE;
-        v = a.oChild[o] == 0 ? A[a.eA[r] + (long long)a.oPos[o] * a.nA] : B[a.eB[r] + (long long)a.oPos[o] * a.nB];
+        const bool fromA = a.oChild[o] == 0;
+        const T* src = fromA ? A + (long long)a.oPos[o] * a.nA : B + (long long)a.oPos[o] * a.nB;
+        const int* ei = fromA ? a.eA : a.eB;
+        for (int r = lane; r < nE; r += 32) dst[r] = src[ei[r]];
       }
-      M[j] = v;
     } else {
-      const int j = i - totP - totM;
-      const int r = j % nO, c = j / nO;
-      C[j] = a.oChild[r] == 0 ? A[a.oPos[r] + (long long)a.eA[c] * a.nA] : B[a.oPos[r] + (long long)a.eB[c] * a.nB];
+      const int c = vc - 2 * nO - nE;
+      const T* sa = A + (long long)a.eA[c] * a.nA;
+      const T* sb = B + (long long)a.eB[c] * a.nB;
+      T* dst = C + (long long)c * nO;
+      for (int r = lane; r < nO; r += 32) dst[r] = a.oChild[r] == 0 ? sa[a.oPos[r]] : sb[a.oPos[r]];
     }
   }
 }
@@ -1007,7 +1007,8 @@ struct EngineImpl : EngineBase {
       const long long per = (long long)b.nO * b.nO + (long long)b.nE * (b.nE + b.nO) + (long long)b.nO * b.nE;
       if (per + 1024LL * 256 >= (1LL << 31))
         return set_error(SLAB_ERR_ARG, "merge of %d + %d unknowns too large", b.nE, b.nO);
-      dim3 grid((unsigned)std::min<long long>((per + 255) / 256, 1024), b.count);
+      const int ncol = 2 * b.nO + 2 * b.nE;  // one warp per column, eight per CTA
+      dim3 grid((unsigned)std::max(1, std::min((ncol + 7) / 8, 1024)), b.count);
       merge_gather_kernel<T><<<grid, 256, 0, s>>>(g, nodepool.as<T>(), nodepool.as<T>(), fpool.as<T>());
       SLAB_CHECK_LAUNCH();
       T* Maug = fpool.as<T>() + b.offM0;
