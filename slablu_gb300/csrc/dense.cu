@@ -281,8 +281,38 @@ int gemm_tn(cudaStream_t s, int m, int n, int k, T alpha, const T* A, const long
   return SLAB_OK;
 }
 
+// The same with the permutation and the pivots in shared memory (2 n ints): the
+// sequential interchanges cost shared-memory latencies instead of global ones.
+__global__ void perm_from_ipiv_smem_kernel(const int* ipiv, int n, int* perm) {
+  extern __shared__ int psm[];
+  int* p = psm;
+  int* iv = psm + n;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    p[i] = i;
+    iv[i] = ipiv[i];
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int j = 0; j < n; ++j) {
+      const int pj = iv[j];
+      if (pj != j && pj >= 0 && pj < n) {
+        const int t = p[j];
+        p[j] = p[pj];
+        p[pj] = t;
+      }
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < n; i += blockDim.x) perm[i] = p[i];
+}
+
 int build_perm(cudaStream_t s, const int* ipiv, int n, int* perm) {
-  perm_from_ipiv_kernel<<<1, 1, 0, s>>>(ipiv, n, perm);
+  const size_t bytes = 2 * (size_t)n * sizeof(int);
+  if (bytes <= 48 * 1024) {
+    perm_from_ipiv_smem_kernel<<<1, 256, bytes, s>>>(ipiv, n, perm);
+  } else {
+    perm_from_ipiv_kernel<<<1, 1, 0, s>>>(ipiv, n, perm);
+  }
   SLAB_CHECK_LAUNCH();
   return SLAB_OK;
 }
@@ -600,7 +630,7 @@ __device__ __forceinline__ void smem_row_update(float* x, int j, float l, const 
 
 template <int NT>
 __global__ void __launch_bounds__(NT, 1)
-    biglu_panel_cta_kernel(float* A, int lda, int n, int k0, int nb, int* ipiv, int* info, float* linv) {
+    biglu_panel_cta_kernel(float* A, int lda, int n, int k0, int nb, int* ipiv, int* info, float* linv, int* gath) {
   constexpr int NW = NT / 32, LDS = 2 * NT, W = kNB;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float* S = reinterpret_cast<float*>(smem_raw);  // LDS x W: physical rows 2NT .. 4NT-1
@@ -752,6 +782,28 @@ __global__ void __launch_bounds__(NT, 1)
     if (li2 != INT_MAX) col[li2] = s2[c * LDS];
     if (li3 != INT_MAX) col[li3] = s3[c * LDS];
   }
+  if (gath) {
+    // the panel's interchanges as a gather: (destination, source) rows of every
+    // row that moved -- at most 2 nb of them
+    __shared__ int gcnt;
+    if (tid == 0) gcnt = 0;
+    __syncthreads();
+    auto emit = [&](int li, int ph) {
+      if (li != INT_MAX && li != ph) {
+        const int t = atomicAdd(&gcnt, 1);
+        if (t < 2 * kNB) {
+          gath[1 + 2 * t] = k0 + li;
+          gath[2 + 2 * t] = k0 + ph;
+        }
+      }
+    };
+    emit(li0, tid);
+    emit(li1, tid + NT);
+    emit(li2, tid + 2 * NT);
+    emit(li3, tid + 3 * NT);
+    __syncthreads();
+    if (tid == 0) gath[0] = gcnt < 2 * kNB ? gcnt : 2 * kNB;
+  }
   if (linv && nb <= m) {
     constexpr int ldx = W + 1;
 #pragma unroll
@@ -795,8 +847,9 @@ namespace {
 // otherwise.
 template <typename T>
 int panel_factor(cudaStream_t s, T* A, int lda, int n, int k0, int nb, int* ipiv, int* info, T* linv,
-                 bool* linv_done, int kind) {
+                 bool* linv_done, int kind, int* gath = nullptr, bool* gath_done = nullptr) {
   *linv_done = false;
+  if (gath_done) *gath_done = false;
   const int m = n - k0;
   if constexpr (std::is_same<T, float>::value) {
     // measured per panel on GB300 (32 columns): the cluster kernel ~69 us at any
@@ -805,16 +858,20 @@ int panel_factor(cudaStream_t s, T* A, int lda, int n, int k0, int nb, int* ipiv
     if (kind == 0 && m <= kPanelCtaMaxRows && m >= nb && nb <= kNB) {
       if (m > 512) {
         SLAB_TRY(ensure_smem(biglu_panel_cta_kernel<512>, panel_cta_smem_bytes<512>(), "biglu_panel_cta"));
-        biglu_panel_cta_kernel<512><<<1, 512, panel_cta_smem_bytes<512>(), s>>>(A, lda, n, k0, nb, ipiv, info, linv);
+        biglu_panel_cta_kernel<512><<<1, 512, panel_cta_smem_bytes<512>(), s>>>(A, lda, n, k0, nb, ipiv, info, linv,
+                                                                                  gath);
       } else if (m > 256) {
         SLAB_TRY(ensure_smem(biglu_panel_cta_kernel<256>, panel_cta_smem_bytes<256>(), "biglu_panel_cta"));
-        biglu_panel_cta_kernel<256><<<1, 256, panel_cta_smem_bytes<256>(), s>>>(A, lda, n, k0, nb, ipiv, info, linv);
+        biglu_panel_cta_kernel<256><<<1, 256, panel_cta_smem_bytes<256>(), s>>>(A, lda, n, k0, nb, ipiv, info, linv,
+                                                                                  gath);
       } else {
         SLAB_TRY(ensure_smem(biglu_panel_cta_kernel<128>, panel_cta_smem_bytes<128>(), "biglu_panel_cta"));
-        biglu_panel_cta_kernel<128><<<1, 128, panel_cta_smem_bytes<128>(), s>>>(A, lda, n, k0, nb, ipiv, info, linv);
+        biglu_panel_cta_kernel<128><<<1, 128, panel_cta_smem_bytes<128>(), s>>>(A, lda, n, k0, nb, ipiv, info, linv,
+                                                                                  gath);
       }
       SLAB_CHECK_LAUNCH();
       *linv_done = linv != nullptr;
+      if (gath_done) *gath_done = gath != nullptr;
       return SLAB_OK;
     }
   }
@@ -991,7 +1048,7 @@ int outer_block_update(cudaStream_t s, T* A, int lda, int n, int ob0, int obe, i
 
 template <typename T>
 int biglu_blocked(cudaStream_t s, T* A, int lda, int n, int* ipiv, int* info, T* panel_linv, T* blk_linv,
-                  int panel_kind, cudaStream_t side, cudaEvent_t fork, cudaEvent_t join, int* perm) {
+                  int panel_kind, cudaStream_t side, cudaEvent_t fork, cudaEvent_t join, int* perm, int* gath) {
   constexpr int kOuter = 256, kB = 64;
   const bool look = side && fork && join && perm;
   bool side_busy = false;
@@ -999,16 +1056,17 @@ int biglu_blocked(cudaStream_t s, T* A, int lda, int n, int* ipiv, int* info, T*
     const int obe = n - ob0 < kOuter ? n : ob0 + kOuter;
     for (int k0 = ob0; k0 < obe; k0 += kNB) {
       const int nb = obe - k0 < kNB ? obe - k0 : kNB;
-      bool linv_done = false;
-      SLAB_TRY(panel_factor<T>(s, A, lda, n, k0, nb, ipiv, info, panel_linv, &linv_done, panel_kind));
-      if (look) {
-        const int ncols = (obe - ob0) - nb;  // interchanges inside the outer block now, the rest after it
-        if (ncols > 0) {
-          swap_cols_kernel<T><<<ceil_div(ncols, 128), 128, 0, s>>>(A, lda, ob0, obe, k0, nb, ipiv);
-          SLAB_CHECK_LAUNCH();
-        }
-      } else if (n - nb > 0) {
-        biglu_swap_kernel<T><<<ceil_div(n - nb, 256), 256, 0, s>>>(A, lda, n, k0, nb, ipiv);
+      bool linv_done = false, gath_done = false;
+      SLAB_TRY(panel_factor<T>(s, A, lda, n, k0, nb, ipiv, info, panel_linv, &linv_done, panel_kind, gath,
+                               &gath_done));
+      // interchanges inside the outer block now (with lookahead), the rest after it
+      const int c_lo = look ? ob0 : 0, c_hi = look ? obe : n;
+      const int ncols = (c_hi - c_lo) - nb;
+      if (ncols > 0) {
+        if (gath_done)
+          swap_gather_kernel<T><<<ceil_div(ncols, 128), 128, 0, s>>>(A, lda, c_lo, c_hi, k0, nb, gath);
+        else
+          swap_cols_kernel<T><<<ceil_div(ncols, 128), 128, 0, s>>>(A, lda, c_lo, c_hi, k0, nb, ipiv);
         SLAB_CHECK_LAUNCH();
       }
       const int inner = obe - k0 - nb;
@@ -1046,7 +1104,7 @@ int biglu_blocked(cudaStream_t s, T* A, int lda, int n, int* ipiv, int* info, T*
   return SLAB_OK;
 }
 template int biglu_blocked<float>(cudaStream_t, float*, int, int, int*, int*, float*, float*, int, cudaStream_t,
-                                  cudaEvent_t, cudaEvent_t, int*);
+                                  cudaEvent_t, cudaEvent_t, int*, int*);
 
 template <typename T>
 int bigtrs_inv(cudaStream_t s, const T* LU, int lda, int n, const int* perm, const T* Linv, const T* Uinv, int bs,

@@ -1812,10 +1812,24 @@ __global__ void __launch_bounds__(128) tri_inv_blocks_kernel(const T* A, int lda
   const int k0 = blk * bs, nb = min(bs, n - k0);
   T* O = out + (size_t)blk * bs * bs;
   T* rdiag = Xs + (size_t)bs * ld;           // bs: reciprocals of the diagonal (upper)
-  for (int idx = threadIdx.x; idx < bs * bs; idx += blockDim.x) {
-    const int i = idx % bs, c = idx / bs;
-    D[i + c * ld] = (i < nb && c < nb) ? A[(size_t)(k0 + c) * lda + k0 + i] : T(0);
-    Xs[i + c * ld] = T(0);
+  // eight loads in flight per thread before their stores
+  for (int base = threadIdx.x; base < bs * bs; base += 8 * blockDim.x) {
+    T t[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int idx = base + u * blockDim.x;
+      const int i = idx % bs, c = idx / bs;
+      t[u] = (idx < bs * bs && i < nb && c < nb) ? A[(size_t)(k0 + c) * lda + k0 + i] : T(0);
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int idx = base + u * blockDim.x;
+      if (idx < bs * bs) {
+        const int i = idx % bs, c = idx / bs;
+        D[i + c * ld] = t[u];
+        Xs[i + c * ld] = T(0);
+      }
+    }
   }
   __syncthreads();
   if (upper)
@@ -1874,7 +1888,21 @@ __global__ void __launch_bounds__(256) trsm_inv_kernel(const T* Inv, int bs, int
   T* Xs = Is + bs * bs;                    // bs x kTrsmCols
   const int c0 = blockIdx.x * kTrsmCols;
   const int nc = min(kTrsmCols, ncols - c0);
-  for (int idx = threadIdx.x; idx < bs * bs; idx += blockDim.x) Is[idx] = Inv[idx];
+  // eight loads in flight per thread before their stores (one memory latency per
+  // eight elements instead of one per element)
+  for (int base = threadIdx.x; base < bs * bs; base += 8 * blockDim.x) {
+    T t[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int idx = base + u * blockDim.x;
+      t[u] = idx < bs * bs ? Inv[idx] : T(0);
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int idx = base + u * blockDim.x;
+      if (idx < bs * bs) Is[idx] = t[u];
+    }
+  }
   for (int idx = threadIdx.x; idx < nb * nc; idx += blockDim.x) {
     const int i = idx % nb, c = idx / nb;
     Xs[i + c * bs] = X[(size_t)(c0 + c) * ldx + k0 + i];
@@ -1882,6 +1910,8 @@ __global__ void __launch_bounds__(256) trsm_inv_kernel(const T* Inv, int bs, int
   __syncthreads();
   for (int idx = threadIdx.x; idx < nb * nc; idx += blockDim.x) {
     const int i = idx % nb, c = idx / nb;
+    // one running sum in ascending k: at N = 4.4M four interleaved partial sums
+    // here cost the FP32 interface two more refinement steps to 1e-10 (12 vs 10)
     T s = T(0);
     for (int k = 0; k < nb; ++k) s += Is[i + k * bs] * Xs[k + c * bs];
     X[(size_t)(c0 + c) * ldx + k0 + i] = s;
@@ -1922,6 +1952,30 @@ __global__ void swap_cols_kernel(T* A, int lda, int c_lo, int c_hi, int k0, int 
       cp[pr] = t;
     }
   }
+}
+
+// A panel's row interchanges given as a gather list (gath[0] = count <= 2 kNB,
+// then (destination, source) row pairs) applied to the columns [c_lo, k0) and
+// [k0+nb, c_hi): every moved value of a column is loaded before any is stored,
+// so the loads of a column are all in flight at once.
+template <typename T>
+__global__ void __launch_bounds__(128) swap_gather_kernel(T* A, int lda, int c_lo, int c_hi, int k0, int nb,
+                                                          const int* __restrict__ gath) {
+  __shared__ int g[1 + 4 * kNB];
+  for (int i = threadIdx.x; i < 1 + 4 * kNB; i += blockDim.x) g[i] = gath[i];
+  __syncthreads();
+  const int c = c_lo + blockIdx.x * blockDim.x + threadIdx.x;
+  const int col = c < k0 ? c : c + nb;
+  if (col >= c_hi) return;
+  T* cp = A + (size_t)col * lda;
+  const int cnt = g[0];
+  T v[2 * kNB];
+#pragma unroll
+  for (int t = 0; t < 2 * kNB; ++t)
+    if (t < cnt) v[t] = cp[g[2 + 2 * t]];
+#pragma unroll
+  for (int t = 0; t < 2 * kNB; ++t)
+    if (t < cnt) cp[g[1 + 2 * t]] = v[t];
 }
 
 // Net effect of the interchanges ipiv[k0 .. k0+npiv) (LAPACK order, rows of an
@@ -2048,9 +2102,11 @@ int biglu(cudaStream_t s, T* A, int lda, int n, int* ipiv, int* info, T* work = 
 // the products grouped differently: the factors agree to rounding (and so do
 // the pivots, but for near ties).  panel_linv: kNB x kNB elements; blk_linv:
 // 256 x 64 elements.
+// gath (1 + 4 kNB ints, may be null): one-CTA panels leave their interchanges
+// there as a gather list, applied to the other columns in one pass of loads.
 template <typename T>
 int biglu_blocked(cudaStream_t s, T* A, int lda, int n, int* ipiv, int* info, T* panel_linv, T* blk_linv,
-                  int panel_kind, cudaStream_t side, cudaEvent_t fork, cudaEvent_t join, int* perm);
+                  int panel_kind, cudaStream_t side, cudaEvent_t fork, cudaEvent_t join, int* perm, int* gath);
 
 // Inverses of the bs x bs diagonal triangles of a factored matrix:
 // Linv/Uinv hold ceil(n/bs) blocks of bs x bs each.

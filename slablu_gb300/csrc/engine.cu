@@ -361,6 +361,7 @@ struct EngineImpl : EngineBase {
   cudaStream_t side = nullptr;
   cudaEvent_t la_fork = nullptr, la_join = nullptr;
   DevBuf laPerm, ifBlkLinv;  // row-interchange gather scratch; inverted 64-row triangles of an FP32 outer block
+  DevBuf ifGath;             // the current FP32 panel's interchanges as a gather list
   bool use_lookahead = true;
   cudaGraphExec_t gfac[3] = {nullptr, nullptr, nullptr}, gapp = nullptr, gapp_t = nullptr;
   int gapp_nrhs = 0, gapp_t_nrhs = 0;
@@ -895,7 +896,10 @@ struct EngineImpl : EngineBase {
         SLAB_CUDA_TRY(cudaMemsetAsync(emuErr.p, 0, sizeof(int), s));
       }
       SLAB_TRY(laPerm.alloc((size_t)(1 + 2 * kRowpermMax) * sizeof(int)));
-      if (std::is_same<TI, float>::value) SLAB_TRY(ifBlkLinv.alloc((size_t)kEmuOuter * 64 * sizeof(TI)));
+      if (std::is_same<TI, float>::value) {
+        SLAB_TRY(ifBlkLinv.alloc((size_t)kEmuOuter * 64 * sizeof(TI)));
+        SLAB_TRY(ifGath.alloc((size_t)(1 + 4 * kNB) * sizeof(int)));
+      }
     }
     if (use_tc_tree) SLAB_TRY(alloc_tc_tree());
     SLAB_TRY(acc.alloc(4 * sizeof(double)));
@@ -1131,7 +1135,7 @@ struct EngineImpl : EngineBase {
             SLAB_TRY(biglu_blocked<TI>(s, Sj, nI, nI, ifPiv.as<int>() + (long long)nI * j, ifInfo.as<int>(),
                                        ifWork.as<TI>(), ifBlkLinv.as<TI>(), panel_kind, la ? side : nullptr,
                                        la ? la_fork : nullptr, la ? la_join : nullptr,
-                                       la ? laPerm.as<int>() : nullptr));
+                                       la ? laPerm.as<int>() : nullptr, ifGath.as<int>()));
             done = true;
           }
         }
