@@ -102,6 +102,8 @@ int build_perm_batched(cudaStream_t s, const int* ipiv, long long strideP, int n
   return SLAB_OK;
 }
 
+static int sm_count();
+
 template <typename T>
 int getrs_small(cudaStream_t s, int n, int nrhs, const T* LU, const long long* offLU, long long strideLU, int lda,
                 const int* perm, const long long* offP, long long strideP, T* B, const long long* offB,
@@ -109,18 +111,26 @@ int getrs_small(cudaStream_t s, int n, int nrhs, const T* LU, const long long* o
   if (n <= 0 || nrhs <= 0 || batch <= 0) return SLAB_OK;
   if (nrhs > 4) return set_error(SLAB_ERR_ARG, "getrs_small: nrhs %d > 4", nrhs);
   if (n > 32 * kWarpSlots) return set_error(SLAB_ERR_ARG, "getrs_small: order %d > %d", n, 32 * kWarpSlots);
-  const size_t bytes = (size_t)kWarpSolveWarps * n * nrhs * sizeof(T);
+  // few large matrices (the top merge levels): one CTA per matrix instead of one warp
+  const bool per_cta = n >= 128 && batch <= 4 * sm_count();
+  const size_t bytes = (size_t)(per_cta ? 1 : kWarpSolveWarps) * n * nrhs * sizeof(T);
   auto launch = [&](auto kern) -> int {
     SLAB_TRY(ensure_smem(kern, bytes, "getrs_small"));
-    kern<<<ceil_div(batch, kWarpSolveWarps), 32 * kWarpSolveWarps, bytes, s>>>(n, LU, offLU, strideLU, lda, perm, offP,
-                                                                               strideP, B, offB, strideB, ldb, batch);
+    if (per_cta)
+      kern<<<batch, 256, bytes, s>>>(n, LU, offLU, strideLU, lda, perm, offP, strideP, B, offB, strideB, ldb, batch);
+    else
+      kern<<<ceil_div(batch, kWarpSolveWarps), 32 * kWarpSolveWarps, bytes, s>>>(n, LU, offLU, strideLU, lda, perm,
+                                                                                 offP, strideP, B, offB, strideB, ldb,
+                                                                                 batch);
     return SLAB_OK;
   };
   switch (nrhs) {
-    case 1: SLAB_TRY(launch(getrs_warp_blocked_kernel<T, 1>)); break;
-    case 2: SLAB_TRY(launch(getrs_warp_blocked_kernel<T, 2>)); break;
-    case 3: SLAB_TRY(launch(getrs_warp_blocked_kernel<T, 3>)); break;
-    default: SLAB_TRY(launch(getrs_warp_blocked_kernel<T, 4>)); break;
+    case 1: SLAB_TRY(per_cta ? launch(getrs_cta_blocked_kernel<T, 1>) : launch(getrs_warp_blocked_kernel<T, 1>)); break;
+    case 2: SLAB_TRY(per_cta ? launch(getrs_cta_blocked_kernel<T, 2>) : launch(getrs_warp_blocked_kernel<T, 2>)); break;
+    case 3: SLAB_TRY(per_cta ? launch(getrs_cta_blocked_kernel<T, 3>) : launch(getrs_warp_blocked_kernel<T, 3>)); break;
+    default:
+      SLAB_TRY(per_cta ? launch(getrs_cta_blocked_kernel<T, 4>) : launch(getrs_warp_blocked_kernel<T, 4>));
+      break;
   }
   SLAB_CHECK_LAUNCH();
   return SLAB_OK;

@@ -989,11 +989,13 @@ __global__ void __launch_bounds__(32 * kWarpSolveWarps)
 // update of the other rows runs one 32-row group at a time over all 32
 // columns of the block, so each lane has 32 independent loads of the factor in
 // flight: about n^2 / 2048 memory round trips per pass instead of n.
+// g0 / ng: this warp takes the row groups g0, g0 + ng, ... (the CTA variant
+// spreads them over its warps).
 template <typename T, int NR>
 __device__ __forceinline__ void warp_block_update(const T* __restrict__ A, int lda, int kb, int nb, int rbeg, int rend,
-                                                  const T (&x)[NR], T* xs, int n, int lane) {
+                                                  const T (&x)[NR], T* xs, int n, int lane, int g0 = 0, int ng = 1) {
 #pragma unroll 1
-  for (int r = rbeg + lane; r - lane < rend; r += 32) {
+  for (int r = rbeg + 32 * g0 + lane; r - lane < rend; r += 32 * ng) {
     const bool ok = r < rend;
     T a[32];
     const T* pc = A + (size_t)kb * lda + (ok ? r : 0);
@@ -1089,6 +1091,95 @@ __global__ void __launch_bounds__(32 * kWarpSolveWarps)
   }
   for (int c = 0; c < NR; ++c)
     for (int i = lane; i < n; i += 32) Bg[i + (size_t)c * ldb] = xs[i + c * n];
+}
+
+// The same solve with one CTA per matrix, for batches of few large matrices
+// (the top merge levels): warp 0 solves each diagonal 32-row triangle as the
+// warp kernel does, then all warps update the rows below (above) it, 32-row
+// groups spread over the warps, with a block barrier around each update.  Each
+// row sees the same operations in the same order as in the warp kernel.
+template <typename T, int NR>
+__global__ void __launch_bounds__(256)
+    getrs_cta_blocked_kernel(int n, const T* __restrict__ LU, const long long* offLU, long long strideLU, int lda,
+                             const int* __restrict__ perm, const long long* offP, long long strideP, T* B,
+                             const long long* offB, long long strideB, int ldb, int batch) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  const int b = blockIdx.x;
+  if (b >= batch) return;
+  T* xs = reinterpret_cast<T*>(smem_raw);
+  const T* __restrict__ A = LU + batch_off(offLU, strideLU, b);
+  const int* pv = perm + batch_off(offP, strideP, b);
+  T* Bg = B + batch_off(offB, strideB, b);
+  for (int c = 0; c < NR; ++c)
+    for (int i = threadIdx.x; i < n; i += blockDim.x) xs[i + c * n] = Bg[pv[i] + (size_t)c * ldb];
+  __syncthreads();
+  // forward, unit lower
+  for (int kb = 0; kb < n; kb += 32) {
+    const int nb = min(32, n - kb);
+    if (warp == 0) {
+      T x[NR];
+#pragma unroll
+      for (int c = 0; c < NR; ++c) x[c] = lane < nb ? xs[kb + lane + c * n] : T(0);
+      T lrow[32];
+      const T* pc = A + (size_t)kb * lda + kb + (lane < nb ? lane : 0);
+#pragma unroll
+      for (int k = 0; k < 32; ++k) {
+        lrow[k] = (k < lane && lane < nb) ? *pc : T(0);
+        pc += lda;
+      }
+#pragma unroll
+      for (int k = 0; k < 31; ++k)
+#pragma unroll
+        for (int c = 0; c < NR; ++c) x[c] -= lrow[k] * __shfl_sync(0xffffffffu, x[c], k);
+#pragma unroll
+      for (int c = 0; c < NR; ++c)
+        if (lane < nb) xs[kb + lane + c * n] = x[c];
+    }
+    __syncthreads();
+    T x[NR];
+#pragma unroll
+    for (int c = 0; c < NR; ++c) x[c] = lane < nb ? xs[kb + lane + c * n] : T(0);
+    warp_block_update<T, NR>(A, lda, kb, nb, kb + nb, n, x, xs, n, lane, warp, nw);
+    __syncthreads();
+  }
+  // backward, upper (non-unit)
+  for (int kb = ((n - 1) / 32) * 32; kb >= 0; kb -= 32) {
+    const int nb = min(32, n - kb);
+    if (warp == 0) {
+      T x[NR];
+#pragma unroll
+      for (int c = 0; c < NR; ++c) x[c] = lane < nb ? xs[kb + lane + c * n] : T(0);
+      T urow[32];
+      const T* pc = A + (size_t)kb * lda + kb + (lane < nb ? lane : 0);
+#pragma unroll
+      for (int k = 0; k < 32; ++k) {
+        urow[k] = (k > lane && k < nb) ? *pc : T(0);
+        pc += lda;
+      }
+      const T d = lane < nb ? A[(kb + lane) + (size_t)(kb + lane) * lda] : T(1);
+#pragma unroll
+      for (int k = 31; k >= 0; --k) {
+        if (k >= nb) continue;
+#pragma unroll
+        for (int c = 0; c < NR; ++c) {
+          if (lane == k) x[c] = x[c] / d;
+          x[c] -= urow[k] * __shfl_sync(0xffffffffu, x[c], k);
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < NR; ++c)
+        if (lane < nb) xs[kb + lane + c * n] = x[c];
+    }
+    __syncthreads();
+    T x[NR];
+#pragma unroll
+    for (int c = 0; c < NR; ++c) x[c] = lane < nb ? xs[kb + lane + c * n] : T(0);
+    warp_block_update<T, NR>(A, lda, kb, nb, 0, kb, x, xs, n, lane, warp, nw);
+    __syncthreads();
+  }
+  for (int c = 0; c < NR; ++c)
+    for (int i = threadIdx.x; i < n; i += blockDim.x) Bg[i + (size_t)c * ldb] = xs[i + c * n];
 }
 
 // Cooperative triangular solves with one large factored matrix (FP64
