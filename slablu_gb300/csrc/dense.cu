@@ -460,6 +460,12 @@ int gemm(cudaStream_t s, int m, int n, int k, T alpha, const T* A, const long lo
          int lda, const T* B, const long long* offB, long long strideB, int ldb, T beta, T* C,
          const long long* offC, long long strideC, int ldc, int batch) {
   if (m <= 0 || n <= 0 || batch <= 0) return SLAB_OK;
+  if (batch > 1 && !offA && !offB && !offC && strideA == 0 && strideB == (long long)ldb * n &&
+      strideC == (long long)ldc * n && (long long)n * batch <= 65535LL * 64) {
+    // one A for every entry and the B and C blocks back to back: a single product
+    // of n * batch columns (the leaves' flux products of a solve)
+    return gemm<T>(s, m, n * batch, k, alpha, A, nullptr, 0, lda, B, nullptr, 0, ldb, beta, C, nullptr, 0, ldc, 1);
+  }
   if (batch > 65535) {
     // grid.z limit: split the batch (offset arrays or strides advance per chunk)
     for (int b0 = 0; b0 < batch; b0 += 65535) {
