@@ -341,6 +341,9 @@ int slab_csr_spmv(int nrows, const long long* d_indptr, const int* d_indices, co
  *                        (one block barrier per column; taller panels in a
  *                        cluster), 1 every panel in a thread-block cluster (one
  *                        cluster barrier per column); same pivots and factors
+ *   SLAB_OPT_GEMM_TILES  FP32 products (merge tree, FP32 interface): 0 128 x 128
+ *                        output tiles where their grid fills the GPU, 64 x 64
+ *                        otherwise; 1 always 64 x 64; same sums in the same order
  * set returns a status; get returns the value (or a negative status). */
 #define SLAB_OPT_LEAF_CTAS 1
 #define SLAB_OPT_IFACE_SOLVE 2
@@ -349,6 +352,7 @@ int slab_csr_spmv(int nrows, const long long* d_indptr, const int* d_indices, co
 #define SLAB_OPT_LEAF_ASSEMBLY 5
 #define SLAB_OPT_IFACE_OUTER_INV 6
 #define SLAB_OPT_IFACE_PANEL 7
+#define SLAB_OPT_GEMM_TILES 8
 int slab_engine_set_option(slab_engine* e, int key, int value);
 int slab_engine_get_option(const slab_engine* e, int key);
 

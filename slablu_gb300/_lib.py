@@ -77,6 +77,7 @@ SLAB_OPT_TREE_TC = 4
 SLAB_OPT_LEAF_ASSEMBLY = 5
 SLAB_OPT_IFACE_OUTER_INV = 6
 SLAB_OPT_IFACE_PANEL = 7
+SLAB_OPT_GEMM_TILES = 8
 
 
 class SlabError(RuntimeError):

@@ -25,6 +25,7 @@ TUNABLES = {
     'leaf_assembly': (_lib.SLAB_OPT_LEAF_ASSEMBLY, (1, 0)),
     'iface_outer_inv': (_lib.SLAB_OPT_IFACE_OUTER_INV, (1, 0)),
     'iface_panel': (_lib.SLAB_OPT_IFACE_PANEL, (0, 1)),
+    'gemm_tiles': (_lib.SLAB_OPT_GEMM_TILES, (0, 1)),
 }
 
 
@@ -89,6 +90,15 @@ def _time_interface(engine, coeffs, reps):
     for _ in range(reps):
         engine.factor(**coeffs)
         best = min(best, engine.timings()['interface_ms'])
+    return best
+
+
+def _time_tree_and_interface(engine, coeffs, reps):
+    best = float('inf')
+    for _ in range(reps):
+        engine.factor(**coeffs)
+        t = engine.timings()
+        best = min(best, t['tree_ms'] + t['interface_ms'])
     return best
 
 
@@ -170,6 +180,15 @@ def tune(engine, coeffs, bnd, reps=2, use_cache=True, path=None, tol=1e-6):
         picks['iface_panel'] = min(cands, key=lambda v: (t_pn[v], cands.index(v)))
         timings['iface_panel_ms'] = {str(v): t for v, t in t_pn.items()}
         _lib.check(engine.L.slab_engine_set_option(engine.h, key, picks['iface_panel']), 'slab_engine_set_option')
+    if engine.precision != 'fp64':
+        key, cands = TUNABLES['gemm_tiles']
+        t_gt = {}
+        for v in cands:
+            _lib.check(engine.L.slab_engine_set_option(engine.h, key, v), 'slab_engine_set_option')
+            t_gt[v] = _time_tree_and_interface(engine, coeffs, reps)
+        picks['gemm_tiles'] = min(cands, key=lambda v: (t_gt[v], cands.index(v)))
+        timings['gemm_tiles_ms'] = {str(v): t for v, t in t_gt.items()}
+        _lib.check(engine.L.slab_engine_set_option(engine.h, key, picks['gemm_tiles']), 'slab_engine_set_option')
     if engine.precision != 'fp64':
         key, cands = TUNABLES['tree_tc']
         t_tc = {}

@@ -348,9 +348,14 @@ static int sm_count() {
   return sms;
 }
 
-// SLAB_GEMM64=1: every FP32 product on the 64 x 64 kernel (for comparisons; read at
-// each launch, so at each graph capture)
+// Tile policy of the FP32 products issued by this host thread: 0 = 128 x 128 tiles
+// where their grid fills the GPU, 1 = always 64 x 64 (an engine sets it from its
+// SLAB_OPT_GEMM_TILES around its work, so graphs capture the policy they ran with;
+// SLAB_GEMM64=1 forces 1 for comparisons).
+static thread_local int g_gemm_tiles = 0;
+void set_gemm_tiles(int policy) { g_gemm_tiles = policy; }
 static bool gemm64_only() {
+  if (g_gemm_tiles == 1) return true;
   const char* e = getenv("SLAB_GEMM64");
   return e && e[0] == '1';
 }

@@ -2176,6 +2176,11 @@ int getrs_batched(cudaStream_t s, int n, int nrhs, const T* LU, const long long*
                   const long long* offB, long long strideB, int ldb, int batch, bool lower = true,
                   bool upper = true);
 
+// Tile policy of the FP32 products (gemm) issued by the calling host thread:
+// 0 = 128 x 128 tiles where their grid fills the GPU, 64 x 64 otherwise; 1 =
+// always 64 x 64.
+void set_gemm_tiles(int policy);
+
 // Large single-matrix LU in place (n x n, lda); ipiv/info device pointers.
 // work: kNB*kNB elements (inverse of the current panel's unit-lower triangle).
 // panel_kind 0: FP32 panels of up to 1536 rows in one CTA; 1: always

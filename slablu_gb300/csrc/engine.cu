@@ -368,6 +368,7 @@ struct EngineImpl : EngineBase {
   bool use_graphs = true;
   bool use_cluster_solve = true;
   int panel_kind = 0;  // SLAB_OPT_IFACE_PANEL
+  int gemm_tiles = 0;  // SLAB_OPT_GEMM_TILES
   // FP32 interface blocks: 1 factors them with the unblocked biglu (SLAB_IFACE_UNBLOCKED=1,
   // for comparison) instead of biglu_blocked
   bool unblocked_iface = false;
@@ -445,11 +446,13 @@ struct EngineImpl : EngineBase {
   }
   // order the engine stream after the caller's stream (and back)
   int enter() {
+    set_gemm_tiles(gemm_tiles);
     SLAB_CUDA_TRY(cudaEventRecord(join, us));
     SLAB_CUDA_TRY(cudaStreamWaitEvent(s, join, 0));
     return SLAB_OK;
   }
   int leave() {
+    set_gemm_tiles(0);
     SLAB_CUDA_TRY(cudaEventRecord(join, s));
     SLAB_CUDA_TRY(cudaStreamWaitEvent(us, join, 0));
     return SLAB_OK;
@@ -561,6 +564,18 @@ struct EngineImpl : EngineBase {
       use_tc_tree = value == 1;
       return SLAB_OK;
     }
+    if (key == SLAB_OPT_GEMM_TILES) {
+      if (value != 0 && value != 1) return set_error(SLAB_ERR_ARG, "gemm_tiles %d not 0 or 1", value);
+      if (value != gemm_tiles) {
+        for (cudaGraphExec_t* gp : {&gfac[1], &gfac[2], &gapp, &gapp_t})
+          if (*gp) {
+            cudaGraphExecDestroy(*gp);
+            *gp = nullptr;
+          }
+      }
+      gemm_tiles = value;
+      return SLAB_OK;
+    }
     if (key == SLAB_OPT_IFACE_PANEL) {
       if (value != 0 && value != 1) return set_error(SLAB_ERR_ARG, "iface_panel %d not 0 or 1", value);
       if (value != panel_kind && gfac[2]) {
@@ -574,6 +589,7 @@ struct EngineImpl : EngineBase {
   }
   int get_option(int key) const override {
     if (key == SLAB_OPT_IFACE_PANEL) return panel_kind;
+    if (key == SLAB_OPT_GEMM_TILES) return gemm_tiles;
     if (key == SLAB_OPT_TREE_TC) return use_tc_tree ? 1 : 0;
     if (key == SLAB_OPT_LEAF_ASSEMBLY) return leaf_split_asm ? 1 : 0;
     if (key == SLAB_OPT_IFACE_OUTER_INV) return use_outer_inv ? 1 : 0;

@@ -36,6 +36,8 @@ def test_tune_picks_valid_choices_and_keeps_the_solution(tmp_path):
     assert picks['leaf_ctas'] in autotune.TUNABLES['leaf_ctas'][1]
     assert picks['iface_solve'] in autotune.TUNABLES['iface_solve'][1]
     assert picks['tree_tc'] in autotune.TUNABLES['tree_tc'][1]
+    assert picks['gemm_tiles'] in autotune.TUNABLES['gemm_tiles'][1]
+    assert eng.L.slab_engine_get_option(eng.h, autotune.TUNABLES['gemm_tiles'][0]) == picks['gemm_tiles']
     assert eng.L.slab_engine_get_option(eng.h, autotune.TUNABLES['leaf_ctas'][0]) == picks['leaf_ctas']
     u1, _, _, _ = eng.solve(bnd, tol=1e-12, max_iter=40)
     assert float(torch.linalg.norm(u1 - u0) / torch.linalg.norm(u0)) < 1e-11

@@ -171,11 +171,11 @@ def test_fp32_blocked_interface_lu_matches_unblocked(monkeypatch):
 
 def test_fp32_products_on_128_tiles_match_64_tiles(monkeypatch):
     """The FP32 products with both sides at least 128 run on 128 x 128 tiles
-    (gemm128_kernel); SLAB_GEMM64=1 keeps them on the 64 x 64 kernel.  The two
-    sum each entry's k terms in different groupings, so the factors agree to
-    rounding and the refined solutions to the refinement level, against each
-    other and against the FP64 engine (interface blocks of 2,080, merge fronts
-    up to 1,040)."""
+    (gemm128_kernel); SLAB_GEMM64=1, or the engine option SLAB_OPT_GEMM_TILES =
+    1, keeps them on the 64 x 64 kernel.  Both sum each entry's k terms in the
+    same order; the refined solutions agree with each other and with the FP64
+    engine to the refinement level (interface blocks of 2,080, merge fronts up
+    to 1,040)."""
     from slablu_gb300 import hps
     from slablu_gb300.engine import SlabEngine
     p, kh, n1 = 6, 20.0, 520
@@ -186,6 +186,7 @@ def test_fp32_products_on_128_tiles_match_64_tiles(monkeypatch):
     one = torch.ones_like(c)
     gen = torch.Generator(device='cuda').manual_seed(5)
     bnd = torch.randn(g.ntot, 2, generator=gen, device='cuda', dtype=torch.float64)
+    from slablu_gb300 import _lib
     sols = {}
     for flag in ('1', '0'):
         monkeypatch.setenv('SLAB_GEMM64', flag)
@@ -195,6 +196,16 @@ def test_fp32_products_on_128_tiles_match_64_tiles(monkeypatch):
             u, _, iters, st = eng.solve(bnd, tol=1e-12, max_iter=60)
             assert st['converged'], (flag, prec, iters, st)
             sols[flag, prec] = u.cpu().numpy()
+    monkeypatch.setenv('SLAB_GEMM64', '0')
+    for prec in ('fp32', 'mixed'):  # the same 64 x 64 choice as an engine option
+        eng = SlabEngine(g, prec)
+        assert eng.L.slab_engine_set_option(eng.h, _lib.SLAB_OPT_GEMM_TILES, 1) == 0
+        assert eng.L.slab_engine_get_option(eng.h, _lib.SLAB_OPT_GEMM_TILES) == 1
+        eng.factor(c11=one, c22=one, c=c)
+        u, _, iters, st = eng.solve(bnd, tol=1e-12, max_iter=60)
+        assert st['converged'], ('option', prec, iters, st)
+        assert np.array_equal(u.cpu().numpy(), sols['1', prec]) or \
+            np.linalg.norm(u.cpu().numpy() - sols['1', prec]) < 1e-11 * np.linalg.norm(sols['1', prec])
     e64 = SlabEngine(g, 'fp64')
     e64.factor(c11=one, c22=one, c=c)
     u64 = e64.solve(bnd, tol=1e-13, max_iter=10)[0].cpu().numpy()
