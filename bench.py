@@ -353,7 +353,9 @@ def bench_config5(dev, nfd=16):
     bnd = torch.ones(geo.ntot, dtype=torch.float64, device=dev)
     probes = torch.as_tensor(problems.probe_nodes(geo.xx_tot, cfg['nprobe']), device=dev)
     eng = SlabEngine(geo, 'fp64')
-    tol = 1e-12
+    # 1e-11: at 1e-12 the relative correction of this FP64 solve sits at the rounding
+    # floor, where the step count (and the timing) varies from call to call
+    tol = 1e-11
     solve = lambda bb: slab_solve(eng, bnd, tol=tol, max_iter=60, c11=ones, c22=ones, c=cfg['c_of_b'](bb))
     with torch.no_grad():
         d = solve(cfg['b_perturbed'](xx))[probes].clone()
