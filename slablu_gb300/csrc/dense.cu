@@ -137,6 +137,24 @@ int getrs_small(cudaStream_t s, int n, int nrhs, const T* LU, const long long* o
 }
 
 template <typename T>
+int getrs_many(cudaStream_t s, int n, int nrhs, const T* LU, long long strideLU, int lda, const int* perm,
+               long long strideP, T* B, long long strideB, int ldb, int batch) {
+  if (n <= 0 || nrhs <= 0 || batch <= 0) return SLAB_OK;
+  const size_t bytes = getrs_many_smem_bytes(n, sizeof(T));
+  SLAB_TRY(ensure_smem(getrs_many_kernel<T>, bytes, "getrs_many"));
+  const int tiles = ceil_div(nrhs, kManyCols);
+  if (tiles > 65535) return set_error(SLAB_ERR_ARG, "getrs_many: %d right-hand sides is too many", nrhs);
+  dim3 grid(batch, tiles);
+  getrs_many_kernel<T><<<grid, 256, bytes, s>>>(n, nrhs, LU, strideLU, lda, perm, strideP, B, strideB, ldb);
+  SLAB_CHECK_LAUNCH();
+  return SLAB_OK;
+}
+template int getrs_many<float>(cudaStream_t, int, int, const float*, long long, int, const int*, long long, float*,
+                               long long, int, int);
+template int getrs_many<double>(cudaStream_t, int, int, const double*, long long, int, const int*, long long,
+                                double*, long long, int, int);
+
+template <typename T>
 int trsv_coop(cudaStream_t s, const T* LU, int lda, int n, const int* perm, const T* Linv, const T* Uinv, int bs,
               const T* B, int ldb, T* X, int ldx, int nrhs, bool trans) {
   if (n <= 0 || nrhs <= 0) return SLAB_OK;

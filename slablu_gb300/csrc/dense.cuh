@@ -1182,6 +1182,129 @@ __global__ void __launch_bounds__(256)
     for (int i = threadIdx.x; i < n; i += blockDim.x) Bg[i + (size_t)c * ldb] = xs[i + c * n];
 }
 
+// Batched X = U^{-1} L^{-1} P B for many right-hand sides (the solve phase with
+// more than four columns): one CTA per (matrix, 32-column tile) with the tile in
+// shared memory.  Per 32-row block the diagonal triangle is solved by lane-per-
+// row substitution with shuffles (each warp four columns, the triangle's rows
+// in registers), then the rows beyond it are updated: the block's factor rows
+// are staged in shared memory 128 rows at a time and each thread keeps one
+// column of the solved block in registers, so an update is four FMAs per
+// shared-memory load.  perm from build_perm_batched.  grid (batch, tiles).
+constexpr int kManyCols = 32;
+constexpr int kManyMaxN = 1024;  // the tile of n rows stays in shared memory
+constexpr int kManyChunk = 128;
+template <typename T>
+__global__ void __launch_bounds__(256) getrs_many_kernel(int n, int nrhs, const T* __restrict__ LU,
+                                                         long long strideLU, int lda, const int* __restrict__ perm,
+                                                         long long strideP, T* B, long long strideB, int ldb) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int NC = kManyCols, CH = kManyChunk;
+  const int ldx = n | 1;
+  T* Xs = reinterpret_cast<T*>(smem_raw);            // n x NC, ld n|1
+  T* Ls = Xs + (size_t)ldx * NC;                      // CH x 33: staged factor rows
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int b = blockIdx.x;
+  const int c0 = blockIdx.y * NC;
+  const int nc = min(NC, nrhs - c0);
+  const T* A = LU + strideLU * b;
+  const int* pv = perm + strideP * b;
+  T* Bg = B + strideB * b + (size_t)c0 * ldb;
+  // loads are issued eight at a time before their stores (one memory latency per
+  // eight elements)
+  for (int base = tid; base < n * NC; base += 8 * blockDim.x) {
+    T v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int idx = base + u * blockDim.x;
+      const int r = idx % n, c = idx / n;
+      v[u] = (idx < n * NC && c < nc) ? Bg[pv[r] + (size_t)c * ldb] : T(0);
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int idx = base + u * blockDim.x;
+      if (idx < n * NC) Xs[(idx % n) + (idx / n) * ldx] = v[u];
+    }
+  }
+  __syncthreads();
+  const int col = tid % NC, rph = tid / NC;  // update: this thread's column and row phase (8 phases)
+  for (int pass = 0; pass < 2; ++pass) {
+    const bool fwd = pass == 0;
+    const int nblk = (n + 31) / 32;
+    for (int st = 0; st < nblk; ++st) {
+      const int kb = fwd ? st * 32 : (nblk - 1 - st) * 32;
+      const int nb = min(32, n - kb);
+      // (a) diagonal triangle: warp w solves columns 4w .. 4w+3
+      {
+        T lrow[32];
+        const T* pc = A + (size_t)kb * lda + kb + (lane < nb ? lane : 0);
+#pragma unroll
+        for (int k = 0; k < 32; ++k) {
+          lrow[k] = (lane < nb && k < nb && (fwd ? k < lane : k > lane)) ? *pc : T(0);
+          pc += lda;
+        }
+        const T d = (!fwd && lane < nb) ? A[(kb + lane) + (size_t)(kb + lane) * lda] : T(1);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int c = 4 * warp + q;
+          T x = lane < nb ? Xs[kb + lane + c * ldx] : T(0);
+          if (fwd) {
+#pragma unroll
+            for (int k = 0; k < 31; ++k) x -= lrow[k] * __shfl_sync(0xffffffffu, x, k);
+          } else {
+#pragma unroll
+            for (int k = 31; k >= 0; --k) {
+              if (k >= nb) continue;
+              if (lane == k) x = x / d;
+              x -= lrow[k] * __shfl_sync(0xffffffffu, x, k);
+            }
+          }
+          if (lane < nb) Xs[kb + lane + c * ldx] = x;
+        }
+      }
+      __syncthreads();
+      // (b) the other rows: below the block (forward) or above it (backward)
+      const int rlo = fwd ? kb + nb : 0, rhi = fwd ? n : kb;
+      T xj[32];
+#pragma unroll
+      for (int k = 0; k < 32; ++k) xj[k] = k < nb ? Xs[kb + k + col * ldx] : T(0);
+      for (int r0 = rlo; r0 < rhi; r0 += CH) {
+        const int rc = min(CH, rhi - r0);
+        for (int base = tid; base < rc * 32; base += 8 * blockDim.x) {
+          T v[8];
+#pragma unroll
+          for (int u = 0; u < 8; ++u) {
+            const int idx = base + u * blockDim.x;
+            const int rr = idx % rc, k = idx / rc;
+            v[u] = (idx < rc * 32 && k < nb) ? A[(r0 + rr) + (size_t)(kb + k) * lda] : T(0);
+          }
+#pragma unroll
+          for (int u = 0; u < 8; ++u) {
+            const int idx = base + u * blockDim.x;
+            if (idx < rc * 32) Ls[(idx % rc) * 33 + idx / rc] = v[u];
+          }
+        }
+        __syncthreads();
+        for (int rr = rph; rr < rc; rr += 256 / NC) {
+          T acc = Xs[r0 + rr + col * ldx];
+          const T* lr = Ls + rr * 33;
+#pragma unroll
+          for (int k = 0; k < 32; ++k) acc -= lr[k] * xj[k];
+          Xs[r0 + rr + col * ldx] = acc;
+        }
+        __syncthreads();
+      }
+    }
+  }
+  for (int idx = tid; idx < n * nc; idx += blockDim.x) {
+    const int r = idx % n, c = idx / n;
+    Bg[r + (size_t)c * ldb] = Xs[r + c * ldx];
+  }
+}
+
+__host__ __device__ inline size_t getrs_many_smem_bytes(int n, size_t elem) {
+  return ((size_t)(n | 1) * kManyCols + (size_t)kManyChunk * 33) * elem;
+}
+
 // Cooperative triangular solves with one large factored matrix (FP64
 // interface blocks): X = U^{-1} L^{-1} P B for nrhs <= 8 columns, using the
 // precomputed inverses of the bs x bs diagonal triangles (tri_inv_blocks).
@@ -2230,6 +2353,12 @@ template <typename T>
 int getrs_small(cudaStream_t s, int n, int nrhs, const T* LU, const long long* offLU, long long strideLU, int lda,
                 const int* perm, const long long* offP, long long strideP, T* B, const long long* offB,
                 long long strideB, int ldb, int batch);
+
+// Batched X = U^{-1} L^{-1} P B for many right-hand sides (getrs_many_kernel,
+// n <= 1024); perm from build_perm_batched.
+template <typename T>
+int getrs_many(cudaStream_t s, int n, int nrhs, const T* LU, long long strideLU, int lda, const int* perm,
+               long long strideP, T* B, long long strideB, int ldb, int batch);
 
 // X = U^{-1} L^{-1} P B for one large factored matrix, nrhs <= 8, cooperative
 // launch; Linv/Uinv from tri_inv_blocks with block size bs.

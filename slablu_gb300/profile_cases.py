@@ -8,7 +8,8 @@
 
 `factor` and `solve` use the Gaussian-lattice Helmholtz field of the benchmark
 (p = 22) on an n x n-point grid ((n/20)^2 leaves): one factorization, and for
-`solve` one refined solve with at most --iters steps.  `dgemm` runs --reps
+`solve` one refined solve with at most --iters steps (u = 1 on the boundary, or
+--nrhs columns of config 4's smoothed random boundary data).  `dgemm` runs --reps
 tensor-core FP64 products C = A B of n x n random matrices (the shape of the
 interface Schur update at n = 2000); `sgemm` runs --reps batched TF32-split FP32
 products C -= A B with A n x k and B k x n (--batch of them: the shape of the
@@ -35,6 +36,7 @@ def main(argv=None):
     ap.add_argument('--k', type=int, default=200)
     ap.add_argument('--batch', type=int, default=10)
     ap.add_argument('--count', type=int, default=8)
+    ap.add_argument('--nrhs', type=int, default=1, help='solve: right-hand sides (config 4 data when > 1)')
     a = ap.parse_args(argv)
     if a.case == 'graph':
         return _graph_case(a)
@@ -80,8 +82,13 @@ def main(argv=None):
     eng = SlabEngine(g, a.precision)
     eng.factor(c11=one, c22=one, c=c)
     if a.case == 'solve':
-        _, _, it, info = eng.solve(torch.ones(g.ntot, dtype=torch.float64, device='cuda'), tol=1e-10,
-                                   max_iter=a.iters, allow_noconv=True)
+        if a.nrhs > 1:
+            B = torch.zeros(g.ntot, a.nrhs, dtype=torch.float64, device='cuda')
+            ix = torch.as_tensor(g.I_Xtot, device='cuda')
+            B[ix] = problems.config4_rhs(len(g.I_Xtot), a.nrhs).to('cuda')
+        else:
+            B = torch.ones(g.ntot, dtype=torch.float64, device='cuda')
+        _, _, it, info = eng.solve(B, tol=1e-10, max_iter=a.iters, allow_noconv=True)
         print('refinement steps', it, info)
     torch.cuda.synchronize()
     print('ok', a.case, g.nboxes, 'leaves', eng.timings())
