@@ -149,6 +149,13 @@ int getrs_many(cudaStream_t s, int n, int nrhs, const T* LU, long long strideLU,
   SLAB_CHECK_LAUNCH();
   return SLAB_OK;
 }
+template <typename T>
+bool getrs_many_fits(int n) {
+  return n <= kManyMaxN &&
+         getrs_many_smem_bytes(n, sizeof(T)) <= allow_dynamic_smem(reinterpret_cast<const void*>(getrs_many_kernel<T>));
+}
+template bool getrs_many_fits<float>(int);
+template bool getrs_many_fits<double>(int);
 template int getrs_many<float>(cudaStream_t, int, int, const float*, long long, int, const int*, long long, float*,
                                long long, int, int);
 template int getrs_many<double>(cudaStream_t, int, int, const double*, long long, int, const int*, long long,

@@ -1201,7 +1201,8 @@ __global__ void __launch_bounds__(256) getrs_many_kernel(int n, int nrhs, const 
   constexpr int NC = kManyCols, CH = kManyChunk;
   const int ldx = n | 1;
   T* Xs = reinterpret_cast<T*>(smem_raw);            // n x NC, ld n|1
-  T* Ls = Xs + (size_t)ldx * NC;                      // CH x 33: staged factor rows
+  constexpr int LS = 36;                              // Ls row stride: rows start 16-byte aligned
+  T* Ls = Xs + (((size_t)ldx * NC + 3) & ~(size_t)3);  // CH x LS: staged factor rows, 16-byte aligned
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int b = blockIdx.x;
   const int c0 = blockIdx.y * NC;
@@ -1242,7 +1243,9 @@ __global__ void __launch_bounds__(256) getrs_many_kernel(int n, int nrhs, const 
           lrow[k] = (lane < nb && k < nb && (fwd ? k < lane : k > lane)) ? *pc : T(0);
           pc += lda;
         }
-        const T d = (!fwd && lane < nb) ? A[(kb + lane) + (size_t)(kb + lane) * lda] : T(1);
+        // the diagonal's reciprocal, once per lane (this is the solve phase: a
+        // product with 1/d instead of the quotient changes only the last bit)
+        const T rd = T(1) / ((!fwd && lane < nb) ? A[(kb + lane) + (size_t)(kb + lane) * lda] : T(1));
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
           const int c = 4 * warp + q;
@@ -1254,7 +1257,7 @@ __global__ void __launch_bounds__(256) getrs_many_kernel(int n, int nrhs, const 
 #pragma unroll
             for (int k = 31; k >= 0; --k) {
               if (k >= nb) continue;
-              if (lane == k) x = x / d;
+              if (lane == k) x *= rd;
               x -= lrow[k] * __shfl_sync(0xffffffffu, x, k);
             }
           }
@@ -1280,15 +1283,21 @@ __global__ void __launch_bounds__(256) getrs_many_kernel(int n, int nrhs, const 
 #pragma unroll
           for (int u = 0; u < 8; ++u) {
             const int idx = base + u * blockDim.x;
-            if (idx < rc * 32) Ls[(idx % rc) * 33 + idx / rc] = v[u];
+            if (idx < rc * 32) Ls[(idx % rc) * LS + idx / rc] = v[u];
           }
         }
         __syncthreads();
         for (int rr = rph; rr < rc; rr += 256 / NC) {
           T acc = Xs[r0 + rr + col * ldx];
-          const T* lr = Ls + rr * 33;
+          const T* lr = Ls + rr * LS;
 #pragma unroll
-          for (int k = 0; k < 32; ++k) acc -= lr[k] * xj[k];
+          for (int k = 0; k < 32; k += 4) {
+            const vec4<T> l4 = ld4(lr + k);  // one shared-memory load for four FMAs
+            acc -= l4.x * xj[k];
+            acc -= l4.y * xj[k + 1];
+            acc -= l4.z * xj[k + 2];
+            acc -= l4.w * xj[k + 3];
+          }
           Xs[r0 + rr + col * ldx] = acc;
         }
         __syncthreads();
@@ -1302,7 +1311,8 @@ __global__ void __launch_bounds__(256) getrs_many_kernel(int n, int nrhs, const 
 }
 
 __host__ __device__ inline size_t getrs_many_smem_bytes(int n, size_t elem) {
-  return ((size_t)(n | 1) * kManyCols + (size_t)kManyChunk * 33) * elem;
+  // Xs, then Ls on a 16-byte boundary (4 spare elements)
+  return ((size_t)(n | 1) * kManyCols + 4 + (size_t)kManyChunk * 36) * elem;
 }
 
 // Cooperative triangular solves with one large factored matrix (FP64
@@ -2359,6 +2369,9 @@ int getrs_small(cudaStream_t s, int n, int nrhs, const T* LU, const long long* o
 template <typename T>
 int getrs_many(cudaStream_t s, int n, int nrhs, const T* LU, long long strideLU, int lda, const int* perm,
                long long strideP, T* B, long long strideB, int ldb, int batch);
+// Whether getrs_many's tile of n rows fits the device's shared memory.
+template <typename T>
+bool getrs_many_fits(int n);
 
 // X = U^{-1} L^{-1} P B for one large factored matrix, nrhs <= 8, cooperative
 // launch; Linv/Uinv from tri_inv_blocks with block size bs.

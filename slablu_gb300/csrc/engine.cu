@@ -1274,7 +1274,7 @@ struct EngineImpl : EngineBase {
     if (nrhs <= 4 && n <= 32 * kWarpSlots)
       SLAB_TRY(getrs_small<T>(s, n, nrhs, G.as<T>(), nullptr, strideG, n, leafperm.as<int>(), nullptr, n, w, nullptr,
                               (long long)n * nrhs, n, (int)nleaf));
-    else if (n <= kManyMaxN)
+    else if (getrs_many_fits<T>(n))
       SLAB_TRY(getrs_many<T>(s, n, nrhs, G.as<T>(), strideG, n, leafperm.as<int>(), n, w, (long long)n * nrhs, n,
                              (int)nleaf));
     else
@@ -1298,7 +1298,7 @@ struct EngineImpl : EngineBase {
       if (nrhs <= 4 && b.nE <= 32 * kWarpSlots)
         SLAB_TRY(getrs_small<T>(s, b.nE, nrhs, Maug, nullptr, strideM, b.nE, permpool.as<int>() + b.offPiv0,
                                 nullptr, b.nE, Y, nullptr, (long long)b.nE * nrhs, b.nE, b.count));
-      else if (b.nE <= kManyMaxN)
+      else if (getrs_many_fits<T>(b.nE))
         SLAB_TRY(getrs_many<T>(s, b.nE, nrhs, Maug, strideM, b.nE, permpool.as<int>() + b.offPiv0, b.nE, Y,
                                (long long)b.nE * nrhs, b.nE, b.count));
       else
