@@ -92,12 +92,20 @@ __global__ void __launch_bounds__(256) residual_kernel(ResidualArgs a) {
       interior_node(r, q, i1, i2);
       const int k = lofs + i1 * p + i2;
       double t11 = 0, t22 = 0, t1 = 0, t2 = 0;
-      for (int j = 0; j < p; ++j) {
-        const double ux1 = u[j * p + i2], ux2 = u[i1 * p + j];
-        t11 += Dsqsh[i1 * p + j] * ux1;
-        t22 += Dsqsh[i2 * p + j] * ux2;
-        t1 += Dsh[i1 * p + j] * ux1;
-        t2 += Dsh[i2 * p + j] * ux2;
+      if (co.c1 || co.c2) {
+        for (int j = 0; j < p; ++j) {
+          const double ux1 = u[j * p + i2], ux2 = u[i1 * p + j];
+          t11 += Dsqsh[i1 * p + j] * ux1;
+          t22 += Dsqsh[i2 * p + j] * ux2;
+          t1 += Dsh[i1 * p + j] * ux1;
+          t2 += Dsh[i2 * p + j] * ux2;
+        }
+      } else {
+        // no first-order terms: half the FP64 products (this kernel is FP64-pipe bound)
+        for (int j = 0; j < p; ++j) {
+          t11 += Dsqsh[i1 * p + j] * u[j * p + i2];
+          t22 += Dsqsh[i2 * p + j] * u[i1 * p + j];
+        }
       }
       double Au = 0.0;
       if (co.c11) Au -= co.c11[k] * t11;
