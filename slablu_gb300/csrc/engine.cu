@@ -375,6 +375,7 @@ struct EngineImpl : EngineBase {
   int leaf_ctas = 0;  // resident leaves per SM in the leaf kernel (0: as many as fit)
   bool leaf_split_asm = false;  // leaf operators assembled by a kernel of their own (no c12)
   DevBuf D, Dsq, Nx, NxcT, NxxT, interp, jxr, leafglob, dirmask;
+  DevBuf ispan;  // per Interp_mat row: [first, last + 1) nonzero column
   DevBuf coef[6];  // c11, c22, c1, c2, c, c12
   bool has[6] = {false, false, false, false, false, false};
   // leaf factors: LU of A_cc and S in G, n x (n + ncolG) per leaf; with a mixed
@@ -852,6 +853,22 @@ struct EngineImpl : EngineBase {
     SLAB_TRY(upload(Dsq, std::vector<double>(hDsq, hDsq + p * p), s));
     SLAB_TRY(upload(Nx, std::vector<double>(hNx, hNx + (size_t)nx * p * p), s));
     SLAB_TRY(upload(interp, std::vector<double>(hinterp, hinterp + (size_t)4 * (p - 1) * nx), s));
+    {
+      // nonzero span of each Interp_mat row (one face's nodes for the reference's
+      // discretisation); the assembly sums only over it
+      std::vector<int> sp(2 * (size_t)4 * (p - 1));
+      for (int t = 0; t < 4 * (p - 1); ++t) {
+        int lo = nx, hi = 0;
+        for (int c = 0; c < nx; ++c)
+          if (hinterp[(size_t)t * nx + c] != 0.0) {
+            lo = std::min(lo, c);
+            hi = c + 1;
+          }
+        sp[2 * t] = lo < hi ? lo : 0;
+        sp[2 * t + 1] = lo < hi ? hi : 0;
+      }
+      SLAB_TRY(upload(ispan, sp, s));
+    }
     SLAB_TRY(upload(jxr, std::vector<int>(hjxr, hjxr + 4 * (p - 1)), s));
     SLAB_TRY(NxcT.alloc((size_t)nx * n * sizeof(T)));
     SLAB_TRY(NxxT.alloc((size_t)nx * nx * sizeof(T)));
@@ -1733,8 +1750,9 @@ struct EngineImpl : EngineBase {
       AssembleArgs aa{};
       aa.p = p; aa.q = q; aa.n = n; aa.nx = nx; aa.nleaf = (int)nleaf; aa.nrhs = nrhs; aa.ntot = ntot;
       aa.leafglob = leafglob.as<int>(); aa.interp = interp.as<double>(); aa.jxreorder = jxr.as<int>();
+      aa.ispan = ispan.as<int>();
       aa.ux = ux_d.as<double>(); aa.uc = uc_d.as<double>(); aa.out = uleaf;
-      assemble_solution_kernel<<<(unsigned)nleaf, 256, (size_t)nx * sizeof(double), s>>>(aa);
+      assemble_solution_kernel<<<(unsigned)nleaf, 256, (size_t)nx * kAssembleRhs * sizeof(double), s>>>(aa);
       SLAB_CHECK_LAUNCH();
     }
     SLAB_CUDA_TRY(cudaEventRecord(ev[5], s));
@@ -1862,8 +1880,9 @@ struct EngineImpl : EngineBase {
       AssembleArgs aa{};
       aa.p = p; aa.q = q; aa.n = n; aa.nx = nx; aa.nleaf = (int)nleaf; aa.nrhs = nrhs; aa.ntot = ntot;
       aa.leafglob = leafglob.as<int>(); aa.interp = interp.as<double>(); aa.jxreorder = jxr.as<int>();
+      aa.ispan = ispan.as<int>();
       aa.ux = ux_d.as<double>(); aa.uc = uc_d.as<double>(); aa.out = uleaf;
-      assemble_solution_kernel<<<(unsigned)nleaf, 256, (size_t)nx * sizeof(double), s>>>(aa);
+      assemble_solution_kernel<<<(unsigned)nleaf, 256, (size_t)nx * kAssembleRhs * sizeof(double), s>>>(aa);
       SLAB_CHECK_LAUNCH();
       return SLAB_OK;
     }();

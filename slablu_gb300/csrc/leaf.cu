@@ -406,27 +406,37 @@ __global__ void __launch_bounds__(256) coeff_grad_kernel(GradArgs a) {
   }
 }
 
+// Leaf-node solution: interior values copied, boundary nodes (faces and corners)
+// through Interp_mat from the face values, kAssembleRhs right-hand sides per
+// pass.  Each row of Interp_mat is summed over its nonzero span only (one face's
+// nodes), in the same column order as the dense sum.
 __global__ void __launch_bounds__(256) assemble_solution_kernel(AssembleArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  double* uxl = reinterpret_cast<double*>(smem_raw);
+  double* uxl = reinterpret_cast<double*>(smem_raw);  // nx x kAssembleRhs
   const int p = a.p, q = a.q, n = a.n, nx = a.nx;
   const int leaf = blockIdx.x, tid = threadIdx.x;
   const int nr = 4 * (p - 1);
   const size_t ldo = (size_t)a.nleaf * p * p;
-  for (int c = 0; c < a.nrhs; ++c) {
+  for (int c0 = 0; c0 < a.nrhs; c0 += kAssembleRhs) {
+    const int gc = min(kAssembleRhs, a.nrhs - c0);
     __syncthreads();
-    for (int s = tid; s < nx; s += blockDim.x) uxl[s] = a.ux[a.leafglob[(size_t)leaf * nx + s] + (size_t)c * a.ntot];
-    __syncthreads();
-    double* out = a.out + (size_t)leaf * p * p + c * ldo;
-    for (int t = tid; t < nr; t += blockDim.x) {
-      double v = 0.0;
-      for (int s = 0; s < nx; ++s) v += a.interp[(size_t)t * nx + s] * uxl[s];
-      out[a.jxreorder[t]] = v;
+    for (int idx = tid; idx < nx * gc; idx += blockDim.x) {
+      const int s = idx % nx, c = idx / nx;
+      uxl[s + c * nx] = a.ux[a.leafglob[(size_t)leaf * nx + s] + (size_t)(c0 + c) * a.ntot];
     }
-    for (int r = tid; r < n; r += blockDim.x) {
+    __syncthreads();
+    for (int idx = tid; idx < nr * gc; idx += blockDim.x) {
+      const int t = idx % nr, c = idx / nr;
+      const int lo = a.ispan ? a.ispan[2 * t] : 0, hi = a.ispan ? a.ispan[2 * t + 1] : nx;
+      double v = 0.0;
+      for (int s = lo; s < hi; ++s) v += a.interp[(size_t)t * nx + s] * uxl[s + c * nx];
+      a.out[(size_t)leaf * p * p + (c0 + c) * ldo + a.jxreorder[t]] = v;
+    }
+    for (int idx = tid; idx < n * gc; idx += blockDim.x) {
+      const int r = idx % n, c = idx / n;
       int i1, i2;
       interior_node(r, q, i1, i2);
-      out[i1 * p + i2] = a.uc[((size_t)leaf * a.nrhs + c) * n + r];
+      a.out[(size_t)leaf * p * p + (c0 + c) * ldo + i1 * p + i2] = a.uc[((size_t)leaf * a.nrhs + c0 + c) * n + r];
     }
   }
 }

@@ -408,8 +408,11 @@ struct AssembleArgs {
   const double* ux;       // ntot x nrhs
   const double* uc;       // leaf-major
   double* out;
+  const int* ispan;       // per row of interp [first, last + 1) nonzero column, or null (all nx)
 };
 
+// Right-hand sides assembled together by one CTA (shared memory nx x this doubles).
+constexpr int kAssembleRhs = 8;
 __global__ void assemble_solution_kernel(AssembleArgs a);
 
 }  // namespace slab
