@@ -270,13 +270,18 @@ __global__ void __launch_bounds__(256) residual_t_kernel(ResidualArgs a) {
         face_node(idx - n, p, q, l1, l2);
       const int l = l1 * p + l2;
       double z = 0.0;
-      for (int k1 = 0; k1 < p; ++k1) {
-        z += Dsqsh[k1 * p + l1] * m11[k1 * p + l2];
-        z += Dsh[k1 * p + l1] * m1[k1 * p + l2];
-      }
-      for (int k2 = 0; k2 < p; ++k2) {
-        z += Dsqsh[k2 * p + l2] * m22[l1 * p + k2];
-        z += Dsh[k2 * p + l2] * m2[l1 * p + k2];
+      if (co.c1 || co.c2) {
+        for (int k1 = 0; k1 < p; ++k1) {
+          z += Dsqsh[k1 * p + l1] * m11[k1 * p + l2];
+          z += Dsh[k1 * p + l1] * m1[k1 * p + l2];
+        }
+        for (int k2 = 0; k2 < p; ++k2) {
+          z += Dsqsh[k2 * p + l2] * m22[l1 * p + k2];
+          z += Dsh[k2 * p + l2] * m2[l1 * p + k2];
+        }
+      } else {  // no first-order terms: their (zero) products skipped
+        for (int k1 = 0; k1 < p; ++k1) z += Dsqsh[k1 * p + l1] * m11[k1 * p + l2];
+        for (int k2 = 0; k2 < p; ++k2) z += Dsqsh[k2 * p + l2] * m22[l1 * p + k2];
       }
       if (idx < n && co.c) z += co.c[lofs + l] * a.uc[((size_t)leaf * a.nrhs + c) * n + idx];
       // Nx^T lx: face rows couple the nodes on their normal line
