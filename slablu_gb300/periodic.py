@@ -159,6 +159,10 @@ class PeriodicEdge:
         relative edge residual."""
         if self.S is None:
             raise RuntimeError('PeriodicEdge.build() first')
+        if fbody is not None:
+            # the edge flux balance is formed from the face values alone (edge_flux); a
+            # body load adds its particular flux at the edge, which that map leaves out
+            raise NotImplementedError('PeriodicEdge.solve: body loads with periodic boundaries')
         L, R = self._idx(bnd.device)
         b = bnd.clone()
         if b.dim() == 1:

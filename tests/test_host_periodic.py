@@ -137,6 +137,9 @@ def test_periodic_edge_schur_solve(golden_dir, name):
     r = periodic.fold(Au[ic], sets)
     ff = periodic.fold(-Ad[ic], sets)
     assert float(torch.linalg.norm(r) / torch.linalg.norm(ff)) < 1e-12
+    # a body load would need its particular flux in the edge balance: refused
+    with pytest.raises(NotImplementedError):
+        edge.solve(bnd, fbody=torch.zeros(md.nboxes * md.p ** 2, 1, dtype=torch.float64))
 
 
 def test_fold_and_row_subset(golden_dir):
