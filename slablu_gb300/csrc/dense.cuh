@@ -807,7 +807,18 @@ __global__ void __launch_bounds__(256) gemm_narrow_kernel(int m, int n, int k, T
     __syncthreads();
     if (r < m) {
       const T* ap = A + r + (size_t)k0 * lda;
-      for (int kk = 0; kk < kc; ++kk) {
+      int kk = 0;
+      // eight loads of A in flight before their products (same order of the sums)
+      for (; kk + 8 <= kc; kk += 8) {
+        T av[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) av[u] = ap[(size_t)(kk + u) * lda];
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+#pragma unroll
+          for (int c = 0; c < NC; ++c) acc[c] += av[u] * Bs[c * KC + kk + u];
+      }
+      for (; kk < kc; ++kk) {
         const T a = ap[(size_t)kk * lda];
 #pragma unroll
         for (int c = 0; c < NC; ++c) acc[c] += a * Bs[c * KC + kk];
