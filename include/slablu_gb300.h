@@ -135,8 +135,9 @@ int slab_engine_destroy(slab_engine* e);
  * curved domains): the c12 branch of form_DtNs (src_disc/hps_parallel_leaf_ops.py
  * :59-65, 84-92) -- leaves couple to their corners through Interp_mat.  Same
  * arguments as slab_engine_create; factor it with slab_engine_factor_mixed.
- * Solves and the residual work as for slab_engine_create; the adjoint and the
- * coefficient gradients return SLAB_ERR_ARG.
+ * Solves, the residual and the adjoint work as for slab_engine_create; the
+ * coefficient gradients, dL/dc12 included, come from
+ * slab_engine_coeff_grad_mixed.
  */
 int slab_engine_create_mixed(slab_engine** out, int p, int n0, int n1, int buf, int precision, const double* h_D,
                              const double* h_Dsq, const double* h_Nx, const double* h_interp,
@@ -248,6 +249,17 @@ int slab_engine_adjoint(slab_engine* e, int nrhs, const double* d_gleaf, const d
 int slab_engine_coeff_grad(slab_engine* e, int nrhs, const double* d_ufaces, const double* d_uleaf,
                            const double* d_lam_leaf, double* d_gc11, double* d_gc22, double* d_gc1, double* d_gc2,
                            double* d_gc);
+
+/* The same for an engine from slab_engine_create_mixed, with dL/dc12 in d_gc12
+ * (NULL to skip): every term is evaluated on the node values the PDE rows see,
+ * the interior values and Interp_mat u_faces on the leaf boundary (corners
+ * included), and dL/dc12 = 2 lam (D12 u) with D12 = kron(D, D) (the c12 term
+ * -2 c12 D12 of Aloc, src_disc/hps_parallel_leaf_ops.py:17-27).  On an engine
+ * without c12 a non-NULL d_gc12 returns SLAB_ERR_ARG; slab_engine_coeff_grad on
+ * a mixed engine gives the other five. */
+int slab_engine_coeff_grad_mixed(slab_engine* e, int nrhs, const double* d_ufaces, const double* d_uleaf,
+                                 const double* d_lam_leaf, double* d_gc11, double* d_gc22, double* d_gc12,
+                                 double* d_gc1, double* d_gc2, double* d_gc);
 
 /* FP64 matrix product on the BF16 tensor cores (tcgen05) by exact slicing:
  * C = alpha A B + beta C with A (m x k), B (k x n), C (m x n), column-major

@@ -8,6 +8,10 @@ without Dirichlet data]:
   interior PDE rows  Aloc[Jc, :] u_leaf = f          (hps_parallel_leaf_ops.py:17-27)
   face flux rows     sum over the leaves of a face of Nx[s, :] u_leaf = 0
                      (the rows that the DtN maps Nx[:,Jc] S + Nx[:,Jx] condense, :50-58).
+With a mixed derivative (c12) the interior PDE rows see the leaf boundary
+through Interp_mat, corners included (the c12 branch of form_DtNs, :59-65,
+84-92): their face columns are Aloc[Jc, Jxreorder] Interp_mat, while the flux
+rows keep Nx on the face values themselves.
 This module assembles that system with SciPy, solves it directly, and computes
 gradients of L = sum(w * u) at the leaf nodes by the transposed solve: a dense
 FP64 reference gradient independent of the GPU engine's factor reuse.
@@ -19,7 +23,7 @@ import scipy.sparse.linalg as spla
 
 from . import leaf as leafmod
 
-KEYS = ('c11', 'c22', 'c1', 'c2', 'c')
+KEYS = ('c11', 'c22', 'c12', 'c1', 'c2', 'c')
 
 
 class Collocation:
@@ -44,12 +48,16 @@ class Collocation:
         self.fidx = fidx
         A = leafmod.aloc(ld, coeffs)                # (nl, p^2, p^2)
         self.A = A
+        self.mixed = coeffs.get('c12') is not None
         rows_uu, cols_uu, vals_uu, rows_ud, cols_ud, vals_ud = [], [], [], [], [], []
         leaf = np.arange(nl)
         # interior PDE rows
         r_int = leaf[:, None] * n + np.arange(n)[None, :]                    # (nl, n)
         Acc = A[:, ld.Jc][:, :, ld.Jc]
-        Acx = A[:, ld.Jc][:, :, ld.Jx]
+        if self.mixed:   # the interpolated boundary, corners included
+            Acx = A[:, ld.Jc][:, :, ld.Jxreorder] @ ld.Interp_mat[None]
+        else:
+            Acx = A[:, ld.Jc][:, :, ld.Jx]
         rows_uu.append(np.repeat(r_int[:, :, None], n, axis=2).ravel())
         cols_uu.append(np.repeat(r_int[:, None, :], n, axis=1).ravel())
         vals_uu.append(Acc.ravel())
@@ -151,8 +159,13 @@ class Collocation:
         lam_faces = np.zeros((md.ntot, nrhs))
         lam_faces[nd] = lam[self.upos[nd]]
         out['lam_faces'] = lam_faces
-        u = self.leaf_full(uU, ufaces)                                             # (nl, p^2, nrhs)
-        ops = {'c11': (ld.D11, -1.0), 'c22': (ld.D22, -1.0), 'c1': (ld.D1, 1.0), 'c2': (ld.D2, 1.0)}
+        # the node values the PDE rows see: face values, or with c12 the interpolated boundary
+        if self.mixed:
+            u = self.assemble(uU, ufaces).reshape(nl, p * p, nrhs)
+        else:
+            u = self.leaf_full(uU, ufaces)                                         # (nl, p^2, nrhs)
+        ops = {'c11': (ld.D11, -1.0), 'c22': (ld.D22, -1.0), 'c12': (ld.D12, -2.0), 'c1': (ld.D1, 1.0),
+               'c2': (ld.D2, 1.0)}
         for key in KEYS:
             if self.coeffs.get(key) is None:
                 continue

@@ -45,6 +45,7 @@ _SIGS = {
     'slab_engine_adjoint': (c_int, [c_void, c_int, c_void, c_void, c_double, c_int, c_void, c_void, c_void,
                                     P_int, P_double]),
     'slab_engine_coeff_grad': (c_int, [c_void, c_int] + [c_void] * 8),
+    'slab_engine_coeff_grad_mixed': (c_int, [c_void, c_int] + [c_void] * 9),
     'slab_engine_factor_bytes': (c_size, [c_void]),
     'slab_engine_solve_bytes': (c_size, [c_void]),
     'slab_engine_timings': (c_int, [c_void, P_double, c_int]),

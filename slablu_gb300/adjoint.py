@@ -3,10 +3,11 @@
 Forward: factor A(c) with the given coefficient fields and solve A u = f with
 Dirichlet data (slab_engine_factor / slab_engine_solve).  Backward: one
 transposed solve with the stored factors (slab_engine_adjoint) and the
-coefficient-gradient kernel (slab_engine_coeff_grad).  The reference has no
-adjoint; its transposed building blocks are lusolve_sweep_transpose
-(src_solver/block_tridiag_solver_dense.py:205-222) and solve_slab(transpose=True)
-(src_solver/slablu_solver.py:901-943).
+coefficient-gradient kernel (slab_engine_coeff_grad; slab_engine_coeff_grad_mixed
+for an engine with a mixed derivative c12, whose gradient it also gives).  The
+reference has no adjoint; its transposed building blocks are
+lusolve_sweep_transpose (src_solver/block_tridiag_solver_dense.py:205-222) and
+solve_slab(transpose=True) (src_solver/slablu_solver.py:901-943).
 
     eng = SlabEngine(geom, 'mixed')
     b = torch.tensor(..., requires_grad=True)           # field at the leaf nodes
@@ -18,7 +19,7 @@ import torch
 
 from .engine import SlabEngine
 
-_KEYS = ('c11', 'c22', 'c1', 'c2', 'c')
+_KEYS = ('c11', 'c22', 'c12', 'c1', 'c2', 'c')
 
 
 class _SlabSolve(torch.autograd.Function):

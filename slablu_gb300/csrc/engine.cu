@@ -334,7 +334,7 @@ struct EngineBase {
   virtual int adjoint(int nrhs, const double* gleaf, const double* gfaces, double tol, int max_iter, double* lam_leaf,
                       double* lam_faces, double* gbnd, int* iters, double* stats) = 0;
   virtual int coeff_grad(int nrhs, const double* ufaces, const double* uleaf, const double* lam_leaf, double* g11,
-                         double* g22, double* g1, double* g2, double* g0) = 0;
+                         double* g22, double* g12, double* g1, double* g2, double* g0) = 0;
   virtual size_t factor_bytes() const = 0;
   virtual size_t solve_bytes() const = 0;
   virtual int capture_solve(cudaGraph_t G, int nrhs, const double* bnd, const double* fbody, double* uleaf,
@@ -1474,7 +1474,14 @@ struct EngineImpl : EngineBase {
     r.co = coeffs(); r.D = D.as<double>(); r.Dsq = Dsq.as<double>();
     r.leafglob = leafglob.as<int>(); r.dirmask = dirmask.as<unsigned char>();
     r.ux = lx; r.uc = lc; r.fbody = gint; r.rc = rc; r.rx = rx; r.all_faces = all_faces ? 1 : 0;
-    residual_t_kernel<<<(unsigned)nleaf, 256, (6 * (size_t)p * p + nx) * sizeof(double), s>>>(r);
+    if (mixed) {
+      r.interp = interp.as<double>(); r.jxr = jxr.as<int>(); r.nxa = 4 * (p - 1);
+      const size_t bytes = (9 * (size_t)p * p + nx) * sizeof(double);
+      SLAB_TRY(ensure_smem(residual_t_mixed_kernel, bytes, "residual_t_mixed"));
+      residual_t_mixed_kernel<<<(unsigned)nleaf, 256, bytes, s>>>(r);
+    } else {
+      residual_t_kernel<<<(unsigned)nleaf, 256, (6 * (size_t)p * p + nx) * sizeof(double), s>>>(r);
+    }
     SLAB_CHECK_LAUNCH();
     return SLAB_OK;
   }
@@ -1490,7 +1497,6 @@ struct EngineImpl : EngineBase {
 
   int adjoint(int nrhs, const double* gleaf, const double* gfaces, double tol, int max_iter, double* lam_leaf,
               double* lam_faces, double* gbnd, int* iters, double* stats) override {
-    if (mixed) return set_error(SLAB_ERR_ARG, "slab_engine_adjoint: not provided with a mixed derivative (c12)");
     SLAB_TRY(enter());
     int st = SLAB_OK, total_it = 0;
     double worst[5] = {0, 0, 0, 0, 0};
@@ -1621,8 +1627,9 @@ struct EngineImpl : EngineBase {
   }
 
   int coeff_grad(int nrhs, const double* ufaces, const double* uleaf, const double* lam_leaf, double* g11,
-                 double* g22, double* g1, double* g2, double* g0) override {
-    if (mixed) return set_error(SLAB_ERR_ARG, "slab_engine_coeff_grad: not provided with a mixed derivative (c12)");
+                 double* g22, double* g12, double* g1, double* g2, double* g0) override {
+    if (g12 && !mixed)
+      return set_error(SLAB_ERR_ARG, "slab_engine_coeff_grad_mixed: the engine has no mixed derivative (c12)");
     if (nrhs <= 0 || !ufaces || !uleaf || !lam_leaf)
       return set_error(SLAB_ERR_ARG, "slab_engine_coeff_grad: invalid arguments");
     if (n > 4 * 256) return set_error(SLAB_ERR_ARG, "slab_engine_coeff_grad: leaf order p=%d too large", p);
@@ -1632,7 +1639,14 @@ struct EngineImpl : EngineBase {
     ga.D = D.as<double>(); ga.Dsq = Dsq.as<double>(); ga.leafglob = leafglob.as<int>();
     ga.uleaf = uleaf; ga.ufaces = ufaces; ga.lam = lam_leaf;
     ga.g11 = g11; ga.g22 = g22; ga.g1 = g1; ga.g2 = g2; ga.g0 = g0;
-    coeff_grad_kernel<<<(unsigned)nleaf, 256, 3 * (size_t)p * p * sizeof(double), s>>>(ga);
+    if (mixed) {
+      ga.g12 = g12; ga.interp = interp.as<double>(); ga.jxr = jxr.as<int>(); ga.nxa = 4 * (p - 1);
+      const size_t bytes = (4 * (size_t)p * p + nx) * sizeof(double);
+      SLAB_TRY(ensure_smem(coeff_grad_mixed_kernel, bytes, "coeff_grad_mixed"));
+      coeff_grad_mixed_kernel<<<(unsigned)nleaf, 256, bytes, s>>>(ga);
+    } else {
+      coeff_grad_kernel<<<(unsigned)nleaf, 256, 3 * (size_t)p * p * sizeof(double), s>>>(ga);
+    }
     SLAB_CHECK_LAUNCH();
     return leave();
   }
@@ -2128,7 +2142,14 @@ extern "C" int slab_engine_coeff_grad(slab_engine* e, int nrhs, const double* uf
                                       const double* lam_leaf, double* g11, double* g22, double* g1, double* g2,
                                       double* g) {
   if (!e) return slab::set_error(SLAB_ERR_ARG, "slab_engine_coeff_grad: null engine");
-  return e->impl->coeff_grad(nrhs, ufaces, uleaf, lam_leaf, g11, g22, g1, g2, g);
+  return e->impl->coeff_grad(nrhs, ufaces, uleaf, lam_leaf, g11, g22, nullptr, g1, g2, g);
+}
+
+extern "C" int slab_engine_coeff_grad_mixed(slab_engine* e, int nrhs, const double* ufaces, const double* uleaf,
+                                            const double* lam_leaf, double* g11, double* g22, double* g12,
+                                            double* g1, double* g2, double* g) {
+  if (!e) return slab::set_error(SLAB_ERR_ARG, "slab_engine_coeff_grad_mixed: null engine");
+  return e->impl->coeff_grad(nrhs, ufaces, uleaf, lam_leaf, g11, g22, g12, g1, g2, g);
 }
 
 extern "C" int slab_engine_residual(slab_engine* e, int nrhs, const double* ufaces, const double* uint,

@@ -306,6 +306,106 @@ __global__ void __launch_bounds__(256) residual_t_kernel(ResidualArgs a) {
   }
 }
 
+// Transposed residual with a mixed derivative: the PDE rows see every leaf node
+// (the boundary through Interp_mat, corners included), so their part of
+// A^T lam is formed on the whole p x p grid and carried back to the face
+// columns by Interp_mat^T; the flux rows see the interior and face nodes only.
+__global__ void __launch_bounds__(256) residual_t_mixed_kernel(ResidualArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int p = a.p, q = a.q, n = a.n, nx = a.nx, nxa = a.nxa, pp = p * p;
+  double* Dsh = reinterpret_cast<double*>(smem_raw);
+  double* Dsqsh = Dsh + pp;
+  double* m11 = Dsqsh + pp;  // -c11 lam, -c22 lam, -2 c12 lam, -c1 lam, -c2 lam on the grid
+  double* m22 = m11 + pp;
+  double* m12 = m22 + pp;
+  double* m1 = m12 + pp;
+  double* m2 = m1 + pp;
+  double* V = m2 + pp;       // m12 D
+  double* zp = V + pp;       // PDE-row part of A^T lam at every leaf node
+  double* lx = zp + pp;      // lambda on the leaf's face nodes (0 on Dirichlet faces)
+  const int leaf = blockIdx.x;
+  const int tid = threadIdx.x;
+  for (int i = tid; i < pp; i += blockDim.x) {
+    Dsh[i] = a.D[i];
+    Dsqsh[i] = a.Dsq[i];
+  }
+  const int lofs = leaf * pp;
+  const LeafCoeffs& co = a.co;
+  for (int c = 0; c < a.nrhs; ++c) {
+    __syncthreads();
+    for (int i = tid; i < pp; i += blockDim.x) m11[i] = m22[i] = m12[i] = m1[i] = m2[i] = 0.0;
+    __syncthreads();
+    for (int r = tid; r < n; r += blockDim.x) {
+      int i1, i2;
+      interior_node(r, q, i1, i2);
+      const int k = i1 * p + i2;
+      const double l = a.uc[((size_t)leaf * a.nrhs + c) * n + r];
+      if (co.c11) m11[k] = -co.c11[lofs + k] * l;
+      if (co.c22) m22[k] = -co.c22[lofs + k] * l;
+      if (co.c12) m12[k] = (-2.0 * co.c12[lofs + k]) * l;
+      if (co.c1) m1[k] = -co.c1[lofs + k] * l;
+      if (co.c2) m2[k] = -co.c2[lofs + k] * l;
+    }
+    for (int s = tid; s < nx; s += blockDim.x) {
+      const int g = a.leafglob[(size_t)leaf * nx + s];
+      lx[s] = a.dirmask[g] ? 0.0 : a.ux[g + (size_t)c * a.ntot];
+    }
+    __syncthreads();
+    for (int idx = tid; idx < pp; idx += blockDim.x) {
+      const int k1 = idx / p, l2 = idx % p;
+      double v = 0.0;
+      for (int k2 = 0; k2 < p; ++k2) v += m12[k1 * p + k2] * Dsh[k2 * p + l2];
+      V[idx] = v;
+    }
+    __syncthreads();
+    // zp[l] = sum_k Aloc[k, l] lam_k over the interior rows k, at every node l
+    for (int idx = tid; idx < pp; idx += blockDim.x) {
+      const int l1 = idx / p, l2 = idx % p;
+      double z = 0.0;
+      for (int k1 = 0; k1 < p; ++k1) {
+        z += Dsqsh[k1 * p + l1] * m11[k1 * p + l2];
+        z += Dsh[k1 * p + l1] * m1[k1 * p + l2];
+        z += Dsh[k1 * p + l1] * V[k1 * p + l2];
+      }
+      for (int k2 = 0; k2 < p; ++k2) {
+        z += Dsqsh[k2 * p + l2] * m22[l1 * p + k2];
+        z += Dsh[k2 * p + l2] * m2[l1 * p + k2];
+      }
+      zp[idx] = z;
+    }
+    __syncthreads();
+    for (int idx = tid; idx < n + nx; idx += blockDim.x) {
+      int l1, l2;
+      if (idx < n)
+        interior_node(idx, q, l1, l2);
+      else
+        face_node(idx - n, p, q, l1, l2);
+      const int l = l1 * p + l2;
+      // Nx^T lx: face rows couple the nodes on their normal line (never a corner)
+      double z = 0.0;
+      if (l2 >= 1 && l2 <= p - 2) {
+        z += Dsh[l1] * lx[l2 - 1];
+        z -= Dsh[(p - 1) * p + l1] * lx[q + l2 - 1];
+      }
+      if (l1 >= 1 && l1 <= p - 2) {
+        z += Dsh[l2] * lx[2 * q + l1 - 1];
+        z -= Dsh[(p - 1) * p + l2] * lx[3 * q + l1 - 1];
+      }
+      if (idx < n) {
+        z += zp[l];
+        if (co.c) z += co.c[lofs + l] * a.uc[((size_t)leaf * a.nrhs + c) * n + idx];
+        const double g = a.fbody ? a.fbody[((size_t)leaf * a.nrhs + c) * n + idx] : 0.0;
+        a.rc[((size_t)leaf * a.nrhs + c) * n + idx] = g - z;
+      } else {
+        const int s = idx - n;
+        for (int t = 0; t < nxa; ++t) z += a.interp[(size_t)t * nx + s] * zp[a.jxr[t]];
+        const int gf = a.leafglob[(size_t)leaf * nx + s];
+        if (a.all_faces || !a.dirmask[gf]) atomicAdd(&a.rx[gf + (size_t)c * a.ntot], -z);
+      }
+    }
+  }
+}
+
 __global__ void __launch_bounds__(256) assemble_t_kernel(AssembleTArgs a) {
   const int p = a.p, q = a.q, n = a.n, nx = a.nx;
   const int leaf = blockIdx.x, tid = threadIdx.x;
@@ -408,6 +508,97 @@ __global__ void __launch_bounds__(256) coeff_grad_kernel(GradArgs a) {
     if (a.g1) a.g1[k] = acc[o][2];
     if (a.g2) a.g2[k] = acc[o][3];
     if (a.g0) a.g0[k] = acc[o][4];
+  }
+}
+
+// Coefficient gradients with a mixed derivative: the PDE rows see the
+// interpolated boundary u[Jxreorder] = Interp_mat u_faces (corners included),
+// and dL/dc12_k = 2 lam_k (D12 u)_k with D12 u = D U D^T on the leaf grid.
+__global__ void __launch_bounds__(256) coeff_grad_mixed_kernel(GradArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int p = a.p, q = a.q, n = a.n, nx = a.nx, nxa = a.nxa, pp = p * p;
+  double* Dsh = reinterpret_cast<double*>(smem_raw);
+  double* Dsqsh = Dsh + pp;
+  double* u = Dsqsh + pp;
+  double* W = u + pp;   // U D^T
+  double* uf = W + pp;  // the leaf's nx face values
+  const int leaf = blockIdx.x, tid = threadIdx.x;
+  for (int i = tid; i < pp; i += blockDim.x) {
+    Dsh[i] = a.D[i];
+    Dsqsh[i] = a.Dsq[i];
+  }
+  const int lofs = leaf * pp;
+  const size_t ldl = (size_t)a.nleaf * pp;
+  double* outs[6] = {a.g11, a.g22, a.g1, a.g2, a.g0, a.g12};
+  for (int i = tid; i < pp; i += blockDim.x) {
+    const int i1 = i / p, i2 = i % p;
+    if (i1 == 0 || i1 == p - 1 || i2 == 0 || i2 == p - 1)
+      for (int t = 0; t < 6; ++t)
+        if (outs[t]) outs[t][lofs + i] = 0.0;
+  }
+  constexpr int kMaxOwn = 4;  // n <= kMaxOwn * blockDim.x
+  double acc[kMaxOwn][6];
+#pragma unroll
+  for (int o = 0; o < kMaxOwn; ++o)
+#pragma unroll
+    for (int t = 0; t < 6; ++t) acc[o][t] = 0.0;
+  for (int c = 0; c < a.nrhs; ++c) {
+    __syncthreads();
+    for (int i = tid; i < pp; i += blockDim.x) u[i] = 0.0;
+    for (int s = tid; s < nx; s += blockDim.x) uf[s] = a.ufaces[a.leafglob[(size_t)leaf * nx + s] + (size_t)c * a.ntot];
+    __syncthreads();
+    for (int r = tid; r < n; r += blockDim.x) {
+      int i1, i2;
+      interior_node(r, q, i1, i2);
+      u[i1 * p + i2] = a.uleaf[lofs + i1 * p + i2 + c * ldl];
+    }
+    for (int t = tid; t < nxa; t += blockDim.x) {
+      double v = 0.0;
+      for (int s = 0; s < nx; ++s) v += a.interp[(size_t)t * nx + s] * uf[s];
+      u[a.jxr[t]] = v;
+    }
+    __syncthreads();
+    for (int idx = tid; idx < pp; idx += blockDim.x) {
+      const int j1 = idx / p, i2 = idx % p;
+      double w = 0.0;
+      for (int j2 = 0; j2 < p; ++j2) w += u[j1 * p + j2] * Dsh[i2 * p + j2];
+      W[idx] = w;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int o = 0; o < kMaxOwn; ++o) {
+      const int r = tid + o * blockDim.x;
+      if (r >= n) break;
+      int i1, i2;
+      interior_node(r, q, i1, i2);
+      const int k = i1 * p + i2;
+      const double l = a.lam[lofs + k + c * ldl];
+      double t11 = 0, t22 = 0, t1 = 0, t2 = 0, t12 = 0;
+      for (int j = 0; j < p; ++j) {
+        const double ux1 = u[j * p + i2], ux2 = u[i1 * p + j];
+        t11 += Dsqsh[i1 * p + j] * ux1;
+        t22 += Dsqsh[i2 * p + j] * ux2;
+        t1 += Dsh[i1 * p + j] * ux1;
+        t2 += Dsh[i2 * p + j] * ux2;
+        t12 += Dsh[i1 * p + j] * W[j * p + i2];
+      }
+      acc[o][0] += l * t11;
+      acc[o][1] += l * t22;
+      acc[o][2] += l * t1;
+      acc[o][3] += l * t2;
+      acc[o][4] -= l * u[k];
+      acc[o][5] += 2.0 * l * t12;
+    }
+  }
+#pragma unroll
+  for (int o = 0; o < kMaxOwn; ++o) {
+    const int r = tid + o * blockDim.x;
+    if (r >= n) break;
+    int i1, i2;
+    interior_node(r, q, i1, i2);
+    const int k = lofs + i1 * p + i2;
+    for (int t = 0; t < 6; ++t)
+      if (outs[t]) outs[t][k] = acc[o][t];
   }
 }
 

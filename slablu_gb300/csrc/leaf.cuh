@@ -358,6 +358,13 @@ __global__ void residual_mixed_kernel(ResidualArgs a);
 // sensitivity of the loss to the Dirichlet data.
 __global__ void residual_t_kernel(ResidualArgs a);
 
+// The same with a mixed derivative c12 (interp, jxr, nxa as for
+// residual_mixed_kernel; shared memory (9 p^2 + nx) doubles): the PDE rows'
+// part of A^T lam is formed at every leaf node, corners included, and reaches
+// the face columns through Interp_mat^T; the flux rows' part (Nx^T lam_x) is
+// added at the interior and face nodes.
+__global__ void residual_t_mixed_kernel(ResidualArgs a);
+
 // Adjoint of the solution assembly (sol_tot from interior and face values):
 // dsol (nleaf*p*p x nrhs, column-major) -> g_int = dsol at interior nodes
 // (leaf-major) and g_faces += Interp^T dsol at the leaf boundary nodes
@@ -395,8 +402,21 @@ struct GradArgs {
   double* g1;
   double* g2;
   double* g0;            // each nleaf*p*p or null
+  // coeff_grad_mixed_kernel only: dL/dc12 (or null), Interp_mat (nxa x nx,
+  // row-major) and the Jxreorder nodes
+  double* g12;
+  const double* interp;
+  const int* jxr;
+  int nxa;
 };
 __global__ void coeff_grad_kernel(GradArgs a);
+
+// The same for an operator with a mixed derivative (shared memory (4 p^2 + nx)
+// doubles): every term is evaluated on the node values the PDE rows see, the
+// interior values and Interp_mat u_faces on the leaf boundary (corners
+// included); with (A u)_k carrying -2 c12_k (D12 u)_k, dL/dc12_k =
+// 2 lam_k (D12 u)_k.
+__global__ void coeff_grad_mixed_kernel(GradArgs a);
 
 // sol_tot assembly: out[(leaf*p*p + k) + c*nleaf*p*p] for every leaf node.
 struct AssembleArgs {

@@ -152,18 +152,19 @@ class SlabEngine:
         ufaces (ntot, nrhs), uleaf (npts, nrhs): forward solution; lam_leaf
         (npts, nrhs) from adjoint().  Returns {key: (npts,) tensor}, summed over rhs.
         """
+        order = ('c11', 'c22', 'c12', 'c1', 'c2', 'c') if self.mixed else ('c11', 'c22', 'c1', 'c2', 'c')
+        for k in keys:
+            if k not in order:
+                raise ValueError(f'unknown coefficient {k}' + (' (c12 needs SlabEngine(mixed=True))'
+                                                               if k == 'c12' else ''))
         nrhs = 1 if uleaf.dim() == 1 else uleaf.shape[1]
         uf = _col_major(ufaces.to(torch.float64), self.ntot)
         ul = _col_major(uleaf.to(torch.float64), self.npts)
         lm = _col_major(lam_leaf.to(torch.float64), self.npts)
         out = {k: torch.empty(self.npts, dtype=torch.float64, device=ul.device) for k in keys}
-        order = ('c11', 'c22', 'c1', 'c2', 'c')
-        for k in keys:
-            if k not in order:
-                raise ValueError(f'unknown coefficient {k}')
-        st = self.L.slab_engine_coeff_grad(self.h, nrhs, _lib.ptr(uf), _lib.ptr(ul), _lib.ptr(lm),
-                                           *[_lib.ptr(out.get(k)) for k in order])
-        _lib.check(st, 'slab_engine_coeff_grad')
+        fn = self.L.slab_engine_coeff_grad_mixed if self.mixed else self.L.slab_engine_coeff_grad
+        st = fn(self.h, nrhs, _lib.ptr(uf), _lib.ptr(ul), _lib.ptr(lm), *[_lib.ptr(out.get(k)) for k in order])
+        _lib.check(st, 'slab_engine_coeff_grad_mixed' if self.mixed else 'slab_engine_coeff_grad')
         return out
 
     def residual(self, ufaces, uint, fbody=None):

@@ -2,7 +2,7 @@
 
 Checked against (a) the dense FP64 reference gradient of the oracle's full
 collocation system (oracle/adjoint.py, itself pinned to finite differences on
-the CPU) and (b) central finite differences of the GPU forward solve through
+the CPU), with and without a mixed derivative c12, and (b) central finite differences of the GPU forward solve through
 the torch.autograd.Function.  Tolerances: 1e-9 relative against the oracle
 (FP64 refinement to 1e-12 on both sides of the solve); 1e-5 relative against
 central differences.
@@ -88,6 +88,72 @@ def test_adjoint_matches_dense_reference_gradient(case, precision):
     grads = eng.coeff_grad(ufaces, uleaf, lam, keys=keys)
     for k in keys:
         assert _rel(grads[k].cpu().numpy(), ref[k]) < 1e-9, k
+
+
+def _mixed_setup(precision):
+    """Curvy-annulus coefficients (c11, c22, c12, c2, c; |c12| up to 1) on 8 x 8
+    leaves of order 8: an engine with the mixed-derivative layout."""
+    from slablu_gb300 import hps
+    from slablu_gb300.engine import SlabEngine
+    p, n, kh = 8, 48, 12.0
+    a = 1 / (2 * (n / (p - 2)))
+    md = odomain.Multidomain([[0, 1], [0, 1]], a, p)
+    part = odomain.SlabPartition(md, 1.0)
+    g = hps.Geometry([[0, 1], [0, 1]], a, p, 1.0)
+    md.ld.Interp_mat = np.array(g.ops.Interp_mat)     # the same fit on both sides
+    pdo, pmap = ofuncs.curvy_annulus_pdo(kh, ofuncs.bfield_constant)
+    co = md.coeffs(pdo)
+    assert np.abs(co['c12']).max() > 0.5
+    return md, part, co, SlabEngine(g, precision, mixed=True), kh
+
+
+@pytest.mark.parametrize('precision', ['fp64', 'mixed'])
+def test_adjoint_with_mixed_derivative_matches_dense_reference_gradient(precision):
+    """Transposed solve and coefficient gradients (dL/dc12 included) of an operator
+    with c12 against the oracle's dense FP64 gradient, 1e-9 relative; the same
+    gradients through slab_solve's backward."""
+    from slablu_gb300 import slab_solve
+    md, part, co, eng, kh = _mixed_setup(precision)
+    rng = np.random.default_rng(21)
+    nrhs = 2
+    B = rng.standard_normal((md.ntot, nrhs))
+    w = rng.standard_normal((md.nboxes * md.p ** 2, nrhs))
+    col = oadj.Collocation(md, part, co)
+    uU, uf, sol = col.solve(B[part.I_Xtot])
+    ref = col.gradient(uU, uf, w)
+    eng.factor(**_dev(co))
+    uleaf, ufaces, it, st = eng.solve(torch.as_tensor(B, device='cuda'), tol=1e-12, max_iter=40, want_faces=True)
+    assert st['converged']
+    assert _rel(uleaf.cpu().numpy(), sol) < 1e-9
+    lam, lamf, gb, it_t, st_t = eng.adjoint(gleaf=torch.as_tensor(w, device='cuda'), tol=1e-12, max_iter=40,
+                                            want_faces=True)
+    assert st_t['converged'], st_t
+    if precision == 'fp64':
+        assert it_t <= 3
+    assert _rel(lam.cpu().numpy(), ref['lam_leaf']) < 1e-9
+    assert _rel(lamf.cpu().numpy(), ref['lam_faces']) < 1e-9
+    gbn = gb.cpu().numpy()
+    assert _rel(gbn[part.I_Xtot], ref['bnd']) < 1e-9
+    nd = np.setdiff1d(np.arange(md.ntot), part.I_Xtot)
+    assert np.abs(gbn[nd]).max() == 0.0
+    keys = tuple(k for k in oadj.KEYS if co.get(k) is not None)
+    assert 'c12' in keys
+    grads = eng.coeff_grad(ufaces, uleaf, lam, keys=keys)
+    for k in keys:
+        if np.abs(ref[k]).max() == 0.0:   # a coefficient that is zero everywhere has no gradient signal
+            assert np.abs(grads[k].cpu().numpy()).max() == 0.0, k
+            continue
+        assert _rel(grads[k].cpu().numpy(), ref[k]) < 1e-9, k
+    # the same gradients through the autograd function (first right-hand side)
+    cs = {k: torch.as_tensor(v.ravel(), device='cuda').requires_grad_(True) for k, v in co.items() if v is not None}
+    u = slab_solve(eng, torch.as_tensor(B[:, 0], device='cuda'), tol=1e-12, max_iter=40, **cs)
+    (torch.as_tensor(w[:, 0], device='cuda') * u).sum().backward()
+    ref1 = col.gradient(uU[:, :1], uf[:, :1], w[:, :1])
+    for k in ('c12', 'c'):
+        assert _rel(cs[k].grad.cpu().numpy(), ref1[k]) < 1e-9, k
+    # an engine without the mixed layout has no c12 gradient
+    with pytest.raises(ValueError):
+        _setup(0, precision)[3].coeff_grad(ufaces, uleaf, lam, keys=('c12',))
 
 
 def test_adjoint_many_right_hand_sides():

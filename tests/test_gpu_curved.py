@@ -59,12 +59,10 @@ def test_mixed_engine_matches_sparse_direct_oracle(precision):
     assert st['converged'], st
     err = np.linalg.norm(uleaf.cpu().numpy() - ref) / np.linalg.norm(ref)
     assert err < 1e-9, err
-    # the engine refuses c12 without the mixed layout, and the adjoint with it
+    # the engine refuses c12 without the mixed layout
     with pytest.raises(ValueError):
         SlabEngine(g, precision).factor(**{k: (None if v is None else torch.as_tensor(v.ravel(), device='cuda'))
                                            for k, v in co.items()})
-    with pytest.raises(RuntimeError):
-        eng.adjoint(gleaf=torch.ones(uleaf.shape[0], 1, dtype=torch.float64, device='cuda'))
 
 
 def _annulus_solver(sg, geom, box, p, n, ppw, periodic, precision='mixed'):
