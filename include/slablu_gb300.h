@@ -219,6 +219,17 @@ int slab_solve_graph_destroy(slab_solve_graph* g);
 int slab_engine_residual(slab_engine* e, int nrhs, const double* d_ufaces, const double* d_uint,
                          const double* d_fbody, double* d_rint, double* d_rfaces);
 
+/* One application of the stored factorization to a residual: the correction
+ * (d_dint, d_dfaces) = M^-1 (d_rint, d_rfaces) that one refinement step of
+ * slab_engine_solve adds, with M the factorization in the engine's precision
+ * (leaf, merge-tree and interface sweeps).  Layouts as for slab_engine_residual;
+ * d_rfaces entries on Dirichlet faces are read as zero and d_dfaces is zero
+ * there.  For callers that drive their own iteration (a Krylov method with the
+ * factorization as preconditioner).  The reference applies its factorization
+ * only inside solve (src_solver/slablu_solver.py:543-666). */
+int slab_engine_apply(slab_engine* e, int nrhs, const double* d_rint, const double* d_rfaces, double* d_dint,
+                      double* d_dfaces);
+
 /* Adjoint (transposed) solve with the stored factors, for the gradient of a
  * loss L(u) through slab_engine_solve.  Extends Domain_Solver.solve
  * (src_solver/slablu_solver.py:623-666); the transposed pieces follow

@@ -37,6 +37,7 @@ _SIGS = {
     'slab_engine_factor_mixed': (c_int, [c_void] * 7),
     'slab_engine_solve': (c_int, [c_void, c_int, c_void, c_void, c_double, c_int, c_void, c_void, P_int, P_double]),
     'slab_engine_residual': (c_int, [c_void, c_int] + [c_void] * 5),
+    'slab_engine_apply': (c_int, [c_void, c_int] + [c_void] * 4),
     'slab_solve_graph_create': (c_int, [ctypes.POINTER(c_void), c_void, c_int, c_void, c_void, c_void, c_void,
                                         c_double, c_int]),
     'slab_solve_graph_launch': (c_int, [c_void, c_void]),

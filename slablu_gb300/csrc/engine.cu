@@ -331,6 +331,7 @@ struct EngineBase {
                     double* uleaf, int* iters, double* stats) = 0;
   virtual int residual(int nrhs, const double* ufaces, const double* uint, const double* fbody, double* rint,
                        double* rfaces) = 0;
+  virtual int apply_once(int nrhs, const double* rint, const double* rfaces, double* dint, double* dfaces) = 0;
   virtual int adjoint(int nrhs, const double* gleaf, const double* gfaces, double tol, int max_iter, double* lam_leaf,
                       double* lam_faces, double* gbnd, int* iters, double* stats) = 0;
   virtual int coeff_grad(int nrhs, const double* ufaces, const double* uleaf, const double* lam_leaf, double* g11,
@@ -1928,6 +1929,43 @@ struct EngineImpl : EngineBase {
     return SLAB_OK;
   }
 
+  // One application of the factorization to a residual (FP64 in and out, the
+  // layouts of residual()): the correction step of the refinement, alone.
+  int apply_once(int nrhs, const double* rint, const double* rfaces, double* dint, double* dfaces) override {
+    if (!factored) return set_error(SLAB_ERR_STATE, "slab_engine_apply: engine not factored");
+    if (nrhs <= 0 || !rint || !rfaces || !dint || !dfaces)
+      return set_error(SLAB_ERR_ARG, "slab_engine_apply: invalid arguments");
+    SLAB_TRY(enter());
+    const int st = apply_once_impl(nrhs, rint, rfaces, dint, dfaces);
+    const int st2 = leave();
+    return st != SLAB_OK ? st : st2;
+  }
+
+  int apply_once_impl(int nrhs, const double* rint, const double* rfaces, double* dint, double* dfaces) {
+    SLAB_TRY(reserve(nrhs));
+    const long long nc_el = nleaf * n * nrhs, nf_el = ntot * nrhs;
+    convert_kernel<T, double><<<grid_for(nc_el), 256, 0, s>>>(rint, rcT.as<T>(), nc_el);
+    SLAB_CHECK_LAUNCH();
+    // Dirichlet faces carry no flux row: their entries are read as zero
+    mask_faces_kernel<<<grid_for(nf_el), 256, 0, s>>>(rfaces, dirmask.as<unsigned char>(), rx_d.as<double>(), ntot,
+                                                      nrhs, 0);
+    SLAB_CHECK_LAUNCH();
+    convert_kernel<T, double><<<grid_for(nf_el), 256, 0, s>>>(rx_d.as<double>(), gvec.as<T>(), nf_el);
+    SLAB_CHECK_LAUNCH();
+    if (gapp && gapp_nrhs != nrhs) {
+      cudaGraphExecDestroy(gapp);
+      gapp = nullptr;
+    }
+    gapp_nrhs = nrhs;
+    SLAB_TRY(run_graph(gapp, [&]() { return apply(nrhs); }));
+    convert_kernel<double, T><<<grid_for(nc_el), 256, 0, s>>>(wc.as<T>(), dint, nc_el);
+    SLAB_CHECK_LAUNCH();
+    convert_kernel<double, T><<<grid_for(nf_el), 256, 0, s>>>(uvec.as<T>(), dfaces, nf_el);
+    SLAB_CHECK_LAUNCH();
+    SLAB_CUDA_TRY(cudaStreamSynchronize(s));
+    return SLAB_OK;
+  }
+
   int residual(int nrhs, const double* ufaces, const double* uint, const double* fbody, double* rint,
                double* rfaces) override {
     if (!factored && !has[0] && !has[1] && !has[4])
@@ -2150,6 +2188,12 @@ extern "C" int slab_engine_coeff_grad_mixed(slab_engine* e, int nrhs, const doub
                                             double* g1, double* g2, double* g) {
   if (!e) return slab::set_error(SLAB_ERR_ARG, "slab_engine_coeff_grad_mixed: null engine");
   return e->impl->coeff_grad(nrhs, ufaces, uleaf, lam_leaf, g11, g22, g12, g1, g2, g);
+}
+
+extern "C" int slab_engine_apply(slab_engine* e, int nrhs, const double* rint, const double* rfaces, double* dint,
+                                 double* dfaces) {
+  if (!e) return slab::set_error(SLAB_ERR_ARG, "slab_engine_apply: null engine");
+  return e->impl->apply_once(nrhs, rint, rfaces, dint, dfaces);
 }
 
 extern "C" int slab_engine_residual(slab_engine* e, int nrhs, const double* ufaces, const double* uint,

@@ -53,6 +53,7 @@ class SlabEngine:
         self.ntot = int(self.L.slab_engine_nfaces(self.h))
         self.nleaf = int(self.L.slab_engine_nleaves(self.h))
         self.npts = self.nleaf * geom.p * geom.p
+        self.n_int = (geom.p - 2) ** 2
         self.generation = 0  # incremented by every factor(); checked by the autograd backward
 
     def __del__(self):
@@ -183,6 +184,22 @@ class SlabEngine:
                                          _lib.ptr(rf))
         _lib.check(st, 'slab_engine_residual')
         return rint, rf.T
+
+    def apply(self, rint, rfaces):
+        """One application of the factorization (slab_engine_apply): the correction
+        M^-1 (rint, rfaces) of one refinement step.  rint: (nleaf, nrhs, (p-2)^2)
+        leaf-major like residual(); rfaces: (ntot, nrhs).  Returns (dint like rint,
+        dfaces (ntot, nrhs))."""
+        nrhs = 1 if rfaces.dim() == 1 else rfaces.shape[1]
+        rf = _col_major(rfaces.to(torch.float64), self.ntot)
+        ri = rint.to(torch.float64).contiguous()
+        if ri.numel() != self.nleaf * nrhs * self.n_int:
+            raise ValueError('rint must hold nleaf x nrhs x (p-2)^2 values')
+        dint = torch.empty_like(ri)
+        df = torch.empty_like(rf)
+        st = self.L.slab_engine_apply(self.h, nrhs, _lib.ptr(ri), _lib.ptr(rf), _lib.ptr(dint), _lib.ptr(df))
+        _lib.check(st, 'slab_engine_apply')
+        return dint, df.T
 
 
 
