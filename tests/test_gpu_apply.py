@@ -3,11 +3,13 @@
 The first refinement step of slab_engine_solve starts from the Dirichlet data
 and zero unknowns, forms the FP64 residual and adds one application of the
 factorization; slab_engine_residual followed by slab_engine_apply reproduces
-that step (to the rounding of the residual's atomically summed face rows,
-1e-12 relative here).  Dirichlet entries of the face residual are ignored and
-the correction is zero there.  In FP64 one application is already the solution
-to 1e-9 against the oracle's sparse direct solve (the engine's solve is held
-to the oracle by test_gpu_parity.py).
+that step, up to the order in which the application adds the two leaves'
+fluxes to each face row (atomics: 1e-12 relative with FP64 factors, 1e-5 with
+FP32 factors, where the measured spread between runs is 2e-6).  Dirichlet
+entries of the face residual are ignored and the correction is zero there, and
+the step reduces the FP64 residual by orders of magnitude.  In FP64 one
+application is already the solution to 1e-9 against the oracle's sparse direct
+solve (the engine's solve is held to the oracle by test_gpu_parity.py).
 """
 import numpy as np
 import pytest
@@ -61,9 +63,14 @@ def test_apply_is_one_refinement_step(precision):
     rf_noise = rf + torch.randn(rf.shape, generator=gen, device='cuda', dtype=torch.float64) * dirm[:, None]
     dint, df = eng.apply(rint, rf_noise)
     assert float(df[dirm].abs().max()) == 0.0
-    assert _rel(bnd + df, uf1) < 1e-12
+    tol = 1e-12 if precision == 'fp64' else 1e-5
+    assert _rel(bnd + df, uf1) < tol
     ref_int = uleaf1.T.reshape(nrhs, eng.nleaf, p * p)[:, :, node].permute(1, 0, 2)
-    assert _rel(dint, ref_int) < 1e-12
+    assert _rel(dint, ref_int) < tol
+    r1i, r1f = eng.residual(bnd + df, dint)
+    r0n = float(torch.sqrt(torch.sum(rint ** 2) + torch.sum(rf ** 2)))
+    r1n = float(torch.sqrt(torch.sum(r1i ** 2) + torch.sum(r1f ** 2)))
+    assert r1n < (1e-9 if precision == 'fp64' else 1e-3) * r0n, (r1n, r0n)
     if precision == 'fp64':
         col = oadj.Collocation(md, part, co)
         _, uf_ref, _ = col.solve(bnd.cpu().numpy()[part.I_Xtot])
