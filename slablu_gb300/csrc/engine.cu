@@ -1056,8 +1056,13 @@ struct EngineImpl : EngineBase {
                                 mergeinfo.as<int>() + info_ofs, b.count));
       SLAB_TRY(build_perm_batched(s, pv, b.nE, b.nE, b.count, permpool.as<int>() + b.offPiv0, b.nE));
       T* R = Maug + (long long)b.nE * b.nE;
-      SLAB_TRY(getrs_batched<T>(s, b.nE, b.nO, Maug, nullptr, strideM, b.nE, pv, nullptr, b.nE, R, nullptr, strideM,
-                                b.nE, b.count));
+      // W = M^{-1} [A|B][E,O]: the tiled many-column substitution where M fits its shared memory
+      if (getrs_many_fits<T>(b.nE))
+        SLAB_TRY(getrs_many<T>(s, b.nE, b.nO, Maug, strideM, b.nE, permpool.as<int>() + b.offPiv0, b.nE, R, strideM,
+                               b.nE, b.count));
+      else
+        SLAB_TRY(getrs_batched<T>(s, b.nE, b.nO, Maug, nullptr, strideM, b.nE, pv, nullptr, b.nE, R, nullptr, strideM,
+                                  b.nE, b.count));
       bool done = false;
       if constexpr (std::is_same<T, float>::value) {
         if (use_tc_tree && b.nE >= kTcMinE && b.nO > 0) {
