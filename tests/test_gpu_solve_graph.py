@@ -103,3 +103,26 @@ def test_solve_graph_refusals():
         graph.launch()
     assert ex.value.status == -4
     np.testing.assert_equal(SolveGraph([eng], nrhs=1).nrhs, [1])
+
+
+def test_solve_graph_with_mixed_derivative_engine():
+    """An engine with c12 (curvy-annulus coefficients, 8 x 8 leaves of order 8) next to
+    one without, in one graph: the same steps and solutions as slab_engine_solve."""
+    from slablu_gb300 import SolveGraph, hps
+    from slablu_gb300.engine import SlabEngine
+    p, n, kh = 8, 48, 12.0
+    a = 1 / (2 * (n / (p - 2)))
+    md = odomain.Multidomain([[0, 1], [0, 1]], a, p)
+    g = hps.Geometry([[0, 1], [0, 1]], a, p, 1.0)
+    pdo, _ = ofuncs.curvy_annulus_pdo(kh, ofuncs.bfield_constant)
+    co = md.coeffs(pdo)
+    emix = SlabEngine(g, 'mixed', mixed=True)
+    emix.factor(**{k: torch.as_tensor(v.ravel(), device='cuda') for k, v in co.items() if v is not None})
+    engines = [emix, _engine(0)]
+    graph = SolveGraph(engines, nrhs=[2, 1], tol=TOL, max_iter=MAXIT)
+    gen = torch.Generator(device='cuda').manual_seed(9)
+    inputs = [(torch.randn(e.ntot, k, generator=gen, device='cuda', dtype=torch.float64), None)
+              for e, k in zip(engines, (2, 1))]
+    for i, (bnd, fb) in enumerate(inputs):
+        graph.set_inputs(i, bnd, fb)
+    _check(graph, engines, inputs)
