@@ -4,7 +4,7 @@ The first refinement step of slab_engine_solve starts from the Dirichlet data
 and zero unknowns, forms the FP64 residual and adds one application of the
 factorization; slab_engine_residual followed by slab_engine_apply reproduces
 that step, up to the order in which the application adds the two leaves'
-fluxes to each face row (atomics: 1e-12 relative with FP64 factors, 1e-5 with
+fluxes to each face row (atomics: 1e-12 relative with FP64 factors, 1e-4 with
 FP32 factors, where the measured spread between runs is 2e-6).  Dirichlet
 entries of the face residual are ignored and the correction is zero there, and
 the step reduces the FP64 residual by orders of magnitude.  In FP64 one
@@ -63,7 +63,7 @@ def test_apply_is_one_refinement_step(precision):
     rf_noise = rf + torch.randn(rf.shape, generator=gen, device='cuda', dtype=torch.float64) * dirm[:, None]
     dint, df = eng.apply(rint, rf_noise)
     assert float(df[dirm].abs().max()) == 0.0
-    tol = 1e-12 if precision == 'fp64' else 1e-5
+    tol = 1e-12 if precision == 'fp64' else 1e-4
     assert _rel(bnd + df, uf1) < tol
     ref_int = uleaf1.T.reshape(nrhs, eng.nleaf, p * p)[:, :, node].permute(1, 0, 2)
     assert _rel(dint, ref_int) < tol
