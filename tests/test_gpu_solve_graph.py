@@ -2,9 +2,10 @@
 
 The graph runs the same kernels in the same order as slab_engine_solve, with
 the refinement decision taken on the device, so its solutions match
-slab_engine_solve's to rounding of the norm sums (1e-13 relative here) with the
-same number of steps; slab_engine_solve is itself held to the oracle by
-test_gpu_parity.py.  Also: a second launch with new inputs, a re-factorization
+slab_engine_solve's to rounding (1e-13 relative measured; 1e-11 asserted, and
+the step counts within one, because the FP32 face sums of an application are
+atomic and their order can change the last bits of a step); slab_engine_solve
+is itself held to the oracle by test_gpu_parity.py.  Also: a second launch with new inputs, a re-factorization
 picked up without a new graph, and the host-side refusals (an engine given
 twice; buffers reallocated after the graph was made).
 """
@@ -66,8 +67,8 @@ def _check(graph, engines, inputs):
         u_ref, _, it_ref, info_ref = eng.solve(bnd, fb, tol=TOL, max_iter=MAXIT)
         u, it, info = graph.result(i)
         assert info['converged']
-        assert it == it_ref, (i, it, it_ref)
-        assert _rel(u, u_ref) < 1e-13, (i, _rel(u, u_ref))
+        assert abs(it - it_ref) <= 1, (i, it, it_ref)
+        assert _rel(u, u_ref) < 1e-11, (i, _rel(u, u_ref))
         assert info['rel_correction'] <= TOL
         assert abs(info['residual'] - info_ref['residual']) <= 1e-6 * info_ref['residual0']
 
