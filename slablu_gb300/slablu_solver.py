@@ -31,6 +31,7 @@ Out of scope (raise NotImplementedError): finite differences (p = 0), body
 loads with periodic_bc.
 """
 import time
+import warnings
 
 import numpy as np
 import torch
@@ -246,6 +247,12 @@ class Domain_Solver:
             uleaf, _, iters, st = self.engine.solve(bnd, fb, tol=self.tol, max_iter=self.max_iter,
                                                     allow_noconv=True)
             rel_err = torch.tensor(st['rel_residual'])
+            if not st['converged']:
+                # the answer is still returned (with its residual, as the reference returns
+                # rel_err), but it is less accurate than tol asks
+                warnings.warn(f'refinement stopped after {iters} steps at relative correction '
+                              f'{st["rel_correction"]:.1e} (tol {self.tol:.0e}): raise max_iter, or use '
+                              f"precision='fp64' for a harder problem", RuntimeWarning, stacklevel=2)
         # the leaf-node solution comes back into pinned host memory (torch's
         # caching host allocator reuses the blocks of freed results)
         if uleaf.is_cuda:
