@@ -1204,8 +1204,11 @@ __global__ void __launch_bounds__(256)
 constexpr int kManyCols = 32;
 constexpr int kManyMaxN = 1024;  // the tile of n rows stays in shared memory
 constexpr int kManyChunk = 128;
+// FP32: registers capped for three resident CTAs per SM (80, a few spilled
+// bytes outside the update loop), measured faster than two (94 registers) and
+// four (64, more spills)
 template <typename T>
-__global__ void __launch_bounds__(256) getrs_many_kernel(int n, int nrhs, const T* __restrict__ LU,
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1) getrs_many_kernel(int n, int nrhs, const T* __restrict__ LU,
                                                          long long strideLU, int lda, const int* __restrict__ perm,
                                                          long long strideP, T* B, long long strideB, int ldb) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
